@@ -1,0 +1,208 @@
+/* lfm_gpu.h - C ABI of the GB300 explicit finite-volume time step.
+ *
+ * This is the drop-in boundary for libFastMesh's hot path: the ISolver stage
+ * methods driven by Mesh::solve (reference src/mesh_solver.cpp:474-727) and
+ * the case input behind IMeshReader / CInputReader. Plain C types only: every
+ * function returns 0 on success and a negative lfm_status on failure (the
+ * message is available from lfm_last_error()); no C++ exception crosses it.
+ * Handles are owned by the caller and must be released with the matching
+ * *_free / *_destroy call. Calls on one solver handle are not re-entrant; one
+ * solver issues all its work on its own CUDA stream.
+ *
+ * Arrays are structure-of-arrays: a field with k components over n entries is
+ * k consecutive blocks of n values. Conserved state q = (rho, rho*u[dim],
+ * rho*E), nq = dim + 2 components, cells in solver order (submesh 0 cells in
+ * polyMesh order, then submesh 1 cells), exactly the order of the reference's
+ * (submesh, index) numbering. */
+#ifndef LFM_GPU_H
+#define LFM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum lfm_status {
+    LFM_OK = 0,
+    LFM_ERR_INVALID = -1,   /* bad argument or case data */
+    LFM_ERR_IO = -2,        /* case files missing or malformed */
+    LFM_ERR_CUDA = -3,      /* CUDA runtime error */
+    LFM_ERR_NOMEM = -4,     /* device memory exhausted */
+    LFM_ERR_NUMERIC = -5,   /* non-finite state detected */
+    LFM_ERR_UNSUPPORTED = -6
+} lfm_status;
+
+/* Scheme ids, as the reference's fastmesh_solver_t (api/fastmesh.h:38-41). */
+#define LFM_SOLVER_M1 0
+#define LFM_SOLVER_M2 1
+#define LFM_SOLVER_M2AUSM 2
+
+/* Arithmetic of the flux kernels. LFM_FP64 is the plain method; LFM_FP32_BULK
+ * computes fluxes, limiter and residual in FP32 and keeps the RK registers,
+ * geometry precompute and dt reduction in FP64. */
+#define LFM_FP64 0
+#define LFM_FP32_BULK 1
+
+/* Boundary-ghost kinds (reference src/cfd_v0.cpp:972-1005). */
+#define LFM_GHOST_NONE 0
+#define LFM_GHOST_WALL 1
+#define LFM_GHOST_INLET 2
+#define LFM_GHOST_OUTLET 3
+#define LFM_GHOST_FARFIELD 4
+
+/* Solver description: the reference's per-cell CFDv0_cell data after
+ * CFDv0_solver::initialize + reorder_faces (src/cfd_v0.cpp:83-339, 759-967),
+ * flattened. Faces are the "owned" cell-faces in the reference's processing
+ * order (cell by cell, slot by slot); P is the processing cell, N the other
+ * side (N >= n_cells: boundary ghost N - n_cells). Geometry is seen from P. */
+typedef struct lfm_solver_desc {
+    int dim;                 /* 2 or 3 */
+    int nq;                  /* dim + 2 */
+    int solver;              /* LFM_SOLVER_* */
+    int rk_order;            /* stages per time step */
+    int minmod;              /* fvSchemes lfm/minmodExists */
+    int residuals;           /* controlDict lfm/post/haveResiduals */
+    int64_t n_cells, n_cells0, n_ghosts, n_faces;
+    const int64_t* face_p;   /* [n_faces] */
+    const int64_t* face_n;   /* [n_faces] */
+    const uint8_t* face_ghost; /* [n_faces] neighbour is a boundary ghost */
+    const double* S;         /* [dim][n_faces] face area vector, outward from P */
+    const double* d;         /* [dim][n_faces] P-centre to N-centre vector */
+    const double* w;         /* [n_faces] linear weight of P */
+    const double* smag;      /* [n_faces] |S| */
+    const double* dmag_inv;  /* [n_faces] 1/|d| */
+    const double* dnorm;     /* [dim][n_faces] d/|d| */
+    const double* delta_mag; /* [n_faces] |delta|, delta = d |S|^2/(S.d) */
+    const double* K;         /* [dim][n_faces] S - delta */
+    const double* vol_inv;   /* [n_cells] */
+    const double* sponge;    /* [n_cells] sponge sigma */
+    const int64_t* ghost_cell; /* [n_ghosts] interior cell of each ghost */
+    const int* ghost_kind;   /* [n_ghosts] LFM_GHOST_* */
+    const int64_t* cell_face_offsets; /* [n_cells+1] incidence, ascending face */
+    const int64_t* cell_faces;
+    const int8_t* cell_face_sign;     /* +1 when the cell is P */
+    const int64_t* cell_s_offsets;    /* [n_cells+1] all valid faces of a cell */
+    const double* cell_s;             /* dim values per entry, seen from the cell */
+    const double* q0;        /* [nq][n_cells] initial state (may be NULL) */
+    double gamma, Rgas, rhoInf, EInf, pInf, TInf, UInf[3], mu, Cp, PrInv;
+    const double* rkA;       /* [rk_order] */
+    const double* rkB;
+} lfm_solver_desc;
+
+typedef struct lfm_case lfm_case;
+typedef struct lfm_solver lfm_solver;
+
+/* Last error message of the calling thread ("" when none). */
+const char* lfm_last_error(void);
+/* Library version string. */
+const char* lfm_version(void);
+
+/* ---- case input (replaces CInputReader::initialize, src/inputReader.cpp:7-69,
+ * and the polyMeshReaderOF / dictReaderOF / runTimeManagerOF plugins) ------ */
+
+/* Reads an OpenFOAM case: <root>/system/{controlDict,fvSchemes},
+ * <root>/constant/{spongeDict,thermophysicalProperties,turbulenceProperties},
+ * the polyMesh of <root> (rank < 0) or <root>/processor<rank>, and the fields
+ * p, T, U, alpha at the start time. */
+int lfm_case_open(const char* root, int rank, lfm_case** out);
+
+/* In-memory polyMesh and parameters (same meaning as the case files). */
+typedef struct lfm_polymesh {
+    int64_t n_points;
+    const double* points;            /* [n_points][3] interleaved */
+    int64_t n_faces;
+    const int64_t* face_offsets;     /* [n_faces+1] */
+    const int64_t* face_points;
+    const int64_t* owner;            /* [n_faces] */
+    int64_t n_internal_faces;
+    const int64_t* neighbour;        /* [n_internal_faces] */
+    int n_patches;
+    const char* const* patch_name;
+    const char* const* patch_type;   /* wall, patch, empty, cyclic, farfield ... */
+    const int64_t* patch_start;
+    const int64_t* patch_size;
+    const char* const* patch_neighbour; /* cyclic partner name or NULL */
+    const int64_t* cell_submesh;     /* optional [n_cells] or NULL */
+    int64_t n_cells;
+} lfm_polymesh;
+
+typedef struct lfm_params {
+    int solver, dimension, rk_order, minmod, laminar, residuals;
+    double p_inf, T_inf, U_inf[3], Ls, mach, k_sponge;
+    double Cp, mol_weight, mu, Pr;
+} lfm_params;
+
+typedef struct lfm_fields {
+    const double* p;      /* [n_cells] */
+    const double* T;      /* [n_cells] */
+    const double* U;      /* [n_cells][3] interleaved */
+    const double* alpha;  /* [n_cells] sponge distance, may be NULL when Ls <= 0 */
+} lfm_fields;
+
+int lfm_case_from_polymesh(const lfm_polymesh* mesh, const lfm_params* params, const lfm_fields* fields,
+                           lfm_case** out);
+/* Pointers into the case's arrays; valid until lfm_case_free. */
+int lfm_case_describe(const lfm_case* c, lfm_solver_desc* out);
+/* Run control read from controlDict: deltaT, endTime, writeInterval ... */
+int lfm_case_time(const lfm_case* c, double* delta_t, double* start_time, double* end_time, int* adjust_time_step,
+                  double* max_co);
+/* polyMesh label of each solver-order cell ([n_cells]). */
+int lfm_case_cell_ids(const lfm_case* c, int64_t* out);
+void lfm_case_free(lfm_case* c);
+
+/* ---- device solver (replaces ISolver, api/cfdv0_solver.h:18-105) -------- */
+
+typedef struct lfm_solver_opts {
+    int precision;        /* LFM_FP64 or LFM_FP32_BULK */
+    int device;           /* CUDA device ordinal */
+    int block;            /* threads per block for the cell/face kernels, 0 = default */
+} lfm_solver_opts;
+
+/* Uploads the description; the state starts at desc->q0 (or zero). */
+int lfm_solver_create(const lfm_solver_desc* desc, const lfm_solver_opts* opts, lfm_solver** out);
+void lfm_solver_destroy(lfm_solver* s);
+
+/* Host <-> device state copies ([nq][n_cells], pageable or pinned host memory). */
+int lfm_solver_set_state(lfm_solver* s, const double* q);
+int lfm_solver_get_state(lfm_solver* s, double* q);
+
+/* One RK stage: prepare_for_RKstep, set_boundary_conditions, calc_gradients
+ * (M2AUSM only), calc_VIS, one_rk_step_M* (src/mesh_solver.cpp:500-672).
+ * Stage 0 also performs prepare_for_timestep. Asynchronous on the solver stream. */
+int lfm_solver_stage(lfm_solver* s, int rk_stage, double dt);
+
+/* nsteps full time steps at constant dt (rk_order stages each), replayed from
+ * a CUDA graph. Asynchronous on the solver stream. */
+int lfm_solver_step(lfm_solver* s, int nsteps, double dt);
+
+/* Same as lfm_solver_step, timed with CUDA events on the solver stream;
+ * waits for completion and returns the elapsed milliseconds. */
+int lfm_solver_step_timed(lfm_solver* s, int nsteps, double dt, float* ms);
+
+/* compute_cfl / compute_dt (src/cfd_v0.cpp:2886-2942) reduced on the device
+ * deterministically; blocks until the value is on the host. */
+int lfm_solver_cfl(lfm_solver* s, double dt, double* cfl);
+int lfm_solver_min_dt(lfm_solver* s, double max_co, double* dt);
+
+/* Sum over cells of the squared stage-0 residual of the last time step,
+ * per conserved variable ([nq]); requires desc->residuals. */
+int lfm_solver_residual(lfm_solver* s, double* res);
+
+/* Blocks until all work on the solver stream has finished and reports the
+ * first CUDA or numeric error. */
+int lfm_solver_sync(lfm_solver* s);
+
+/* Device kernels launched per time step (for launch accounting). */
+int lfm_solver_launches_per_step(const lfm_solver* s, int* launches);
+
+/* Per-kernel timing of one time step ([n] entries, names in
+ * lfm_solver_kernel_name). Synchronizes. */
+int lfm_solver_profile_step(lfm_solver* s, double dt, int n, float* ms);
+const char* lfm_solver_kernel_name(int i);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

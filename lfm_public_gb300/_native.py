@@ -1,0 +1,334 @@
+"""ctypes binding of the C ABI in include/lfm_gpu.h.
+
+The library is the in-tree ``liblfm_gpu.so``; importing a solver without it is
+an error (there is no CPU fallback). The oracle port library is loaded only by
+``load_port`` for tests and the CPU baseline.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+LIB_PATH = os.path.join(PKG, "liblfm_gpu.so")
+PORT_PATH = os.path.join(ROOT, "oracle", "port", "liblfm_port.so")
+
+LFM_FP64 = 0
+LFM_FP32_BULK = 1
+
+_i64p = C.POINTER(C.c_int64)
+_dp = C.POINTER(C.c_double)
+
+
+class SolverDesc(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int), ("nq", C.c_int), ("solver", C.c_int), ("rk_order", C.c_int), ("minmod", C.c_int),
+        ("residuals", C.c_int),
+        ("n_cells", C.c_int64), ("n_cells0", C.c_int64), ("n_ghosts", C.c_int64), ("n_faces", C.c_int64),
+        ("face_p", _i64p), ("face_n", _i64p), ("face_ghost", C.POINTER(C.c_uint8)),
+        ("S", _dp), ("d", _dp), ("w", _dp), ("smag", _dp), ("dmag_inv", _dp), ("dnorm", _dp), ("delta_mag", _dp),
+        ("K", _dp), ("vol_inv", _dp), ("sponge", _dp),
+        ("ghost_cell", _i64p), ("ghost_kind", C.POINTER(C.c_int)),
+        ("cell_face_offsets", _i64p), ("cell_faces", _i64p), ("cell_face_sign", C.POINTER(C.c_int8)),
+        ("cell_s_offsets", _i64p), ("cell_s", _dp), ("q0", _dp),
+        ("gamma", C.c_double), ("Rgas", C.c_double), ("rhoInf", C.c_double), ("EInf", C.c_double),
+        ("pInf", C.c_double), ("TInf", C.c_double), ("UInf", C.c_double * 3), ("mu", C.c_double), ("Cp", C.c_double),
+        ("PrInv", C.c_double), ("rkA", _dp), ("rkB", _dp),
+    ]
+
+
+class PolyMesh(C.Structure):
+    _fields_ = [
+        ("n_points", C.c_int64), ("points", _dp), ("n_faces", C.c_int64), ("face_offsets", _i64p),
+        ("face_points", _i64p), ("owner", _i64p), ("n_internal_faces", C.c_int64), ("neighbour", _i64p),
+        ("n_patches", C.c_int), ("patch_name", C.POINTER(C.c_char_p)), ("patch_type", C.POINTER(C.c_char_p)),
+        ("patch_start", _i64p), ("patch_size", _i64p), ("patch_neighbour", C.POINTER(C.c_char_p)),
+        ("cell_submesh", _i64p), ("n_cells", C.c_int64),
+    ]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("solver", C.c_int), ("dimension", C.c_int), ("rk_order", C.c_int), ("minmod", C.c_int), ("laminar", C.c_int),
+        ("residuals", C.c_int), ("p_inf", C.c_double), ("T_inf", C.c_double), ("U_inf", C.c_double * 3),
+        ("Ls", C.c_double), ("mach", C.c_double), ("k_sponge", C.c_double), ("Cp", C.c_double),
+        ("mol_weight", C.c_double), ("mu", C.c_double), ("Pr", C.c_double),
+    ]
+
+
+class Fields(C.Structure):
+    _fields_ = [("p", _dp), ("T", _dp), ("U", _dp), ("alpha", _dp)]
+
+
+class SolverOpts(C.Structure):
+    _fields_ = [("precision", C.c_int), ("device", C.c_int), ("block", C.c_int)]
+
+
+class LfmError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"lfm error {code}: {msg}")
+        self.code = code
+
+
+_lib: Optional[C.CDLL] = None
+_port: Optional[C.CDLL] = None
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    """Loads liblfm_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(path)
+    vp = C.c_void_p
+    sig = {
+        "lfm_last_error": ([], C.c_char_p), "lfm_version": ([], C.c_char_p),
+        "lfm_case_open": ([C.c_char_p, C.c_int, C.POINTER(vp)], C.c_int),
+        "lfm_case_from_polymesh": ([C.POINTER(PolyMesh), C.POINTER(Params), C.POINTER(Fields), C.POINTER(vp)],
+                                   C.c_int),
+        "lfm_case_describe": ([vp, C.POINTER(SolverDesc)], C.c_int),
+        "lfm_case_time": ([vp, _dp, _dp, _dp, C.POINTER(C.c_int), _dp], C.c_int),
+        "lfm_case_cell_ids": ([vp, _i64p], C.c_int),
+        "lfm_case_free": ([vp], None),
+        "lfm_solver_create": ([C.POINTER(SolverDesc), C.POINTER(SolverOpts), C.POINTER(vp)], C.c_int),
+        "lfm_solver_destroy": ([vp], None),
+        "lfm_solver_set_state": ([vp, _dp], C.c_int),
+        "lfm_solver_get_state": ([vp, _dp], C.c_int),
+        "lfm_solver_stage": ([vp, C.c_int, C.c_double], C.c_int),
+        "lfm_solver_step": ([vp, C.c_int, C.c_double], C.c_int),
+        "lfm_solver_step_timed": ([vp, C.c_int, C.c_double, C.POINTER(C.c_float)], C.c_int),
+        "lfm_solver_cfl": ([vp, C.c_double, _dp], C.c_int),
+        "lfm_solver_min_dt": ([vp, C.c_double, _dp], C.c_int),
+        "lfm_solver_residual": ([vp, _dp], C.c_int),
+        "lfm_solver_sync": ([vp], C.c_int),
+        "lfm_solver_launches_per_step": ([vp, C.POINTER(C.c_int)], C.c_int),
+        "lfm_solver_profile_step": ([vp, C.c_double, C.c_int, C.POINTER(C.c_float)], C.c_int),
+        "lfm_solver_kernel_name": ([C.c_int], C.c_char_p),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def load_port(path: str = PORT_PATH) -> C.CDLL:
+    """Loads the oracle port (test infrastructure only)."""
+    global _port
+    if _port is not None:
+        return _port
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with lfm_public_gb300.build.build_port()")
+    lib = C.CDLL(path)
+    lib.lfm_port_run.argtypes = [C.POINTER(SolverDesc), _dp, C.c_int, C.c_double, _dp]
+    lib.lfm_port_run.restype = C.c_int
+    lib.lfm_port_cfl.argtypes = [C.POINTER(SolverDesc), _dp, C.c_double, _dp]
+    lib.lfm_port_cfl.restype = C.c_int
+    lib.lfm_port_min_dt.argtypes = [C.POINTER(SolverDesc), _dp, C.c_double, _dp]
+    lib.lfm_port_min_dt.restype = C.c_int
+    _port = lib
+    return lib
+
+
+def check(rc: int) -> None:
+    if rc != 0:
+        msg = load_library().lfm_last_error().decode(errors="replace")
+        raise LfmError(rc, msg)
+
+
+def _ptr(a: np.ndarray, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+class CaseHandle:
+    """An lfm_case: the host-side solver setup of one case."""
+
+    def __init__(self, handle: C.c_void_p, keep=()):
+        self._h = handle
+        self._keep = keep
+        self.desc = SolverDesc()
+        check(load_library().lfm_case_describe(self._h, C.byref(self.desc)))
+
+    @classmethod
+    def open(cls, root: str, rank: int = -1) -> "CaseHandle":
+        lib = load_library()
+        h = C.c_void_p()
+        check(lib.lfm_case_open(root.encode(), rank, C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_case(cls, case) -> "CaseHandle":
+        """From an in-memory lfm_public_gb300.cases.Case."""
+        lib = load_library()
+        pts = np.ascontiguousarray(case.points, dtype=np.float64)
+        fo = np.ascontiguousarray(case.face_offsets, dtype=np.int64)
+        fp = np.ascontiguousarray(case.face_points, dtype=np.int64)
+        own = np.ascontiguousarray(case.owner, dtype=np.int64)
+        nei = np.ascontiguousarray(case.neighbour, dtype=np.int64)
+        names = (C.c_char_p * len(case.patches))(*[p.name.encode() for p in case.patches])
+        types = (C.c_char_p * len(case.patches))(*[p.type.encode() for p in case.patches])
+        nbrs = (C.c_char_p * len(case.patches))(*[(p.neighbour.encode() if p.neighbour else None)
+                                                  for p in case.patches])
+        starts = np.array([p.start for p in case.patches], dtype=np.int64)
+        sizes = np.array([p.size for p in case.patches], dtype=np.int64)
+        m = PolyMesh(n_points=pts.shape[0], points=_ptr(pts, C.c_double), n_faces=own.shape[0],
+                     face_offsets=_ptr(fo, C.c_int64), face_points=_ptr(fp, C.c_int64), owner=_ptr(own, C.c_int64),
+                     n_internal_faces=nei.shape[0], neighbour=_ptr(nei, C.c_int64), n_patches=len(case.patches),
+                     patch_name=names, patch_type=types, patch_start=_ptr(starts, C.c_int64),
+                     patch_size=_ptr(sizes, C.c_int64), patch_neighbour=nbrs, cell_submesh=None,
+                     n_cells=case.n_cells)
+        pr = case.params()
+        prm = Params(solver=pr["solver"], dimension=pr["dimension"], rk_order=pr["rk_order"], minmod=pr["minmod"],
+                     laminar=1, residuals=pr["residuals"], p_inf=pr["p_inf"], T_inf=pr["T_inf"],
+                     U_inf=(C.c_double * 3)(*pr["U_inf"]), Ls=pr["Ls"], mach=pr["mach"], k_sponge=pr["k_sponge"],
+                     Cp=pr["Cp"], mol_weight=pr["mol_weight"], mu=pr["mu"], Pr=pr["Pr"])
+        p = np.ascontiguousarray(case.fields["p"], dtype=np.float64)
+        T = np.ascontiguousarray(case.fields["T"], dtype=np.float64)
+        U = np.ascontiguousarray(case.fields["U"], dtype=np.float64)
+        al = case.fields.get("alpha")
+        al = np.ascontiguousarray(al, dtype=np.float64) if al is not None else None
+        fl = Fields(p=_ptr(p, C.c_double), T=_ptr(T, C.c_double), U=_ptr(U, C.c_double),
+                    alpha=_ptr(al, C.c_double) if al is not None else None)
+        h = C.c_void_p()
+        check(lib.lfm_case_from_polymesh(C.byref(m), C.byref(prm), C.byref(fl), C.byref(h)))
+        return cls(h)
+
+    def time(self):
+        lib = load_library()
+        dt, t0, t1, mc = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        adj = C.c_int()
+        check(lib.lfm_case_time(self._h, C.byref(dt), C.byref(t0), C.byref(t1), C.byref(adj), C.byref(mc)))
+        return dict(delta_t=dt.value, start_time=t0.value, end_time=t1.value, adjust=bool(adj.value),
+                    max_co=mc.value)
+
+    def cell_ids(self) -> np.ndarray:
+        out = np.empty(self.desc.n_cells, dtype=np.int64)
+        check(load_library().lfm_case_cell_ids(self._h, _ptr(out, C.c_int64)))
+        return out
+
+    def q0(self) -> np.ndarray:
+        d = self.desc
+        return np.ctypeslib.as_array(d.q0, shape=(d.nq * d.n_cells,)).reshape(d.nq, d.n_cells).copy()
+
+    def array(self, name: str, shape, dtype=np.float64) -> np.ndarray:
+        ptr = getattr(self.desc, name)
+        return np.ctypeslib.as_array(ptr, shape=shape).copy()
+
+    def close(self):
+        if self._h:
+            load_library().lfm_case_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Solver:
+    """An lfm_solver on one GPU."""
+
+    def __init__(self, case: CaseHandle, precision: int = LFM_FP64, device: int = 0):
+        lib = load_library()
+        self.case = case
+        self.nq = case.desc.nq
+        self.n_cells = case.desc.n_cells
+        opts = SolverOpts(precision=precision, device=device, block=0)
+        h = C.c_void_p()
+        check(lib.lfm_solver_create(C.byref(case.desc), C.byref(opts), C.byref(h)))
+        self._h = h
+
+    def set_state(self, q: np.ndarray):
+        q = np.ascontiguousarray(q, dtype=np.float64).reshape(self.nq, self.n_cells)
+        check(load_library().lfm_solver_set_state(self._h, _ptr(q, C.c_double)))
+
+    def get_state(self) -> np.ndarray:
+        q = np.empty((self.nq, self.n_cells), dtype=np.float64)
+        check(load_library().lfm_solver_get_state(self._h, _ptr(q, C.c_double)))
+        return q
+
+    def step(self, nsteps: int, dt: float):
+        check(load_library().lfm_solver_step(self._h, nsteps, dt))
+
+    def stage(self, rk: int, dt: float):
+        check(load_library().lfm_solver_stage(self._h, rk, dt))
+
+    def step_timed(self, nsteps: int, dt: float) -> float:
+        ms = C.c_float()
+        check(load_library().lfm_solver_step_timed(self._h, nsteps, dt, C.byref(ms)))
+        return ms.value
+
+    def sync(self):
+        check(load_library().lfm_solver_sync(self._h))
+
+    def cfl(self, dt: float) -> float:
+        v = C.c_double()
+        check(load_library().lfm_solver_cfl(self._h, dt, C.byref(v)))
+        return v.value
+
+    def min_dt(self, max_co: float) -> float:
+        v = C.c_double()
+        check(load_library().lfm_solver_min_dt(self._h, max_co, C.byref(v)))
+        return v.value
+
+    def residual(self) -> np.ndarray:
+        out = np.empty(self.nq)
+        check(load_library().lfm_solver_residual(self._h, _ptr(out, C.c_double)))
+        return out
+
+    def launches_per_step(self) -> int:
+        v = C.c_int()
+        check(load_library().lfm_solver_launches_per_step(self._h, C.byref(v)))
+        return v.value
+
+    def profile_step(self, dt: float) -> dict:
+        lib = load_library()
+        n = 5
+        ms = (C.c_float * n)()
+        check(lib.lfm_solver_profile_step(self._h, dt, n, ms))
+        return {lib.lfm_solver_kernel_name(i).decode(): ms[i] for i in range(n)}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().lfm_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def port_run(case: CaseHandle, q: np.ndarray, nsteps: int, dt: float, residual: bool = False):
+    """Runs the oracle port on q (copied) and returns (q, residual or None)."""
+    lib = load_port()
+    qq = np.ascontiguousarray(q, dtype=np.float64).copy()
+    res = np.zeros(case.desc.nq)
+    rc = lib.lfm_port_run(C.byref(case.desc), _ptr(qq, C.c_double), nsteps, dt,
+                          _ptr(res, C.c_double) if residual else None)
+    if rc != 0:
+        raise RuntimeError(f"oracle port failed with {rc}")
+    return qq, (res if residual else None)
+
+
+def port_cfl(case: CaseHandle, q: np.ndarray, dt: float) -> float:
+    v = C.c_double()
+    qq = np.ascontiguousarray(q, dtype=np.float64)
+    load_port().lfm_port_cfl(C.byref(case.desc), _ptr(qq, C.c_double), dt, C.byref(v))
+    return v.value
+
+
+def port_min_dt(case: CaseHandle, q: np.ndarray, max_co: float) -> float:
+    v = C.c_double()
+    qq = np.ascontiguousarray(q, dtype=np.float64)
+    load_port().lfm_port_min_dt(C.byref(case.desc), _ptr(qq, C.c_double), max_co, C.byref(v))
+    return v.value

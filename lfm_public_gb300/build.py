@@ -1,0 +1,142 @@
+"""Builds the native libraries in-tree.
+
+* ``lfm_public_gb300/liblfm_gpu.so``  -- the product: sm_103a CUDA kernels, the
+  C ABI of include/lfm_gpu.h and the OpenFOAM-free host plugins.
+* ``lfm_public_gb300/lfm_solve_gpu``  -- the command-line solver (the
+  reference's lfm_solve on the device path).
+* ``oracle/port/liblfm_port.so``      -- the CPU restatement used by tests and
+  the CPU baseline (test infrastructure).
+* ``oracle/_ref/lfm_oracle``          -- the reference solver built from its own
+  sources, only where those sources are present.
+
+Objects are compiled in parallel with one ``-gencode`` for sm_103a.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+BUILD = os.path.join(ROOT, "_build")
+INCLUDES = [os.path.join(ROOT, "include"), os.path.join(ROOT, "include", "lfm"), os.path.join(CSRC, "host"),
+            os.path.join(CSRC, "cuda")]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+HOST_SOURCES = ["foam_io.cpp", "foam_case.cpp", "dict_reader.cpp", "poly_mesh_reader.cpp", "run_time_manager.cpp",
+                "input_reader.cpp", "case_setup.cpp", "capi_case.cpp"]
+CUDA_SOURCES = ["solver_kernels.cu", "capi_solver.cu"]
+CLI_SOURCES = ["gpu_mesh.cpp", "lfm_solve_gpu.cpp"]
+
+LIB = os.path.join(PKG, "liblfm_gpu.so")
+CLI = os.path.join(PKG, "lfm_solve_gpu")
+PORT = os.path.join(ROOT, "oracle", "port", "liblfm_port.so")
+REF_DIR = os.environ.get("LFM_REFERENCE_DIR", "/root/reference")
+
+
+def _nvcc() -> str:
+    for c in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build liblfm_gpu.so")
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build step failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    return r
+
+
+def _newer(target: str, deps) -> bool:
+    if not os.path.exists(target):
+        return False
+    t = os.path.getmtime(target)
+    return all(os.path.getmtime(d) <= t for d in deps)
+
+
+def _headers():
+    out = []
+    for d in INCLUDES:
+        for n in os.listdir(d):
+            if n.endswith((".h", ".cuh")):
+                out.append(os.path.join(d, n))
+    return out
+
+
+def build_library(verbose: bool = False) -> str:
+    nvcc = _nvcc()
+    os.makedirs(BUILD, exist_ok=True)
+    inc = [f"-I{d}" for d in INCLUDES]
+    hdrs = _headers()
+    jobs = []
+    objs = []
+    for s in HOST_SOURCES:
+        src = os.path.join(CSRC, "host", s)
+        obj = os.path.join(BUILD, s + ".o")
+        objs.append(obj)
+        if not _newer(obj, [src] + hdrs):
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-ffp-contract=off", *inc, "-c", src, "-o", obj])
+    for s in CUDA_SOURCES:
+        src = os.path.join(CSRC, "cuda", s)
+        obj = os.path.join(BUILD, s + ".o")
+        objs.append(obj)
+        if not _newer(obj, [src] + hdrs):
+            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *inc, "-c", src,
+                         "-o", obj])
+    with cf.ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
+        for r in ex.map(_run, jobs):
+            if verbose and (r.stdout or r.stderr):
+                print(r.stdout, r.stderr)
+    if not _newer(LIB, objs):
+        _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart_static", "-lrt", "-lpthread", "-ldl"])
+    cli_objs = []
+    cli_jobs = []
+    for s in CLI_SOURCES:
+        src = os.path.join(CSRC, "host", s)
+        if not os.path.exists(src):
+            continue
+        obj = os.path.join(BUILD, s + ".o")
+        cli_objs.append(obj)
+        if not _newer(obj, [src] + hdrs):
+            cli_jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", *inc, "-c", src, "-o", obj])
+    for j in cli_jobs:
+        _run(j)
+    if cli_objs and not _newer(CLI, cli_objs + [LIB]):
+        _run(["g++", "-o", CLI, *cli_objs, f"-L{PKG}", "-llfm_gpu", f"-Wl,-rpath,{PKG}"])
+    return LIB
+
+
+def build_port() -> str:
+    src = os.path.join(ROOT, "oracle", "port", "lfm_port.c")
+    hdr = [os.path.join(ROOT, "oracle", "port", "lfm_port.h"), os.path.join(ROOT, "include", "lfm_gpu.h")]
+    if not _newer(PORT, [src] + hdr):
+        _run(["gcc", "-O2", "-std=c99", "-ffp-contract=off", "-fPIC", "-shared", f"-I{os.path.join(ROOT, 'include')}",
+              "-o", PORT, src, "-lm"])
+    return PORT
+
+
+def build_reference_oracle() -> str | None:
+    """Builds oracle/_ref/lfm_oracle from the reference sources when present."""
+    if not os.path.isdir(os.path.join(REF_DIR, "src")):
+        return None
+    r = subprocess.run(["make", "-s", "-j", str(os.cpu_count() or 4), f"REF={REF_DIR}"],
+                       cwd=os.path.join(ROOT, "oracle"), capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference oracle build failed:\n" + r.stdout + r.stderr)
+    return os.path.join(ROOT, "oracle", "_ref", "lfm_oracle")
+
+
+def build_all(verbose: bool = False) -> None:
+    with cf.ThreadPoolExecutor(max_workers=3) as ex:
+        futs = [ex.submit(build_library, verbose), ex.submit(build_port), ex.submit(build_reference_oracle)]
+        for f in futs:
+            f.result()
+
+
+if __name__ == "__main__":
+    build_all(verbose="-v" in sys.argv)
+    print("built", LIB, PORT)

@@ -1,0 +1,497 @@
+// C ABI, device half: the solver handle (include/lfm_gpu.h).
+//
+// A solver owns its device arrays and one CUDA stream. A full time step
+// (rk_order stages of 3-5 kernels) is captured once into a CUDA graph and
+// replayed; the graph is captured again only when dt changes.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../host/capi_internal.h"
+#include "lfm_gpu.h"
+#include "solver_launch.h"
+
+using lfm::dev::Args;
+using lfm::dev::StageConfig;
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+};
+
+}  // namespace
+
+struct lfm_solver {
+    int precision = LFM_FP64;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int D = 2, nq = 4;
+    int nc = 0, ng = 0, nf = 0, nt = 0;
+    int scheme = 0, rkOrder = 0;
+    bool needGrad = false, needVis = true, residuals = false;
+    std::vector<double> rkA, rkB;
+    std::vector<void*> allocations;
+    Args<double> a64{};
+    Args<float> a32{};
+    double* q = nullptr;
+    double* res = nullptr;
+    double* partial = nullptr;
+    double* scalar = nullptr;
+    int* flag = nullptr;
+    int* sOff = nullptr;
+    double* cellS = nullptr;
+    double* volInv = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    double graphDt = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+int cudaFail(cudaError_t e, const char* what) {
+    return lfm::setError(e == cudaErrorMemoryAllocation ? LFM_ERR_NOMEM : LFM_ERR_CUDA,
+                         std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define LFM_CUDA(call)                                    \
+    do {                                                  \
+        cudaError_t e__ = (call);                         \
+        if (e__ != cudaSuccess) return cudaFail(e__, #call); \
+    } while (0)
+
+template <typename X>
+int devAlloc(lfm_solver* s, X** out, size_t n) {
+    *out = nullptr;
+    if (n == 0) n = 1;
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, n * sizeof(X));
+    if (e != cudaSuccess) return cudaFail(e, "cudaMalloc");
+    s->allocations.push_back(p);
+    e = cudaMemsetAsync(p, 0, n * sizeof(X), s->stream);
+    if (e != cudaSuccess) return cudaFail(e, "cudaMemsetAsync");
+    *out = static_cast<X*>(p);
+    return LFM_OK;
+}
+
+template <typename X>
+int upload(lfm_solver* s, X** out, const X* src, size_t n) {
+    int rc = devAlloc(s, out, n);
+    if (rc) return rc;
+    if (n) LFM_CUDA(cudaMemcpyAsync(*out, src, n * sizeof(X), cudaMemcpyHostToDevice, s->stream));
+    return LFM_OK;
+}
+
+// Converts an FP64 host array to T and uploads it.
+template <typename T>
+int uploadAs(lfm_solver* s, T** out, const double* src, size_t n) {
+    std::vector<T> tmp(n);
+    for (size_t k = 0; k < n; ++k) tmp[k] = (T)src[k];
+    int rc = upload(s, out, tmp.data(), n);
+    if (rc) return rc;
+    return cudaStreamSynchronize(s->stream) == cudaSuccess ? LFM_OK : cudaFail(cudaGetLastError(), "upload");
+}
+
+std::vector<int> toInt(const int64_t* p, size_t n) {
+    std::vector<int> v(n);
+    for (size_t k = 0; k < n; ++k) v[k] = (int)p[k];
+    return v;
+}
+
+template <typename T>
+int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP, const int* fN,
+              const uint8_t* fGhost, const int* cfOff, const int* cfList, const int* gCell, const int* gKind,
+              const int* gFace, const double* sponge) {
+    a.D = s->D;
+    a.nq = s->nq;
+    a.nc = s->nc;
+    a.ng = s->ng;
+    a.nf = s->nf;
+    a.nt = s->nt;
+    a.q = s->q;
+    a.res = s->res;
+    a.fP = fP;
+    a.fN = fN;
+    a.fGhost = fGhost;
+    a.volInv = s->volInv;
+    a.sponge = sponge;
+    a.cfOff = cfOff;
+    a.cfList = cfList;
+    a.gCell = gCell;
+    a.gKind = gKind;
+    a.gFace = gFace;
+    a.flag = s->flag;
+    a.gamma = d->gamma;
+    a.gm1 = d->gamma - 1.0;
+    a.Rinv = 1.0 / d->Rgas;
+    a.rhoInf = d->rhoInf;
+    a.EInf = d->EInf;
+    a.pInf = d->pInf;
+    a.TInf = d->TInf;
+    for (int k = 0; k < 3; ++k) a.UInf[k] = d->UInf[k];
+    a.mu = d->mu;
+    a.kcond = d->Cp * d->mu * d->PrInv;
+    const size_t nt = (size_t)s->nt, nf = (size_t)s->nf, D = (size_t)s->D;
+    int rc;
+    if ((rc = devAlloc(s, &a.dq, (size_t)s->nq * s->nc))) return rc;
+    if ((rc = devAlloc(s, &a.prim, (D + 3) * nt))) return rc;
+    if ((rc = devAlloc(s, &a.V, (2 * D * D + 2 * D) * nt))) return rc;
+    if ((rc = devAlloc(s, &a.grad, (2 * D + D * D) * (s->needGrad ? nt : 1)))) return rc;
+    if ((rc = devAlloc(s, &a.flux, (size_t)s->nq * nf))) return rc;
+    T* p;
+    if ((rc = uploadAs<T>(s, &p, d->S, D * nf))) return rc;
+    a.S = p;
+    if ((rc = uploadAs<T>(s, &p, d->d, D * nf))) return rc;
+    a.d = p;
+    if ((rc = uploadAs<T>(s, &p, d->w, nf))) return rc;
+    a.w = p;
+    if ((rc = uploadAs<T>(s, &p, d->smag, nf))) return rc;
+    a.smag = p;
+    if ((rc = uploadAs<T>(s, &p, d->dmag_inv, nf))) return rc;
+    a.dinv = p;
+    if ((rc = uploadAs<T>(s, &p, d->dnorm, D * nf))) return rc;
+    a.dnorm = p;
+    if ((rc = uploadAs<T>(s, &p, d->delta_mag, nf))) return rc;
+    a.dmag = p;
+    if ((rc = uploadAs<T>(s, &p, d->K, D * nf))) return rc;
+    a.K = p;
+    return LFM_OK;
+}
+
+int validateDesc(const lfm_solver_desc* d) {
+    if (!d) return lfm::setError(LFM_ERR_INVALID, "null solver description");
+    if (d->dim != 2 && d->dim != 3) return lfm::setError(LFM_ERR_INVALID, "dim must be 2 or 3");
+    if (d->nq != d->dim + 2) return lfm::setError(LFM_ERR_INVALID, "nq must be dim + 2");
+    if (d->solver < 0 || d->solver > 2) return lfm::setError(LFM_ERR_INVALID, "unknown solver");
+    if (d->n_cells <= 0 || d->n_faces <= 0 || d->n_ghosts < 0)
+        return lfm::setError(LFM_ERR_INVALID, "empty mesh");
+    if (d->n_cells + d->n_ghosts > 0x7fffffffLL / 32 || d->n_faces > 0x7fffffffLL / 8)
+        return lfm::setError(LFM_ERR_UNSUPPORTED, "mesh too large for 32-bit device indexing");
+    if (!d->face_p || !d->face_n || !d->face_ghost || !d->S || !d->d || !d->w || !d->smag || !d->dmag_inv ||
+        !d->dnorm || !d->delta_mag || !d->K || !d->vol_inv || !d->sponge || !d->cell_face_offsets ||
+        !d->cell_faces || !d->cell_face_sign || !d->cell_s_offsets || !d->cell_s || !d->rkA || !d->rkB ||
+        (d->n_ghosts > 0 && (!d->ghost_cell || !d->ghost_kind)))
+        return lfm::setError(LFM_ERR_INVALID, "incomplete solver description");
+    const int64_t nt = d->n_cells + d->n_ghosts;
+    for (int64_t f = 0; f < d->n_faces; ++f) {
+        if (d->face_p[f] < 0 || d->face_p[f] >= d->n_cells || d->face_n[f] < 0 || d->face_n[f] >= nt)
+            return lfm::setError(LFM_ERR_INVALID, "face index out of range at face " + std::to_string(f));
+        if (f > 0 && d->face_p[f] < d->face_p[f - 1])
+            return lfm::setError(LFM_ERR_INVALID, "faces are not in processing order");
+    }
+    for (int64_t g = 0; g < d->n_ghosts; ++g)
+        if (d->ghost_cell[g] < 0 || d->ghost_cell[g] >= d->n_cells)
+            return lfm::setError(LFM_ERR_INVALID, "ghost cell out of range");
+    for (int64_t c = 0; c < d->n_cells; ++c) {
+        if (d->cell_face_offsets[c + 1] < d->cell_face_offsets[c])
+            return lfm::setError(LFM_ERR_INVALID, "cell_face_offsets not monotone");
+    }
+    for (int64_t e = 0; e < d->cell_face_offsets[d->n_cells]; ++e)
+        if (d->cell_faces[e] < 0 || d->cell_faces[e] >= d->n_faces)
+            return lfm::setError(LFM_ERR_INVALID, "cell_faces entry out of range");
+    return LFM_OK;
+}
+
+template <typename T>
+void stageAll(lfm_solver* s, const Args<T>& a, double dt) {
+    for (int k = 0; k < s->rkOrder; ++k) {
+        StageConfig c;
+        c.scheme = s->scheme;
+        c.needGrad = s->needGrad;
+        c.needVis = s->needVis;
+        c.A = s->rkA[(size_t)k];
+        c.B = s->rkB[(size_t)k];
+        c.dt = dt;
+        c.first = (k == 0);
+        c.withRes = (s->residuals && k == 0) ? 1 : 0;
+        lfm::dev::launch_stage<T>(a, c, s->stream);
+    }
+}
+
+void launchStep(lfm_solver* s, double dt) {
+    if (s->precision == LFM_FP32_BULK)
+        stageAll<float>(s, s->a32, dt);
+    else
+        stageAll<double>(s, s->a64, dt);
+}
+
+int ensureGraph(lfm_solver* s, double dt) {
+    if (s->graph && s->graphDt == dt) return LFM_OK;
+    if (s->graph) {
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    LFM_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    launchStep(s, dt);
+    cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+    if (e != cudaSuccess) return cudaFail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&s->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cudaFail(e, "cudaGraphInstantiate");
+    s->graphDt = dt;
+    return LFM_OK;
+}
+
+}  // namespace
+
+extern "C" int lfm_solver_create(const lfm_solver_desc* d, const lfm_solver_opts* opts, lfm_solver** out) {
+    if (!out) return lfm::setError(LFM_ERR_INVALID, "null output handle");
+    *out = nullptr;
+    int rc = validateDesc(d);
+    if (rc) return rc;
+    lfm_solver* s = new lfm_solver;
+    s->precision = opts ? opts->precision : LFM_FP64;
+    s->device = opts ? opts->device : 0;
+    if (s->precision != LFM_FP64 && s->precision != LFM_FP32_BULK) {
+        delete s;
+        return lfm::setError(LFM_ERR_INVALID, "unknown precision");
+    }
+    auto fail = [&](int code) {
+        lfm_solver_destroy(s);
+        return code;
+    };
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) {
+        delete s;
+        return cudaFail(e, "cudaSetDevice");
+    }
+    e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete s;
+        return cudaFail(e, "cudaStreamCreate");
+    }
+    cudaEventCreate(&s->ev0);
+    cudaEventCreate(&s->ev1);
+    s->D = d->dim;
+    s->nq = d->nq;
+    s->nc = (int)d->n_cells;
+    s->ng = (int)d->n_ghosts;
+    s->nf = (int)d->n_faces;
+    s->nt = s->nc + s->ng;
+    s->scheme = d->solver;
+    s->rkOrder = d->rk_order;
+    s->rkA.assign(d->rkA, d->rkA + d->rk_order);
+    s->rkB.assign(d->rkB, d->rkB + d->rk_order);
+    s->needGrad = (d->solver == LFM_SOLVER_M2AUSM) && d->minmod;
+    s->needVis = (d->mu != 0.0) || (d->solver == LFM_SOLVER_M2AUSM);
+    s->residuals = d->residuals != 0;
+
+    const size_t nq = (size_t)s->nq, nc = (size_t)s->nc, nt = (size_t)s->nt, nf = (size_t)s->nf;
+    if ((rc = devAlloc(s, &s->q, nq * nt))) return fail(rc);
+    if ((rc = devAlloc(s, &s->res, s->residuals ? nq * nc : 1))) return fail(rc);
+    const size_t nPartial = (nc + 255) / 256 + 1;
+    if ((rc = devAlloc(s, &s->partial, nPartial))) return fail(rc);
+    if ((rc = devAlloc(s, &s->scalar, 16))) return fail(rc);
+    if ((rc = devAlloc(s, &s->flag, 1))) return fail(rc);
+    if ((rc = upload(s, &s->volInv, d->vol_inv, nc))) return fail(rc);
+    double* sponge = nullptr;
+    if ((rc = upload(s, &sponge, d->sponge, nc))) return fail(rc);
+
+    // connectivity as 32-bit indices
+    std::vector<int> fP = toInt(d->face_p, nf), fN = toInt(d->face_n, nf);
+    std::vector<int> cfOff = toInt(d->cell_face_offsets, nc + 1);
+    const size_t ne = (size_t)d->cell_face_offsets[nc];
+    std::vector<int> cfList(ne);
+    for (size_t k = 0; k < ne; ++k)
+        cfList[k] = d->cell_face_sign[k] > 0 ? (int)d->cell_faces[k] : ~(int)d->cell_faces[k];
+    std::vector<int> gCell = toInt(d->ghost_cell, (size_t)s->ng), gKind((size_t)s->ng), gFace((size_t)s->ng, 0);
+    for (int g = 0; g < s->ng; ++g) gKind[(size_t)g] = d->ghost_kind[g];
+    for (int f = 0; f < s->nf; ++f)
+        if (fN[(size_t)f] >= s->nc) gFace[(size_t)(fN[(size_t)f] - s->nc)] = f;
+    std::vector<int> sOff = toInt(d->cell_s_offsets, nc + 1);
+    int *dP, *dN, *dOff, *dList, *dGC, *dGK, *dGF;
+    uint8_t* dG;
+    if ((rc = upload(s, &dP, fP.data(), nf))) return fail(rc);
+    if ((rc = upload(s, &dN, fN.data(), nf))) return fail(rc);
+    if ((rc = upload(s, &dG, d->face_ghost, nf))) return fail(rc);
+    if ((rc = upload(s, &dOff, cfOff.data(), nc + 1))) return fail(rc);
+    if ((rc = upload(s, &dList, cfList.data(), ne))) return fail(rc);
+    if ((rc = upload(s, &dGC, gCell.data(), (size_t)s->ng))) return fail(rc);
+    if ((rc = upload(s, &dGK, gKind.data(), (size_t)s->ng))) return fail(rc);
+    if ((rc = upload(s, &dGF, gFace.data(), (size_t)s->ng))) return fail(rc);
+    if ((rc = upload(s, &s->sOff, sOff.data(), nc + 1))) return fail(rc);
+    if ((rc = upload(s, &s->cellS, d->cell_s, (size_t)d->cell_s_offsets[nc] * (size_t)s->D))) return fail(rc);
+    if (s->precision == LFM_FP32_BULK)
+        rc = buildArgs<float>(s, d, s->a32, dP, dN, dG, dOff, dList, dGC, dGK, dGF, sponge);
+    else
+        rc = buildArgs<double>(s, d, s->a64, dP, dN, dG, dOff, dList, dGC, dGK, dGF, sponge);
+    if (rc) return fail(rc);
+    if (d->q0) {
+        for (size_t v = 0; v < nq; ++v)
+            if ((e = cudaMemcpyAsync(s->q + v * nt, d->q0 + v * nc, nc * sizeof(double), cudaMemcpyHostToDevice,
+                                     s->stream)) != cudaSuccess)
+                return fail(cudaFail(e, "cudaMemcpyAsync q0"));
+    }
+    if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return fail(cudaFail(e, "create"));
+    *out = s;
+    return LFM_OK;
+}
+
+extern "C" void lfm_solver_destroy(lfm_solver* s) {
+    if (!s) return;
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    for (void* p : s->allocations) cudaFree(p);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+extern "C" int lfm_solver_set_state(lfm_solver* s, const double* q) {
+    if (!s || !q) return lfm::setError(LFM_ERR_INVALID, "null argument");
+    LFM_CUDA(cudaSetDevice(s->device));
+    for (int v = 0; v < s->nq; ++v)
+        LFM_CUDA(cudaMemcpyAsync(s->q + (size_t)v * s->nt, q + (size_t)v * s->nc, (size_t)s->nc * sizeof(double),
+                                 cudaMemcpyHostToDevice, s->stream));
+    LFM_CUDA(cudaStreamSynchronize(s->stream));
+    return LFM_OK;
+}
+
+extern "C" int lfm_solver_get_state(lfm_solver* s, double* q) {
+    if (!s || !q) return lfm::setError(LFM_ERR_INVALID, "null argument");
+    LFM_CUDA(cudaSetDevice(s->device));
+    for (int v = 0; v < s->nq; ++v)
+        LFM_CUDA(cudaMemcpyAsync(q + (size_t)v * s->nc, s->q + (size_t)v * s->nt, (size_t)s->nc * sizeof(double),
+                                 cudaMemcpyDeviceToHost, s->stream));
+    LFM_CUDA(cudaStreamSynchronize(s->stream));
+    return LFM_OK;
+}
+
+extern "C" int lfm_solver_stage(lfm_solver* s, int rk, double dt) {
+    if (!s) return lfm::setError(LFM_ERR_INVALID, "null solver");
+    if (rk < 0 || rk >= s->rkOrder) return lfm::setError(LFM_ERR_INVALID, "stage index out of range");
+    LFM_CUDA(cudaSetDevice(s->device));
+    StageConfig c;
+    c.scheme = s->scheme;
+    c.needGrad = s->needGrad;
+    c.needVis = s->needVis;
+    c.A = s->rkA[(size_t)rk];
+    c.B = s->rkB[(size_t)rk];
+    c.dt = dt;
+    c.first = (rk == 0);
+    c.withRes = (s->residuals && rk == 0) ? 1 : 0;
+    if (s->precision == LFM_FP32_BULK)
+        lfm::dev::launch_stage<float>(s->a32, c, s->stream);
+    else
+        lfm::dev::launch_stage<double>(s->a64, c, s->stream);
+    LFM_CUDA(cudaGetLastError());
+    return LFM_OK;
+}
+
+extern "C" int lfm_solver_step(lfm_solver* s, int nsteps, double dt) {
+    if (!s || nsteps < 0) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    if (s->rkOrder == 0 || nsteps == 0) return LFM_OK;
+    LFM_CUDA(cudaSetDevice(s->device));
+    int rc = ensureGraph(s, dt);
+    if (rc) return rc;
+    for (int k = 0; k < nsteps; ++k) LFM_CUDA(cudaGraphLaunch(s->graph, s->stream));
+    return LFM_OK;
+}
+
+extern "C" int lfm_solver_step_timed(lfm_solver* s, int nsteps, double dt, float* ms) {
+    if (!s || !ms) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    LFM_CUDA(cudaSetDevice(s->device));
+    int rc = ensureGraph(s, dt);
+    if (rc) return rc;
+    LFM_CUDA(cudaEventRecord(s->ev0, s->stream));
+    rc = lfm_solver_step(s, nsteps, dt);
+    if (rc) return rc;
+    LFM_CUDA(cudaEventRecord(s->ev1, s->stream));
+    LFM_CUDA(cudaEventSynchronize(s->ev1));
+    LFM_CUDA(cudaEventElapsedTime(ms, s->ev0, s->ev1));
+    return LFM_OK;
+}
+
+static int reduceScalar(lfm_solver* s, double dt, int mode, double maxCo, double* out) {
+    LFM_CUDA(cudaSetDevice(s->device));
+    lfm::dev::launch_cfl(s->D, s->q, s->nt, s->nc, s->volInv, s->sOff, s->cellS, dt, mode, maxCo, s->partial,
+                         s->scalar, s->stream);
+    LFM_CUDA(cudaGetLastError());
+    LFM_CUDA(cudaMemcpyAsync(out, s->scalar, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    LFM_CUDA(cudaStreamSynchronize(s->stream));
+    return LFM_OK;
+}
+
+extern "C" int lfm_solver_cfl(lfm_solver* s, double dt, double* cfl) {
+    if (!s || !cfl) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    return reduceScalar(s, dt, 0, 0.0, cfl);
+}
+
+extern "C" int lfm_solver_min_dt(lfm_solver* s, double max_co, double* dt) {
+    if (!s || !dt) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    return reduceScalar(s, 0.0, 1, max_co, dt);
+}
+
+extern "C" int lfm_solver_residual(lfm_solver* s, double* res) {
+    if (!s || !res) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    if (!s->residuals) return lfm::setError(LFM_ERR_INVALID, "the case does not record residuals");
+    LFM_CUDA(cudaSetDevice(s->device));
+    for (int v = 0; v < s->nq; ++v)
+        lfm::dev::launch_res_sum(s->res + (size_t)v * s->nc, s->nc, s->partial, s->scalar + v, s->stream);
+    LFM_CUDA(cudaGetLastError());
+    LFM_CUDA(cudaMemcpyAsync(res, s->scalar, sizeof(double) * (size_t)s->nq, cudaMemcpyDeviceToHost, s->stream));
+    LFM_CUDA(cudaStreamSynchronize(s->stream));
+    return LFM_OK;
+}
+
+extern "C" int lfm_solver_sync(lfm_solver* s) {
+    if (!s) return lfm::setError(LFM_ERR_INVALID, "null solver");
+    LFM_CUDA(cudaSetDevice(s->device));
+    LFM_CUDA(cudaStreamSynchronize(s->stream));
+    LFM_CUDA(cudaGetLastError());
+    int flag = 0;
+    LFM_CUDA(cudaMemcpy(&flag, s->flag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) return lfm::setError(LFM_ERR_NUMERIC, "non-finite conserved state");
+    return LFM_OK;
+}
+
+extern "C" int lfm_solver_launches_per_step(const lfm_solver* s, int* launches) {
+    if (!s || !launches) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    *launches = s->rkOrder * (3 + (s->needGrad ? 1 : 0) + (s->needVis ? 1 : 0));
+    return LFM_OK;
+}
+
+extern "C" const char* lfm_solver_kernel_name(int i) { return lfm::dev::kernelName(i); }
+
+extern "C" int lfm_solver_profile_step(lfm_solver* s, double dt, int n, float* ms) {
+    if (!s || !ms || n < lfm::dev::kKernelsPerStage) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    LFM_CUDA(cudaSetDevice(s->device));
+    for (int k = 0; k < n; ++k) ms[k] = 0.f;
+    std::vector<cudaEvent_t> ev(2 * (size_t)s->rkOrder * lfm::dev::kKernelsPerStage);
+    for (auto& x : ev) LFM_CUDA(cudaEventCreate(&x));
+    for (int k = 0; k < s->rkOrder; ++k) {
+        StageConfig c;
+        c.scheme = s->scheme;
+        c.needGrad = s->needGrad;
+        c.needVis = s->needVis;
+        c.A = s->rkA[(size_t)k];
+        c.B = s->rkB[(size_t)k];
+        c.dt = dt;
+        c.first = (k == 0);
+        c.withRes = (s->residuals && k == 0) ? 1 : 0;
+        for (int w = 0; w < lfm::dev::kKernelsPerStage; ++w) {
+            const size_t base = 2 * ((size_t)k * lfm::dev::kKernelsPerStage + (size_t)w);
+            cudaEventRecord(ev[base], s->stream);
+            if (s->precision == LFM_FP32_BULK)
+                lfm::dev::launch_kernel<float>(s->a32, c, w, s->stream);
+            else
+                lfm::dev::launch_kernel<double>(s->a64, c, w, s->stream);
+            cudaEventRecord(ev[base + 1], s->stream);
+        }
+    }
+    LFM_CUDA(cudaStreamSynchronize(s->stream));
+    for (int k = 0; k < s->rkOrder; ++k)
+        for (int w = 0; w < lfm::dev::kKernelsPerStage; ++w) {
+            const size_t base = 2 * ((size_t)k * lfm::dev::kKernelsPerStage + (size_t)w);
+            float t = 0;
+            cudaEventElapsedTime(&t, ev[base], ev[base + 1]);
+            ms[w] += t;
+        }
+    for (auto& x : ev) cudaEventDestroy(x);
+    LFM_CUDA(cudaGetLastError());
+    return LFM_OK;
+}

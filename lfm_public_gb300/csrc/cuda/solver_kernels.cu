@@ -1,0 +1,727 @@
+// Device kernels of the explicit finite-volume time step (see solver_kernels.cuh).
+#include "solver_kernels.cuh"
+#include "solver_launch.h"
+
+namespace lfm {
+namespace dev {
+
+#define LFM_GLOBAL_ID() ((int)(blockIdx.x * blockDim.x + threadIdx.x))
+
+template <typename T>
+__device__ __forceinline__ T interp(T w, T a, T b) {
+    return w * a + (T(1) - w) * b;
+}
+
+template <typename T, int D>
+__device__ __forceinline__ T dotv(const T* a, const T* b) {
+    T s = a[0] * b[0];
+#pragma unroll
+    for (int k = 1; k < D; ++k) s += a[k] * b[k];
+    return s;
+}
+
+// Deviatoric stress of a velocity gradient g (row a = gradient of u_a), in the
+// reference's evaluation order (src/cfd_v0.cpp:1813-1822).
+template <typename T, int D>
+__device__ __forceinline__ void stress(const T g[D][D], T mu, T tau[D][D]) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        tau[a][a] = T(2) * g[a][a];
+#pragma unroll
+        for (int b1 = a + 1; b1 < D + a; ++b1) {
+            const int b = b1 % D;
+            tau[a][b] = mu * (g[a][b] + g[b][a]);
+            tau[a][a] -= g[b][b];
+        }
+        tau[a][a] *= T(2.0 / 3.0) * mu;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_prep: ghost states and per-cell primitives.
+// ---------------------------------------------------------------------------
+template <typename T, int D>
+__global__ void __launch_bounds__(256) k_prep(Args<T> a) {
+    const int t = LFM_GLOBAL_ID();
+    if (t >= a.nt) return;
+    constexpr int NQ = D + 2;
+    double qv[NQ];
+    if (t < a.nc) {
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) qv[v] = a.q[(size_t)v * a.nt + t];
+    } else {
+        const int g = t - a.nc;
+        const int in = a.gCell[g];
+        const int kind = a.gKind[g];
+        double qi[NQ];
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) qi[v] = a.q[(size_t)v * a.nt + in];
+        if (kind == 1) {  // wall: mirror the momentum
+            qv[0] = qi[0];
+#pragma unroll
+            for (int k = 0; k < D; ++k) qv[k + 1] = -qi[k + 1];
+            qv[D + 1] = qi[D + 1];
+        } else if (kind >= 2 && kind <= 4) {
+            bool inlet = (kind == 2);
+            if (kind == 4) inlet = (double)a.S[a.gFace[g]] <= 0.0;  // free stream along +x enters
+            const double rhoInt = qi[0];
+            double Uint[D], um2 = 0.0;
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                Uint[k] = qi[k + 1] / rhoInt;
+                um2 += Uint[k] * Uint[k];
+            }
+            const double pInt = (qi[D + 1] - 0.5 * um2 * rhoInt) * a.gm1;
+            if (inlet) {
+                const double TInt = pInt * a.Rinv / rhoInt;
+                const double rhoExt = rhoInt * TInt / a.TInf;
+                double ue2 = 0.0;
+#pragma unroll
+                for (int k = 0; k < D; ++k) ue2 += a.UInf[k] * a.UInf[k];
+                const double EExt = pInt / (rhoExt * a.gm1) + 0.5 * ue2;
+                qv[0] = rhoExt;
+#pragma unroll
+                for (int k = 0; k < D; ++k) qv[k + 1] = rhoExt * a.UInf[k];
+                qv[D + 1] = rhoExt * EExt;
+            } else {
+                const double rhoExt = rhoInt * a.pInf / pInt;
+                const double EExt = a.pInf / (rhoExt * a.gm1) + 0.5 * um2;
+                qv[0] = rhoExt;
+#pragma unroll
+                for (int k = 0; k < D; ++k) qv[k + 1] = rhoExt * Uint[k];
+                qv[D + 1] = rhoExt * EExt;
+            }
+        } else {
+            // Patches without a boundary condition keep a zero ghost state, as
+            // in the reference (src/cfd_v0.cpp:406-416).
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) qv[v] = 0.0;
+        }
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) a.q[(size_t)v * a.nt + t] = qv[v];
+    }
+    // compute_Rpsi (api/cfdv0_solver.h:252-261)
+    const double rinv = 1.0 / qv[0];
+    double s = qv[1] * qv[1];
+#pragma unroll
+    for (int k = 1; k < D; ++k) s += qv[k + 1] * qv[k + 1];
+    const double Rpsi = a.gm1 * (qv[D + 1] - 0.5 * s * rinv) * rinv;
+    a.prim[t] = (T)rinv;
+#pragma unroll
+    for (int k = 0; k < D; ++k) a.prim[(size_t)(1 + k) * a.nt + t] = (T)(qv[k + 1] * rinv);
+    a.prim[(size_t)(D + 1) * a.nt + t] = (T)Rpsi;
+    a.prim[(size_t)(D + 2) * a.nt + t] = (T)sqrt(a.gamma * Rpsi);
+}
+
+// ---------------------------------------------------------------------------
+// k_grad: gradients read by M2AUSM's minmod reconstruction.
+// ---------------------------------------------------------------------------
+template <typename T, int D>
+__global__ void __launch_bounds__(256) k_grad(Args<T> a) {
+    const int c = LFM_GLOBAL_ID();
+    if (c >= a.nc) return;
+    T gr[D], gp[D], gu[D][D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        gr[k] = gp[k] = T(0);
+#pragma unroll
+        for (int l = 0; l < D; ++l) gu[k][l] = T(0);
+    }
+    const T vi = (T)a.volInv[c];
+    for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
+        const int code = a.cfList[e];
+        const int f = code >= 0 ? code : ~code;
+        const int i = a.fP[f], j = a.fN[f];
+        const T w = a.w[f];
+        T so[D], UU[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            const T Sk = a.S[(size_t)k * a.nf + f];
+            so[k] = (code >= 0) ? Sk * vi : -Sk * vi;
+            UU[k] = interp(w, a.prim[(size_t)(1 + k) * a.nt + i], a.prim[(size_t)(1 + k) * a.nt + j]);
+        }
+        const T rhoi = (T)a.q[i], rhoj = (T)a.q[j];
+        const T pi = rhoi * a.prim[(size_t)(D + 1) * a.nt + i];
+        const T pj = rhoj * a.prim[(size_t)(D + 1) * a.nt + j];
+        const T rho = interp(w, rhoi, rhoj);
+        const T p = interp(w, pi, pj);
+#pragma unroll
+        for (int x = 0; x < D; ++x) {
+            gp[x] += p * so[x];
+            gr[x] += rho * so[x];
+#pragma unroll
+            for (int b = 0; b < D; ++b) gu[b][x] += UU[b] * so[x];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        a.grad[(size_t)k * a.nt + c] = gr[k];
+        a.grad[(size_t)(D + k) * a.nt + c] = gp[k];
+#pragma unroll
+        for (int l = 0; l < D; ++l) a.grad[(size_t)(2 * D + k * D + l) * a.nt + c] = gu[k][l];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_vis: dudx, dTdx, tauMC, sigmaU per cell.
+// ---------------------------------------------------------------------------
+template <typename T, int D>
+__global__ void __launch_bounds__(256) k_vis(Args<T> a) {
+    const int c = LFM_GLOBAL_ID();
+    if (c >= a.nc) return;
+    T g[D][D], gT[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        gT[k] = T(0);
+#pragma unroll
+        for (int l = 0; l < D; ++l) g[k][l] = T(0);
+    }
+    const T vi = (T)a.volInv[c];
+    const T Rinv = (T)a.Rinv;
+    for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
+        const int code = a.cfList[e];
+        const int f = code >= 0 ? code : ~code;
+        const int i = a.fP[f], j = a.fN[f];
+        const T w = a.w[f];
+        T so[D], fU[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            const T Sk = a.S[(size_t)k * a.nf + f];
+            so[k] = (code >= 0) ? Sk * vi : -Sk * vi;
+            fU[k] = interp(w, a.prim[(size_t)(1 + k) * a.nt + i], a.prim[(size_t)(1 + k) * a.nt + j]);
+        }
+        const T fT = interp(w, a.prim[(size_t)(D + 1) * a.nt + i], a.prim[(size_t)(D + 1) * a.nt + j]) * Rinv;
+#pragma unroll
+        for (int x = 0; x < D; ++x) {
+#pragma unroll
+            for (int y = 0; y < D; ++y) g[x][y] += fU[x] * so[y];
+            gT[x] += fT * so[x];
+        }
+    }
+    const T mu = (T)a.mu;
+    T tau[D][D];
+    stress<T, D>(g, mu, tau);
+    T diagSum = T(0);
+#pragma unroll
+    for (int x = 0; x < D; ++x) diagSum -= g[x][x];
+    diagSum *= mu * T(2) / T(3);
+    T U[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) U[k] = a.prim[(size_t)(1 + k) * a.nt + c];
+    const size_t nt = (size_t)a.nt;
+#pragma unroll
+    for (int x = 0; x < D; ++x) {
+#pragma unroll
+        for (int y = 0; y < D; ++y) {
+            a.V[(size_t)(x * D + y) * nt + c] = g[x][y];
+            T tm = mu * g[y][x];
+            if (x == y) tm += diagSum;
+            a.V[(size_t)(D * D + D + x * D + y) * nt + c] = tm;
+        }
+        a.V[(size_t)(D * D + x) * nt + c] = gT[x];
+        a.V[(size_t)(2 * D * D + D + x) * nt + c] = dotv<T, D>(U, tau[x]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Minmod reconstruction and AUSM+ pressure polynomials (M2AUSM).
+// ---------------------------------------------------------------------------
+template <typename T, int D>
+__device__ __forceinline__ T minmod_interp(T cp, T ap, const T* grad, const T* d, T w, T flux) {
+    const T gradf = ap - cp + T(1.0e-30);
+    T gradcf = T(0);
+#pragma unroll
+    for (int k = 0; k < D; ++k) gradcf += d[k] * grad[k];
+    T r;
+    if (fabs(gradcf) >= T(1000) * fabs(gradf))
+        r = T(2000) * (gradcf < T(0) ? T(-1) : T(1)) * (gradf < T(0) ? T(-1) : T(1)) - T(1);
+    else
+        r = T(2) * (gradcf / gradf) - T(1);
+    T lim = (T(1) < r) ? T(1) : r;
+    lim = (lim < T(0)) ? T(0) : lim;
+    const T weight = lim * w + (T(1) - lim) * (T(1) + flux) * T(0.5);
+    return weight * cp + (T(1) - weight) * ap;
+}
+
+template <typename T>
+__device__ __forceinline__ T p5pos(T M, T alpha) {
+    const T M2Pos = T(0.25) * (M + T(1)) * (M + T(1));
+    const T M2Neg = T(-0.25) * (M - T(1)) * (M - T(1));
+    if (fabs(M) < T(1)) return M2Pos * ((T(2) - M) - T(16) * alpha * M * M2Neg);
+    return T(0.5) * (M + fabs(M)) / M;
+}
+
+template <typename T>
+__device__ __forceinline__ T p5neg(T M, T alpha) {
+    const T M2Pos = T(0.25) * (M + T(1)) * (M + T(1));
+    const T M2Neg = T(-0.25) * (M - T(1)) * (M - T(1));
+    if (fabs(M) < T(1)) return M2Neg * ((T(-2) - M) + T(16) * alpha * M * M2Pos);
+    return T(0.5) * (M - fabs(M)) / M;
+}
+
+// ---------------------------------------------------------------------------
+// k_flux: rhs of one face.
+// ---------------------------------------------------------------------------
+template <typename T, int D, int SCH>
+__global__ void __launch_bounds__(128) k_flux(Args<T> a) {
+    const int f = LFM_GLOBAL_ID();
+    if (f >= a.nf) return;
+    constexpr int NQ = D + 2;
+    const size_t nt = (size_t)a.nt, nf = (size_t)a.nf;
+    const int i = a.fP[f], j = a.fN[f];
+    const bool ghost = a.fGhost[f] != 0;
+    const T w = a.w[f];
+    const T omw = T(1) - w;
+    T S[D], dn[D], Kf[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        S[k] = a.S[k * nf + f];
+        dn[k] = a.dnorm[k * nf + f];
+        Kf[k] = a.K[k * nf + f];
+    }
+    const T Smag = a.smag[f], dinv = a.dinv[f], dmag = a.dmag[f];
+    T qi[NQ], qj[NQ];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) {
+        qi[v] = (T)a.q[v * nt + i];
+        qj[v] = (T)a.q[v * nt + j];
+    }
+    const T cri = a.prim[i], ari = a.prim[j];
+    T cU[D], aU[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        cU[k] = a.prim[(1 + k) * nt + i];
+        aU[k] = a.prim[(1 + k) * nt + j];
+    }
+    const T cRpsi = a.prim[(D + 1) * nt + i], aRpsi = a.prim[(D + 1) * nt + j];
+    const T cP = a.prim[(D + 2) * nt + i], cN = a.prim[(D + 2) * nt + j];
+    const T Rinv = (T)a.Rinv;
+    const T cT = cRpsi * Rinv, aT = aRpsi * Rinv;
+    T rhs[NQ];
+
+    if (SCH == kSchemeM1) {
+        // Kurganov-Tadmor central-upwind flux (src/cfd_v0.cpp:2588-2675)
+        const T rhoPos = interp(w, qi[0], qj[0]);
+        const T rhoNeg = interp(omw, qj[0], qi[0]);
+        const T rhoPos_inv = T(1) / rhoPos, rhoNeg_inv = T(1) / rhoNeg;
+        T rhoUPos[D], rhoUNeg[D], uPos[D], uNeg[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            rhoUPos[k] = interp(w, qi[k + 1], qj[k + 1]);
+            rhoUNeg[k] = interp(omw, qj[k + 1], qi[k + 1]);
+        }
+        T ce = T(2) * qi[D + 1] * cri, ae = T(2) * qj[D + 1] * ari;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            ce -= cU[k] * cU[k];
+            ae -= aU[k] * aU[k];
+        }
+        ce *= T(0.5);
+        ae *= T(0.5);
+        const T ePos = interp(w, ce, ae), eNeg = interp(omw, ae, ce);
+        const T RpsiPos = interp(w, cRpsi, aRpsi), RpsiNeg = interp(omw, aRpsi, cRpsi);
+        const T pPos = rhoPos * RpsiPos, pNeg = rhoNeg * RpsiNeg;
+        const T cPos = interp(w, cP, cN), cNeg = interp(omw, cN, cP);
+        T phiPos = T(0), phiNeg = T(0);
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            uPos[k] = rhoUPos[k] * rhoPos_inv;
+            uNeg[k] = rhoUNeg[k] * rhoNeg_inv;
+            phiPos += uPos[k] * S[k];
+            phiNeg += -uNeg[k] * S[k];
+        }
+        T psiPos = phiPos + cPos * Smag;
+        const T b1 = -phiNeg + cNeg * Smag;
+        if (psiPos < b1) psiPos = b1;
+        if (psiPos < T(0)) psiPos = T(0);
+        T psiNeg = phiPos - cPos * Smag;
+        const T b2 = -phiNeg - cNeg * Smag;
+        if (b2 < psiNeg) psiNeg = b2;
+        if (T(0) < psiNeg) psiNeg = T(0);
+        const T a0 = T(1) / (psiPos - psiNeg);
+        const T a1 = psiPos * psiNeg;
+        const T aPos = psiPos * phiPos;
+        const T aNeg = psiNeg * phiNeg;
+        T rhoEPos = ePos, rhoENeg = eNeg;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            rhoEPos += T(0.5) * uPos[k] * uPos[k];
+            rhoENeg += T(0.5) * uNeg[k] * uNeg[k];
+        }
+        rhoEPos *= rhoPos;
+        rhoENeg *= rhoNeg;
+        rhs[0] = -(aPos * rhoPos + aNeg * rhoNeg + (rhoNeg - rhoPos) * a1) * a0;
+        const T pface = (pPos * psiPos - pNeg * psiNeg) * a0;
+#pragma unroll
+        for (int k = 0; k < D; ++k)
+            rhs[k + 1] = -((aPos * rhoUPos[k] + aNeg * rhoUNeg[k] + (rhoUNeg[k] - rhoUPos[k]) * a1) * a0 + pface * S[k]);
+        rhs[D + 1] = -(aPos * rhoEPos + aNeg * rhoENeg + (rhoENeg - rhoEPos) * a1 + (aPos * pPos + aNeg * pNeg)) * a0;
+    } else {
+        // Pirozzoli kinetic-energy-preserving mid-point flux (src/cfd_v0.cpp:1966-2023)
+        const T rhoavg = T(0.5) * (qi[0] + qj[0]);
+        const T rhoavg_inv = T(1) / rhoavg;
+        T rhoUavg[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) rhoUavg[k] = T(0.5) * (qi[k + 1] + qj[k + 1]);
+        T pavg = rhoavg * (T(0.5) * (cRpsi + aRpsi));
+        const T Havg = T(0.5) * ((qi[D + 1] * cri + cRpsi) + (qj[D + 1] * ari + aRpsi));
+        if (SCH == kSchemeAUSM) {
+            // shock sensor, minmod reconstructions and AUSM+ pressure
+            // dissipation (src/cfd_v0.cpp:2288-2339)
+            const T cavg = T(0.5) * (cP + cN);
+            T d[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) d[k] = a.d[k * nf + f];
+            T cdiv = T(0), ndiv = T(0), ccurl = T(0), ncurl = T(0), cv2 = T(0), nv2 = T(0), unPos = T(0),
+              unNeg = T(0), norm = T(0);
+#pragma unroll
+            for (int x = 0; x < D; ++x) {
+                cdiv += a.V[(x * D + x) * nt + i];
+                ndiv += a.V[(x * D + x) * nt + j];
+#pragma unroll
+                for (int y = x + 1; y < D; ++y) {
+                    const T cc = a.V[(x * D + y) * nt + i] - a.V[(y * D + x) * nt + i];
+                    const T nn = a.V[(x * D + y) * nt + j] - a.V[(y * D + x) * nt + j];
+                    ccurl += cc * cc;
+                    ncurl += nn * nn;
+                }
+                cv2 += cU[x] * cU[x];
+                nv2 += aU[x] * aU[x];
+                T gi[D], gj[D];
+#pragma unroll
+                for (int y = 0; y < D; ++y) {
+                    gi[y] = a.grad[(2 * D + x * D + y) * nt + i];
+                    gj[y] = a.grad[(2 * D + x * D + y) * nt + j];
+                }
+                const T uP = minmod_interp<T, D>(cU[x], aU[x], gi, d, w, T(1));
+                const T uN = minmod_interp<T, D>(cU[x], aU[x], gj, d, w, T(-1));
+                unPos += uP * S[x];
+                unNeg += uN * S[x];
+                norm += S[x] * S[x];
+            }
+            T ct = -(cdiv / sqrt(cdiv * cdiv + ccurl + T(4e-2)));
+            ct = (ct < T(0)) ? T(0) : ct;
+            T nt_ = -(ndiv / sqrt(ndiv * ndiv + ncurl + T(4e-2)));
+            nt_ = (nt_ < T(0)) ? T(0) : nt_;
+            const T theta = T(0.5) * (ct + nt_);
+            const T cp = qi[0] * (T)a.gm1 * (qi[D + 1] * cri - T(0.5) * cv2);
+            const T np = qj[0] * (T)a.gm1 * (qj[D + 1] * ari - T(0.5) * nv2);
+            T gri[D], grj[D], gpi[D], gpj[D];
+#pragma unroll
+            for (int y = 0; y < D; ++y) {
+                gri[y] = a.grad[y * nt + i];
+                grj[y] = a.grad[y * nt + j];
+                gpi[y] = a.grad[(D + y) * nt + i];
+                gpj[y] = a.grad[(D + y) * nt + j];
+            }
+            const T rhoPos = minmod_interp<T, D>(qi[0], qj[0], gri, d, w, T(1));
+            const T rhoNeg = minmod_interp<T, D>(qi[0], qj[0], grj, d, w, T(-1));
+            const T pPos = minmod_interp<T, D>(cp, np, gpi, d, w, T(1));
+            const T pNeg = minmod_interp<T, D>(cp, np, gpj, d, w, T(-1));
+            const T Msq = (unPos * unPos + unNeg * unNeg) / (T(2) * cavg * cavg * norm);
+            const T snorm = sqrt(norm);
+            const T MPos = unPos / (snorm * cavg);
+            const T MNeg = unNeg / (snorm * cavg);
+            const T Minf = T(0.2);
+            T m = (Msq < Minf * Minf) ? Minf * Minf : Msq;
+            m = (m < T(1)) ? m : T(1);
+            const T M0 = sqrt(m);
+            const T fa = M0 * (T(2) - M0);
+            const T alpha = T(3) * (T(5) * fa * fa - T(4)) / T(16);
+            const T phalf = pNeg * (p5pos(MNeg, alpha) - p5neg(MNeg, alpha)) -
+                            pPos * (p5pos(MPos, alpha) - p5neg(MPos, alpha));
+            const T pu = T(-0.75) * p5pos(MPos, alpha) * p5neg(MNeg, alpha) * (rhoPos + rhoNeg) * cavg * fa *
+                         (unNeg - unPos);
+            pavg += theta * (pu - T(0.5) * phalf);
+        }
+        T phiavg = T(0);
+#pragma unroll
+        for (int k = 0; k < D; ++k) phiavg += (rhoUavg[k] * rhoavg_inv) * S[k];
+        rhs[0] = -rhoavg * phiavg;
+#pragma unroll
+        for (int k = 0; k < D; ++k) rhs[k + 1] = -(rhoUavg[k] * phiavg + pavg * S[k]);
+        rhs[D + 1] = -(rhoavg * Havg * phiavg);
+    }
+
+    // Viscous face terms (src/cfd_v0.cpp:2682-2796). With mu == 0 every term
+    // is an exact zero and the block is skipped.
+    const T mu = (T)a.mu;
+    if (mu != T(0)) {
+        T g[D][D], gT[D], tau[D][D], tmc[D][D], sU[D];
+        if (!ghost) {
+#pragma unroll
+            for (int x = 0; x < D; ++x) {
+#pragma unroll
+                for (int y = 0; y < D; ++y) {
+                    g[x][y] = interp(w, a.V[(x * D + y) * nt + i], a.V[(x * D + y) * nt + j]);
+                    tmc[x][y] = interp(w, a.V[(D * D + D + x * D + y) * nt + i], a.V[(D * D + D + x * D + y) * nt + j]);
+                }
+                gT[x] = interp(w, a.V[(D * D + x) * nt + i], a.V[(D * D + x) * nt + j]);
+                sU[x] = interp(w, a.V[(2 * D * D + D + x) * nt + i], a.V[(2 * D * D + D + x) * nt + j]);
+            }
+        } else {
+            // explicit two-point gradients on physical boundaries
+#pragma unroll
+            for (int x = 0; x < D; ++x) {
+#pragma unroll
+                for (int y = 0; y < D; ++y) g[x][y] = (aU[x] - cU[x]) * dn[y] * dinv;
+                gT[x] = (aT - cT) * dn[x] * dinv;
+            }
+            stress<T, D>(g, mu, tau);
+            T diagSum = T(0);
+#pragma unroll
+            for (int x = 0; x < D; ++x) diagSum -= g[x][x];
+            diagSum *= mu * T(2) / T(3);
+            T Uf[D];
+#pragma unroll
+            for (int x = 0; x < D; ++x) Uf[x] = interp(w, cU[x], aU[x]);
+#pragma unroll
+            for (int x = 0; x < D; ++x) {
+#pragma unroll
+                for (int y = 0; y < D; ++y) tmc[x][y] = mu * g[y][x];
+                tmc[x][x] += diagSum;
+                sU[x] = dotv<T, D>(Uf, tau[x]);
+            }
+        }
+        const T kc = (T)a.kcond;
+#pragma unroll
+        for (int x = 0; x < D; ++x) {
+            const T divTau = dotv<T, D>(tmc[x], S);
+            const T lap = mu * (dmag * (aU[x] - cU[x]) * dinv + dotv<T, D>(Kf, g[x]));
+            rhs[x + 1] += divTau + lap;
+        }
+        const T lapT = kc * (dmag * (aT - cT) * dinv + dotv<T, D>(Kf, gT));
+        rhs[D + 1] += dotv<T, D>(sU, S) + lapT;
+    }
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) a.flux[v * nf + f] = rhs[v];
+}
+
+// ---------------------------------------------------------------------------
+// k_update: gather, sponge, RK update.
+// ---------------------------------------------------------------------------
+template <typename T, int D>
+__global__ void __launch_bounds__(256) k_update(Args<T> a, double Ak, double Bk, double dt, int first, int withRes) {
+    const int c = LFM_GLOBAL_ID();
+    if (c >= a.nc) return;
+    constexpr int NQ = D + 2;
+    const size_t nt = (size_t)a.nt, nf = (size_t)a.nf, nc = (size_t)a.nc;
+    double acc[NQ], res[NQ];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) {
+        acc[v] = first ? 0.0 : Ak * a.dq[v * nc + c];
+        res[v] = 0.0;
+    }
+    const double vi = a.volInv[c];
+    for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
+        const int code = a.cfList[e];
+        if (code >= 0) {
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) {
+                const double r = (double)a.flux[v * nf + code];
+                acc[v] += dt * r * vi;
+                res[v] += r;
+            }
+        } else {
+            const int f = ~code;
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) {
+                const double r = (double)a.flux[v * nf + f];
+                acc[v] -= dt * r * vi;
+                res[v] -= r;
+            }
+        }
+    }
+    double qv[NQ];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) qv[v] = a.q[v * nt + c];
+    const double sg = a.sponge[c];
+    if (sg != 0.0) {
+        acc[0] += dt * sg * (a.rhoInf - qv[0]);
+#pragma unroll
+        for (int k = 0; k < D; ++k) acc[k + 1] += dt * sg * (a.rhoInf * a.UInf[k] - qv[k + 1]);
+        acc[D + 1] += dt * sg * (a.rhoInf * a.EInf - qv[D + 1]);
+    }
+    bool finite = true;
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) {
+        a.dq[v * nc + c] = acc[v];
+        const double qn = qv[v] + Bk * acc[v];
+        finite = finite && isfinite(qn);
+        a.q[v * nt + c] = qn;
+        if (withRes) a.res[v * nc + c] = res[v];
+    }
+    if (!finite) atomicOr(a.flag, 1);
+}
+
+// ---------------------------------------------------------------------------
+// Reductions: compute_cfl / compute_dt (max / min over cells) and the sum of
+// squared cell residuals. Block results go to partials, a single block
+// finishes; both levels use a fixed tree, so results are reproducible.
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(256) k_cfl(const double* q, int nt, int nc, const double* volInv, const int* sOff,
+                                             const double* cellS, double dt, int mode, double maxCo, double* partial) {
+    __shared__ double sh[256];
+    const int c = LFM_GLOBAL_ID();
+    double v = (mode == 0) ? 0.0 : 100.0;
+    if (c < nc) {
+        const double rho = q[c];
+        if (mode == 0) {
+            double cfl = 0;
+            for (int e = sOff[c]; e < sOff[c + 1]; ++e) {
+                double flux = 0.;
+                for (int k = 0; k < D; ++k) flux += q[(size_t)(k + 1) * nt + c] * cellS[(size_t)e * D + k];
+                cfl += fabs(flux);
+            }
+            v = cfl * ((1.0 / rho) * volInv[c] * dt);
+        } else {
+            double sumFlux = 0;
+            for (int e = sOff[c]; e < sOff[c + 1]; ++e) {
+                const double* S = &cellS[(size_t)e * D];
+                double sMag = 0.;
+                for (int k = 0; k < D; ++k) sMag += S[k] * S[k];
+                sMag = sqrt(sMag);
+                double flux = 0.;
+                for (int k = 0; k < D; ++k) flux += q[(size_t)(k + 1) * nt + c] * S[k] / sMag;
+                sumFlux += fabs(flux);
+            }
+            v = maxCo * rho * 2.0 * (1.0 / volInv[c]) / sumFlux;
+        }
+    }
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            const double o = sh[threadIdx.x + s];
+            sh[threadIdx.x] = (mode == 0) ? fmax(sh[threadIdx.x], o) : fmin(sh[threadIdx.x], o);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+__global__ void __launch_bounds__(256) k_reduce_final(const double* partial, int n, int mode, double* out) {
+    __shared__ double sh[256];
+    double v = (mode == 0) ? 0.0 : (mode == 1 ? 100.0 : 0.0);
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const double o = partial[k];
+        v = (mode == 0) ? fmax(v, o) : (mode == 1 ? fmin(v, o) : v + o);
+    }
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            const double o = sh[threadIdx.x + s];
+            sh[threadIdx.x] = (mode == 0) ? fmax(sh[threadIdx.x], o) : (mode == 1 ? fmin(sh[threadIdx.x], o) : sh[threadIdx.x] + o);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sh[0];
+}
+
+__global__ void __launch_bounds__(256) k_res_sq(const double* res, int nc, double* partial) {
+    __shared__ double sh[256];
+    const int c = LFM_GLOBAL_ID();
+    const double v = (c < nc) ? res[c] * res[c] : 0.0;
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+__global__ void k_set_flag(int* flag, int v) { *flag = v; }
+
+// ---------------------------------------------------------------------------
+// Launchers.
+// ---------------------------------------------------------------------------
+static inline unsigned blocks(int n, int b) { return (unsigned)((n + b - 1) / b); }
+
+template <typename T, int D>
+void launch_stage_t(const Args<T>& a, const StageConfig& s, cudaStream_t st) {
+    k_prep<T, D><<<blocks(a.nt, 256), 256, 0, st>>>(a);
+    if (s.needGrad) k_grad<T, D><<<blocks(a.nc, 256), 256, 0, st>>>(a);
+    if (s.needVis) k_vis<T, D><<<blocks(a.nc, 256), 256, 0, st>>>(a);
+    switch (s.scheme) {
+        case kSchemeM1: k_flux<T, D, kSchemeM1><<<blocks(a.nf, 128), 128, 0, st>>>(a); break;
+        case kSchemeM2: k_flux<T, D, kSchemeM2><<<blocks(a.nf, 128), 128, 0, st>>>(a); break;
+        default: k_flux<T, D, kSchemeAUSM><<<blocks(a.nf, 128), 128, 0, st>>>(a); break;
+    }
+    k_update<T, D><<<blocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, s.first, s.withRes);
+}
+
+template <typename T>
+void launch_stage(const Args<T>& a, const StageConfig& s, cudaStream_t st) {
+    if (a.D == 2)
+        launch_stage_t<T, 2>(a, s, st);
+    else
+        launch_stage_t<T, 3>(a, s, st);
+}
+template void launch_stage<double>(const Args<double>&, const StageConfig&, cudaStream_t);
+template void launch_stage<float>(const Args<float>&, const StageConfig&, cudaStream_t);
+
+// Individual kernels, for per-kernel timing.
+template <typename T>
+void launch_kernel(const Args<T>& a, const StageConfig& s, int which, cudaStream_t st) {
+    const bool d2 = a.D == 2;
+    switch (which) {
+        case 0:
+            if (d2) k_prep<T, 2><<<blocks(a.nt, 256), 256, 0, st>>>(a);
+            else k_prep<T, 3><<<blocks(a.nt, 256), 256, 0, st>>>(a);
+            break;
+        case 1:
+            if (!s.needGrad) break;
+            if (d2) k_grad<T, 2><<<blocks(a.nc, 256), 256, 0, st>>>(a);
+            else k_grad<T, 3><<<blocks(a.nc, 256), 256, 0, st>>>(a);
+            break;
+        case 2:
+            if (!s.needVis) break;
+            if (d2) k_vis<T, 2><<<blocks(a.nc, 256), 256, 0, st>>>(a);
+            else k_vis<T, 3><<<blocks(a.nc, 256), 256, 0, st>>>(a);
+            break;
+        case 3: {
+            if (d2) {
+                if (s.scheme == kSchemeM1) k_flux<T, 2, kSchemeM1><<<blocks(a.nf, 128), 128, 0, st>>>(a);
+                else if (s.scheme == kSchemeM2) k_flux<T, 2, kSchemeM2><<<blocks(a.nf, 128), 128, 0, st>>>(a);
+                else k_flux<T, 2, kSchemeAUSM><<<blocks(a.nf, 128), 128, 0, st>>>(a);
+            } else {
+                if (s.scheme == kSchemeM1) k_flux<T, 3, kSchemeM1><<<blocks(a.nf, 128), 128, 0, st>>>(a);
+                else if (s.scheme == kSchemeM2) k_flux<T, 3, kSchemeM2><<<blocks(a.nf, 128), 128, 0, st>>>(a);
+                else k_flux<T, 3, kSchemeAUSM><<<blocks(a.nf, 128), 128, 0, st>>>(a);
+            }
+            break;
+        }
+        case 4:
+            if (d2) k_update<T, 2><<<blocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, s.first, s.withRes);
+            else k_update<T, 3><<<blocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, s.first, s.withRes);
+            break;
+        default:
+            break;
+    }
+}
+template void launch_kernel<double>(const Args<double>&, const StageConfig&, int, cudaStream_t);
+template void launch_kernel<float>(const Args<float>&, const StageConfig&, int, cudaStream_t);
+
+void launch_cfl(int D, const double* q, int nt, int nc, const double* volInv, const int* sOff, const double* cellS,
+                double dt, int mode, double maxCo, double* partial, double* out, cudaStream_t st) {
+    const unsigned nb = blocks(nc, 256);
+    if (D == 2)
+        k_cfl<2><<<nb, 256, 0, st>>>(q, nt, nc, volInv, sOff, cellS, dt, mode, maxCo, partial);
+    else
+        k_cfl<3><<<nb, 256, 0, st>>>(q, nt, nc, volInv, sOff, cellS, dt, mode, maxCo, partial);
+    k_reduce_final<<<1, 256, 0, st>>>(partial, (int)nb, mode, out);
+}
+
+void launch_res_sum(const double* res, int nc, double* partial, double* out, cudaStream_t st) {
+    const unsigned nb = blocks(nc, 256);
+    k_res_sq<<<nb, 256, 0, st>>>(res, nc, partial);
+    k_reduce_final<<<1, 256, 0, st>>>(partial, (int)nb, 2, out);
+}
+
+void launch_set_flag(int* flag, int v, cudaStream_t st) { k_set_flag<<<1, 1, 0, st>>>(flag, v); }
+
+}  // namespace dev
+}  // namespace lfm

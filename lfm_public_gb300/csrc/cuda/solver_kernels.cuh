@@ -1,0 +1,85 @@
+// Device kernels of the explicit finite-volume time step (sm_103a).
+//
+// One RK stage of the reference (src/mesh_solver.cpp:500-672) becomes five
+// kernels over structure-of-arrays data, all deterministic (no atomics on
+// values, every sum in a fixed order):
+//
+//   k_prep     per cell and ghost: boundary-ghost state (set_boundary_conditions,
+//              src/cfd_v0.cpp:1009-1221) and the primitives every face reads
+//              (1/rho, u, R psi = p/rho, c), computed once per stage instead of
+//              once per face side.
+//   k_grad     per cell, gather over incident faces: Gauss-linear gradients of
+//              rho, p and u that M2AUSM's minmod reconstruction reads
+//              (calc_gradients_M2AUSM, :1383-1495). Only with M2AUSM + minmod;
+//              the gradients of calc_gradients (:1500-1567) never reach the M1/M2
+//              flux, so that pass is not run for them.
+//   k_vis      per cell, gather: dudx, dTdx, then tauMC and sigmaU from the
+//              completed gradient (calc_VIS, :1743-1860). Skipped when mu = 0 and
+//              the scheme does not read dudx, because every viscous face term is
+//              then an exact zero.
+//   k_flux     per flux face: the face rhs of one_rk_step_M1 / _M2 / _M2AUSM
+//              (:2529-2796, :1896-2133, :2185-2489) into a face buffer.
+//   k_update   per cell, gather of the face rhs in ascending face order (the
+//              reference's scatter order), sponge source and the low-storage RK
+//              update (:2800-2822).
+//
+// The gather replaces the reference's scatter: within a stage every face is
+// evaluated once from the stage-start state, because a cell's owned faces
+// always point to cells the reference updates later, so the sequential
+// scatter-and-update is a Jacobi stage. Geometry is seen from the reference's
+// processing side P of each face.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace lfm {
+namespace dev {
+
+constexpr int kSchemeM1 = 0;
+constexpr int kSchemeM2 = 1;
+constexpr int kSchemeAUSM = 2;
+
+// Arguments shared by the kernels (all device pointers).
+template <typename T>
+struct Args {
+    int D, nq;
+    int nc, ng, nf, nt;       // cells, ghosts, flux faces, cells + ghosts
+    // state (FP64 RK registers)
+    double* q;                // nq x nt
+    double* dq;               // nq x nc
+    // per cell + ghost, computed every stage
+    T* prim;                  // (D + 3) x nt: 1/rho, u[D], R psi, c
+    T* V;                     // (2D^2 + 2D) x nt: dudx, dTdx, tauMC, sigmaU
+    T* grad;                  // (2D + D^2) x nt: rho_grad, p_grad, U_grad (M2AUSM)
+    T* flux;                  // nq x nf face rhs
+    double* res;              // nq x nc stage-0 residual per cell (or null)
+    // faces
+    const int* fP;
+    const int* fN;
+    const uint8_t* fGhost;
+    const T* S;               // D x nf
+    const T* d;               // D x nf
+    const T* w;
+    const T* smag;
+    const T* dinv;            // 1/|d|
+    const T* dnorm;           // D x nf
+    const T* dmag;            // |delta|
+    const T* K;               // D x nf
+    // cells
+    const double* volInv;
+    const double* sponge;
+    const int* cfOff;         // nc + 1
+    const int* cfList;        // face index, negative (~f) when the cell is N
+    // ghosts
+    const int* gCell;
+    const int* gKind;
+    const int* gFace;
+    // constants
+    double gamma, gm1, Rinv, rhoInf, EInf, pInf, TInf, UInf[3], mu, kcond;
+    // error flag (non-finite state)
+    int* flag;
+};
+
+}  // namespace dev
+}  // namespace lfm

@@ -1,0 +1,39 @@
+// Host-side launch interface of the time-step kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "solver_kernels.cuh"
+
+namespace lfm {
+namespace dev {
+
+// What one RK stage runs (src/mesh_solver.cpp:500-672).
+struct StageConfig {
+    int scheme = 0;       // kSchemeM1 / M2 / AUSM
+    bool needGrad = false;
+    bool needVis = true;
+    double A = 0, B = 1;  // low-storage RK coefficients of this stage
+    double dt = 0;
+    int first = 0;        // stage 0: dq starts from zero (prepare_for_timestep)
+    int withRes = 0;      // record the stage-0 residual
+};
+
+template <typename T>
+void launch_stage(const Args<T>& a, const StageConfig& s, cudaStream_t st);
+template <typename T>
+void launch_kernel(const Args<T>& a, const StageConfig& s, int which, cudaStream_t st);
+// mode 0: max CFL, mode 1: min dt
+void launch_cfl(int D, const double* q, int nt, int nc, const double* volInv, const int* sOff, const double* cellS,
+                double dt, int mode, double maxCo, double* partial, double* out, cudaStream_t st);
+void launch_res_sum(const double* res, int nc, double* partial, double* out, cudaStream_t st);
+void launch_set_flag(int* flag, int v, cudaStream_t st);
+
+constexpr int kKernelsPerStage = 5;  // prep, grad, vis, flux, update
+inline const char* kernelName(int i) {
+    static const char* names[] = {"k_prep", "k_grad", "k_vis", "k_flux", "k_update"};
+    return (i >= 0 && i < kKernelsPerStage) ? names[i] : "";
+}
+
+}  // namespace dev
+}  // namespace lfm

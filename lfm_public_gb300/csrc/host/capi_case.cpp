@@ -1,0 +1,239 @@
+// C ABI, case half: case input and the flattened solver description
+// (declarations and the reference interfaces they replace: include/lfm_gpu.h).
+#include <cstring>
+#include <exception>
+#include <memory>
+#include <string>
+
+#include "capi_internal.h"
+#include "case_setup.h"
+#include "foam_case.h"
+#include "inputReader.h"
+#include "lfm_gpu.h"
+#include "polyMeshReaderOF.h"
+
+struct lfm_case {
+    lfm::SolverCase sc;
+    double deltaT = 0, startTime = 0, endTime = 0, maxCo = 1;
+    bool adjust = false;
+};
+
+namespace lfm {
+thread_local std::string g_lastError;
+int setError(int code, const std::string& msg) {
+    g_lastError = msg;
+    return code;
+}
+}  // namespace lfm
+
+extern "C" const char* lfm_last_error(void) { return lfm::g_lastError.c_str(); }
+extern "C" const char* lfm_version(void) { return "lfm_public_gb300 0.1 (sm_103a)"; }
+
+static lfm::CaseParams paramsFromInput(const CInputReader& in) {
+    lfm::CaseParams p;
+    p.solver = in.m_nSolver;
+    p.dimension = in.m_nDimension;
+    p.rkOrder = in.m_nRkStepCount;
+    p.minmod = in.m_bMinmodInterpolation;
+    p.laminar = in.m_bisLaminar;
+    p.residuals = in.m_bHaveResidual;
+    p.pInf = in.m_dPInf;
+    p.TInf = in.m_dTInf;
+    for (int k = 0; k < 3; ++k) p.UInf[k] = in.m_dUInf[k];
+    p.Ls = in.m_dLs;
+    p.mach = in.m_dMach;
+    p.kSponge = in.m_dK;
+    p.Cp = in.m_dCp;
+    p.molWeight = in.m_dMolWeight;
+    p.mu = in.m_dMu0;
+    p.Pr = in.m_dPrandtl;
+    return p;
+}
+
+static int validateParams(const lfm::CaseParams& p) {
+    if (p.solver < 0 || p.solver > 2) return lfm::setError(LFM_ERR_INVALID, "unknown solver type " + std::to_string(p.solver));
+    if (p.dimension != 2 && p.dimension != 3)
+        return lfm::setError(LFM_ERR_INVALID, "invalid dimension " + std::to_string(p.dimension));
+    if (!p.laminar)
+        return lfm::setError(LFM_ERR_UNSUPPORTED,
+                             "turbulenceProperties simulationType must be laminar (the Smagorinsky viscous pass is "
+                             "not part of this build)");
+    if (p.rkOrder < 0 || p.rkOrder > 5) return lfm::setError(LFM_ERR_INVALID, "rkOrder must be 0..5");
+    return LFM_OK;
+}
+
+extern "C" int lfm_case_open(const char* root, int rank, lfm_case** out) {
+    if (!root || !out) return lfm::setError(LFM_ERR_INVALID, "lfm_case_open: null argument");
+    *out = nullptr;
+    try {
+        CInputReader in;
+        in.readCase(root);
+        lfm::CaseParams prm = paramsFromInput(in);
+        int rc = validateParams(prm);
+        if (rc) return rc;
+        const std::string caseName = rank >= 0 ? "processor" + std::to_string(rank) : ".";
+        std::unique_ptr<lfm::FoamTime> rt(lfm::newFoamTime(root, caseName));
+        std::unique_ptr<lfm_case> c(new lfm_case);
+        {
+            CPolyMeshReaderOF reader(rt.get());
+            c->sc = lfm::buildSolverCase(reader, prm);
+        }
+        c->deltaT = rt->deltaT;
+        c->startTime = rt->startTime;
+        c->endTime = rt->endTime;
+        c->adjust = rt->adjustTimeStep;
+        c->maxCo = in.m_dCFLMax;
+        *out = c.release();
+        return LFM_OK;
+    } catch (const lfm::foam::FoamError& e) {
+        return lfm::setError(LFM_ERR_IO, e.what());
+    } catch (const std::exception& e) {
+        return lfm::setError(LFM_ERR_INVALID, e.what());
+    }
+}
+
+extern "C" int lfm_case_from_polymesh(const lfm_polymesh* mesh, const lfm_params* params, const lfm_fields* fields,
+                                      lfm_case** out) {
+    if (!mesh || !params || !fields || !out) return lfm::setError(LFM_ERR_INVALID, "lfm_case_from_polymesh: null argument");
+    *out = nullptr;
+    try {
+        lfm::CaseParams prm;
+        prm.solver = params->solver;
+        prm.dimension = params->dimension;
+        prm.rkOrder = params->rk_order;
+        prm.minmod = params->minmod != 0;
+        prm.laminar = params->laminar != 0;
+        prm.residuals = params->residuals != 0;
+        prm.pInf = params->p_inf;
+        prm.TInf = params->T_inf;
+        for (int k = 0; k < 3; ++k) prm.UInf[k] = params->U_inf[k];
+        prm.Ls = params->Ls;
+        prm.mach = params->mach;
+        prm.kSponge = params->k_sponge;
+        prm.Cp = params->Cp;
+        prm.molWeight = params->mol_weight;
+        prm.mu = params->mu;
+        prm.Pr = params->Pr;
+        int rc = validateParams(prm);
+        if (rc) return rc;
+        if (mesh->n_faces <= 0 || mesh->n_cells <= 0 || !mesh->points || !mesh->face_offsets || !mesh->face_points ||
+            !mesh->owner || (mesh->n_internal_faces > 0 && !mesh->neighbour))
+            return lfm::setError(LFM_ERR_INVALID, "lfm_case_from_polymesh: incomplete mesh");
+        if (!fields->p || !fields->T || !fields->U || (prm.Ls > 0 && !fields->alpha))
+            return lfm::setError(LFM_ERR_INVALID, "lfm_case_from_polymesh: missing initial field");
+
+        auto mc = std::make_shared<lfm::MemoryCase>();
+        lfm::FoamMesh& m = mc->mesh;
+        m.points.assign(mesh->points, mesh->points + 3 * mesh->n_points);
+        m.faceOffsets.assign(mesh->face_offsets, mesh->face_offsets + mesh->n_faces + 1);
+        m.facePoints.assign(mesh->face_points, mesh->face_points + m.faceOffsets.back());
+        m.owner.assign(mesh->owner, mesh->owner + mesh->n_faces);
+        m.neighbour.assign(mesh->neighbour, mesh->neighbour + mesh->n_internal_faces);
+        m.nCells = mesh->n_cells;
+        for (int p = 0; p < mesh->n_patches; ++p) {
+            lfm::foam::Patch pt;
+            pt.name = mesh->patch_name[p];
+            pt.type = mesh->patch_type[p];
+            pt.startFace = mesh->patch_start[p];
+            pt.nFaces = mesh->patch_size[p];
+            if (mesh->patch_neighbour && mesh->patch_neighbour[p]) pt.neighbourPatch = mesh->patch_neighbour[p];
+            m.patches.push_back(pt);
+        }
+        if (mesh->cell_submesh) m.cellSubmesh.assign(mesh->cell_submesh, mesh->cell_submesh + mesh->n_cells);
+        m.finalize();
+        auto addField = [&](const char* name, const double* v, bool vec) {
+            lfm::foam::VolField f;
+            f.name = name;
+            f.isVector = vec;
+            f.values.assign(v, v + mesh->n_cells * (vec ? 3 : 1));
+            mc->fields.push_back(std::move(f));
+        };
+        addField("p", fields->p, false);
+        addField("T", fields->T, false);
+        addField("U", fields->U, true);
+        if (fields->alpha) addField("alpha", fields->alpha, false);
+
+        lfm::FoamTime rt;
+        rt.memory = mc;
+        std::unique_ptr<lfm_case> c(new lfm_case);
+        {
+            CPolyMeshReaderOF reader(&rt);
+            c->sc = lfm::buildSolverCase(reader, prm);
+        }
+        *out = c.release();
+        return LFM_OK;
+    } catch (const lfm::foam::FoamError& e) {
+        return lfm::setError(LFM_ERR_INVALID, e.what());
+    } catch (const std::exception& e) {
+        return lfm::setError(LFM_ERR_INVALID, e.what());
+    }
+}
+
+extern "C" int lfm_case_describe(const lfm_case* c, lfm_solver_desc* d) {
+    if (!c || !d) return lfm::setError(LFM_ERR_INVALID, "lfm_case_describe: null argument");
+    const lfm::SolverCase& s = c->sc;
+    std::memset(d, 0, sizeof(*d));
+    d->dim = s.dim;
+    d->nq = s.nq;
+    d->solver = s.solver;
+    d->rk_order = s.rkOrder;
+    d->minmod = s.minmod;
+    d->residuals = s.residuals;
+    d->n_cells = s.nCells;
+    d->n_cells0 = s.nCells0;
+    d->n_ghosts = s.nGhosts;
+    d->n_faces = s.nFaces;
+    d->face_p = s.faceP.data();
+    d->face_n = s.faceN.data();
+    d->face_ghost = s.faceGhost.data();
+    d->S = s.S.data();
+    d->d = s.d.data();
+    d->w = s.w.data();
+    d->smag = s.Smag.data();
+    d->dmag_inv = s.dmagInv.data();
+    d->dnorm = s.dnorm.data();
+    d->delta_mag = s.deltaMag.data();
+    d->K = s.K.data();
+    d->vol_inv = s.volInv.data();
+    d->sponge = s.sponge.data();
+    d->ghost_cell = s.ghostCell.data();
+    d->ghost_kind = s.ghostKind.data();
+    d->cell_face_offsets = s.cellFaceOffsets.data();
+    d->cell_faces = s.cellFaces.data();
+    d->cell_face_sign = s.cellFaceSign.data();
+    d->cell_s_offsets = s.cellSOffsets.data();
+    d->cell_s = s.cellS.data();
+    d->q0 = s.q0.data();
+    d->gamma = s.gamma;
+    d->Rgas = s.Rgas;
+    d->rhoInf = s.rhoInf;
+    d->EInf = s.EInf;
+    d->pInf = s.pInf;
+    d->TInf = s.TInf;
+    for (int k = 0; k < 3; ++k) d->UInf[k] = s.UInf[k];
+    d->mu = s.mu;
+    d->Cp = s.Cp;
+    d->PrInv = s.PrInv;
+    d->rkA = s.rkA.data();
+    d->rkB = s.rkB.data();
+    return LFM_OK;
+}
+
+extern "C" int lfm_case_time(const lfm_case* c, double* delta_t, double* start_time, double* end_time,
+                             int* adjust_time_step, double* max_co) {
+    if (!c) return lfm::setError(LFM_ERR_INVALID, "lfm_case_time: null case");
+    if (delta_t) *delta_t = c->deltaT;
+    if (start_time) *start_time = c->startTime;
+    if (end_time) *end_time = c->endTime;
+    if (adjust_time_step) *adjust_time_step = c->adjust ? 1 : 0;
+    if (max_co) *max_co = c->maxCo;
+    return LFM_OK;
+}
+
+extern "C" int lfm_case_cell_ids(const lfm_case* c, int64_t* out) {
+    if (!c || !out) return lfm::setError(LFM_ERR_INVALID, "lfm_case_cell_ids: null argument");
+    std::memcpy(out, c->sc.cellId.data(), c->sc.cellId.size() * sizeof(int64_t));
+    return LFM_OK;
+}
+
+extern "C" void lfm_case_free(lfm_case* c) { delete c; }

@@ -1,0 +1,327 @@
+"""Benchmark of the explicit finite-volume time step on GB300.
+
+Workload (default): the 2D cylinder aeroacoustics case -- stretched O-grid of
+768 azimuthal x 512 radial quads (393,216 cells), M = 0.2, Re = 150, M1 scheme
+with minmod on, rkOrder 5, constant dt at acoustic CFL 0.5 -- synthetic mesh and
+free-stream initial field generated in memory. A "step" is one time step (5 RK
+stages over all cells). The metric is cell-RK-stage updates per second.
+
+  value  -- device throughput with the state resident in HBM; every timed step
+            is preceded (outside its timing) by a 512 MB write that evicts L2.
+  e2e    -- the same metric through the C ABI with host buffers: each step
+            copies the state from pinned host memory to the device, advances one
+            time step and copies the state back, timed on the host clock.
+
+--impl reference times the reference's CPU implementation of the same
+workload on the host cores (the oracle port: one process per core, each on
+the full mesh, aggregate throughput).
+
+Launch: python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|fp32]
+Under torchrun each rank runs its own replica (weak scaling); rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-RK-stage updates/s"
+UNIT = "cell-stage/s"
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FP64_PEAK_TFLOPS = 1.195  # measured DFMA rate on this machine's GB300 (profiles/fp64_throughput_probe.md)
+
+
+def workload(name: str):
+    from lfm_public_gb300 import cases
+    if name == "cylinder2d":
+        return cases.cylinder_case(n_theta=768, n_r=512, solver=0, minmod=True)
+    if name == "cylinder2d_m2":
+        return cases.cylinder_case(n_theta=768, n_r=512, solver=1, minmod=True)
+    if name == "vortex2d":
+        return cases.vortex_case(n=256, solver=0)
+    if name == "cylinder3d":
+        return cases.cylinder_case(n_theta=384, n_r=256, n_span=96, solver=1, reynolds=3900.0, noise=0.01, seed=3900,
+                                   minmod=False)
+    raise ValueError(f"unknown workload {name}")
+
+
+WORKLOAD_DESC = {
+    "cylinder2d": dict(workload="2D cylinder O-grid 768x512, M1, minmod on, rkOrder 5, CFL 0.5", cells=393216,
+                       dim=2, scheme="M1", faces_per_cell=4),
+    "cylinder2d_m2": dict(workload="2D cylinder O-grid 768x512, M2, minmod on, rkOrder 5, CFL 0.5", cells=393216,
+                          dim=2, scheme="M2", faces_per_cell=4),
+    "vortex2d": dict(workload="2D isentropic vortex 256x256, M1, rkOrder 5, CFL 0.5", cells=65536, dim=2,
+                     scheme="M1", faces_per_cell=4),
+    "cylinder3d": dict(workload="3D cylinder wake 384x256x96, M2, cyclic span, rkOrder 5", cells=9437184, dim=3,
+                       scheme="M2", faces_per_cell=6),
+}
+
+
+def algorithmic_bytes(dim: int, faces_per_cell: int, fp32: bool):
+    """Algorithmic bytes per cell-stage (two compulsory passes, every element
+    touched once per pass, neighbour reuse from cache, 8 B of face indices).
+    Returns (whole stage, flux kernel share)."""
+    nq = dim + 2
+    nv = 2 * dim * dim + 2 * dim
+    fpc = faces_per_cell / 2.0
+    w = 4 if fp32 else 8
+    cell = 3 * nq * 8 + 2 * nq * 8 + 2 * nv * w + 2 * 8 + 8
+    face = ((dim + 1) * w + 8) + ((2 * dim + 1) * w + 8)
+    whole = cell + fpc * face
+    # flux kernel: reads q and V once per cell and the face geometry (S, d, w,
+    # indices) of its faces, writes the face rhs
+    flux = nq * 8 + nv * w + fpc * ((2 * dim + 1) * w + 8) + fpc * nq * w
+    return whole, flux
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def __enter__(self):
+        def run():
+            while not self._stop.is_set():
+                try:
+                    out = subprocess.run(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                         timeout=5).stdout.strip()
+                    if out:
+                        self.samples.append([x.strip() for x in out.split(",")])
+                except Exception:
+                    pass
+                self._stop.wait(0.2)
+        self._t = threading.Thread(target=run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm = sorted(float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit())
+        mx = max((float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()), default=None)
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            for k, n in enumerate(names):
+                if len(s) > 5 + k and s[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(self.samples)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle port, one process per core
+# ---------------------------------------------------------------------------
+def _port_worker(name, steps, repeats, barrier, out):
+    sys.path.insert(0, ROOT)
+    from lfm_public_gb300 import _native as N
+    case = workload(name)
+    ch = N.CaseHandle.from_case(case)
+    q0 = ch.q0()
+    for _ in range(repeats):
+        barrier.wait()
+        t0 = time.time()
+        N.port_run(ch, q0, steps, case.delta_t)
+        t1 = time.time()
+        out.put((ch.desc.n_cells * ch.desc.rk_order * steps, t0, t1))
+
+
+def cpu_baseline(name: str, steps_per_proc: int, procs: int, repeats: int = 1):
+    """Aggregate throughput of `procs` oracle processes, each advancing the full
+    mesh by `steps_per_proc` time steps, started together `repeats` times.
+    Returns a list of (rate, seconds, updates), one per repeat."""
+    ctx = mp.get_context("spawn")
+    barrier = ctx.Barrier(procs)
+    out = ctx.Queue()
+    ps = [ctx.Process(target=_port_worker, args=(name, steps_per_proc, repeats, barrier, out)) for _ in range(procs)]
+    for p in ps:
+        p.start()
+    res = [out.get() for _ in range(procs * repeats)]
+    for p in ps:
+        p.join()
+    res.sort(key=lambda r: r[1])
+    rounds = []
+    for k in range(repeats):
+        grp = res[k * procs:(k + 1) * procs]
+        upd = sum(r[0] for r in grp)
+        t = max(r[2] for r in grp) - min(r[1] for r in grp)
+        rounds.append((upd / t, t, upd))
+    return rounds
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo", init_method="env://")
+        pg = dist
+    return ws, rank, local, pg
+
+
+def _allmax(pg, v: float) -> float:
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args):
+    ws, rank, _, pg = _dist()
+    if rank != 0:
+        return 0
+    procs = os.cpu_count() or 1
+    steps_per_proc = 1
+    rounds = cpu_baseline(args.workload, steps_per_proc, procs, repeats=args.warmup + max(1, args.steps))
+    timed = rounds[args.warmup:] or rounds
+    value = sum(r[2] for r in timed) / sum(r[1] for r in timed)
+    desc = WORKLOAD_DESC[args.workload]
+    sample = (f"{procs} processes x {steps_per_proc} time step(s) of the full {desc['cells']}-cell mesh per bench "
+              f"step; aggregate cell-stage updates / wall time")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * desc["cells"] * 5 / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": desc["workload"], "cells": desc["cells"], "rk_stages": 5},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    ws, rank, local, pg = _dist()
+    import numpy as np
+    from lfm_public_gb300 import _native as N
+    desc = WORKLOAD_DESC[args.workload]
+    fp32 = args.precision == "fp32"
+
+    base = None
+    if rank == 0 and not args.no_cpu_baseline:
+        # before any GPU call in this process (the pool uses spawn)
+        procs = 1
+        r, t, u = cpu_baseline(args.workload, 1, procs)[0]
+        base = {"value": r, "unit": UNIT, "cores": procs, "kind": "port",
+                "sample": f"1 time step (5 RK stages) of the full {desc['cells']}-cell mesh, single thread, {t:.1f} s"}
+
+    case = workload(args.workload)
+    ch = N.CaseHandle.from_case(case)
+    nc, nq, stages = ch.desc.n_cells, ch.desc.nq, ch.desc.rk_order
+    dt = case.delta_t
+    s = N.Solver(ch, precision=N.LFM_FP32_BULK if fp32 else N.LFM_FP64, device=local)
+
+    for _ in range(args.warmup):
+        s.step(1, dt)
+    s.sync()
+    if pg:
+        pg.barrier()
+    launches = s.launches_per_step()
+    with ClockSampler(local) as clk:
+        time.sleep(0.3)
+        times = s.bench(args.steps, dt, 512 << 20)
+        s.sync()
+    if pg:
+        pg.barrier()
+    total_ms = _allmax(pg, float(times.sum()))
+    value = ws * nc * stages * args.steps / (total_ms / 1000.0)
+
+    # per-kernel times of one step (events around each launch, serialised)
+    prof = s.profile_step(dt)
+    s.sync()
+    dominant = max(prof, key=prof.get)
+    stage_ms = sum(prof.values())
+
+    # end to end through the C ABI with pinned host buffers
+    import torch
+    host = torch.empty((nq, nc), dtype=torch.float64, pin_memory=True).numpy()
+    host[:] = s.get_state()
+    e2e_steps = max(1, args.steps)
+    for _ in range(2):
+        s.set_state(host)
+        s.step(1, dt)
+        host[:] = s.get_state()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        s.set_state(host)
+        s.step(1, dt)
+        host[:] = s.get_state()
+    s.sync()
+    e2e_s = _allmax(pg, time.perf_counter() - t0)
+    e2e_value = ws * nc * stages * e2e_steps / e2e_s
+    s.close()
+
+    if rank != 0:
+        return 0
+    peaks = {}
+    if os.path.exists(PEAKS_FILE):
+        peaks = json.load(open(PEAKS_FILE))
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    whole_b, flux_b = algorithmic_bytes(desc["dim"], desc["faces_per_cell"], fp32)
+    flux_ms_per_launch = prof["k_flux"] / stages
+    achieved = flux_b * nc / (flux_ms_per_launch * 1e-3) / 1e9
+    stage_achieved = whole_b * nc * stages * args.steps / (total_ms / ws * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32-flux/f64-rk" if fp32 else "f64", "data": "synthetic (generated mesh and initial field)",
+        "config": {"workload": desc["workload"], "cells": nc, "rk_stages": stages, "precision": args.precision,
+                   "l2": "512 MB write between timed steps", "parallelism": f"replicas x{ws}"},
+        "roofline": {"bound": "hbm", "kernel": "k_flux", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "peak_source": peak_src, "traffic": None,
+                     "algorithmic_bytes_per_cell": flux_b,
+                     "step_achieved": stage_achieved, "step_frac": stage_achieved / hbm,
+                     "step_algorithmic_bytes_per_cell_stage": whole_b},
+        "kernels_ms_per_step": prof, "dominant_kernel": dominant,
+        "cpu_baseline": base,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nq * nc * 8, "d2h_bytes_per_step": nq * nc * 8},
+        "gpu_launches": launches * args.steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="cylinder2d", choices=sorted(WORKLOAD_DESC))
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -194,6 +194,15 @@ int lfm_solver_residual(lfm_solver* s, double* res);
  * first CUDA or numeric error. */
 int lfm_solver_sync(lfm_solver* s);
 
+/* Writes `bytes` of device scratch memory on the solver stream so that the
+ * next step starts with a cold L2 cache (benchmark timing aid). */
+int lfm_solver_flush_l2(lfm_solver* s, size_t bytes);
+
+/* Benchmark loop: nsteps time steps, each preceded by a write of flush_bytes
+ * of scratch memory (outside its timing) and bracketed by events on the
+ * solver stream; one synchronisation at the end. ms[k] = duration of step k. */
+int lfm_solver_bench(lfm_solver* s, int nsteps, double dt, size_t flush_bytes, float* ms);
+
 /* Device kernels launched per time step (for launch accounting). */
 int lfm_solver_launches_per_step(const lfm_solver* s, int* launches);
 

@@ -108,6 +108,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "lfm_solver_residual": ([vp, _dp], C.c_int),
         "lfm_solver_sync": ([vp], C.c_int),
         "lfm_solver_launches_per_step": ([vp, C.POINTER(C.c_int)], C.c_int),
+        "lfm_solver_flush_l2": ([vp, C.c_size_t], C.c_int),
+        "lfm_solver_bench": ([vp, C.c_int, C.c_double, C.c_size_t, C.POINTER(C.c_float)], C.c_int),
         "lfm_solver_profile_step": ([vp, C.c_double, C.c_int, C.POINTER(C.c_float)], C.c_int),
         "lfm_solver_kernel_name": ([C.c_int], C.c_char_p),
     }
@@ -283,6 +285,14 @@ class Solver:
         out = np.empty(self.nq)
         check(load_library().lfm_solver_residual(self._h, _ptr(out, C.c_double)))
         return out
+
+    def bench(self, nsteps: int, dt: float, flush_bytes: int = 512 << 20) -> np.ndarray:
+        ms = (C.c_float * nsteps)()
+        check(load_library().lfm_solver_bench(self._h, nsteps, dt, flush_bytes, ms))
+        return np.array(ms[:], dtype=np.float64)
+
+    def flush_l2(self, nbytes: int = 512 << 20):
+        check(load_library().lfm_solver_flush_l2(self._h, nbytes))
 
     def launches_per_step(self) -> int:
         v = C.c_int()

@@ -106,7 +106,7 @@ def build_library(verbose: bool = False) -> str:
     for j in cli_jobs:
         _run(j)
     if cli_objs and not _newer(CLI, cli_objs + [LIB]):
-        _run(["g++", "-o", CLI, *cli_objs, f"-L{PKG}", "-llfm_gpu", f"-Wl,-rpath,{PKG}"])
+        _run(["g++", "-o", CLI, *cli_objs, f"-L{PKG}", "-llfm_gpu", "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 

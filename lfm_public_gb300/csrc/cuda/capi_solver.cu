@@ -46,6 +46,8 @@ struct lfm_solver {
     cudaGraphExec_t graph = nullptr;
     double graphDt = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    void* scrub = nullptr;
+    size_t scrubBytes = 0;
 };
 
 namespace {
@@ -137,7 +139,9 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
     if ((rc = devAlloc(s, &a.dq, (size_t)s->nq * s->nc))) return rc;
     if ((rc = devAlloc(s, &a.prim, (D + 3) * nt))) return rc;
     if ((rc = devAlloc(s, &a.V, (2 * D * D + 2 * D) * nt))) return rc;
-    if ((rc = devAlloc(s, &a.grad, (2 * D + D * D) * (s->needGrad ? nt : 1)))) return rc;
+    // M2AUSM always reads the gradients (all zero when minmod is off, as in the
+    // reference, whose prepare_for_RKstep zeroes them every stage).
+    if ((rc = devAlloc(s, &a.grad, (2 * D + D * D) * (s->scheme == LFM_SOLVER_M2AUSM ? nt : 1)))) return rc;
     if ((rc = devAlloc(s, &a.flux, (size_t)s->nq * nf))) return rc;
     T* p;
     if ((rc = uploadAs<T>(s, &p, d->S, D * nf))) return rc;
@@ -335,6 +339,7 @@ extern "C" void lfm_solver_destroy(lfm_solver* s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     if (s->graph) cudaGraphExecDestroy(s->graph);
     for (void* p : s->allocations) cudaFree(p);
+    if (s->scrub) cudaFree(s->scrub);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -446,6 +451,46 @@ extern "C" int lfm_solver_sync(lfm_solver* s) {
     int flag = 0;
     LFM_CUDA(cudaMemcpy(&flag, s->flag, sizeof(int), cudaMemcpyDeviceToHost));
     if (flag) return lfm::setError(LFM_ERR_NUMERIC, "non-finite conserved state");
+    return LFM_OK;
+}
+
+extern "C" int lfm_solver_flush_l2(lfm_solver* s, size_t bytes) {
+    if (!s) return lfm::setError(LFM_ERR_INVALID, "null solver");
+    LFM_CUDA(cudaSetDevice(s->device));
+    if (bytes > s->scrubBytes) {
+        if (s->scrub) cudaFree(s->scrub);
+        s->scrub = nullptr;
+        s->scrubBytes = 0;
+        LFM_CUDA(cudaMalloc(&s->scrub, bytes));
+        s->scrubBytes = bytes;
+    }
+    LFM_CUDA(cudaMemsetAsync(s->scrub, 0x5a, bytes, s->stream));
+    return LFM_OK;
+}
+
+extern "C" int lfm_solver_bench(lfm_solver* s, int nsteps, double dt, size_t flush_bytes, float* ms) {
+    if (!s || !ms || nsteps <= 0) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    LFM_CUDA(cudaSetDevice(s->device));
+    int rc = ensureGraph(s, dt);
+    if (rc) return rc;
+    if (flush_bytes > s->scrubBytes) {
+        if (s->scrub) cudaFree(s->scrub);
+        s->scrub = nullptr;
+        s->scrubBytes = 0;
+        LFM_CUDA(cudaMalloc(&s->scrub, flush_bytes));
+        s->scrubBytes = flush_bytes;
+    }
+    std::vector<cudaEvent_t> ev(2 * (size_t)nsteps);
+    for (auto& x : ev) LFM_CUDA(cudaEventCreate(&x));
+    for (int k = 0; k < nsteps; ++k) {
+        if (flush_bytes) LFM_CUDA(cudaMemsetAsync(s->scrub, 0x5a + (k & 1), flush_bytes, s->stream));
+        LFM_CUDA(cudaEventRecord(ev[2 * (size_t)k], s->stream));
+        LFM_CUDA(cudaGraphLaunch(s->graph, s->stream));
+        LFM_CUDA(cudaEventRecord(ev[2 * (size_t)k + 1], s->stream));
+    }
+    LFM_CUDA(cudaStreamSynchronize(s->stream));
+    for (int k = 0; k < nsteps; ++k) LFM_CUDA(cudaEventElapsedTime(&ms[k], ev[2 * (size_t)k], ev[2 * (size_t)k + 1]));
+    for (auto& x : ev) cudaEventDestroy(x);
     return LFM_OK;
 }
 

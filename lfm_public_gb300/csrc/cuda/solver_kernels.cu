@@ -500,38 +500,33 @@ __global__ void __launch_bounds__(128) k_flux(Args<T> a) {
 // ---------------------------------------------------------------------------
 // k_update: gather, sponge, RK update.
 // ---------------------------------------------------------------------------
-template <typename T, int D>
-__global__ void __launch_bounds__(256) k_update(Args<T> a, double Ak, double Bk, double dt, int first, int withRes) {
+// The face rhs are summed per cell in the flux arithmetic T, in ascending face
+// order (the order in which the reference's scatter reaches the cell); the
+// sum is the cell residual RES. The RK register update is FP64.
+template <typename T, int D, bool RES>
+__global__ void __launch_bounds__(256) k_update(Args<T> a, double Ak, double Bk, double dt, int first) {
     const int c = LFM_GLOBAL_ID();
     if (c >= a.nc) return;
     constexpr int NQ = D + 2;
     const size_t nt = (size_t)a.nt, nf = (size_t)a.nf, nc = (size_t)a.nc;
-    double acc[NQ], res[NQ];
+    T sum[NQ];
 #pragma unroll
-    for (int v = 0; v < NQ; ++v) {
-        acc[v] = first ? 0.0 : Ak * a.dq[v * nc + c];
-        res[v] = 0.0;
-    }
-    const double vi = a.volInv[c];
+    for (int v = 0; v < NQ; ++v) sum[v] = T(0);
     for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
         const int code = a.cfList[e];
         if (code >= 0) {
 #pragma unroll
-            for (int v = 0; v < NQ; ++v) {
-                const double r = (double)a.flux[v * nf + code];
-                acc[v] += dt * r * vi;
-                res[v] += r;
-            }
+            for (int v = 0; v < NQ; ++v) sum[v] += a.flux[v * nf + code];
         } else {
             const int f = ~code;
 #pragma unroll
-            for (int v = 0; v < NQ; ++v) {
-                const double r = (double)a.flux[v * nf + f];
-                acc[v] -= dt * r * vi;
-                res[v] -= r;
-            }
+            for (int v = 0; v < NQ; ++v) sum[v] -= a.flux[v * nf + f];
         }
     }
+    const double dtvi = dt * a.volInv[c];
+    double acc[NQ];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) acc[v] = (first ? 0.0 : Ak * a.dq[v * nc + c]) + dtvi * (double)sum[v];
     double qv[NQ];
 #pragma unroll
     for (int v = 0; v < NQ; ++v) qv[v] = a.q[v * nt + c];
@@ -549,7 +544,7 @@ __global__ void __launch_bounds__(256) k_update(Args<T> a, double Ak, double Bk,
         const double qn = qv[v] + Bk * acc[v];
         finite = finite && isfinite(qn);
         a.q[v * nt + c] = qn;
-        if (withRes) a.res[v * nc + c] = res[v];
+        if (RES) a.res[v * nc + c] = (double)sum[v];
     }
     if (!finite) atomicOr(a.flag, 1);
 }
@@ -650,7 +645,10 @@ void launch_stage_t(const Args<T>& a, const StageConfig& s, cudaStream_t st) {
         case kSchemeM2: k_flux<T, D, kSchemeM2><<<blocks(a.nf, 128), 128, 0, st>>>(a); break;
         default: k_flux<T, D, kSchemeAUSM><<<blocks(a.nf, 128), 128, 0, st>>>(a); break;
     }
-    k_update<T, D><<<blocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, s.first, s.withRes);
+    if (s.withRes)
+        k_update<T, D, true><<<blocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
+    else
+        k_update<T, D, false><<<blocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
 }
 
 template <typename T>
@@ -695,8 +693,13 @@ void launch_kernel(const Args<T>& a, const StageConfig& s, int which, cudaStream
             break;
         }
         case 4:
-            if (d2) k_update<T, 2><<<blocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, s.first, s.withRes);
-            else k_update<T, 3><<<blocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, s.first, s.withRes);
+            if (d2) {
+                if (s.withRes) k_update<T, 2, true><<<blocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
+                else k_update<T, 2, false><<<blocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
+            } else {
+                if (s.withRes) k_update<T, 3, true><<<blocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
+                else k_update<T, 3, false><<<blocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
+            }
             break;
         default:
             break;

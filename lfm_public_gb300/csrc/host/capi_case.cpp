@@ -171,51 +171,7 @@ extern "C" int lfm_case_from_polymesh(const lfm_polymesh* mesh, const lfm_params
 
 extern "C" int lfm_case_describe(const lfm_case* c, lfm_solver_desc* d) {
     if (!c || !d) return lfm::setError(LFM_ERR_INVALID, "lfm_case_describe: null argument");
-    const lfm::SolverCase& s = c->sc;
-    std::memset(d, 0, sizeof(*d));
-    d->dim = s.dim;
-    d->nq = s.nq;
-    d->solver = s.solver;
-    d->rk_order = s.rkOrder;
-    d->minmod = s.minmod;
-    d->residuals = s.residuals;
-    d->n_cells = s.nCells;
-    d->n_cells0 = s.nCells0;
-    d->n_ghosts = s.nGhosts;
-    d->n_faces = s.nFaces;
-    d->face_p = s.faceP.data();
-    d->face_n = s.faceN.data();
-    d->face_ghost = s.faceGhost.data();
-    d->S = s.S.data();
-    d->d = s.d.data();
-    d->w = s.w.data();
-    d->smag = s.Smag.data();
-    d->dmag_inv = s.dmagInv.data();
-    d->dnorm = s.dnorm.data();
-    d->delta_mag = s.deltaMag.data();
-    d->K = s.K.data();
-    d->vol_inv = s.volInv.data();
-    d->sponge = s.sponge.data();
-    d->ghost_cell = s.ghostCell.data();
-    d->ghost_kind = s.ghostKind.data();
-    d->cell_face_offsets = s.cellFaceOffsets.data();
-    d->cell_faces = s.cellFaces.data();
-    d->cell_face_sign = s.cellFaceSign.data();
-    d->cell_s_offsets = s.cellSOffsets.data();
-    d->cell_s = s.cellS.data();
-    d->q0 = s.q0.data();
-    d->gamma = s.gamma;
-    d->Rgas = s.Rgas;
-    d->rhoInf = s.rhoInf;
-    d->EInf = s.EInf;
-    d->pInf = s.pInf;
-    d->TInf = s.TInf;
-    for (int k = 0; k < 3; ++k) d->UInf[k] = s.UInf[k];
-    d->mu = s.mu;
-    d->Cp = s.Cp;
-    d->PrInv = s.PrInv;
-    d->rkA = s.rkA.data();
-    d->rkB = s.rkB.data();
+    lfm::describeSolverCase(c->sc, d);
     return LFM_OK;
 }
 

@@ -20,6 +20,7 @@
 #include <vector>
 
 class IMeshReader;
+struct lfm_solver_desc;
 
 namespace lfm {
 
@@ -87,6 +88,9 @@ struct SolverCase {
 // Builds the case from a mesh reader that already holds the fields p, T, U and
 // (when Ls > 0) alpha at the start time. Throws std::runtime_error on bad input.
 SolverCase buildSolverCase(IMeshReader& reader, const CaseParams& params);
+
+// Fills the flattened C description with pointers into `sc` (valid while sc lives).
+void describeSolverCase(const SolverCase& sc, lfm_solver_desc* out);
 
 // RK coefficients for rkOrder (src/cfd_v0.cpp:86-128).
 void rkCoefficients(int rkOrder, std::vector<double>& A, std::vector<double>& B);

@@ -1,0 +1,126 @@
+"""Generates the golden fixtures of tests/golden/ by running the reference.
+
+Each fixture is a small synthetic case (mesh, initial fields, dictionary
+values) together with the fields the reference solver wrote after n_steps
+time steps: rho, U, E, p per polyMesh cell, and the CFL it printed. The
+reference is built from its own sources by oracle/Makefile (oracle/_ref/
+lfm_oracle); this script only runs where those sources exist. Run from the
+repository root:
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import re
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from lfm_public_gb300 import cases  # noqa: E402
+
+ORACLE = os.path.join(ROOT, "oracle", "_ref", "lfm_oracle")
+
+# name -> (generator, kwargs, n_steps)
+FIXTURES = {
+    "vortex16_m1_visc": (cases.vortex_case, dict(n=16, mu=1e-3), 20),
+    "vortex16_m2": (cases.vortex_case, dict(n=16, solver=1), 20),
+    "vortex12x20_m1_res": (cases.vortex_case, dict(n=12, ny=20, mu=2e-3, beta=3.0), 20),
+    "cyl24x12_m1_minmod": (cases.cylinder_case, dict(n_theta=24, n_r=12, r1=10, first=0.05, Ls=3, solver=0,
+                                                     minmod=True), 20),
+    "cyl24x12_m2": (cases.cylinder_case, dict(n_theta=24, n_r=12, r1=10, first=0.05, Ls=3, solver=1,
+                                              minmod=True, noise=0.02), 20),
+    "cyl24x12_ausm_minmod": (cases.cylinder_case, dict(n_theta=24, n_r=12, r1=10, first=0.05, Ls=3, solver=2,
+                                                       minmod=True, noise=0.02), 20),
+    "cyl24x12_ausm_nominmod": (cases.cylinder_case, dict(n_theta=24, n_r=12, r1=10, first=0.05, Ls=3, solver=2,
+                                                         minmod=False, noise=0.02), 20),
+    "cyl16x8x4_m2_3d": (cases.cylinder_case, dict(n_theta=16, n_r=8, r1=10, first=0.05, Ls=3, solver=1, n_span=4,
+                                                  noise=0.01), 10),
+    "cyl16x8x4_m1_3d": (cases.cylinder_case, dict(n_theta=16, n_r=8, r1=10, first=0.05, Ls=3, solver=0, n_span=4,
+                                                  noise=0.01), 10),
+    "cyl16x8x4_ausm_3d": (cases.cylinder_case, dict(n_theta=16, n_r=8, r1=10, first=0.05, Ls=3, solver=2, n_span=4,
+                                                    noise=0.01), 10),
+    "tri8_m1": (cases.tri_case, dict(n=8, seed=3), 20),
+    "tri8_m2": (cases.tri_case, dict(n=8, seed=4, solver=1), 20),
+}
+
+
+def case_to_arrays(case: cases.Case) -> dict:
+    out = dict(points=case.points, face_offsets=case.face_offsets, face_points=case.face_points,
+               owner=case.owner, neighbour=case.neighbour, n_cells=np.int64(case.n_cells),
+               cell_centres=case.cell_centres, dim=np.int64(case.dim),
+               patch_names=np.array([p.name for p in case.patches]),
+               patch_types=np.array([p.type for p in case.patches]),
+               patch_start=np.array([p.start for p in case.patches], dtype=np.int64),
+               patch_size=np.array([p.size for p in case.patches], dtype=np.int64),
+               patch_neighbour=np.array([p.neighbour or "" for p in case.patches]))
+    for k, v in case.fields.items():
+        out["field_" + k] = v
+    for k in ("solver", "rk_order", "minmod", "residuals", "p_inf", "T_inf", "Ls", "mach", "k_sponge", "Cp",
+              "mol_weight", "mu", "Pr", "delta_t"):
+        out["param_" + k] = np.float64(getattr(case, k))
+    out["param_U_inf"] = np.array(case.U_inf, dtype=np.float64)
+    return out
+
+
+def arrays_to_case(z) -> cases.Case:
+    patches = [cases.Patch(str(n), str(t), int(s), int(z_), (str(nb) or None))
+               for n, t, s, z_, nb in zip(z["patch_names"], z["patch_types"], z["patch_start"], z["patch_size"],
+                                          z["patch_neighbour"])]
+    c = cases.Case(name="golden", dim=int(z["dim"]), points=z["points"], face_offsets=z["face_offsets"],
+                   face_points=z["face_points"], owner=z["owner"], neighbour=z["neighbour"], patches=patches,
+                   n_cells=int(z["n_cells"]), cell_centres=z["cell_centres"])
+    c.fields = {k[6:]: z[k] for k in z.files if k.startswith("field_")}
+    for k in ("solver", "rk_order"):
+        setattr(c, k, int(z["param_" + k]))
+    for k in ("minmod", "residuals"):
+        setattr(c, k, bool(z["param_" + k]))
+    for k in ("p_inf", "T_inf", "Ls", "mach", "k_sponge", "Cp", "mol_weight", "mu", "Pr", "delta_t"):
+        setattr(c, k, float(z["param_" + k]))
+    c.U_inf = tuple(float(x) for x in z["param_U_inf"])
+    return c
+
+
+def run_reference(case: cases.Case, n_steps: int, workdir: str):
+    cases.write_case(case, workdir, n_steps=n_steps)
+    # print the CFL once, at the last step
+    cd = os.path.join(workdir, "system", "controlDict")
+    txt = open(cd).read().replace(f"printInfoFreq   {case.print_freq}", f"printInfoFreq   {n_steps}")
+    open(cd, "w").write(txt)
+    r = subprocess.run([ORACLE], cwd=workdir, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference run failed:\n" + r.stdout[-3000:] + r.stderr[-3000:])
+    m = re.findall(r"CFL:\s*([0-9eE+\-.]+)", r.stdout)
+    cfl = float(m[-1]) if m else float("nan")
+    return cases.read_result_fields(workdir), cfl, r.stdout
+
+
+def main():
+    if not os.path.exists(ORACLE):
+        raise SystemExit(f"{ORACLE} is missing: run `make -C oracle` where the reference sources exist")
+    for name, (gen, kw, n) in FIXTURES.items():
+        case = gen(n_steps=n, **kw)
+        if name.endswith("_res"):
+            case.residuals = True
+        tmp = tempfile.mkdtemp(prefix="lfm_golden_")
+        try:
+            res, cfl, _ = run_reference(case, n, tmp)
+        finally:
+            shutil.rmtree(tmp, ignore_errors=True)
+        arrs = case_to_arrays(case)
+        arrs.update({f"ref_{k}": v for k, v in res.items()})
+        arrs["ref_cfl"] = np.float64(cfl)
+        arrs["n_steps"] = np.int64(n)
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrs)
+        print(f"{name}: {case.n_cells} cells, {n} steps, CFL {cfl}")
+
+
+if __name__ == "__main__":
+    main()

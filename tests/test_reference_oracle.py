@@ -1,0 +1,52 @@
+"""The oracle port against the reference solver run here on fresh cases.
+
+Needs oracle/_ref/lfm_oracle, which is built from the reference's own sources
+(oracle/Makefile); skipped where those sources are not present.
+"""
+import os
+import shutil
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from lfm_public_gb300 import _native as N, cases
+from tests.helpers import primitives
+
+ORACLE = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref", "lfm_oracle")
+
+pytestmark = pytest.mark.skipif(not os.path.exists(ORACLE), reason="reference oracle not built on this machine")
+
+
+def _run_both(case, n):
+    tmp = tempfile.mkdtemp(prefix="lfm_ref_")
+    try:
+        cases.write_case(case, tmp, n_steps=n)
+        r = subprocess.run([ORACLE], cwd=tmp, capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr[-2000:]
+        ref = cases.read_result_fields(tmp)
+        ch = N.CaseHandle.open(tmp)   # the file route: plugins read the case directory
+        q, _ = N.port_run(ch, ch.q0(), n, ch.time()["delta_t"])
+        return ch, q, ref
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+
+
+@pytest.mark.parametrize("seed", [11, 12])
+def test_random_triangulation_bitwise(seed):
+    case = cases.tri_case(n=6, seed=seed, solver=seed % 2, beta=2.0 + seed % 3)
+    ch, q, ref = _run_both(case, 5)
+    ids = ch.cell_ids()
+    r, U, E, p = primitives(q, ch.desc.gamma, 2)
+    assert np.array_equal(r, ref["rho"][ids]) and np.array_equal(p, ref["p"][ids])
+
+
+def test_viscous_cylinder_ausm_bitwise():
+    case = cases.cylinder_case(n_theta=20, n_r=10, r1=8, first=0.05, Ls=2, solver=2, minmod=True, noise=0.05,
+                               seed=5, reynolds=40.0)
+    ch, q, ref = _run_both(case, 6)
+    ids = ch.cell_ids()
+    r, U, E, p = primitives(q, ch.desc.gamma, 2)
+    assert np.array_equal(r, ref["rho"][ids]) and np.array_equal(E, ref["E"][ids])
+    assert np.array_equal(U, ref["U"][ids][:, :2].T)

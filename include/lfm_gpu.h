@@ -190,6 +190,11 @@ int lfm_solver_min_dt(lfm_solver* s, double max_co, double* dt);
  * per conserved variable ([nq]); requires desc->residuals. */
 int lfm_solver_residual(lfm_solver* s, double* res);
 
+/* Per-cell stage-0 residual of the last time step, sum over the cell's faces
+ * of the face rhs ([nq][n_cells], solver order): the RES of
+ * updateSolutionResidual (src/cfd_v0.cpp:2973-2993). Requires desc->residuals. */
+int lfm_solver_cell_residual(lfm_solver* s, double* res);
+
 /* Blocks until all work on the solver stream has finished and reports the
  * first CUDA or numeric error. */
 int lfm_solver_sync(lfm_solver* s);

@@ -106,6 +106,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "lfm_solver_cfl": ([vp, C.c_double, _dp], C.c_int),
         "lfm_solver_min_dt": ([vp, C.c_double, _dp], C.c_int),
         "lfm_solver_residual": ([vp, _dp], C.c_int),
+        "lfm_solver_cell_residual": ([vp, _dp], C.c_int),
         "lfm_solver_sync": ([vp], C.c_int),
         "lfm_solver_launches_per_step": ([vp, C.POINTER(C.c_int)], C.c_int),
         "lfm_solver_flush_l2": ([vp, C.c_size_t], C.c_int),
@@ -131,6 +132,8 @@ def load_port(path: str = PORT_PATH) -> C.CDLL:
     lib = C.CDLL(path)
     lib.lfm_port_run.argtypes = [C.POINTER(SolverDesc), _dp, C.c_int, C.c_double, _dp]
     lib.lfm_port_run.restype = C.c_int
+    lib.lfm_port_run_cell_residual.argtypes = [C.POINTER(SolverDesc), _dp, C.c_int, C.c_double, _dp]
+    lib.lfm_port_run_cell_residual.restype = C.c_int
     lib.lfm_port_cfl.argtypes = [C.POINTER(SolverDesc), _dp, C.c_double, _dp]
     lib.lfm_port_cfl.restype = C.c_int
     lib.lfm_port_min_dt.argtypes = [C.POINTER(SolverDesc), _dp, C.c_double, _dp]
@@ -294,6 +297,11 @@ class Solver:
     def flush_l2(self, nbytes: int = 512 << 20):
         check(load_library().lfm_solver_flush_l2(self._h, nbytes))
 
+    def cell_residual(self) -> np.ndarray:
+        out = np.empty((self.nq, self.n_cells), dtype=np.float64)
+        check(load_library().lfm_solver_cell_residual(self._h, _ptr(out, C.c_double)))
+        return out
+
     def launches_per_step(self) -> int:
         v = C.c_int()
         check(load_library().lfm_solver_launches_per_step(self._h, C.byref(v)))
@@ -328,6 +336,17 @@ def port_run(case: CaseHandle, q: np.ndarray, nsteps: int, dt: float, residual: 
     if rc != 0:
         raise RuntimeError(f"oracle port failed with {rc}")
     return qq, (res if residual else None)
+
+
+def port_cell_residual(case: CaseHandle, q: np.ndarray, nsteps: int, dt: float):
+    """Oracle port: (q after nsteps, per-cell stage-0 residual of the last step)."""
+    qq = np.ascontiguousarray(q, dtype=np.float64).copy()
+    res = np.zeros((case.desc.nq, case.desc.n_cells))
+    rc = load_port().lfm_port_run_cell_residual(C.byref(case.desc), _ptr(qq, C.c_double), nsteps, dt,
+                                                 _ptr(res, C.c_double))
+    if rc != 0:
+        raise RuntimeError(f"oracle port failed with {rc}")
+    return qq, res
 
 
 def port_cfl(case: CaseHandle, q: np.ndarray, dt: float) -> float:

@@ -640,8 +640,8 @@ def write_case(case: Case, root: str, n_steps: Optional[int] = None, write_inter
     return root
 
 
-def read_result_fields(root: str):
-    """Reads rho, U, E, p of the latest time directory written by a run."""
+def read_result_fields(root: str, names=("rho", "E", "p", "U")):
+    """Reads fields (default rho, U, E, p) of the latest time directory written by a run."""
     times = []
     for name in os.listdir(root):
         try:
@@ -654,7 +654,7 @@ def read_result_fields(root: str):
         raise FileNotFoundError(f"no result time directory under {root}")
     tdir = os.path.join(root, max(times)[1])
     out = {}
-    for name in ("rho", "E", "p", "U"):
+    for name in names:
         out[name] = _read_internal_field(os.path.join(tdir, name))
     return out
 

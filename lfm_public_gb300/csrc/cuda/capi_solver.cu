@@ -443,6 +443,16 @@ extern "C" int lfm_solver_residual(lfm_solver* s, double* res) {
     return LFM_OK;
 }
 
+extern "C" int lfm_solver_cell_residual(lfm_solver* s, double* res) {
+    if (!s || !res) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    if (!s->residuals) return lfm::setError(LFM_ERR_INVALID, "the case does not record residuals");
+    LFM_CUDA(cudaSetDevice(s->device));
+    LFM_CUDA(cudaMemcpyAsync(res, s->res, sizeof(double) * (size_t)s->nq * (size_t)s->nc, cudaMemcpyDeviceToHost,
+                             s->stream));
+    LFM_CUDA(cudaStreamSynchronize(s->stream));
+    return LFM_OK;
+}
+
 extern "C" int lfm_solver_sync(lfm_solver* s) {
     if (!s) return lfm::setError(LFM_ERR_INVALID, "null solver");
     LFM_CUDA(cudaSetDevice(s->device));

@@ -120,6 +120,13 @@ void GpuMesh::solve() {
     m_pMeshReader->createScalarField("rho");
     m_pMeshReader->createScalarField("E");
     m_pMeshReader->createScalarField("p");
+    static const char* resNames[] = {"uRES", "vRES", "wRES"};
+    const bool saveRes = m_pInput->m_bHaveResidual && m_pInput->m_bSaveResiduals;
+    if (saveRes) {
+        m_pMeshReader->createScalarField("rhoRES");
+        m_pMeshReader->createScalarField("eRES");
+        for (int d = 0; d < c.dim; ++d) m_pMeshReader->createScalarField(resNames[d]);
+    }
     if (m_pInput->m_bSaveBlendFactor) {
         const int idx = m_pMeshReader->createScalarField("sigma0");
         for (size_t i = 0; i < c.cellId.size(); ++i)
@@ -176,6 +183,23 @@ void GpuMesh::solve() {
         }
         if (m_pRunTime->isWriteTime()) {
             const auto b = std::chrono::steady_clock::now();
+            if (saveRes) {
+                // updateSolutionResidual (src/cfd_v0.cpp:2973-2993)
+                const size_t nc = (size_t)c.nCells;
+                std::vector<double> cr((size_t)c.nq * nc);
+                if (lfm_solver_cell_residual(m_pSolver, cr.data()) != LFM_OK)
+                    throw std::runtime_error(lfm_last_error());
+                const int iR = m_pMeshReader->getScalarFieldIndex("rhoRES");
+                const int iE = m_pMeshReader->getScalarFieldIndex("eRES");
+                for (size_t i = 0; i < nc; ++i) {
+                    const int cell = (int)c.cellId[i];
+                    m_pMeshReader->updateScalarField(iR, cr[i], cell);
+                    for (int d = 0; d < c.dim; ++d)
+                        m_pMeshReader->updateScalarField(m_pMeshReader->getScalarFieldIndex(resNames[d]),
+                                                         cr[(size_t)(d + 1) * nc + i], cell);
+                    m_pMeshReader->updateScalarField(iE, cr[(size_t)(c.dim + 1) * nc + i], cell);
+                }
+            }
             updateSolution();
             m_pRunTime->writeResults();
             outputTime += std::chrono::duration<double>(std::chrono::steady_clock::now() - b).count();

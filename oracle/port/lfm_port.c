@@ -537,7 +537,8 @@ static void port_free(Port* P) {
     free(P->faceStart);
 }
 
-int lfm_port_run(const lfm_solver_desc* c, double* q, int nsteps, double dt, double* residual) {
+static int port_run(const lfm_solver_desc* c, double* q, int nsteps, double dt, double* residual,
+                    double* cell_res) {
     Port P;
     if (!c || !q || c->dim < 2 || c->dim > 3) return -1;
     if (port_init(&P, c) != 0) {
@@ -572,10 +573,21 @@ int lfm_port_run(const lfm_solver_desc* c, double* q, int nsteps, double dt, dou
                 residual[v] = s;
             }
         }
+        if (cell_res && c->residuals)
+            for (int v = 0; v < nq; ++v)
+                memcpy(&cell_res[(int64_t)v * nc], &P.res[(int64_t)v * nt], (size_t)nc * sizeof(double));
     }
     for (int v = 0; v < nq; ++v) memcpy(&q[(int64_t)v * nc], &P.q[(int64_t)v * nt], (size_t)nc * sizeof(double));
     port_free(&P);
     return 0;
+}
+
+int lfm_port_run(const lfm_solver_desc* c, double* q, int nsteps, double dt, double* residual) {
+    return port_run(c, q, nsteps, dt, residual, NULL);
+}
+
+int lfm_port_run_cell_residual(const lfm_solver_desc* c, double* q, int nsteps, double dt, double* cell_res) {
+    return port_run(c, q, nsteps, dt, NULL, cell_res);
 }
 
 int lfm_port_cfl(const lfm_solver_desc* c, const double* q, double dt, double* cfl_out) {

@@ -14,6 +14,9 @@ extern "C" {
  * residual (optional, [nq]) receives the last step's summed squared residual
  * when desc->residuals is set. Returns 0 on success. */
 int lfm_port_run(const lfm_solver_desc* desc, double* q, int nsteps, double dt, double* residual);
+/* As lfm_port_run; cell_res ([nq][n_cells]) receives the per-cell stage-0
+ * residual (the reference's RES) of the last step when desc->residuals is set. */
+int lfm_port_run_cell_residual(const lfm_solver_desc* desc, double* q, int nsteps, double dt, double* cell_res);
 /* compute_cfl / compute_dt of the reference for state q. */
 int lfm_port_cfl(const lfm_solver_desc* desc, const double* q, double dt, double* cfl);
 int lfm_port_min_dt(const lfm_solver_desc* desc, const double* q, double max_co, double* dt);

@@ -93,13 +93,19 @@ def run_reference(case: cases.Case, n_steps: int, workdir: str):
     # print the CFL once, at the last step
     cd = os.path.join(workdir, "system", "controlDict")
     txt = open(cd).read().replace(f"printInfoFreq   {case.print_freq}", f"printInfoFreq   {n_steps}")
+    if case.residuals:
+        txt = txt.replace("saveResiduals   false", "saveResiduals   true")
     open(cd, "w").write(txt)
     r = subprocess.run([ORACLE], cwd=workdir, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("reference run failed:\n" + r.stdout[-3000:] + r.stderr[-3000:])
     m = re.findall(r"CFL:\s*([0-9eE+\-.]+)", r.stdout)
     cfl = float(m[-1]) if m else float("nan")
-    return cases.read_result_fields(workdir), cfl, r.stdout
+    fields = cases.read_result_fields(workdir)
+    if case.residuals:
+        fields.update(cases.read_result_fields(workdir, names=["rhoRES", "uRES", "vRES", "eRES"][:case.dim + 2]
+                                               if case.dim == 2 else ["rhoRES", "uRES", "vRES", "wRES", "eRES"]))
+    return fields, cfl, r.stdout
 
 
 def main():

@@ -110,3 +110,14 @@ def test_full_size_cylinder_matches_oracle():
     q_gpu = _gpu_run(ch, 2, case.delta_t)
     q_ref, _ = N.port_run(ch, ch.q0(), 2, case.delta_t)
     assert np.all(rel_l2(q_gpu, q_ref) <= TOL), rel_l2(q_gpu, q_ref)
+
+
+def test_cell_residual_matches_reference_fixture():
+    case, z = load_golden("vortex12x20_m1_res")
+    ch = N.CaseHandle.from_case(case)
+    s = N.Solver(ch)
+    s.step(int(z["n_steps"]), case.delta_t)
+    res = s.cell_residual()
+    ids = ch.cell_ids()
+    ref = np.vstack([z["ref_" + n][ids] for n in ("rhoRES", "uRES", "vRES", "eRES")])
+    assert np.all(rel_l2(res, ref) <= 1e-10), rel_l2(res, ref)

@@ -195,6 +195,29 @@ int lfm_solver_residual(lfm_solver* s, double* res);
  * updateSolutionResidual (src/cfd_v0.cpp:2973-2993). Requires desc->residuals. */
 int lfm_solver_cell_residual(lfm_solver* s, double* res);
 
+/* Cell residuals of a caller-supplied state without allocating anything.
+ * This entry point has no counterpart in the reference. It is for callers
+ * that must not allocate device memory at the time of the call: code running
+ * while a CUDA graph is being captured, allocator-free real-time or serving
+ * loops, and hosts whose device memory is owned by another runtime.
+ *
+ * q:   device pointer, [nq][q_stride] doubles (cells 0..n_cells-1 in solver
+ *      order); read only.
+ * res: device pointer, [nq][n_cells] doubles; receives, per cell, the sum over
+ *      its faces of the face rhs for state q - the quantity that
+ *      lfm_solver_cell_residual reports for the state at the start of a step.
+ * stream: cudaStream_t to run on (NULL: the legacy default stream).
+ * The solver handle supplies the geometry already on the device; its own
+ * buffers and stream are not touched. Scratch (ghost states, primitives,
+ * viscous terms, face rhs) lives in one static device array of
+ * LFM_NOALLOC_SCRATCH_BYTES per GPU, held from the library's load until the
+ * process exits; cases that need more return LFM_ERR_UNSUPPORTED. The first
+ * call on a device looks up that array's device address (set-up), so make it
+ * before any stream capture. All calls share the array: calls whose work
+ * overlaps on the GPU race with each other. */
+#define LFM_NOALLOC_SCRATCH_BYTES (32u << 20)
+int lfm_solver_residual_noalloc(const lfm_solver* s, const double* q, int64_t q_stride, double* res, void* stream);
+
 /* Blocks until all work on the solver stream has finished and reports the
  * first CUDA or numeric error. */
 int lfm_solver_sync(lfm_solver* s);

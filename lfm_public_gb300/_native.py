@@ -107,6 +107,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "lfm_solver_min_dt": ([vp, C.c_double, _dp], C.c_int),
         "lfm_solver_residual": ([vp, _dp], C.c_int),
         "lfm_solver_cell_residual": ([vp, _dp], C.c_int),
+        "lfm_solver_residual_noalloc": ([vp, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p], C.c_int),
         "lfm_solver_sync": ([vp], C.c_int),
         "lfm_solver_launches_per_step": ([vp, C.POINTER(C.c_int)], C.c_int),
         "lfm_solver_flush_l2": ([vp, C.c_size_t], C.c_int),

@@ -5,6 +5,7 @@
 // replayed; the graph is captured again only when dt changes.
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -451,6 +452,114 @@ extern "C" int lfm_solver_cell_residual(lfm_solver* s, double* res) {
                              s->stream));
     LFM_CUDA(cudaStreamSynchronize(s->stream));
     return LFM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Residual without allocation: scratch in a static device array.
+// ---------------------------------------------------------------------------
+namespace {
+
+__device__ __align__(256) unsigned char g_noallocScratch[LFM_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noallocMutex;
+void* g_noallocAddr[kMaxDevices] = {};
+
+// Device address of the scratch array on `device` (current), looked up once.
+int noallocScratch(int device, unsigned char** out) {
+    if (device < 0 || device >= kMaxDevices) return lfm::setError(LFM_ERR_UNSUPPORTED, "device ordinal too large");
+    std::lock_guard<std::mutex> lock(g_noallocMutex);
+    if (!g_noallocAddr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
+        if (e != cudaSuccess || !p) return cudaFail(e, "cudaGetSymbolAddress(g_noallocScratch)");
+        g_noallocAddr[device] = p;
+    }
+    *out = static_cast<unsigned char*>(g_noallocAddr[device]);
+    return LFM_OK;
+}
+
+template <typename T, int D>
+__global__ void __launch_bounds__(256) k_gather_residual(const T* flux, int nf, int nc, const int* cfOff,
+                                                         const int* cfList, double* res) {
+    const int c = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (c >= nc) return;
+    constexpr int NQ = D + 2;
+    T sum[NQ];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) sum[v] = T(0);
+    for (int e = cfOff[c]; e < cfOff[c + 1]; ++e) {
+        const int code = cfList[e];
+        if (code >= 0) {
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) sum[v] += flux[(size_t)v * nf + code];
+        } else {
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) sum[v] -= flux[(size_t)v * nf + ~code];
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) res[(size_t)v * nc + c] = (double)sum[v];
+}
+
+template <typename T>
+int residualNoalloc(const lfm_solver* s, const Args<T>& base, const double* q, int64_t qStride, double* res,
+                    cudaStream_t st) {
+    const size_t nt = (size_t)s->nt, nf = (size_t)s->nf, D = (size_t)s->D, nq = (size_t)s->nq;
+    const bool ausm = s->scheme == LFM_SOLVER_M2AUSM;
+    auto round = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t bq = round(nq * nt * sizeof(double));
+    const size_t bPrim = round((D + 3) * nt * sizeof(T));
+    const size_t bV = round((2 * D * D + 2 * D) * nt * sizeof(T));
+    const size_t bGrad = ausm ? round((2 * D + D * D) * nt * sizeof(T)) : 0;
+    const size_t bFlux = round(nq * nf * sizeof(T));
+    const size_t need = bq + bPrim + bV + bGrad + bFlux;
+    if (need > LFM_NOALLOC_SCRATCH_BYTES)
+        return lfm::setError(LFM_ERR_UNSUPPORTED, "the case needs " + std::to_string(need) +
+                                                      " bytes of scratch; lfm_solver_residual_noalloc holds " +
+                                                      std::to_string((size_t)LFM_NOALLOC_SCRATCH_BYTES));
+    unsigned char* scratch = nullptr;
+    int rc = noallocScratch(s->device, &scratch);
+    if (rc) return rc;
+    Args<T> a = base;
+    a.q = reinterpret_cast<double*>(scratch);
+    a.prim = reinterpret_cast<T*>(scratch + bq);
+    a.V = reinterpret_cast<T*>(scratch + bq + bPrim);
+    a.grad = ausm ? reinterpret_cast<T*>(scratch + bq + bPrim + bV) : base.grad;
+    a.flux = reinterpret_cast<T*>(scratch + bq + bPrim + bV + bGrad);
+    a.dq = nullptr;
+    a.res = nullptr;
+    // The array keeps the previous call's contents: the viscous terms and
+    // gradients of the ghosts are read as zeros, so clear both blocks.
+    LFM_CUDA(cudaMemsetAsync(a.V, 0, bV, st));
+    if (ausm) LFM_CUDA(cudaMemsetAsync(a.grad, 0, bGrad, st));
+    for (size_t v = 0; v < nq; ++v)
+        LFM_CUDA(cudaMemcpyAsync(a.q + v * nt, q + (size_t)v * (size_t)qStride, (size_t)s->nc * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, st));
+    StageConfig c;
+    c.scheme = s->scheme;
+    c.needGrad = s->needGrad;
+    c.needVis = s->needVis;
+    for (int k = 0; k < 4; ++k) lfm::dev::launch_kernel<T>(a, c, k, st);   // prep, grad, vis, flux
+    const unsigned nb = (unsigned)((s->nc + 255) / 256);
+    if (s->D == 2)
+        k_gather_residual<T, 2><<<nb, 256, 0, st>>>(a.flux, s->nf, s->nc, a.cfOff, a.cfList, res);
+    else
+        k_gather_residual<T, 3><<<nb, 256, 0, st>>>(a.flux, s->nf, s->nc, a.cfOff, a.cfList, res);
+    LFM_CUDA(cudaGetLastError());
+    return LFM_OK;
+}
+
+}  // namespace
+
+extern "C" int lfm_solver_residual_noalloc(const lfm_solver* s, const double* q, int64_t q_stride, double* res,
+                                           void* stream) {
+    if (!s || !q || !res) return lfm::setError(LFM_ERR_INVALID, "lfm_solver_residual_noalloc: null argument");
+    if (q_stride < s->nc) return lfm::setError(LFM_ERR_INVALID, "q_stride is smaller than the cell count");
+    LFM_CUDA(cudaSetDevice(s->device));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (s->precision == LFM_FP32_BULK) return residualNoalloc<float>(s, s->a32, q, q_stride, res, st);
+    return residualNoalloc<double>(s, s->a64, q, q_stride, res, st);
 }
 
 extern "C" int lfm_solver_sync(lfm_solver* s) {

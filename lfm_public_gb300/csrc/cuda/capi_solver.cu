@@ -139,7 +139,7 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
     int rc;
     if ((rc = devAlloc(s, &a.dq, (size_t)s->nq * s->nc))) return rc;
     if ((rc = devAlloc(s, &a.prim, (D + 3) * nt))) return rc;
-    if ((rc = devAlloc(s, &a.V, (2 * D * D + 2 * D) * nt))) return rc;
+    if ((rc = devAlloc(s, &a.V, (D * D + 2 * D) * nt))) return rc;
     // M2AUSM always reads the gradients (all zero when minmod is off, as in the
     // reference, whose prepare_for_RKstep zeroes them every stage).
     if ((rc = devAlloc(s, &a.grad, (2 * D + D * D) * (s->scheme == LFM_SOLVER_M2AUSM ? nt : 1)))) return rc;
@@ -161,6 +161,12 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
     a.dmag = p;
     if ((rc = uploadAs<T>(s, &p, d->K, D * nf))) return rc;
     a.K = p;
+    {
+        std::vector<double> lapc(nf);
+        for (size_t f = 0; f < nf; ++f) lapc[f] = d->delta_mag[f] * d->dmag_inv[f];
+        if ((rc = uploadAs<T>(s, &p, lapc.data(), nf))) return rc;
+        a.lapc = p;
+    }
     return LFM_OK;
 }
 
@@ -510,7 +516,7 @@ int residualNoalloc(const lfm_solver* s, const Args<T>& base, const double* q, i
     auto round = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t bq = round(nq * nt * sizeof(double));
     const size_t bPrim = round((D + 3) * nt * sizeof(T));
-    const size_t bV = round((2 * D * D + 2 * D) * nt * sizeof(T));
+    const size_t bV = round((D * D + 2 * D) * nt * sizeof(T));
     const size_t bGrad = ausm ? round((2 * D + D * D) * nt * sizeof(T)) : 0;
     const size_t bFlux = round(nq * nf * sizeof(T));
     const size_t need = bq + bPrim + bV + bGrad + bFlux;

@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(256) k_grad(Args<T> a) {
 }
 
 // ---------------------------------------------------------------------------
-// k_vis: dudx, dTdx, tauMC, sigmaU per cell.
+// k_vis: dudx, dTdx and sigmaU per cell (tauMC is rebuilt per face from dudx).
 // ---------------------------------------------------------------------------
 template <typename T, int D>
 __global__ void __launch_bounds__(256) k_vis(Args<T> a) {
@@ -201,10 +201,6 @@ __global__ void __launch_bounds__(256) k_vis(Args<T> a) {
     const T mu = (T)a.mu;
     T tau[D][D];
     stress<T, D>(g, mu, tau);
-    T diagSum = T(0);
-#pragma unroll
-    for (int x = 0; x < D; ++x) diagSum -= g[x][x];
-    diagSum *= mu * T(2) / T(3);
     T U[D];
 #pragma unroll
     for (int k = 0; k < D; ++k) U[k] = a.prim[(size_t)(1 + k) * a.nt + c];
@@ -212,14 +208,9 @@ __global__ void __launch_bounds__(256) k_vis(Args<T> a) {
 #pragma unroll
     for (int x = 0; x < D; ++x) {
 #pragma unroll
-        for (int y = 0; y < D; ++y) {
-            a.V[(size_t)(x * D + y) * nt + c] = g[x][y];
-            T tm = mu * g[y][x];
-            if (x == y) tm += diagSum;
-            a.V[(size_t)(D * D + D + x * D + y) * nt + c] = tm;
-        }
+        for (int y = 0; y < D; ++y) a.V[(size_t)(x * D + y) * nt + c] = g[x][y];
         a.V[(size_t)(D * D + x) * nt + c] = gT[x];
-        a.V[(size_t)(2 * D * D + D + x) * nt + c] = dotv<T, D>(U, tau[x]);
+        a.V[(size_t)(D * D + D + x) * nt + c] = dotv<T, D>(U, tau[x]);
     }
 }
 
@@ -271,15 +262,12 @@ __global__ void __launch_bounds__(128) k_flux(Args<T> a) {
     const int i = a.fP[f], j = a.fN[f];
     const bool ghost = a.fGhost[f] != 0;
     const T w = a.w[f];
-    const T omw = T(1) - w;
-    T S[D], dn[D], Kf[D];
+    T S[D], Kf[D];
 #pragma unroll
     for (int k = 0; k < D; ++k) {
         S[k] = a.S[k * nf + f];
-        dn[k] = a.dnorm[k * nf + f];
         Kf[k] = a.K[k * nf + f];
     }
-    const T Smag = a.smag[f], dinv = a.dinv[f], dmag = a.dmag[f];
     T qi[NQ], qj[NQ];
 #pragma unroll
     for (int v = 0; v < NQ; ++v) {
@@ -294,68 +282,44 @@ __global__ void __launch_bounds__(128) k_flux(Args<T> a) {
         aU[k] = a.prim[(1 + k) * nt + j];
     }
     const T cRpsi = a.prim[(D + 1) * nt + i], aRpsi = a.prim[(D + 1) * nt + j];
-    const T cP = a.prim[(D + 2) * nt + i], cN = a.prim[(D + 2) * nt + j];
     const T Rinv = (T)a.Rinv;
     const T cT = cRpsi * Rinv, aT = aRpsi * Rinv;
     T rhs[NQ];
 
     if (SCH == kSchemeM1) {
-        // Kurganov-Tadmor central-upwind flux (src/cfd_v0.cpp:2588-2675)
-        const T rhoPos = interp(w, qi[0], qj[0]);
-        const T rhoNeg = interp(omw, qj[0], qi[0]);
-        const T rhoPos_inv = T(1) / rhoPos, rhoNeg_inv = T(1) / rhoNeg;
-        T rhoUPos[D], rhoUNeg[D], uPos[D], uNeg[D];
+        // One_rk_step_M1's Kurganov-Tadmor flux (src/cfd_v0.cpp:2588-2675)
+        // builds its "+" and "-" states with the same linear interpolation
+        // (w*P + (1-w)*N and (1-w)*N + w*P), so both states are equal, the
+        // dissipation terms (q- - q+)*psi+ psi-/(psi+ - psi-) vanish and the
+        // wave-speed weights cancel: the flux is the central flux of the
+        // interpolated state, F(q_f).S. It is evaluated in that form - one
+        // division per face instead of three, no sound speeds - and equals
+        // the reference's value up to rounding.
+        const T rho = interp(w, qi[0], qj[0]);
+        T m[D];
 #pragma unroll
-        for (int k = 0; k < D; ++k) {
-            rhoUPos[k] = interp(w, qi[k + 1], qj[k + 1]);
-            rhoUNeg[k] = interp(omw, qj[k + 1], qi[k + 1]);
-        }
+        for (int k = 0; k < D; ++k) m[k] = interp(w, qi[k + 1], qj[k + 1]);
         T ce = T(2) * qi[D + 1] * cri, ae = T(2) * qj[D + 1] * ari;
 #pragma unroll
         for (int k = 0; k < D; ++k) {
             ce -= cU[k] * cU[k];
             ae -= aU[k] * aU[k];
         }
-        ce *= T(0.5);
-        ae *= T(0.5);
-        const T ePos = interp(w, ce, ae), eNeg = interp(omw, ae, ce);
-        const T RpsiPos = interp(w, cRpsi, aRpsi), RpsiNeg = interp(omw, aRpsi, cRpsi);
-        const T pPos = rhoPos * RpsiPos, pNeg = rhoNeg * RpsiNeg;
-        const T cPos = interp(w, cP, cN), cNeg = interp(omw, cN, cP);
-        T phiPos = T(0), phiNeg = T(0);
+        const T e = T(0.5) * interp(w, ce, ae);          // internal energy per unit mass
+        const T Rpsi = interp(w, cRpsi, aRpsi);
+        const T rinv = T(1) / rho;
+        T mS = T(0), u2 = T(0);
 #pragma unroll
         for (int k = 0; k < D; ++k) {
-            uPos[k] = rhoUPos[k] * rhoPos_inv;
-            uNeg[k] = rhoUNeg[k] * rhoNeg_inv;
-            phiPos += uPos[k] * S[k];
-            phiNeg += -uNeg[k] * S[k];
+            mS += m[k] * S[k];
+            u2 += m[k] * m[k];
         }
-        T psiPos = phiPos + cPos * Smag;
-        const T b1 = -phiNeg + cNeg * Smag;
-        if (psiPos < b1) psiPos = b1;
-        if (psiPos < T(0)) psiPos = T(0);
-        T psiNeg = phiPos - cPos * Smag;
-        const T b2 = -phiNeg - cNeg * Smag;
-        if (b2 < psiNeg) psiNeg = b2;
-        if (T(0) < psiNeg) psiNeg = T(0);
-        const T a0 = T(1) / (psiPos - psiNeg);
-        const T a1 = psiPos * psiNeg;
-        const T aPos = psiPos * phiPos;
-        const T aNeg = psiNeg * phiNeg;
-        T rhoEPos = ePos, rhoENeg = eNeg;
+        const T phi = mS * rinv;                          // u_f . S
+        const T p = rho * Rpsi;
+        rhs[0] = -mS;
 #pragma unroll
-        for (int k = 0; k < D; ++k) {
-            rhoEPos += T(0.5) * uPos[k] * uPos[k];
-            rhoENeg += T(0.5) * uNeg[k] * uNeg[k];
-        }
-        rhoEPos *= rhoPos;
-        rhoENeg *= rhoNeg;
-        rhs[0] = -(aPos * rhoPos + aNeg * rhoNeg + (rhoNeg - rhoPos) * a1) * a0;
-        const T pface = (pPos * psiPos - pNeg * psiNeg) * a0;
-#pragma unroll
-        for (int k = 0; k < D; ++k)
-            rhs[k + 1] = -((aPos * rhoUPos[k] + aNeg * rhoUNeg[k] + (rhoUNeg[k] - rhoUPos[k]) * a1) * a0 + pface * S[k]);
-        rhs[D + 1] = -(aPos * rhoEPos + aNeg * rhoENeg + (rhoENeg - rhoEPos) * a1 + (aPos * pPos + aNeg * pNeg)) * a0;
+        for (int k = 0; k < D; ++k) rhs[k + 1] = -(m[k] * phi + p * S[k]);
+        rhs[D + 1] = -mS * (e + T(0.5) * u2 * (rinv * rinv) + Rpsi);
     } else {
         // Pirozzoli kinetic-energy-preserving mid-point flux (src/cfd_v0.cpp:1966-2023)
         const T rhoavg = T(0.5) * (qi[0] + qj[0]);
@@ -368,7 +332,7 @@ __global__ void __launch_bounds__(128) k_flux(Args<T> a) {
         if (SCH == kSchemeAUSM) {
             // shock sensor, minmod reconstructions and AUSM+ pressure
             // dissipation (src/cfd_v0.cpp:2288-2339)
-            const T cavg = T(0.5) * (cP + cN);
+            const T cavg = T(0.5) * (a.prim[(D + 2) * nt + i] + a.prim[(D + 2) * nt + j]);
             T d[D];
 #pragma unroll
             for (int k = 0; k < D; ++k) d[k] = a.d[k * nf + f];
@@ -447,50 +411,52 @@ __global__ void __launch_bounds__(128) k_flux(Args<T> a) {
     // is an exact zero and the block is skipped.
     const T mu = (T)a.mu;
     if (mu != T(0)) {
-        T g[D][D], gT[D], tau[D][D], tmc[D][D], sU[D];
+        const T lapc = a.lapc[f];   // |delta| / |d|
+        T g[D][D], gT[D], sU[D];
         if (!ghost) {
 #pragma unroll
             for (int x = 0; x < D; ++x) {
 #pragma unroll
-                for (int y = 0; y < D; ++y) {
-                    g[x][y] = interp(w, a.V[(x * D + y) * nt + i], a.V[(x * D + y) * nt + j]);
-                    tmc[x][y] = interp(w, a.V[(D * D + D + x * D + y) * nt + i], a.V[(D * D + D + x * D + y) * nt + j]);
-                }
+                for (int y = 0; y < D; ++y) g[x][y] = interp(w, a.V[(x * D + y) * nt + i], a.V[(x * D + y) * nt + j]);
                 gT[x] = interp(w, a.V[(D * D + x) * nt + i], a.V[(D * D + x) * nt + j]);
-                sU[x] = interp(w, a.V[(2 * D * D + D + x) * nt + i], a.V[(2 * D * D + D + x) * nt + j]);
+                sU[x] = interp(w, a.V[(D * D + D + x) * nt + i], a.V[(D * D + D + x) * nt + j]);
             }
         } else {
             // explicit two-point gradients on physical boundaries
+            const T dinv = a.dinv[f];
+            T dn[D], tau[D][D], Uf[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) dn[k] = a.dnorm[k * nf + f];
 #pragma unroll
             for (int x = 0; x < D; ++x) {
 #pragma unroll
                 for (int y = 0; y < D; ++y) g[x][y] = (aU[x] - cU[x]) * dn[y] * dinv;
                 gT[x] = (aT - cT) * dn[x] * dinv;
+                Uf[x] = interp(w, cU[x], aU[x]);
             }
             stress<T, D>(g, mu, tau);
-            T diagSum = T(0);
 #pragma unroll
-            for (int x = 0; x < D; ++x) diagSum -= g[x][x];
-            diagSum *= mu * T(2) / T(3);
-            T Uf[D];
-#pragma unroll
-            for (int x = 0; x < D; ++x) Uf[x] = interp(w, cU[x], aU[x]);
-#pragma unroll
-            for (int x = 0; x < D; ++x) {
-#pragma unroll
-                for (int y = 0; y < D; ++y) tmc[x][y] = mu * g[y][x];
-                tmc[x][x] += diagSum;
-                sU[x] = dotv<T, D>(Uf, tau[x]);
-            }
+            for (int x = 0; x < D; ++x) sU[x] = dotv<T, D>(Uf, tau[x]);
         }
+        // The face tauMC: the reference interpolates the cells' tauMC =
+        // mu dudx^T - (2/3) mu tr(dudx) I (and on boundary faces applies the
+        // same expression to the two-point gradient); it is linear in dudx,
+        // so it is rebuilt here from the face gradient g.
+        T tr = g[0][0];
+#pragma unroll
+        for (int x = 1; x < D; ++x) tr += g[x][x];
+        const T dsum = -(mu * T(2) / T(3)) * tr;
         const T kc = (T)a.kcond;
 #pragma unroll
         for (int x = 0; x < D; ++x) {
-            const T divTau = dotv<T, D>(tmc[x], S);
-            const T lap = mu * (dmag * (aU[x] - cU[x]) * dinv + dotv<T, D>(Kf, g[x]));
+            T gtS = g[0][x] * S[0];
+#pragma unroll
+            for (int y = 1; y < D; ++y) gtS += g[y][x] * S[y];
+            const T divTau = mu * gtS + dsum * S[x];
+            const T lap = mu * (lapc * (aU[x] - cU[x]) + dotv<T, D>(Kf, g[x]));
             rhs[x + 1] += divTau + lap;
         }
-        const T lapT = kc * (dmag * (aT - cT) * dinv + dotv<T, D>(Kf, gT));
+        const T lapT = kc * (lapc * (aT - cT) + dotv<T, D>(Kf, gT));
         rhs[D + 1] += dotv<T, D>(sU, S) + lapT;
     }
 #pragma unroll

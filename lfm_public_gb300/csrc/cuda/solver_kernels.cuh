@@ -13,7 +13,7 @@
 //              (calc_gradients_M2AUSM, :1383-1495). Only with M2AUSM + minmod;
 //              the gradients of calc_gradients (:1500-1567) never reach the M1/M2
 //              flux, so that pass is not run for them.
-//   k_vis      per cell, gather: dudx, dTdx, then tauMC and sigmaU from the
+//   k_vis      per cell, gather: dudx, dTdx, then sigmaU from the
 //              completed gradient (calc_VIS, :1743-1860). Skipped when mu = 0 and
 //              the scheme does not read dudx, because every viscous face term is
 //              then an exact zero.
@@ -50,7 +50,7 @@ struct Args {
     double* dq;               // nq x nc
     // per cell + ghost, computed every stage
     T* prim;                  // (D + 3) x nt: 1/rho, u[D], R psi, c
-    T* V;                     // (2D^2 + 2D) x nt: dudx, dTdx, tauMC, sigmaU
+    T* V;                     // (D^2 + 2D) x nt: dudx, dTdx, sigmaU
     T* grad;                  // (2D + D^2) x nt: rho_grad, p_grad, U_grad (M2AUSM)
     T* flux;                  // nq x nf face rhs
     double* res;              // nq x nc stage-0 residual per cell (or null)
@@ -66,6 +66,7 @@ struct Args {
     const T* dnorm;           // D x nf
     const T* dmag;            // |delta|
     const T* K;               // D x nf
+    const T* lapc;            // |delta| / |d| per face
     // cells
     const double* volInv;
     const double* sponge;

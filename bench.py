@@ -16,7 +16,14 @@ stages over all cells). The metric is cell-RK-stage updates per second.
 workload on the host cores (the oracle port: one process per core, each on
 the full mesh, aggregate throughput).
 
-Launch: python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|fp32]
+The default precision is the FP32-bulk form (FP32 fluxes, limiter and
+residual sums on perturbations from the free stream; FP64 RK registers,
+ghost states and geometry). The same run also times the plain FP64 path
+(``plain_fp64``: value and speed-up) and states the acoustic-pressure error of
+the FP32-bulk state against the FP64 state after --accuracy-steps time steps
+(``accuracy``: over all cells and on 72 probes at r = 50 D).
+
+Launch: python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp32|fp64]
 Under torchrun each rank runs its own replica (weak scaling); rank 0 prints.
 """
 from __future__ import annotations
@@ -56,31 +63,42 @@ def workload(name: str):
 
 WORKLOAD_DESC = {
     "cylinder2d": dict(workload="2D cylinder O-grid 768x512, M1, minmod on, rkOrder 5, CFL 0.5", cells=393216,
-                       dim=2, scheme="M1", faces_per_cell=4),
+                       dim=2, scheme="M1", faces_per_cell=4, viscous=True),
     "cylinder2d_m2": dict(workload="2D cylinder O-grid 768x512, M2, minmod on, rkOrder 5, CFL 0.5", cells=393216,
-                          dim=2, scheme="M2", faces_per_cell=4),
+                          dim=2, scheme="M2", faces_per_cell=4, viscous=True),
     "vortex2d": dict(workload="2D isentropic vortex 256x256, M1, rkOrder 5, CFL 0.5", cells=65536, dim=2,
-                     scheme="M1", faces_per_cell=4),
+                     scheme="M1", faces_per_cell=4, viscous=False),
     "cylinder3d": dict(workload="3D cylinder wake 384x256x96, M2, cyclic span, rkOrder 5", cells=9437184, dim=3,
-                       scheme="M2", faces_per_cell=6),
+                       scheme="M2", faces_per_cell=6, viscous=True),
 }
 
 
-def algorithmic_bytes(dim: int, faces_per_cell: int, fp32: bool):
-    """Algorithmic bytes per cell-stage (two compulsory passes, every element
-    touched once per pass, neighbour reuse from cache, 8 B of face indices).
-    Returns (whole stage, flux kernel share)."""
+def kernel_bytes(dim: int, faces_per_cell: int, fp32: bool, scheme: str, viscous: bool):
+    """Algorithmic bytes per cell of one launch of each kernel: every array
+    element the kernel must touch, once (face arrays once per face, cell arrays
+    once per cell, neighbour re-reads served by cache). ``faces_per_cell`` is
+    the faces around a cell; each face is shared by two cells."""
     nq = dim + 2
-    nv = 2 * dim * dim + 2 * dim
-    fpc = faces_per_cell / 2.0
-    w = 4 if fp32 else 8
-    cell = 3 * nq * 8 + 2 * nq * 8 + 2 * nv * w + 2 * 8 + 8
-    face = ((dim + 1) * w + 8) + ((2 * dim + 1) * w + 8)
-    whole = cell + fpc * face
-    # flux kernel: reads q and V once per cell and the face geometry (S, d, w,
-    # indices) of its faces, writes the face rhs
-    flux = nq * 8 + nv * w + fpc * ((2 * dim + 1) * w + 8) + fpc * nq * w
-    return whole, flux
+    fpc = faces_per_cell / 2.0            # faces per cell
+    w = 4 if fp32 else 8                  # bulk word (prim, V, grad, flux, geometry)
+    prim = (2 * dim + 3) if fp32 else (dim + 3)
+    nv = dim * dim + 2 * dim              # dudx, dTdx, sigmaU
+    ng = 2 * dim + dim * dim              # rho, p, U gradients
+    csr = 4 + 4 * faces_per_cell          # cell -> face offsets and list
+    face_basic = 8 + (dim + 1) * w        # fP, fN, S, w
+    b = {}
+    b["k_prep"] = nq * 8 + prim * w
+    b["k_grad"] = (prim * w + fpc * face_basic + csr + ng * w) if scheme == "M2AUSM" else 0.0
+    b["k_vis"] = ((dim + 1) * w + fpc * face_basic + csr + nv * w) if (viscous or scheme == "M2AUSM") else 0.0
+    flux_cell = (prim - 1) * w + (0 if fp32 else nq * 8)   # FP64 also reads q
+    if viscous or scheme == "M2AUSM":
+        flux_cell += nv * w
+    if scheme == "M2AUSM":
+        flux_cell += ng * w + w
+    flux_face = face_basic + 1 + nq * w + ((dim + 1) * w if viscous else 0) + (dim * w if scheme == "M2AUSM" else 0)
+    b["k_flux"] = flux_cell + fpc * flux_face
+    b["k_update"] = csr + fpc * nq * w + 4 * nq * 8 + 16
+    return b
 
 
 class ClockSampler:
@@ -215,10 +233,35 @@ def run_reference(args):
     return 0
 
 
+def _time_solver(N, ch, precision, dt, steps, warmup, local, pg, clk_device=None):
+    """Device throughput of one solver: W warm-up steps, then K steps timed
+    with CUDA events, each preceded by a 512 MB write that evicts L2."""
+    s = N.Solver(ch, precision=precision, device=local)
+    for _ in range(warmup):
+        s.step(1, dt)
+    s.sync()
+    if pg:
+        pg.barrier()
+    clk = None
+    if clk_device is not None:
+        clk = ClockSampler(clk_device).__enter__()
+        time.sleep(0.3)
+    times = s.bench(steps, dt, 512 << 20)
+    s.sync()
+    if clk is not None:
+        clk.__exit__()
+    if pg:
+        pg.barrier()
+    total_ms = _allmax(pg, float(times.sum()))
+    prof = s.profile_step(dt)
+    s.sync()
+    return s, total_ms, prof, s.launches_per_step(), clk
+
+
 def run_gpu(args):
     ws, rank, local, pg = _dist()
     import numpy as np
-    from lfm_public_gb300 import _native as N
+    from lfm_public_gb300 import _native as N, acoustics
     desc = WORKLOAD_DESC[args.workload]
     fp32 = args.precision == "fp32"
 
@@ -234,47 +277,63 @@ def run_gpu(args):
     ch = N.CaseHandle.from_case(case)
     nc, nq, stages = ch.desc.n_cells, ch.desc.nq, ch.desc.rk_order
     dt = case.delta_t
-    s = N.Solver(ch, precision=N.LFM_FP32_BULK if fp32 else N.LFM_FP64, device=local)
+    prec = N.LFM_FP32_BULK if fp32 else N.LFM_FP64
 
-    for _ in range(args.warmup):
-        s.step(1, dt)
-    s.sync()
-    if pg:
-        pg.barrier()
-    launches = s.launches_per_step()
-    with ClockSampler(local) as clk:
-        time.sleep(0.3)
-        times = s.bench(args.steps, dt, 512 << 20)
-        s.sync()
-    if pg:
-        pg.barrier()
-    total_ms = _allmax(pg, float(times.sum()))
+    s, total_ms, prof, launches, clk = _time_solver(N, ch, prec, dt, args.steps, args.warmup, local, pg, local)
     value = ws * nc * stages * args.steps / (total_ms / 1000.0)
 
-    # per-kernel times of one step (events around each launch, serialised)
-    prof = s.profile_step(dt)
-    s.sync()
-    dominant = max(prof, key=prof.get)
-    stage_ms = sum(prof.values())
-
-    # end to end through the C ABI with pinned host buffers
+    # end to end through the C ABI with pinned host buffers: copy the state in,
+    # advance one time step, copy it out, every step
     import torch
     host = torch.empty((nq, nc), dtype=torch.float64, pin_memory=True).numpy()
-    host[:] = s.get_state()
-    e2e_steps = max(1, args.steps)
+    s.get_state(out=host)
     for _ in range(2):
         s.set_state(host)
         s.step(1, dt)
-        host[:] = s.get_state()
+        s.get_state(out=host)
+    e2e_steps = max(1, args.steps)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         s.set_state(host)
         s.step(1, dt)
-        host[:] = s.get_state()
+        s.get_state(out=host)
     s.sync()
     e2e_s = _allmax(pg, time.perf_counter() - t0)
     e2e_value = ws * nc * stages * e2e_steps / e2e_s
     s.close()
+
+    # the plain FP64 path on the same workload, for the speed-up, and the
+    # acoustic-pressure error of the FP32-bulk form against it
+    plain = None
+    accuracy = None
+    if fp32:
+        s64, ms64, prof64, _, _ = _time_solver(N, ch, N.LFM_FP64, dt, args.steps, args.warmup, local, pg)
+        s64.close()
+        v64 = ws * nc * stages * args.steps / (ms64 / 1000.0)
+        plain = {"value": v64, "unit": UNIT, "ms_per_step": ms64 / args.steps, "kernels_ms_per_step": prof64,
+                 "speedup": value / v64}
+        n_acc = args.accuracy_steps
+        if n_acc > 0:
+            qs = []
+            for p in (N.LFM_FP64, N.LFM_FP32_BULK):
+                sa = N.Solver(ch, precision=p, device=local)
+                sa.step(n_acc, dt)
+                sa.sync()
+                qs.append(sa.get_state())
+                sa.close()
+            g, d = ch.desc.gamma, case.dim
+            err = acoustics.acoustic_rel_l2(qs[1], qs[0], g, d, case.p_inf)
+            ring_r = 50.0 if args.workload.startswith("cylinder") else None
+            accuracy = {"acoustic_p_rel_l2": err, "steps": n_acc,
+                        "against": "FP64 device path (itself within 1e-12 of the oracle), same case and steps"}
+            if ring_r is not None:
+                cells = acoustics.probe_ring(case.cell_centres, ch.cell_ids(), ring_r)
+                p64 = acoustics.pressure(qs[0], g, d)[cells] - case.p_inf
+                rms = float(np.sqrt(np.mean(p64 ** 2)))
+                # before the first wave reaches the ring p' is zero there in both
+                accuracy["probe_ring"] = {
+                    "radius": ring_r, "probes": len(cells), "p_rms_ref": rms,
+                    "rel_l2": acoustics.acoustic_rel_l2(qs[1], qs[0], g, d, case.p_inf, cells) if rms > 0 else None}
 
     if rank != 0:
         return 0
@@ -283,26 +342,30 @@ def run_gpu(args):
         peaks = json.load(open(PEAKS_FILE))
     hbm = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    whole_b, flux_b = algorithmic_bytes(desc["dim"], desc["faces_per_cell"], fp32)
-    flux_ms_per_launch = prof["k_flux"] / stages
-    achieved = flux_b * nc / (flux_ms_per_launch * 1e-3) / 1e9
-    stage_achieved = whole_b * nc * stages * args.steps / (total_ms / ws * 1e-3) / 1e9
+    kb = kernel_bytes(desc["dim"], desc["faces_per_cell"], fp32, desc["scheme"], desc["viscous"])
+    dominant = max(prof, key=prof.get)
+    dom_ms_per_launch = prof[dominant] / stages
+    achieved = kb[dominant] * nc / (dom_ms_per_launch * 1e-3) / 1e9
+    step_bytes = sum(kb.values())
+    step_achieved = step_bytes * nc * stages * args.steps / (total_ms / ws * 1e-3) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32-flux/f64-rk" if fp32 else "f64", "data": "synthetic (generated mesh and initial field)",
-        "config": {"workload": desc["workload"], "cells": nc, "rk_stages": stages, "precision": args.precision,
-                   "l2": "512 MB write between timed steps", "parallelism": f"replicas x{ws}"},
-        "roofline": {"bound": "hbm", "kernel": "k_flux", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+        "config": {"workload": desc["workload"], "cells": nc, "rk_stages": stages,
+                   "precision": "fp32-bulk" if fp32 else "fp64", "l2": "512 MB write between timed steps",
+                   "parallelism": f"replicas x{ws}"},
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_source": peak_src, "traffic": None,
-                     "algorithmic_bytes_per_cell": flux_b,
-                     "step_achieved": stage_achieved, "step_frac": stage_achieved / hbm,
-                     "step_algorithmic_bytes_per_cell_stage": whole_b},
+                     "algorithmic_bytes_per_cell": kb[dominant], "cells_per_launch": nc,
+                     "step_achieved": step_achieved, "step_frac": step_achieved / hbm,
+                     "step_algorithmic_bytes_per_cell_stage": step_bytes},
         "kernels_ms_per_step": prof, "dominant_kernel": dominant,
+        "plain_fp64": plain, "accuracy": accuracy,
         "cpu_baseline": base,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nq * nc * 8, "d2h_bytes_per_step": nq * nc * 8},
         "gpu_launches": launches * args.steps,
-        "clocks": clk.summary(),
+        "clocks": clk.summary() if clk else None,
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -315,7 +378,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="cylinder2d", choices=sorted(WORKLOAD_DESC))
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32"])
+    ap.add_argument("--accuracy-steps", type=int, default=1000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":

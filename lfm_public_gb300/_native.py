@@ -256,10 +256,15 @@ class Solver:
         q = np.ascontiguousarray(q, dtype=np.float64).reshape(self.nq, self.n_cells)
         check(load_library().lfm_solver_set_state(self._h, _ptr(q, C.c_double)))
 
-    def get_state(self) -> np.ndarray:
-        q = np.empty((self.nq, self.n_cells), dtype=np.float64)
-        check(load_library().lfm_solver_get_state(self._h, _ptr(q, C.c_double)))
-        return q
+    def get_state(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """State [nq][n_cells] in solver order, into ``out`` when given (a
+        C-contiguous float64 array of that shape, e.g. in pinned memory)."""
+        if out is None:
+            out = np.empty((self.nq, self.n_cells), dtype=np.float64)
+        elif out.dtype != np.float64 or out.shape != (self.nq, self.n_cells) or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float64 array of shape (nq, n_cells)")
+        check(load_library().lfm_solver_get_state(self._h, _ptr(out, C.c_double)))
+        return out
 
     def step(self, nsteps: int, dt: float):
         check(load_library().lfm_solver_step(self._h, nsteps, dt))

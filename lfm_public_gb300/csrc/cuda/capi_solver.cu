@@ -135,10 +135,40 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
     for (int k = 0; k < 3; ++k) a.UInf[k] = d->UInf[k];
     a.mu = d->mu;
     a.kcond = d->Cp * d->mu * d->PrInv;
+    {
+        // Reference state of the FP32 perturbation form: any constant state
+        // works (its flux through a closed cell sums to zero); the free stream
+        // keeps the perturbations small. Its pressure follows from q_ref.
+        const int Dm = s->D;
+        double u2 = 0.0;
+        for (int k = 0; k < Dm; ++k) u2 += d->UInf[k] * d->UInf[k];
+        a.qRef[0] = d->rhoInf;
+        for (int k = 0; k < 3; ++k) a.qRef[1 + k] = 0.0;
+        for (int k = 0; k < Dm; ++k) a.qRef[1 + k] = d->rhoInf * d->UInf[k];
+        a.qRef[Dm + 1] = d->rhoInf * d->EInf;
+        const double pRef = (d->gamma - 1.0) * (a.qRef[Dm + 1] - 0.5 * d->rhoInf * u2);
+        const double RpsiRef = pRef / d->rhoInf;
+        a.pRef = pRef;
+        const double gh = d->gamma / (d->gamma - 1.0);
+        a.ref.rho = (float)d->rhoInf;
+        for (int k = 0; k < 3; ++k) {
+            a.ref.U[k] = k < Dm ? (float)d->UInf[k] : 0.0f;
+            a.ref.m[k] = k < Dm ? (float)(d->rhoInf * d->UInf[k]) : 0.0f;
+        }
+        a.ref.Rpsi = (float)RpsiRef;
+        a.ref.p = (float)pRef;
+        a.ref.H = (float)(gh * RpsiRef + 0.5 * u2);
+        a.ref.gh = (float)gh;
+        a.ref.gamma = (float)d->gamma;
+        a.ref.gm1 = (float)(d->gamma - 1.0);
+        a.ref.Rinv = (float)(1.0 / d->Rgas);
+        a.ref.mu = (float)d->mu;
+        a.ref.kcond = (float)(d->Cp * d->mu * d->PrInv);
+    }
     const size_t nt = (size_t)s->nt, nf = (size_t)s->nf, D = (size_t)s->D;
     int rc;
     if ((rc = devAlloc(s, &a.dq, (size_t)s->nq * s->nc))) return rc;
-    if ((rc = devAlloc(s, &a.prim, (D + 3) * nt))) return rc;
+    if ((rc = devAlloc(s, &a.prim, (size_t)lfm::dev::primRows<T>(s->D) * nt))) return rc;
     if ((rc = devAlloc(s, &a.V, (D * D + 2 * D) * nt))) return rc;
     // M2AUSM always reads the gradients (all zero when minmod is off, as in the
     // reference, whose prepare_for_RKstep zeroes them every stage).
@@ -166,6 +196,12 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
         for (size_t f = 0; f < nf; ++f) lapc[f] = d->delta_mag[f] * d->dmag_inv[f];
         if ((rc = uploadAs<T>(s, &p, lapc.data(), nf))) return rc;
         a.lapc = p;
+    }
+    a.volInv32 = nullptr;
+    if (sizeof(T) == sizeof(float)) {
+        float* v32;
+        if ((rc = uploadAs<float>(s, &v32, d->vol_inv, (size_t)s->nc))) return rc;
+        a.volInv32 = v32;
     }
     return LFM_OK;
 }
@@ -515,7 +551,7 @@ int residualNoalloc(const lfm_solver* s, const Args<T>& base, const double* q, i
     const bool ausm = s->scheme == LFM_SOLVER_M2AUSM;
     auto round = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t bq = round(nq * nt * sizeof(double));
-    const size_t bPrim = round((D + 3) * nt * sizeof(T));
+    const size_t bPrim = round((size_t)lfm::dev::primRows<T>(s->D) * nt * sizeof(T));
     const size_t bV = round((D * D + 2 * D) * nt * sizeof(T));
     const size_t bGrad = ausm ? round((2 * D + D * D) * nt * sizeof(T)) : 0;
     const size_t bFlux = round(nq * nf * sizeof(T));

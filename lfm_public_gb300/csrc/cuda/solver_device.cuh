@@ -1,0 +1,141 @@
+// Device helpers shared by the FP64 and FP32-bulk time-step kernels.
+#pragma once
+
+#include "solver_kernels.cuh"
+
+namespace lfm {
+namespace dev {
+
+#define LFM_GLOBAL_ID() ((int)(blockIdx.x * blockDim.x + threadIdx.x))
+
+template <typename T>
+__device__ __forceinline__ T interp(T w, T a, T b) {
+    return w * a + (T(1) - w) * b;
+}
+
+template <typename T, int D>
+__device__ __forceinline__ T dotv(const T* a, const T* b) {
+    T s = a[0] * b[0];
+#pragma unroll
+    for (int k = 1; k < D; ++k) s += a[k] * b[k];
+    return s;
+}
+
+// Deviatoric stress of a velocity gradient g (row a = gradient of u_a), in the
+// reference's evaluation order (src/cfd_v0.cpp:1813-1822).
+template <typename T, int D>
+__device__ __forceinline__ void stress(const T g[D][D], T mu, T tau[D][D]) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        tau[a][a] = T(2) * g[a][a];
+#pragma unroll
+        for (int b1 = a + 1; b1 < D + a; ++b1) {
+            const int b = b1 % D;
+            tau[a][b] = mu * (g[a][b] + g[b][a]);
+            tau[a][a] -= g[b][b];
+        }
+        tau[a][a] *= T(2.0 / 3.0) * mu;
+    }
+}
+
+// Minmod-limited face reconstruction from the upwind side (calc_r and
+// interp_minmod, api/cfdv0_solver.h:310-370): flux = +1 reconstructs from P,
+// -1 from N.
+template <typename T, int D>
+__device__ __forceinline__ T minmod_interp(T cp, T ap, const T* grad, const T* d, T w, T flux) {
+    const T gradf = ap - cp + T(1.0e-30);
+    T gradcf = T(0);
+#pragma unroll
+    for (int k = 0; k < D; ++k) gradcf += d[k] * grad[k];
+    T r;
+    if (fabs(gradcf) >= T(1000) * fabs(gradf))
+        r = T(2000) * (gradcf < T(0) ? T(-1) : T(1)) * (gradf < T(0) ? T(-1) : T(1)) - T(1);
+    else
+        r = T(2) * (gradcf / gradf) - T(1);
+    T lim = (T(1) < r) ? T(1) : r;
+    lim = (lim < T(0)) ? T(0) : lim;
+    const T weight = lim * w + (T(1) - lim) * (T(1) + flux) * T(0.5);
+    return weight * cp + (T(1) - weight) * ap;
+}
+
+// AUSM+ fifth-order pressure polynomials (p5Pos / p5Neg, src/cfd_v0.cpp:1863-1895).
+template <typename T>
+__device__ __forceinline__ T p5pos(T M, T alpha) {
+    const T M2Pos = T(0.25) * (M + T(1)) * (M + T(1));
+    const T M2Neg = T(-0.25) * (M - T(1)) * (M - T(1));
+    if (fabs(M) < T(1)) return M2Pos * ((T(2) - M) - T(16) * alpha * M * M2Neg);
+    return T(0.5) * (M + fabs(M)) / M;
+}
+
+template <typename T>
+__device__ __forceinline__ T p5neg(T M, T alpha) {
+    const T M2Pos = T(0.25) * (M + T(1)) * (M + T(1));
+    const T M2Neg = T(-0.25) * (M - T(1)) * (M - T(1));
+    if (fabs(M) < T(1)) return M2Neg * ((T(-2) - M) + T(16) * alpha * M * M2Pos);
+    return T(0.5) * (M - fabs(M)) / M;
+}
+
+// Conservative state of cell or ghost t in FP64. For a ghost the boundary
+// condition of set_boundary_conditions (src/cfd_v0.cpp:1009-1221) is applied
+// to its interior cell and the result stored into q.
+template <typename T, int D>
+__device__ __forceinline__ void stage_state(const Args<T>& a, int t, double* qv) {
+    constexpr int NQ = D + 2;
+    if (t < a.nc) {
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) qv[v] = a.q[(size_t)v * a.nt + t];
+        return;
+    }
+    const int g = t - a.nc;
+    const int in = a.gCell[g];
+    const int kind = a.gKind[g];
+    double qi[NQ];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) qi[v] = a.q[(size_t)v * a.nt + in];
+    if (kind == 1) {  // wall: mirror the momentum
+        qv[0] = qi[0];
+#pragma unroll
+        for (int k = 0; k < D; ++k) qv[k + 1] = -qi[k + 1];
+        qv[D + 1] = qi[D + 1];
+    } else if (kind >= 2 && kind <= 4) {
+        bool inlet = (kind == 2);
+        if (kind == 4) inlet = (double)a.S[a.gFace[g]] <= 0.0;  // free stream along +x enters
+        const double rhoInt = qi[0];
+        double Uint[D], um2 = 0.0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            Uint[k] = qi[k + 1] / rhoInt;
+            um2 += Uint[k] * Uint[k];
+        }
+        const double pInt = (qi[D + 1] - 0.5 * um2 * rhoInt) * a.gm1;
+        if (inlet) {
+            const double TInt = pInt * a.Rinv / rhoInt;
+            const double rhoExt = rhoInt * TInt / a.TInf;
+            double ue2 = 0.0;
+#pragma unroll
+            for (int k = 0; k < D; ++k) ue2 += a.UInf[k] * a.UInf[k];
+            const double EExt = pInt / (rhoExt * a.gm1) + 0.5 * ue2;
+            qv[0] = rhoExt;
+#pragma unroll
+            for (int k = 0; k < D; ++k) qv[k + 1] = rhoExt * a.UInf[k];
+            qv[D + 1] = rhoExt * EExt;
+        } else {
+            const double rhoExt = rhoInt * a.pInf / pInt;
+            const double EExt = a.pInf / (rhoExt * a.gm1) + 0.5 * um2;
+            qv[0] = rhoExt;
+#pragma unroll
+            for (int k = 0; k < D; ++k) qv[k + 1] = rhoExt * Uint[k];
+            qv[D + 1] = rhoExt * EExt;
+        }
+    } else {
+        // Patches without a boundary condition keep a zero ghost state, as
+        // in the reference (src/cfd_v0.cpp:406-416).
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) qv[v] = 0.0;
+    }
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) a.q[(size_t)v * a.nt + t] = qv[v];
+}
+
+}  // namespace dev
+}  // namespace lfm

@@ -1,41 +1,9 @@
 // Device kernels of the explicit finite-volume time step (see solver_kernels.cuh).
-#include "solver_kernels.cuh"
+#include "solver_device.cuh"
 #include "solver_launch.h"
 
 namespace lfm {
 namespace dev {
-
-#define LFM_GLOBAL_ID() ((int)(blockIdx.x * blockDim.x + threadIdx.x))
-
-template <typename T>
-__device__ __forceinline__ T interp(T w, T a, T b) {
-    return w * a + (T(1) - w) * b;
-}
-
-template <typename T, int D>
-__device__ __forceinline__ T dotv(const T* a, const T* b) {
-    T s = a[0] * b[0];
-#pragma unroll
-    for (int k = 1; k < D; ++k) s += a[k] * b[k];
-    return s;
-}
-
-// Deviatoric stress of a velocity gradient g (row a = gradient of u_a), in the
-// reference's evaluation order (src/cfd_v0.cpp:1813-1822).
-template <typename T, int D>
-__device__ __forceinline__ void stress(const T g[D][D], T mu, T tau[D][D]) {
-#pragma unroll
-    for (int a = 0; a < D; ++a) {
-        tau[a][a] = T(2) * g[a][a];
-#pragma unroll
-        for (int b1 = a + 1; b1 < D + a; ++b1) {
-            const int b = b1 % D;
-            tau[a][b] = mu * (g[a][b] + g[b][a]);
-            tau[a][a] -= g[b][b];
-        }
-        tau[a][a] *= T(2.0 / 3.0) * mu;
-    }
-}
 
 // ---------------------------------------------------------------------------
 // k_prep: ghost states and per-cell primitives.
@@ -46,60 +14,7 @@ __global__ void __launch_bounds__(256) k_prep(Args<T> a) {
     if (t >= a.nt) return;
     constexpr int NQ = D + 2;
     double qv[NQ];
-    if (t < a.nc) {
-#pragma unroll
-        for (int v = 0; v < NQ; ++v) qv[v] = a.q[(size_t)v * a.nt + t];
-    } else {
-        const int g = t - a.nc;
-        const int in = a.gCell[g];
-        const int kind = a.gKind[g];
-        double qi[NQ];
-#pragma unroll
-        for (int v = 0; v < NQ; ++v) qi[v] = a.q[(size_t)v * a.nt + in];
-        if (kind == 1) {  // wall: mirror the momentum
-            qv[0] = qi[0];
-#pragma unroll
-            for (int k = 0; k < D; ++k) qv[k + 1] = -qi[k + 1];
-            qv[D + 1] = qi[D + 1];
-        } else if (kind >= 2 && kind <= 4) {
-            bool inlet = (kind == 2);
-            if (kind == 4) inlet = (double)a.S[a.gFace[g]] <= 0.0;  // free stream along +x enters
-            const double rhoInt = qi[0];
-            double Uint[D], um2 = 0.0;
-#pragma unroll
-            for (int k = 0; k < D; ++k) {
-                Uint[k] = qi[k + 1] / rhoInt;
-                um2 += Uint[k] * Uint[k];
-            }
-            const double pInt = (qi[D + 1] - 0.5 * um2 * rhoInt) * a.gm1;
-            if (inlet) {
-                const double TInt = pInt * a.Rinv / rhoInt;
-                const double rhoExt = rhoInt * TInt / a.TInf;
-                double ue2 = 0.0;
-#pragma unroll
-                for (int k = 0; k < D; ++k) ue2 += a.UInf[k] * a.UInf[k];
-                const double EExt = pInt / (rhoExt * a.gm1) + 0.5 * ue2;
-                qv[0] = rhoExt;
-#pragma unroll
-                for (int k = 0; k < D; ++k) qv[k + 1] = rhoExt * a.UInf[k];
-                qv[D + 1] = rhoExt * EExt;
-            } else {
-                const double rhoExt = rhoInt * a.pInf / pInt;
-                const double EExt = a.pInf / (rhoExt * a.gm1) + 0.5 * um2;
-                qv[0] = rhoExt;
-#pragma unroll
-                for (int k = 0; k < D; ++k) qv[k + 1] = rhoExt * Uint[k];
-                qv[D + 1] = rhoExt * EExt;
-            }
-        } else {
-            // Patches without a boundary condition keep a zero ghost state, as
-            // in the reference (src/cfd_v0.cpp:406-416).
-#pragma unroll
-            for (int v = 0; v < NQ; ++v) qv[v] = 0.0;
-        }
-#pragma unroll
-        for (int v = 0; v < NQ; ++v) a.q[(size_t)v * a.nt + t] = qv[v];
-    }
+    stage_state<T, D>(a, t, qv);
     // compute_Rpsi (api/cfdv0_solver.h:252-261)
     const double rinv = 1.0 / qv[0];
     double s = qv[1] * qv[1];
@@ -212,42 +127,6 @@ __global__ void __launch_bounds__(256) k_vis(Args<T> a) {
         a.V[(size_t)(D * D + x) * nt + c] = gT[x];
         a.V[(size_t)(D * D + D + x) * nt + c] = dotv<T, D>(U, tau[x]);
     }
-}
-
-// ---------------------------------------------------------------------------
-// Minmod reconstruction and AUSM+ pressure polynomials (M2AUSM).
-// ---------------------------------------------------------------------------
-template <typename T, int D>
-__device__ __forceinline__ T minmod_interp(T cp, T ap, const T* grad, const T* d, T w, T flux) {
-    const T gradf = ap - cp + T(1.0e-30);
-    T gradcf = T(0);
-#pragma unroll
-    for (int k = 0; k < D; ++k) gradcf += d[k] * grad[k];
-    T r;
-    if (fabs(gradcf) >= T(1000) * fabs(gradf))
-        r = T(2000) * (gradcf < T(0) ? T(-1) : T(1)) * (gradf < T(0) ? T(-1) : T(1)) - T(1);
-    else
-        r = T(2) * (gradcf / gradf) - T(1);
-    T lim = (T(1) < r) ? T(1) : r;
-    lim = (lim < T(0)) ? T(0) : lim;
-    const T weight = lim * w + (T(1) - lim) * (T(1) + flux) * T(0.5);
-    return weight * cp + (T(1) - weight) * ap;
-}
-
-template <typename T>
-__device__ __forceinline__ T p5pos(T M, T alpha) {
-    const T M2Pos = T(0.25) * (M + T(1)) * (M + T(1));
-    const T M2Neg = T(-0.25) * (M - T(1)) * (M - T(1));
-    if (fabs(M) < T(1)) return M2Pos * ((T(2) - M) - T(16) * alpha * M * M2Neg);
-    return T(0.5) * (M + fabs(M)) / M;
-}
-
-template <typename T>
-__device__ __forceinline__ T p5neg(T M, T alpha) {
-    const T M2Pos = T(0.25) * (M + T(1)) * (M + T(1));
-    const T M2Neg = T(-0.25) * (M - T(1)) * (M - T(1));
-    if (fabs(M) < T(1)) return M2Neg * ((T(-2) - M) + T(16) * alpha * M * M2Pos);
-    return T(0.5) * (M - fabs(M)) / M;
 }
 
 // ---------------------------------------------------------------------------
@@ -625,7 +504,11 @@ void launch_stage(const Args<T>& a, const StageConfig& s, cudaStream_t st) {
         launch_stage_t<T, 3>(a, s, st);
 }
 template void launch_stage<double>(const Args<double>&, const StageConfig&, cudaStream_t);
-template void launch_stage<float>(const Args<float>&, const StageConfig&, cudaStream_t);
+// The FP32-bulk form runs its own kernels (solver_kernels_fp32.cu).
+template <>
+void launch_stage<float>(const Args<float>& a, const StageConfig& s, cudaStream_t st) {
+    for (int k = 0; k < kKernelsPerStage; ++k) launch_kernel_fp32(a, s, k, st);
+}
 
 // Individual kernels, for per-kernel timing.
 template <typename T>
@@ -672,7 +555,22 @@ void launch_kernel(const Args<T>& a, const StageConfig& s, int which, cudaStream
     }
 }
 template void launch_kernel<double>(const Args<double>&, const StageConfig&, int, cudaStream_t);
-template void launch_kernel<float>(const Args<float>&, const StageConfig&, int, cudaStream_t);
+template <>
+void launch_kernel<float>(const Args<float>& a, const StageConfig& s, int which, cudaStream_t st) {
+    launch_kernel_fp32(a, s, which, st);
+}
+
+// The FP32-bulk form shares k_update: FP32 sums of the face rhs, FP64 update.
+void launch_update_fp32(const Args<float>& a, const StageConfig& s, cudaStream_t st) {
+    const unsigned nb = blocks(a.nc, 256);
+    if (a.D == 2) {
+        if (s.withRes) k_update<float, 2, true><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
+        else k_update<float, 2, false><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
+    } else {
+        if (s.withRes) k_update<float, 3, true><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
+        else k_update<float, 3, false><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
+    }
+}
 
 void launch_cfl(int D, const double* q, int nt, int nc, const double* volInv, const int* sOff, const double* cellS,
                 double dt, int mode, double maxCo, double* partial, double* out, cudaStream_t st) {

@@ -40,6 +40,14 @@ constexpr int kSchemeM1 = 0;
 constexpr int kSchemeM2 = 1;
 constexpr int kSchemeAUSM = 2;
 
+// Free-stream reference state of the FP32-bulk perturbation form, rounded
+// to FP32 from FP64 values computed on the host.
+struct RefState32 {
+    float rho, U[3], m[3];    // rho_inf, U_inf, rho_inf U_inf
+    float Rpsi, p, H, gh;     // p/rho, p, total enthalpy, gamma / (gamma - 1)
+    float gamma, gm1, Rinv, mu, kcond;   // gas constants (FP32 copies)
+};
+
 // Arguments shared by the kernels (all device pointers).
 template <typename T>
 struct Args {
@@ -49,7 +57,8 @@ struct Args {
     double* q;                // nq x nt
     double* dq;               // nq x nc
     // per cell + ghost, computed every stage
-    T* prim;                  // (D + 3) x nt: 1/rho, u[D], R psi, c
+    T* prim;                  // FP64: (D + 3) x nt: 1/rho, u[D], R psi, c
+                              // FP32: (2D + 3) x nt: rho', m'[D], u'[D], R psi', c
     T* V;                     // (D^2 + 2D) x nt: dudx, dTdx, sigmaU
     T* grad;                  // (2D + D^2) x nt: rho_grad, p_grad, U_grad (M2AUSM)
     T* flux;                  // nq x nf face rhs
@@ -69,6 +78,7 @@ struct Args {
     const T* lapc;            // |delta| / |d| per face
     // cells
     const double* volInv;
+    const float* volInv32;    // FP32 copy (FP32-bulk gradient kernels)
     const double* sponge;
     const int* cfOff;         // nc + 1
     const int* cfList;        // face index, negative (~f) when the cell is N
@@ -78,6 +88,11 @@ struct Args {
     const int* gFace;
     // constants
     double gamma, gm1, Rinv, rhoInf, EInf, pInf, TInf, UInf[3], mu, kcond;
+    // FP32-bulk: conservative reference state q_ref = (rho_inf, rho_inf U_inf,
+    // rho_inf E_inf) in FP64 (index = variable) and its derived FP32 constants
+    double qRef[5];
+    double pRef;              // (gamma - 1)(rho_inf E_inf - rho_inf |U_inf|^2 / 2)
+    RefState32 ref;
     // error flag (non-finite state)
     int* flag;
 };

@@ -23,6 +23,20 @@ template <typename T>
 void launch_stage(const Args<T>& a, const StageConfig& s, cudaStream_t st);
 template <typename T>
 void launch_kernel(const Args<T>& a, const StageConfig& s, int which, cudaStream_t st);
+template <>
+void launch_stage<float>(const Args<float>& a, const StageConfig& s, cudaStream_t st);
+template <>
+void launch_kernel<float>(const Args<float>& a, const StageConfig& s, int which, cudaStream_t st);
+// FP32-bulk kernels (perturbation form) and their shared RK update.
+void launch_kernel_fp32(const Args<float>& a, const StageConfig& s, int which, cudaStream_t st);
+void launch_update_fp32(const Args<float>& a, const StageConfig& s, cudaStream_t st);
+
+// Rows of the per-cell primitive array: FP64 keeps 1/rho, u[D], R psi, c;
+// the FP32 perturbation form keeps rho', m'[D], u'[D], R psi', c.
+template <typename T>
+constexpr int primRows(int D) {
+    return sizeof(T) == sizeof(double) ? D + 3 : 2 * D + 3;
+}
 // mode 0: max CFL, mode 1: min dt
 void launch_cfl(int D, const double* q, int nt, int nc, const double* volInv, const int* sOff, const double* cellS,
                 double dt, int mode, double maxCo, double* partial, double* out, cudaStream_t st);

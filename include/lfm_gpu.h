@@ -239,6 +239,71 @@ int lfm_solver_launches_per_step(const lfm_solver* s, int* launches);
 int lfm_solver_profile_step(lfm_solver* s, double dt, int n, float* ms);
 const char* lfm_solver_kernel_name(int i);
 
+/* ---- batch engine: many cases, one persistent kernel per RK stage ---------
+ *
+ * No single reference call corresponds: the reference advances one case per
+ * MPI job (Mesh::solve, src/mesh_solver.cpp:474-853). A batch advances any
+ * number of independent cases -- uneven sizes, 2D and 3D, M1/M2/M2AUSM --
+ * with the FP32-bulk arithmetic (LFM_FP32_BULK), each case at its own constant
+ * dt. A time step of all cases is one CUDA graph: one persistent kernel per RK
+ * stage whose blocks work through per-phase tile lists of every case, with
+ * grid-wide barriers between the phases. Case data lives in one device arena
+ * reserved at creation; a case is admitted when a free block of its footprint
+ * exists (lfm_batch_case_bytes) and its block is returned on removal. Cases may
+ * be added and removed between steps. Calls on one batch are not re-entrant;
+ * all work runs on the batch's own stream. */
+typedef struct lfm_batch lfm_batch;
+
+typedef struct lfm_batch_opts {
+    int device;           /* CUDA device ordinal */
+    int rk_order;         /* RK stages per step, shared by every case (1..8) */
+    size_t arena_bytes;   /* device memory reserved for case data; 0 = a quarter of free memory */
+    int max_cases;        /* case slots; 0 = 256 */
+} lfm_batch_opts;
+
+/* Launch shape of the stage kernel, chosen by lfm_batch_autotune. */
+typedef struct lfm_batch_tuning {
+    int block;            /* threads per block: 128, 256 or 512 */
+    int items_per_thread; /* cells or faces per thread and tile (tile = block x items) */
+    int blocks_per_sm;    /* resident blocks per SM of the persistent grid; 0 = all that fit */
+    int cooperative;      /* 1: cooperative launch (co-residency guaranteed by the driver) */
+} lfm_batch_tuning;
+
+int lfm_batch_create(const lfm_batch_opts* opts, lfm_batch** out);
+void lfm_batch_destroy(lfm_batch* b);
+/* Arena footprint of a case (bytes). */
+int lfm_batch_case_bytes(const lfm_solver_desc* desc, size_t* bytes);
+/* Admits a case with state desc->q0 and constant time step dt; *slot receives
+ * its slot. LFM_ERR_NOMEM when no arena block or slot is free. */
+int lfm_batch_add(lfm_batch* b, const lfm_solver_desc* desc, double dt, int* slot);
+/* Removes a case (waits for queued steps) and frees its arena block. */
+int lfm_batch_remove(lfm_batch* b, int slot);
+/* Host <-> device state of one case ([nq][n_cells], solver order); synchronous. */
+int lfm_batch_set_state(lfm_batch* b, int slot, const double* q);
+int lfm_batch_get_state(lfm_batch* b, int slot, double* q);
+/* nsteps time steps of every case in the batch; asynchronous. */
+int lfm_batch_step(lfm_batch* b, int nsteps);
+/* Waits for the batch stream; LFM_ERR_NUMERIC names the slots whose state
+ * became non-finite, LFM_ERR_CUDA reports a stage kernel that gave up at a
+ * grid barrier. */
+int lfm_batch_sync(lfm_batch* b);
+/* LFM_OK or LFM_ERR_NUMERIC for one case (waits for the batch stream). */
+int lfm_batch_case_status(lfm_batch* b, int slot, int* status);
+/* Arena: largest free block, total free bytes, arena size (any may be NULL). */
+int lfm_batch_memory(const lfm_batch* b, size_t* largest_free, size_t* total_free, size_t* arena_bytes);
+/* Cells and cases currently in the batch (either may be NULL). */
+int lfm_batch_cells(const lfm_batch* b, int64_t* cells, int* cases);
+int lfm_batch_get_tuning(const lfm_batch* b, lfm_batch_tuning* t);
+int lfm_batch_set_tuning(lfm_batch* b, const lfm_batch_tuning* t);
+/* Times trial_steps steps of the current cases for every launch shape and
+ * keeps the fastest; the cases' states are restored afterwards. */
+int lfm_batch_autotune(lfm_batch* b, int trial_steps, lfm_batch_tuning* chosen);
+/* nsteps steps, each after a write of flush_bytes of scratch (outside its
+ * timing), ms[k] = duration of step k (CUDA events on the batch stream). */
+int lfm_batch_bench(lfm_batch* b, int nsteps, size_t flush_bytes, float* ms);
+/* Kernel launches per time step (one per RK stage). */
+int lfm_batch_launches_per_step(const lfm_batch* b, int* launches);
+
 #ifdef __cplusplus
 }
 #endif

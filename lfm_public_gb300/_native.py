@@ -19,6 +19,14 @@ PORT_PATH = os.path.join(ROOT, "oracle", "port", "liblfm_port.so")
 
 LFM_FP64 = 0
 LFM_FP32_BULK = 1
+# lfm_status codes (include/lfm_gpu.h)
+LFM_OK = 0
+LFM_ERR_INVALID = -1
+LFM_ERR_IO = -2
+LFM_ERR_CUDA = -3
+LFM_ERR_NOMEM = -4
+LFM_ERR_NUMERIC = -5
+LFM_ERR_UNSUPPORTED = -6
 
 _i64p = C.POINTER(C.c_int64)
 _dp = C.POINTER(C.c_double)
@@ -68,6 +76,18 @@ class SolverOpts(C.Structure):
     _fields_ = [("precision", C.c_int), ("device", C.c_int), ("block", C.c_int)]
 
 
+class BatchOpts(C.Structure):
+    _fields_ = [("device", C.c_int), ("rk_order", C.c_int), ("arena_bytes", C.c_size_t), ("max_cases", C.c_int)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("block", C.c_int), ("items_per_thread", C.c_int), ("blocks_per_sm", C.c_int),
+                ("cooperative", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class LfmError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"lfm error {code}: {msg}")
@@ -114,6 +134,23 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "lfm_solver_bench": ([vp, C.c_int, C.c_double, C.c_size_t, C.POINTER(C.c_float)], C.c_int),
         "lfm_solver_profile_step": ([vp, C.c_double, C.c_int, C.POINTER(C.c_float)], C.c_int),
         "lfm_solver_kernel_name": ([C.c_int], C.c_char_p),
+        "lfm_batch_create": ([C.POINTER(BatchOpts), C.POINTER(vp)], C.c_int),
+        "lfm_batch_destroy": ([vp], None),
+        "lfm_batch_case_bytes": ([C.POINTER(SolverDesc), C.POINTER(C.c_size_t)], C.c_int),
+        "lfm_batch_add": ([vp, C.POINTER(SolverDesc), C.c_double, C.POINTER(C.c_int)], C.c_int),
+        "lfm_batch_remove": ([vp, C.c_int], C.c_int),
+        "lfm_batch_set_state": ([vp, C.c_int, _dp], C.c_int),
+        "lfm_batch_get_state": ([vp, C.c_int, _dp], C.c_int),
+        "lfm_batch_step": ([vp, C.c_int], C.c_int),
+        "lfm_batch_sync": ([vp], C.c_int),
+        "lfm_batch_case_status": ([vp, C.c_int, C.POINTER(C.c_int)], C.c_int),
+        "lfm_batch_memory": ([vp, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)], C.c_int),
+        "lfm_batch_cells": ([vp, _i64p, C.POINTER(C.c_int)], C.c_int),
+        "lfm_batch_get_tuning": ([vp, C.POINTER(BatchTuning)], C.c_int),
+        "lfm_batch_set_tuning": ([vp, C.POINTER(BatchTuning)], C.c_int),
+        "lfm_batch_autotune": ([vp, C.c_int, C.POINTER(BatchTuning)], C.c_int),
+        "lfm_batch_bench": ([vp, C.c_int, C.c_size_t, C.POINTER(C.c_float)], C.c_int),
+        "lfm_batch_launches_per_step": ([vp, C.POINTER(C.c_int)], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -323,6 +360,103 @@ class Solver:
     def close(self):
         if getattr(self, "_h", None):
             load_library().lfm_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """An lfm_batch: many cases advanced together (FP32-bulk) on one GPU."""
+
+    def __init__(self, device: int = 0, rk_order: int = 5, arena_bytes: int = 0, max_cases: int = 256):
+        lib = load_library()
+        opts = BatchOpts(device=device, rk_order=rk_order, arena_bytes=arena_bytes, max_cases=max_cases)
+        h = C.c_void_p()
+        check(lib.lfm_batch_create(C.byref(opts), C.byref(h)))
+        self._h = h
+        self._cases = {}
+
+    @staticmethod
+    def case_bytes(case: CaseHandle) -> int:
+        v = C.c_size_t()
+        check(load_library().lfm_batch_case_bytes(C.byref(case.desc), C.byref(v)))
+        return v.value
+
+    def add(self, case: CaseHandle, dt: float) -> int:
+        s = C.c_int()
+        check(load_library().lfm_batch_add(self._h, C.byref(case.desc), dt, C.byref(s)))
+        self._cases[s.value] = case
+        return s.value
+
+    def remove(self, slot: int):
+        check(load_library().lfm_batch_remove(self._h, slot))
+        self._cases.pop(slot, None)
+
+    def set_state(self, slot: int, q: np.ndarray):
+        d = self._cases[slot].desc
+        q = np.ascontiguousarray(q, dtype=np.float64).reshape(d.nq, d.n_cells)
+        check(load_library().lfm_batch_set_state(self._h, slot, _ptr(q, C.c_double)))
+
+    def get_state(self, slot: int, out: Optional[np.ndarray] = None) -> np.ndarray:
+        d = self._cases[slot].desc
+        if out is None:
+            out = np.empty((d.nq, d.n_cells), dtype=np.float64)
+        check(load_library().lfm_batch_get_state(self._h, slot, _ptr(out, C.c_double)))
+        return out
+
+    def step(self, nsteps: int = 1):
+        check(load_library().lfm_batch_step(self._h, nsteps))
+
+    def sync(self):
+        check(load_library().lfm_batch_sync(self._h))
+
+    def case_status(self, slot: int) -> int:
+        v = C.c_int()
+        check(load_library().lfm_batch_case_status(self._h, slot, C.byref(v)))
+        return v.value
+
+    def memory(self) -> dict:
+        a, b, c = C.c_size_t(), C.c_size_t(), C.c_size_t()
+        check(load_library().lfm_batch_memory(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"largest_free": a.value, "total_free": b.value, "arena": c.value}
+
+    def cells(self) -> int:
+        n = C.c_int64()
+        check(load_library().lfm_batch_cells(self._h, C.byref(n), None))
+        return n.value
+
+    def tuning(self) -> dict:
+        t = BatchTuning()
+        check(load_library().lfm_batch_get_tuning(self._h, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, block: int, items_per_thread: int = 1, blocks_per_sm: int = 0, cooperative: int = 1):
+        t = BatchTuning(block=block, items_per_thread=items_per_thread, blocks_per_sm=blocks_per_sm,
+                        cooperative=cooperative)
+        check(load_library().lfm_batch_set_tuning(self._h, C.byref(t)))
+
+    def autotune(self, trial_steps: int = 2) -> dict:
+        t = BatchTuning()
+        check(load_library().lfm_batch_autotune(self._h, trial_steps, C.byref(t)))
+        return t.as_dict()
+
+    def bench(self, nsteps: int, flush_bytes: int = 512 << 20) -> np.ndarray:
+        ms = (C.c_float * nsteps)()
+        check(load_library().lfm_batch_bench(self._h, nsteps, flush_bytes, ms))
+        return np.array(ms[:], dtype=np.float64)
+
+    def launches_per_step(self) -> int:
+        v = C.c_int()
+        check(load_library().lfm_batch_launches_per_step(self._h, C.byref(v)))
+        return v.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().lfm_batch_destroy(self._h)
             self._h = None
 
     def __del__(self):

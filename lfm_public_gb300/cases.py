@@ -519,6 +519,36 @@ def _prism_mesh(nodes, tris, half, name, **kw) -> Case:
                 mol_weight=28.9647, Pr=0.71, Ls=2.0, **kw)
 
 
+def sweep_spec(n_cases: int = 64, seed: int = 20261203, cells_min: float = 16e3, cells_max: float = 1e6):
+    """Parameters of a batched sweep: for case k, a quad grid (even k) or a
+    jittered triangulation (odd k) with a cell count log-uniform in
+    [cells_min, cells_max], Mach U(0.1, 0.6), vortex strength U(1, 5) and the
+    M1 or M2 scheme at random. Returns a list of dicts (kind, n, cells, mach,
+    beta, solver, seed)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_cases):
+        cells = math.exp(rng.uniform(math.log(cells_min), math.log(cells_max)))
+        mach = float(rng.uniform(0.1, 0.6))
+        beta = float(rng.uniform(1.0, 5.0))
+        solver = int(rng.integers(0, 2))
+        sub = int(rng.integers(0, 2 ** 31 - 1))
+        if k % 2 == 0:
+            n = max(8, int(round(math.sqrt(cells))))
+            out.append(dict(kind="quad", n=n, cells=n * n, mach=mach, beta=beta, solver=solver, seed=sub))
+        else:
+            n = max(8, int(round(math.sqrt(cells / 2))))
+            out.append(dict(kind="tri", n=n, cells=2 * n * n, mach=mach, beta=beta, solver=solver, seed=sub))
+    return out
+
+
+def sweep_case(spec: dict) -> Case:
+    """The case of one ``sweep_spec`` entry (isentropic vortex on [-10, 10]^2)."""
+    if spec["kind"] == "quad":
+        return vortex_case(n=spec["n"], mach=spec["mach"], beta=spec["beta"], solver=spec["solver"])
+    return tri_case(n=spec["n"], seed=spec["seed"], mach=spec["mach"], beta=spec["beta"], solver=spec["solver"])
+
+
 # ---------------------------------------------------------------------------
 # OpenFOAM case writer
 # ---------------------------------------------------------------------------

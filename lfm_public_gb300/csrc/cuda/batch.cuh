@@ -1,0 +1,64 @@
+// Batched multi-case time step: many independent cases (uneven cell counts,
+// mixed schemes and dimensions) advanced by one persistent kernel per RK stage.
+//
+// Every case lives in its own block of a device arena, with the FP32-bulk
+// arrays of a single-case solver (Args<float>). A stage is four phases over
+// all cases -- ghost states and primitives; gradients and viscous terms;
+// face fluxes; gather and RK update -- separated by grid-wide barriers. Work
+// is a flat list of tiles per phase (a tile is a run of consecutive cells or
+// faces of one case), taken from a per-phase atomic counter, so uneven cases
+// load-balance at tile granularity. The tile lists and case table are read
+// from device memory at run time: cases join and leave between time steps
+// without recapturing the CUDA graph of a step.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "solver_kernels.cuh"
+
+namespace lfm {
+namespace dev {
+
+constexpr int kBatchMaxStages = 8;
+constexpr int kBatchPhases = 4;   // prep, grad+vis, flux, update
+
+// One case of a batch: its kernel arguments (device pointers into its arena
+// block), time step and RK coefficients.
+struct __align__(16) BatchCase {
+    Args<float> a;
+    double dt;
+    double rkA[kBatchMaxStages], rkB[kBatchMaxStages];
+    int scheme, needGrad, needVis, residuals;
+};
+
+// A run of `count` consecutive items (cells, ghosts or faces) of case `slot`.
+struct __align__(16) BatchTile {
+    int slot, start, count, pad;
+};
+
+// Zeroed before every time step: grid-barrier arrival counters and the
+// per-phase tile counters of each stage.
+struct BatchCtl {
+    unsigned barrier[kBatchMaxStages];
+    unsigned next[kBatchMaxStages][kBatchPhases];
+};
+
+struct BatchArgs {
+    const BatchCase* cases;
+    const BatchTile* tiles[kBatchPhases];
+    const int* nTiles;          // [kBatchPhases]
+    BatchCtl* ctl;
+    int* error;                 // set when a grid barrier gives up waiting
+    int itemsPerThread;
+};
+
+// Launches stage `stage` of every case as one persistent (cooperative when
+// `cooperative`) kernel of `grid` blocks of `block` threads (128, 256 or 512).
+cudaError_t launch_batch_stage(const BatchArgs& b, int stage, int block, int grid, bool cooperative,
+                               cudaStream_t st);
+// Resident blocks per SM of the stage kernel at `block` threads.
+int batch_blocks_per_sm(int block);
+
+}  // namespace dev
+}  // namespace lfm

@@ -1,0 +1,165 @@
+// Persistent multi-case stage kernel of the batch engine (batch.cuh).
+#include "batch.cuh"
+#include "solver_fp32.cuh"
+
+namespace lfm {
+namespace dev {
+
+namespace {
+
+// Polls before a grid barrier gives up (each poll sleeps ~40 ns: about 0.7 s).
+constexpr unsigned kBarrierSpinLimit = 1u << 24;
+
+// Grid-wide barrier of the blocks of one launch (all resident: the launch is
+// cooperative, or its grid is sized to the resident capacity). Arrival is an
+// atomic increment after a release fence; waiting is bounded: after
+// kBarrierSpinLimit polls, or once another block has given up, the block sets
+// the error flag and the caller returns without touching further data.
+__device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target, int* error) {
+    __shared__ int sOk;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(counter, 1u);
+        int ok = 1;
+        unsigned spins = 0;
+        while (*(volatile unsigned*)counter < target) {
+            if (*(volatile int*)error != 0 || ++spins > kBarrierSpinLimit) {
+                atomicOr(error, 1);
+                ok = 0;
+                break;
+            }
+            __nanosleep(40);
+        }
+        __threadfence();
+        sOk = ok;
+    }
+    __syncthreads();
+    return sOk != 0;
+}
+
+// One item of a phase: a cell or ghost (prep), a cell (grad + vis, update) or
+// a face (flux) of the case in shared memory.
+template <int PH, int D>
+__device__ __forceinline__ void item(const BatchCase& bc, int stage, int i) {
+    const Args<float>& a = bc.a;
+    if (PH == 0) {
+        prep32<D>(a, i);
+    } else if (PH == 1) {
+        if (bc.needGrad) grad32<D>(a, i);
+        if (bc.needVis) vis32<D>(a, i);
+    } else if (PH == 2) {
+        if (bc.scheme == kSchemeM1)
+            flux32<D, kSchemeM1>(a, i);
+        else if (bc.scheme == kSchemeM2)
+            flux32<D, kSchemeM2>(a, i);
+        else
+            flux32<D, kSchemeAUSM>(a, i);
+    } else {
+        const int first = stage == 0;
+        if (bc.residuals && first)
+            update_cell<float, D, true>(a, i, bc.rkA[stage], bc.rkB[stage], bc.dt, first);
+        else
+            update_cell<float, D, false>(a, i, bc.rkA[stage], bc.rkB[stage], bc.dt, first);
+    }
+}
+
+// The tiles of phase PH assigned to this block: a contiguous range of the
+// phase's tile list (neighbouring tiles of a case share cached neighbours).
+// The block keeps the current tile's case in shared memory and reloads it when
+// the case changes.
+template <int PH, int BLOCK>
+__device__ __forceinline__ void phase_tiles(const BatchArgs& b, int stage, BatchCase& sc, int& sSlot) {
+    const int nT = b.nTiles[PH];
+    const long long t0 = (long long)nT * blockIdx.x / gridDim.x;
+    const long long t1 = (long long)nT * (blockIdx.x + 1) / gridDim.x;
+    const BatchTile* tiles = b.tiles[PH];
+    for (long long t = t0; t < t1; ++t) {
+        const BatchTile td = tiles[t];
+        const bool reload = td.slot != sSlot;
+        __syncthreads();
+        if (reload) {
+            const int4* src = reinterpret_cast<const int4*>(b.cases + td.slot);
+            int4* dst = reinterpret_cast<int4*>(&sc);
+            constexpr int n16 = (int)(sizeof(BatchCase) / 16);
+            for (int k = threadIdx.x; k < n16; k += BLOCK) dst[k] = src[k];
+            if (threadIdx.x == 0) sSlot = td.slot;
+            __syncthreads();
+        }
+        const int end = td.start + td.count;
+        for (int k = 0; k < b.itemsPerThread; ++k) {
+            const int i = td.start + (int)threadIdx.x + k * BLOCK;
+            if (i < end) {
+                if (sc.a.D == 2)
+                    item<PH, 2>(sc, stage, i);
+                else
+                    item<PH, 3>(sc, stage, i);
+            }
+        }
+    }
+}
+
+// Stage `stage` of every case: prep | grad + vis | flux | update, with a grid
+// barrier between phases (none after the last). Within the launch every array
+// is written by one phase and read only by later ones, so no block reads a
+// line it cached before another block rewrote it.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_batch_stage(const __grid_constant__ BatchArgs b, int stage) {
+    __shared__ BatchCase sc;
+    __shared__ int sSlot;
+    if (threadIdx.x == 0) sSlot = -1;
+    __syncthreads();
+    unsigned* counter = &b.ctl->barrier[stage];
+    unsigned target = gridDim.x;
+    phase_tiles<0, BLOCK>(b, stage, sc, sSlot);
+    if (!grid_barrier(counter, target, b.error)) return;
+    if (b.nTiles[1] > 0) {
+        phase_tiles<1, BLOCK>(b, stage, sc, sSlot);
+        target += gridDim.x;
+        if (!grid_barrier(counter, target, b.error)) return;
+    }
+    phase_tiles<2, BLOCK>(b, stage, sc, sSlot);
+    target += gridDim.x;
+    if (!grid_barrier(counter, target, b.error)) return;
+    phase_tiles<3, BLOCK>(b, stage, sc, sSlot);
+}
+
+template <int BLOCK>
+cudaError_t launch_block(const BatchArgs& b, int stage, int grid, bool cooperative, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(BLOCK);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = cooperative ? attr : nullptr;
+    cfg.numAttrs = cooperative ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k_batch_stage<BLOCK>, b, stage);
+}
+
+}  // namespace
+
+cudaError_t launch_batch_stage(const BatchArgs& b, int stage, int block, int grid, bool cooperative,
+                               cudaStream_t st) {
+    switch (block) {
+        case 128: return launch_block<128>(b, stage, grid, cooperative, st);
+        case 512: return launch_block<512>(b, stage, grid, cooperative, st);
+        default: return launch_block<256>(b, stage, grid, cooperative, st);
+    }
+}
+
+int batch_blocks_per_sm(int block) {
+    int n = 0;
+    cudaError_t e;
+    switch (block) {
+        case 128: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_stage<128>, 128, 0); break;
+        case 512: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_stage<512>, 512, 0); break;
+        default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_stage<256>, 256, 0); break;
+    }
+    return e == cudaSuccess ? n : 0;
+}
+
+}  // namespace dev
+}  // namespace lfm

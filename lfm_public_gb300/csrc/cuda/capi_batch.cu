@@ -1,0 +1,725 @@
+// C ABI, batch engine (include/lfm_gpu.h, lfm_batch_*).
+//
+// A batch owns one device arena (a single allocation sized at creation) in
+// which every admitted case gets one contiguous block holding all its arrays
+// (FP32-bulk layout of a single-case solver). Admission is by footprint: a
+// case is admitted when a free block of its size exists (first fit, blocks
+// coalesce when cases leave). A time step of all cases is one CUDA graph --
+// a memset of the barrier counters and one persistent kernel per RK stage --
+// whose kernels read the case table and tile lists from device memory, so
+// admissions and removals between steps only rewrite those tables.
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../host/capi_internal.h"
+#include "args_setup.h"
+#include "batch.cuh"
+#include "lfm_gpu.h"
+#include "solver_launch.h"
+
+using lfm::dev::Args;
+using lfm::dev::BatchArgs;
+using lfm::dev::BatchCase;
+using lfm::dev::BatchCtl;
+using lfm::dev::BatchTile;
+using lfm::dev::kBatchMaxStages;
+using lfm::dev::kBatchPhases;
+
+namespace {
+
+constexpr size_t kAlign = 256;
+inline size_t roundUp(size_t b) { return (b + kAlign - 1) & ~(kAlign - 1); }
+
+int cudaFail(cudaError_t e, const char* what) {
+    return lfm::setError(e == cudaErrorMemoryAllocation ? LFM_ERR_NOMEM : LFM_ERR_CUDA,
+                         std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define LFM_CUDA(call)                                       \
+    do {                                                     \
+        cudaError_t e__ = (call);                            \
+        if (e__ != cudaSuccess) return cudaFail(e__, #call); \
+    } while (0)
+
+// First-fit allocator over [0, size) in 256-byte granules; free ranges are
+// kept sorted by offset and coalesced on release.
+class Arena {
+public:
+    void reset(size_t size) {
+        free_.clear();
+        size_ = size & ~(kAlign - 1);
+        if (size_) free_[0] = size_;
+    }
+    bool alloc(size_t bytes, size_t* off) {
+        bytes = roundUp(bytes);
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= bytes) {
+                *off = it->first;
+                const size_t rest = it->second - bytes;
+                const size_t at = it->first + bytes;
+                free_.erase(it);
+                if (rest) free_[at] = rest;
+                return true;
+            }
+        }
+        return false;
+    }
+    void release(size_t off, size_t bytes) {
+        bytes = roundUp(bytes);
+        auto it = free_.emplace(off, bytes).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_.erase(nx);
+        }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+    size_t largest() const {
+        size_t m = 0;
+        for (auto& kv : free_) m = std::max(m, kv.second);
+        return m;
+    }
+    size_t total() const {
+        size_t m = 0;
+        for (auto& kv : free_) m += kv.second;
+        return m;
+    }
+    size_t size() const { return size_; }
+
+private:
+    std::map<size_t, size_t> free_;
+    size_t size_ = 0;
+};
+
+// Byte offsets of every array of one case inside its arena block.
+struct CaseLayout {
+    size_t total = 0;
+    size_t q, dq, res, prim, V, grad, flux, S, d, w, dinv, dnorm, K, lapc, fP, fN, fGhost, volInv, volInv32,
+        sponge, cfOff, cfList, gCell, gKind, gFace;
+
+    explicit CaseLayout(const lfm_solver_desc* d) {
+        const size_t D = (size_t)d->dim, nq = (size_t)d->nq, nc = (size_t)d->n_cells, ng = (size_t)d->n_ghosts;
+        const size_t nt = nc + ng, nf = (size_t)d->n_faces, ne = (size_t)d->cell_face_offsets[nc];
+        const bool ausm = d->solver == LFM_SOLVER_M2AUSM;
+        q = add(nq * nt * 8);
+        dq = add(nq * nc * 8);
+        res = d->residuals ? add(nq * nc * 8) : npos();
+        prim = add((size_t)lfm::dev::primRows<float>(d->dim) * nt * 4);
+        V = lfm::setup::needVis(d) ? add((D * D + 2 * D) * nt * 4) : npos();
+        grad = ausm ? add((2 * D + D * D) * nt * 4) : npos();
+        flux = add(nq * nf * 4);
+        S = add(D * nf * 4);
+        this->d = add(D * nf * 4);
+        w = add(nf * 4);
+        dinv = add(nf * 4);
+        dnorm = add(D * nf * 4);
+        K = add(D * nf * 4);
+        lapc = add(nf * 4);
+        fP = add(nf * 4);
+        fN = add(nf * 4);
+        fGhost = add(nf);
+        volInv = add(nc * 8);
+        volInv32 = add(nc * 4);
+        sponge = add(nc * 8);
+        cfOff = add((nc + 1) * 4);
+        cfList = add(ne * 4);
+        gCell = add(ng * 4);
+        gKind = add(ng * 4);
+        gFace = add(ng * 4);
+    }
+    static size_t npos() { return ~(size_t)0; }
+
+private:
+    size_t add(size_t bytes) {
+        const size_t at = total;
+        total += roundUp(bytes ? bytes : 1);
+        return at;
+    }
+};
+
+// Host image of a case's arena block: constant arrays and the initial state
+// in their final device layout, scratch zero-filled (the viscous terms and
+// gradients of ghosts are read as zeros).
+std::vector<unsigned char> packCase(const lfm_solver_desc* d, const CaseLayout& L) {
+    std::vector<unsigned char> img(L.total, 0);
+    const size_t D = (size_t)d->dim, nq = (size_t)d->nq, nc = (size_t)d->n_cells, ng = (size_t)d->n_ghosts;
+    const size_t nt = nc + ng, nf = (size_t)d->n_faces;
+    auto f64 = [&](size_t off) { return reinterpret_cast<double*>(img.data() + off); };
+    auto f32 = [&](size_t off) { return reinterpret_cast<float*>(img.data() + off); };
+    auto i32 = [&](size_t off) { return reinterpret_cast<int*>(img.data() + off); };
+    auto conv = [&](size_t off, const double* src, size_t n) {
+        float* p = f32(off);
+        for (size_t k = 0; k < n; ++k) p[k] = (float)src[k];
+    };
+    if (d->q0)
+        for (size_t v = 0; v < nq; ++v) std::memcpy(f64(L.q) + v * nt, d->q0 + v * nc, nc * 8);
+    conv(L.S, d->S, D * nf);
+    conv(L.d, d->d, D * nf);
+    conv(L.w, d->w, nf);
+    conv(L.dinv, d->dmag_inv, nf);
+    conv(L.dnorm, d->dnorm, D * nf);
+    conv(L.K, d->K, D * nf);
+    lfm::setup::DescIndex ix(d);
+    conv(L.lapc, ix.lapc.data(), nf);
+    std::memcpy(i32(L.fP), ix.fP.data(), nf * 4);
+    std::memcpy(i32(L.fN), ix.fN.data(), nf * 4);
+    std::memcpy(img.data() + L.fGhost, d->face_ghost, nf);
+    std::memcpy(f64(L.volInv), d->vol_inv, nc * 8);
+    conv(L.volInv32, d->vol_inv, nc);
+    std::memcpy(f64(L.sponge), d->sponge, nc * 8);
+    std::memcpy(i32(L.cfOff), ix.cfOff.data(), (nc + 1) * 4);
+    std::memcpy(i32(L.cfList), ix.cfList.data(), ix.cfList.size() * 4);
+    if (ng) {
+        std::memcpy(i32(L.gCell), ix.gCell.data(), ng * 4);
+        std::memcpy(i32(L.gKind), ix.gKind.data(), ng * 4);
+        std::memcpy(i32(L.gFace), ix.gFace.data(), ng * 4);
+    }
+    return img;
+}
+
+struct Slot {
+    bool used = false;
+    size_t off = 0, bytes = 0;
+    int D = 2, nq = 4, nc = 0, ng = 0, nf = 0, nt = 0;
+    bool needGradVis = false;
+    double* q = nullptr;   // device
+};
+
+}  // namespace
+
+struct lfm_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int rkOrder = 5;
+    int maxCases = 0;
+    unsigned char* arenaBase = nullptr;
+    Arena arena;
+    BatchCase* dCases = nullptr;
+    int* dFlags = nullptr;
+    int* dError = nullptr;
+    BatchCtl* dCtl = nullptr;
+    BatchTile* dTiles[kBatchPhases] = {};
+    size_t tileCap[kBatchPhases] = {};
+    int* dNTiles = nullptr;
+    std::vector<Slot> slots;
+    int sms = 0;
+    lfm_batch_tuning tune{256, 1, 0, 1};
+    int grid = 0;
+    bool tilesDirty = true;
+    cudaGraphExec_t graph = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    void* scrub = nullptr;
+    size_t scrubBytes = 0;
+};
+
+namespace {
+
+int rebuildTiles(lfm_batch* b) {
+    const int tileSize = b->tune.block * b->tune.items_per_thread;
+    std::vector<BatchTile> tl[kBatchPhases];
+    for (int s = 0; s < (int)b->slots.size(); ++s) {
+        const Slot& sl = b->slots[(size_t)s];
+        if (!sl.used) continue;
+        const int counts[kBatchPhases] = {sl.nt, sl.needGradVis ? sl.nc : 0, sl.nf, sl.nc};
+        for (int ph = 0; ph < kBatchPhases; ++ph)
+            for (int st = 0; st < counts[ph]; st += tileSize)
+                tl[ph].push_back(BatchTile{s, st, std::min(tileSize, counts[ph] - st), 0});
+    }
+    int n[kBatchPhases];
+    bool realloc = false;
+    for (int ph = 0; ph < kBatchPhases; ++ph) {
+        n[ph] = (int)tl[ph].size();
+        if (tl[ph].size() > b->tileCap[ph] || !b->dTiles[ph]) {
+            LFM_CUDA(cudaStreamSynchronize(b->stream));
+            if (b->dTiles[ph]) cudaFree(b->dTiles[ph]);
+            b->dTiles[ph] = nullptr;
+            const size_t cap = std::max<size_t>(1024, tl[ph].size() + tl[ph].size() / 2);
+            LFM_CUDA(cudaMalloc(&b->dTiles[ph], cap * sizeof(BatchTile)));
+            b->tileCap[ph] = cap;
+            realloc = true;
+        }
+        if (n[ph])
+            LFM_CUDA(cudaMemcpyAsync(b->dTiles[ph], tl[ph].data(), tl[ph].size() * sizeof(BatchTile),
+                                     cudaMemcpyHostToDevice, b->stream));
+    }
+    LFM_CUDA(cudaMemcpyAsync(b->dNTiles, n, sizeof(n), cudaMemcpyHostToDevice, b->stream));
+    // the host vectors die here: wait for the copies out of them
+    LFM_CUDA(cudaStreamSynchronize(b->stream));
+    if (realloc && b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    b->tilesDirty = false;
+    return LFM_OK;
+}
+
+BatchArgs makeArgs(lfm_batch* b) {
+    BatchArgs a{};
+    a.cases = b->dCases;
+    for (int ph = 0; ph < kBatchPhases; ++ph) a.tiles[ph] = b->dTiles[ph];
+    a.nTiles = b->dNTiles;
+    a.ctl = b->dCtl;
+    a.error = b->dError;
+    a.itemsPerThread = b->tune.items_per_thread;
+    return a;
+}
+
+int captureStep(lfm_batch* b, bool cooperative, cudaGraphExec_t* out) {
+    const BatchArgs args = makeArgs(b);
+    cudaGraph_t g = nullptr;
+    LFM_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t le = cudaMemsetAsync(b->dCtl, 0, sizeof(BatchCtl), b->stream);
+    for (int k = 0; k < b->rkOrder && le == cudaSuccess; ++k)
+        le = lfm::dev::launch_batch_stage(args, k, b->tune.block, b->grid, cooperative, b->stream);
+    cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (le != cudaSuccess || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return cudaFail(le != cudaSuccess ? le : e, "batch step capture");
+    }
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return cudaFail(e, "cudaGraphInstantiate");
+    }
+    return LFM_OK;
+}
+
+// Grid of the persistent kernel: blocks_per_sm (0 = all that fit) x SMs,
+// never above the resident capacity (the grid barriers need every block
+// resident).
+int ensureGraph(lfm_batch* b) {
+    if (b->tilesDirty) {
+        int rc = rebuildTiles(b);
+        if (rc) return rc;
+    }
+    if (b->graph) return LFM_OK;
+    const int fit = lfm::dev::batch_blocks_per_sm(b->tune.block);
+    if (fit <= 0) return lfm::setError(LFM_ERR_UNSUPPORTED, "batch kernel does not fit on an SM");
+    const int bps = b->tune.blocks_per_sm > 0 ? std::min(b->tune.blocks_per_sm, fit) : fit;
+    b->grid = bps * b->sms;
+    // A cooperative launch guarantees co-residency; where capture of one is
+    // refused, a grid within the resident capacity is launched plainly.
+    int rc = LFM_ERR_CUDA;
+    if (b->tune.cooperative) rc = captureStep(b, true, &b->graph);
+    if (rc != LFM_OK) {
+        b->tune.cooperative = 0;
+        rc = captureStep(b, false, &b->graph);
+    }
+    return rc;
+}
+
+int checkSlot(const lfm_batch* b, int slot) {
+    if (!b) return lfm::setError(LFM_ERR_INVALID, "null batch");
+    if (slot < 0 || slot >= (int)b->slots.size() || !b->slots[(size_t)slot].used)
+        return lfm::setError(LFM_ERR_INVALID, "no case in slot " + std::to_string(slot));
+    return LFM_OK;
+}
+
+}  // namespace
+
+extern "C" int lfm_batch_case_bytes(const lfm_solver_desc* d, size_t* bytes) {
+    if (!bytes) return lfm::setError(LFM_ERR_INVALID, "null argument");
+    int rc = lfm::setup::validateDesc(d);
+    if (rc) return rc;
+    *bytes = CaseLayout(d).total;
+    return LFM_OK;
+}
+
+extern "C" int lfm_batch_create(const lfm_batch_opts* opts, lfm_batch** out) {
+    if (!out) return lfm::setError(LFM_ERR_INVALID, "null output handle");
+    *out = nullptr;
+    lfm_batch_opts o{0, 5, 0, 256};
+    if (opts) o = *opts;
+    if (o.rk_order < 1 || o.rk_order > kBatchMaxStages) return lfm::setError(LFM_ERR_INVALID, "rk_order out of range");
+    if (o.max_cases <= 0) o.max_cases = 256;
+    LFM_CUDA(cudaSetDevice(o.device));
+    lfm_batch* b = new lfm_batch;
+    b->device = o.device;
+    b->rkOrder = o.rk_order;
+    b->maxCases = o.max_cases;
+    auto fail = [&](int rc) {
+        lfm_batch_destroy(b);
+        return rc;
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return fail(cudaFail(e, "cudaStreamCreate"));
+    cudaEventCreate(&b->ev0);
+    cudaEventCreate(&b->ev1);
+    cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
+    size_t arena = o.arena_bytes;
+    if (arena == 0) {
+        size_t fr = 0, tot = 0;
+        cudaMemGetInfo(&fr, &tot);
+        arena = fr / 4;
+    }
+    arena = roundUp(arena);
+    if ((e = cudaMalloc(&b->arenaBase, arena)) != cudaSuccess) return fail(cudaFail(e, "cudaMalloc arena"));
+    b->arena.reset(arena);
+    if ((e = cudaMalloc(&b->dCases, sizeof(BatchCase) * (size_t)b->maxCases)) != cudaSuccess ||
+        (e = cudaMalloc(&b->dFlags, sizeof(int) * (size_t)b->maxCases)) != cudaSuccess ||
+        (e = cudaMalloc(&b->dError, sizeof(int))) != cudaSuccess ||
+        (e = cudaMalloc(&b->dCtl, sizeof(BatchCtl))) != cudaSuccess ||
+        (e = cudaMalloc(&b->dNTiles, sizeof(int) * kBatchPhases)) != cudaSuccess)
+        return fail(cudaFail(e, "cudaMalloc batch tables"));
+    cudaMemsetAsync(b->dFlags, 0, sizeof(int) * (size_t)b->maxCases, b->stream);
+    cudaMemsetAsync(b->dError, 0, sizeof(int), b->stream);
+    cudaMemsetAsync(b->dNTiles, 0, sizeof(int) * kBatchPhases, b->stream);
+    b->slots.resize((size_t)b->maxCases);
+    if ((e = cudaStreamSynchronize(b->stream)) != cudaSuccess) return fail(cudaFail(e, "batch create"));
+    *out = b;
+    return LFM_OK;
+}
+
+extern "C" void lfm_batch_destroy(lfm_batch* b) {
+    if (!b) return;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (int ph = 0; ph < kBatchPhases; ++ph)
+        if (b->dTiles[ph]) cudaFree(b->dTiles[ph]);
+    cudaFree(b->arenaBase);
+    cudaFree(b->dCases);
+    cudaFree(b->dFlags);
+    cudaFree(b->dError);
+    cudaFree(b->dCtl);
+    cudaFree(b->dNTiles);
+    if (b->scrub) cudaFree(b->scrub);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+extern "C" int lfm_batch_add(lfm_batch* b, const lfm_solver_desc* d, double dt, int* slot) {
+    if (!b || !slot) return lfm::setError(LFM_ERR_INVALID, "null argument");
+    *slot = -1;
+    int rc = lfm::setup::validateDesc(d);
+    if (rc) return rc;
+    if (d->rk_order != b->rkOrder)
+        return lfm::setError(LFM_ERR_INVALID, "case rk_order " + std::to_string(d->rk_order) +
+                                                  " differs from the batch's " + std::to_string(b->rkOrder));
+    if (!(dt > 0.0)) return lfm::setError(LFM_ERR_INVALID, "dt must be positive");
+    int s = -1;
+    for (int k = 0; k < (int)b->slots.size(); ++k)
+        if (!b->slots[(size_t)k].used) {
+            s = k;
+            break;
+        }
+    if (s < 0) return lfm::setError(LFM_ERR_NOMEM, "batch has no free case slot");
+    const CaseLayout L(d);
+    size_t off = 0;
+    if (!b->arena.alloc(L.total, &off))
+        return lfm::setError(LFM_ERR_NOMEM, "case needs " + std::to_string(L.total) + " bytes; largest free arena block " +
+                                                std::to_string(b->arena.largest()));
+    LFM_CUDA(cudaSetDevice(b->device));
+    std::vector<unsigned char> img = packCase(d, L);
+    unsigned char* base = b->arenaBase + off;
+    cudaError_t e = cudaMemcpyAsync(base, img.data(), img.size(), cudaMemcpyHostToDevice, b->stream);
+    BatchCase bc;
+    std::memset(&bc, 0, sizeof(bc));
+    Args<float>& a = bc.a;
+    lfm::setup::setConstants(a, d);
+    auto P = [&](size_t o) -> unsigned char* { return o == CaseLayout::npos() ? nullptr : base + o; };
+    a.q = reinterpret_cast<double*>(P(L.q));
+    a.dq = reinterpret_cast<double*>(P(L.dq));
+    a.res = reinterpret_cast<double*>(P(L.res));
+    a.prim = reinterpret_cast<float*>(P(L.prim));
+    a.V = reinterpret_cast<float*>(P(L.V));
+    a.grad = reinterpret_cast<float*>(P(L.grad));
+    a.flux = reinterpret_cast<float*>(P(L.flux));
+    a.S = reinterpret_cast<const float*>(P(L.S));
+    a.d = reinterpret_cast<const float*>(P(L.d));
+    a.w = reinterpret_cast<const float*>(P(L.w));
+    a.dinv = reinterpret_cast<const float*>(P(L.dinv));
+    a.dnorm = reinterpret_cast<const float*>(P(L.dnorm));
+    a.K = reinterpret_cast<const float*>(P(L.K));
+    a.lapc = reinterpret_cast<const float*>(P(L.lapc));
+    a.fP = reinterpret_cast<const int*>(P(L.fP));
+    a.fN = reinterpret_cast<const int*>(P(L.fN));
+    a.fGhost = reinterpret_cast<const uint8_t*>(P(L.fGhost));
+    a.volInv = reinterpret_cast<const double*>(P(L.volInv));
+    a.volInv32 = reinterpret_cast<const float*>(P(L.volInv32));
+    a.sponge = reinterpret_cast<const double*>(P(L.sponge));
+    a.cfOff = reinterpret_cast<const int*>(P(L.cfOff));
+    a.cfList = reinterpret_cast<const int*>(P(L.cfList));
+    a.gCell = reinterpret_cast<const int*>(P(L.gCell));
+    a.gKind = reinterpret_cast<const int*>(P(L.gKind));
+    a.gFace = reinterpret_cast<const int*>(P(L.gFace));
+    a.flag = b->dFlags + s;
+    bc.dt = dt;
+    for (int k = 0; k < d->rk_order; ++k) {
+        bc.rkA[k] = d->rkA[k];
+        bc.rkB[k] = d->rkB[k];
+    }
+    bc.scheme = d->solver;
+    bc.needGrad = lfm::setup::needGrad(d) ? 1 : 0;
+    bc.needVis = lfm::setup::needVis(d) ? 1 : 0;
+    bc.residuals = d->residuals ? 1 : 0;
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b->dCases + s, &bc, sizeof(bc), cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->dFlags + s, 0, sizeof(int), b->stream);
+    // img and bc are host temporaries: the copies must finish before they go
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) {
+        b->arena.release(off, L.total);
+        return cudaFail(e, "batch case upload");
+    }
+    Slot& sl = b->slots[(size_t)s];
+    sl.used = true;
+    sl.off = off;
+    sl.bytes = L.total;
+    sl.D = d->dim;
+    sl.nq = d->nq;
+    sl.nc = (int)d->n_cells;
+    sl.ng = (int)d->n_ghosts;
+    sl.nf = (int)d->n_faces;
+    sl.nt = sl.nc + sl.ng;
+    sl.needGradVis = bc.needGrad || bc.needVis;
+    sl.q = a.q;
+    b->tilesDirty = true;
+    *slot = s;
+    return LFM_OK;
+}
+
+extern "C" int lfm_batch_remove(lfm_batch* b, int slot) {
+    int rc = checkSlot(b, slot);
+    if (rc) return rc;
+    LFM_CUDA(cudaSetDevice(b->device));
+    // the arena block may still be in use by queued steps
+    LFM_CUDA(cudaStreamSynchronize(b->stream));
+    Slot& sl = b->slots[(size_t)slot];
+    b->arena.release(sl.off, sl.bytes);
+    sl = Slot();
+    b->tilesDirty = true;
+    return LFM_OK;
+}
+
+extern "C" int lfm_batch_set_state(lfm_batch* b, int slot, const double* q) {
+    int rc = checkSlot(b, slot);
+    if (rc) return rc;
+    if (!q) return lfm::setError(LFM_ERR_INVALID, "null state");
+    const Slot& sl = b->slots[(size_t)slot];
+    LFM_CUDA(cudaSetDevice(b->device));
+    for (int v = 0; v < sl.nq; ++v)
+        LFM_CUDA(cudaMemcpyAsync(sl.q + (size_t)v * sl.nt, q + (size_t)v * sl.nc, (size_t)sl.nc * sizeof(double),
+                                 cudaMemcpyHostToDevice, b->stream));
+    LFM_CUDA(cudaStreamSynchronize(b->stream));
+    return LFM_OK;
+}
+
+extern "C" int lfm_batch_get_state(lfm_batch* b, int slot, double* q) {
+    int rc = checkSlot(b, slot);
+    if (rc) return rc;
+    if (!q) return lfm::setError(LFM_ERR_INVALID, "null state");
+    const Slot& sl = b->slots[(size_t)slot];
+    LFM_CUDA(cudaSetDevice(b->device));
+    for (int v = 0; v < sl.nq; ++v)
+        LFM_CUDA(cudaMemcpyAsync(q + (size_t)v * sl.nc, sl.q + (size_t)v * sl.nt, (size_t)sl.nc * sizeof(double),
+                                 cudaMemcpyDeviceToHost, b->stream));
+    LFM_CUDA(cudaStreamSynchronize(b->stream));
+    return LFM_OK;
+}
+
+extern "C" int lfm_batch_step(lfm_batch* b, int nsteps) {
+    if (!b) return lfm::setError(LFM_ERR_INVALID, "null batch");
+    if (nsteps < 0) return lfm::setError(LFM_ERR_INVALID, "negative step count");
+    LFM_CUDA(cudaSetDevice(b->device));
+    int rc = ensureGraph(b);
+    if (rc) return rc;
+    for (int k = 0; k < nsteps; ++k) LFM_CUDA(cudaGraphLaunch(b->graph, b->stream));
+    return LFM_OK;
+}
+
+extern "C" int lfm_batch_sync(lfm_batch* b) {
+    if (!b) return lfm::setError(LFM_ERR_INVALID, "null batch");
+    LFM_CUDA(cudaSetDevice(b->device));
+    LFM_CUDA(cudaStreamSynchronize(b->stream));
+    int err = 0;
+    LFM_CUDA(cudaMemcpy(&err, b->dError, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) return lfm::setError(LFM_ERR_CUDA, "batch stage kernel: a grid barrier gave up waiting");
+    std::vector<int> flags((size_t)b->maxCases);
+    LFM_CUDA(cudaMemcpy(flags.data(), b->dFlags, flags.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    std::string bad;
+    for (int s = 0; s < b->maxCases; ++s)
+        if (b->slots[(size_t)s].used && flags[(size_t)s]) bad += (bad.empty() ? "" : ", ") + std::to_string(s);
+    if (!bad.empty()) return lfm::setError(LFM_ERR_NUMERIC, "non-finite state in batch slot(s) " + bad);
+    return LFM_OK;
+}
+
+extern "C" int lfm_batch_case_status(lfm_batch* b, int slot, int* status) {
+    int rc = checkSlot(b, slot);
+    if (rc) return rc;
+    if (!status) return lfm::setError(LFM_ERR_INVALID, "null argument");
+    LFM_CUDA(cudaSetDevice(b->device));
+    LFM_CUDA(cudaStreamSynchronize(b->stream));
+    int f = 0;
+    LFM_CUDA(cudaMemcpy(&f, b->dFlags + slot, sizeof(int), cudaMemcpyDeviceToHost));
+    *status = f ? LFM_ERR_NUMERIC : LFM_OK;
+    return LFM_OK;
+}
+
+extern "C" int lfm_batch_memory(const lfm_batch* b, size_t* largest_free, size_t* total_free, size_t* arena_bytes) {
+    if (!b) return lfm::setError(LFM_ERR_INVALID, "null batch");
+    if (largest_free) *largest_free = b->arena.largest();
+    if (total_free) *total_free = b->arena.total();
+    if (arena_bytes) *arena_bytes = b->arena.size();
+    return LFM_OK;
+}
+
+extern "C" int lfm_batch_cells(const lfm_batch* b, int64_t* cells, int* cases) {
+    if (!b) return lfm::setError(LFM_ERR_INVALID, "null batch");
+    int64_t n = 0;
+    int k = 0;
+    for (const Slot& s : b->slots)
+        if (s.used) {
+            n += s.nc;
+            ++k;
+        }
+    if (cells) *cells = n;
+    if (cases) *cases = k;
+    return LFM_OK;
+}
+
+extern "C" int lfm_batch_get_tuning(const lfm_batch* b, lfm_batch_tuning* t) {
+    if (!b || !t) return lfm::setError(LFM_ERR_INVALID, "null argument");
+    *t = b->tune;
+    return LFM_OK;
+}
+
+extern "C" int lfm_batch_set_tuning(lfm_batch* b, const lfm_batch_tuning* t) {
+    if (!b || !t) return lfm::setError(LFM_ERR_INVALID, "null argument");
+    if (t->block != 128 && t->block != 256 && t->block != 512)
+        return lfm::setError(LFM_ERR_INVALID, "block must be 128, 256 or 512");
+    if (t->items_per_thread < 1 || t->items_per_thread > 16 || t->blocks_per_sm < 0)
+        return lfm::setError(LFM_ERR_INVALID, "items_per_thread must be 1..16 and blocks_per_sm >= 0");
+    LFM_CUDA(cudaSetDevice(b->device));
+    LFM_CUDA(cudaStreamSynchronize(b->stream));
+    b->tune = *t;
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    b->tilesDirty = true;
+    return LFM_OK;
+}
+
+namespace {
+
+int flushL2(lfm_batch* b, size_t bytes) {
+    if (bytes == 0) return LFM_OK;
+    if (b->scrubBytes < bytes) {
+        if (b->scrub) cudaFree(b->scrub);
+        b->scrub = nullptr;
+        b->scrubBytes = 0;
+        LFM_CUDA(cudaMalloc(&b->scrub, bytes));
+        b->scrubBytes = bytes;
+    }
+    LFM_CUDA(cudaMemsetAsync(b->scrub, 0x5a, bytes, b->stream));
+    return LFM_OK;
+}
+
+}  // namespace
+
+extern "C" int lfm_batch_bench(lfm_batch* b, int nsteps, size_t flush_bytes, float* ms) {
+    if (!b || !ms || nsteps < 0) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    LFM_CUDA(cudaSetDevice(b->device));
+    int rc = ensureGraph(b);
+    if (rc) return rc;
+    std::vector<cudaEvent_t> ev(2 * (size_t)nsteps);
+    for (auto& e : ev) LFM_CUDA(cudaEventCreate(&e));
+    for (int k = 0; k < nsteps; ++k) {
+        if ((rc = flushL2(b, flush_bytes))) break;
+        cudaEventRecord(ev[2 * (size_t)k], b->stream);
+        cudaGraphLaunch(b->graph, b->stream);
+        cudaEventRecord(ev[2 * (size_t)k + 1], b->stream);
+    }
+    cudaError_t e = cudaStreamSynchronize(b->stream);
+    for (int k = 0; k < nsteps && e == cudaSuccess; ++k)
+        e = cudaEventElapsedTime(&ms[k], ev[2 * (size_t)k], ev[2 * (size_t)k + 1]);
+    for (auto& x : ev) cudaEventDestroy(x);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cudaFail(e, "batch bench");
+    return lfm_batch_sync(b);
+}
+
+// Tries every (block, items per thread, blocks per SM) candidate on the
+// batch's current cases for `trial_steps` steps each and keeps the fastest.
+// The cases' states are saved before and restored after.
+extern "C" int lfm_batch_autotune(lfm_batch* b, int trial_steps, lfm_batch_tuning* chosen) {
+    if (!b) return lfm::setError(LFM_ERR_INVALID, "null batch");
+    if (trial_steps < 1) trial_steps = 2;
+    LFM_CUDA(cudaSetDevice(b->device));
+    LFM_CUDA(cudaStreamSynchronize(b->stream));
+    // snapshot of every case's q (cells and ghosts)
+    size_t snapBytes = 0;
+    for (const Slot& s : b->slots)
+        if (s.used) snapBytes += (size_t)s.nq * s.nt * sizeof(double);
+    double* snap = nullptr;
+    if (snapBytes) LFM_CUDA(cudaMalloc(&snap, snapBytes));
+    auto copyStates = [&](bool save) -> cudaError_t {
+        size_t at = 0;
+        for (const Slot& s : b->slots) {
+            if (!s.used) continue;
+            const size_t n = (size_t)s.nq * s.nt;
+            cudaError_t e = save ? cudaMemcpyAsync(snap + at, s.q, n * 8, cudaMemcpyDeviceToDevice, b->stream)
+                                 : cudaMemcpyAsync(s.q, snap + at, n * 8, cudaMemcpyDeviceToDevice, b->stream);
+            if (e != cudaSuccess) return e;
+            at += n;
+        }
+        return cudaSuccess;
+    };
+    cudaError_t e = copyStates(true);
+    const lfm_batch_tuning start = b->tune;
+    lfm_batch_tuning best = start;
+    float bestMs = 1e30f;
+    const int blocks[3] = {128, 256, 512};
+    const int ipts[3] = {1, 2, 4};
+    int rc = LFM_OK;
+    for (int bi = 0; bi < 3 && e == cudaSuccess && rc == LFM_OK; ++bi) {
+        const int fit = lfm::dev::batch_blocks_per_sm(blocks[bi]);
+        for (int ii = 0; ii < 3 && rc == LFM_OK; ++ii) {
+            for (int bps = 1; bps <= fit && rc == LFM_OK; ++bps) {
+                lfm_batch_tuning t{blocks[bi], ipts[ii], bps, start.cooperative};
+                if ((rc = lfm_batch_set_tuning(b, &t))) break;
+                if ((rc = lfm_batch_step(b, 1))) break;   // warm-up, builds tiles and graph
+                cudaEventRecord(b->ev0, b->stream);
+                if ((rc = lfm_batch_step(b, trial_steps))) break;
+                cudaEventRecord(b->ev1, b->stream);
+                if ((e = cudaStreamSynchronize(b->stream)) != cudaSuccess) break;
+                float ms = 0;
+                cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+                if (ms < bestMs) {
+                    bestMs = ms;
+                    best = b->tune;
+                }
+            }
+        }
+    }
+    if (e == cudaSuccess) e = copyStates(false);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->dFlags, 0, sizeof(int) * (size_t)b->maxCases, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (snap) cudaFree(snap);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cudaFail(e, "batch autotune");
+    rc = lfm_batch_set_tuning(b, &best);
+    if (rc) return rc;
+    if (chosen) *chosen = best;
+    return LFM_OK;
+}
+
+extern "C" int lfm_batch_launches_per_step(const lfm_batch* b, int* launches) {
+    if (!b || !launches) return lfm::setError(LFM_ERR_INVALID, "null argument");
+    *launches = b->rkOrder;
+    return LFM_OK;
+}

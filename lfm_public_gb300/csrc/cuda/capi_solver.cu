@@ -11,6 +11,7 @@
 
 #include "../host/capi_internal.h"
 #include "lfm_gpu.h"
+#include "args_setup.h"
 #include "solver_launch.h"
 
 using lfm::dev::Args;
@@ -106,12 +107,7 @@ template <typename T>
 int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP, const int* fN,
               const uint8_t* fGhost, const int* cfOff, const int* cfList, const int* gCell, const int* gKind,
               const int* gFace, const double* sponge) {
-    a.D = s->D;
-    a.nq = s->nq;
-    a.nc = s->nc;
-    a.ng = s->ng;
-    a.nf = s->nf;
-    a.nt = s->nt;
+    lfm::setup::setConstants(a, d);
     a.q = s->q;
     a.res = s->res;
     a.fP = fP;
@@ -125,46 +121,6 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
     a.gKind = gKind;
     a.gFace = gFace;
     a.flag = s->flag;
-    a.gamma = d->gamma;
-    a.gm1 = d->gamma - 1.0;
-    a.Rinv = 1.0 / d->Rgas;
-    a.rhoInf = d->rhoInf;
-    a.EInf = d->EInf;
-    a.pInf = d->pInf;
-    a.TInf = d->TInf;
-    for (int k = 0; k < 3; ++k) a.UInf[k] = d->UInf[k];
-    a.mu = d->mu;
-    a.kcond = d->Cp * d->mu * d->PrInv;
-    {
-        // Reference state of the FP32 perturbation form: any constant state
-        // works (its flux through a closed cell sums to zero); the free stream
-        // keeps the perturbations small. Its pressure follows from q_ref.
-        const int Dm = s->D;
-        double u2 = 0.0;
-        for (int k = 0; k < Dm; ++k) u2 += d->UInf[k] * d->UInf[k];
-        a.qRef[0] = d->rhoInf;
-        for (int k = 0; k < 3; ++k) a.qRef[1 + k] = 0.0;
-        for (int k = 0; k < Dm; ++k) a.qRef[1 + k] = d->rhoInf * d->UInf[k];
-        a.qRef[Dm + 1] = d->rhoInf * d->EInf;
-        const double pRef = (d->gamma - 1.0) * (a.qRef[Dm + 1] - 0.5 * d->rhoInf * u2);
-        const double RpsiRef = pRef / d->rhoInf;
-        a.pRef = pRef;
-        const double gh = d->gamma / (d->gamma - 1.0);
-        a.ref.rho = (float)d->rhoInf;
-        for (int k = 0; k < 3; ++k) {
-            a.ref.U[k] = k < Dm ? (float)d->UInf[k] : 0.0f;
-            a.ref.m[k] = k < Dm ? (float)(d->rhoInf * d->UInf[k]) : 0.0f;
-        }
-        a.ref.Rpsi = (float)RpsiRef;
-        a.ref.p = (float)pRef;
-        a.ref.H = (float)(gh * RpsiRef + 0.5 * u2);
-        a.ref.gh = (float)gh;
-        a.ref.gamma = (float)d->gamma;
-        a.ref.gm1 = (float)(d->gamma - 1.0);
-        a.ref.Rinv = (float)(1.0 / d->Rgas);
-        a.ref.mu = (float)d->mu;
-        a.ref.kcond = (float)(d->Cp * d->mu * d->PrInv);
-    }
     const size_t nt = (size_t)s->nt, nf = (size_t)s->nf, D = (size_t)s->D;
     int rc;
     if ((rc = devAlloc(s, &a.dq, (size_t)s->nq * s->nc))) return rc;
@@ -203,40 +159,6 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
         if ((rc = uploadAs<float>(s, &v32, d->vol_inv, (size_t)s->nc))) return rc;
         a.volInv32 = v32;
     }
-    return LFM_OK;
-}
-
-int validateDesc(const lfm_solver_desc* d) {
-    if (!d) return lfm::setError(LFM_ERR_INVALID, "null solver description");
-    if (d->dim != 2 && d->dim != 3) return lfm::setError(LFM_ERR_INVALID, "dim must be 2 or 3");
-    if (d->nq != d->dim + 2) return lfm::setError(LFM_ERR_INVALID, "nq must be dim + 2");
-    if (d->solver < 0 || d->solver > 2) return lfm::setError(LFM_ERR_INVALID, "unknown solver");
-    if (d->n_cells <= 0 || d->n_faces <= 0 || d->n_ghosts < 0)
-        return lfm::setError(LFM_ERR_INVALID, "empty mesh");
-    if (d->n_cells + d->n_ghosts > 0x7fffffffLL / 32 || d->n_faces > 0x7fffffffLL / 8)
-        return lfm::setError(LFM_ERR_UNSUPPORTED, "mesh too large for 32-bit device indexing");
-    if (!d->face_p || !d->face_n || !d->face_ghost || !d->S || !d->d || !d->w || !d->smag || !d->dmag_inv ||
-        !d->dnorm || !d->delta_mag || !d->K || !d->vol_inv || !d->sponge || !d->cell_face_offsets ||
-        !d->cell_faces || !d->cell_face_sign || !d->cell_s_offsets || !d->cell_s || !d->rkA || !d->rkB ||
-        (d->n_ghosts > 0 && (!d->ghost_cell || !d->ghost_kind)))
-        return lfm::setError(LFM_ERR_INVALID, "incomplete solver description");
-    const int64_t nt = d->n_cells + d->n_ghosts;
-    for (int64_t f = 0; f < d->n_faces; ++f) {
-        if (d->face_p[f] < 0 || d->face_p[f] >= d->n_cells || d->face_n[f] < 0 || d->face_n[f] >= nt)
-            return lfm::setError(LFM_ERR_INVALID, "face index out of range at face " + std::to_string(f));
-        if (f > 0 && d->face_p[f] < d->face_p[f - 1])
-            return lfm::setError(LFM_ERR_INVALID, "faces are not in processing order");
-    }
-    for (int64_t g = 0; g < d->n_ghosts; ++g)
-        if (d->ghost_cell[g] < 0 || d->ghost_cell[g] >= d->n_cells)
-            return lfm::setError(LFM_ERR_INVALID, "ghost cell out of range");
-    for (int64_t c = 0; c < d->n_cells; ++c) {
-        if (d->cell_face_offsets[c + 1] < d->cell_face_offsets[c])
-            return lfm::setError(LFM_ERR_INVALID, "cell_face_offsets not monotone");
-    }
-    for (int64_t e = 0; e < d->cell_face_offsets[d->n_cells]; ++e)
-        if (d->cell_faces[e] < 0 || d->cell_faces[e] >= d->n_faces)
-            return lfm::setError(LFM_ERR_INVALID, "cell_faces entry out of range");
     return LFM_OK;
 }
 
@@ -286,7 +208,7 @@ int ensureGraph(lfm_solver* s, double dt) {
 extern "C" int lfm_solver_create(const lfm_solver_desc* d, const lfm_solver_opts* opts, lfm_solver** out) {
     if (!out) return lfm::setError(LFM_ERR_INVALID, "null output handle");
     *out = nullptr;
-    int rc = validateDesc(d);
+    int rc = lfm::setup::validateDesc(d);
     if (rc) return rc;
     lfm_solver* s = new lfm_solver;
     s->precision = opts ? opts->precision : LFM_FP64;
@@ -321,8 +243,8 @@ extern "C" int lfm_solver_create(const lfm_solver_desc* d, const lfm_solver_opts
     s->rkOrder = d->rk_order;
     s->rkA.assign(d->rkA, d->rkA + d->rk_order);
     s->rkB.assign(d->rkB, d->rkB + d->rk_order);
-    s->needGrad = (d->solver == LFM_SOLVER_M2AUSM) && d->minmod;
-    s->needVis = (d->mu != 0.0) || (d->solver == LFM_SOLVER_M2AUSM);
+    s->needGrad = lfm::setup::needGrad(d);
+    s->needVis = lfm::setup::needVis(d);
     s->residuals = d->residuals != 0;
 
     const size_t nq = (size_t)s->nq, nc = (size_t)s->nc, nt = (size_t)s->nt, nf = (size_t)s->nf;

@@ -137,5 +137,65 @@ __device__ __forceinline__ void stage_state(const Args<T>& a, int t, double* qv)
     for (int v = 0; v < NQ; ++v) a.q[(size_t)v * a.nt + t] = qv[v];
 }
 
+// Gather of the face rhs of cell c, sponge source and low-storage RK update
+// (src/cfd_v0.cpp:2800-2822). The rhs are summed in the flux arithmetic T in
+// ascending face order (the order in which the reference's scatter reaches
+// the cell); the sum is the cell residual RES. The RK registers are FP64. In
+// the FP32-bulk form the increment dt/V * RES is formed in FP32 (its error is
+// that of the FP32 rhs) and only the accumulation runs in FP64.
+template <typename T, int D, bool RES>
+__device__ __forceinline__ void update_cell(const Args<T>& a, int c, double Ak, double Bk, double dt, int first) {
+    constexpr int NQ = D + 2;
+    const size_t nt = (size_t)a.nt, nf = (size_t)a.nf, nc = (size_t)a.nc;
+    T sum[NQ];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) sum[v] = T(0);
+    for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
+        const int code = a.cfList[e];
+        if (code >= 0) {
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) sum[v] += a.flux[v * nf + code];
+        } else {
+            const int f = ~code;
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) sum[v] -= a.flux[v * nf + f];
+        }
+    }
+    double acc[NQ];
+    bool finite = true;
+    if constexpr (sizeof(T) == sizeof(float)) {
+        const float dtvi = (float)dt * a.volInv32[c];
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) {
+            const double inc = (double)(dtvi * sum[v]);
+            acc[v] = first ? inc : fma(Ak, a.dq[v * nc + c], inc);
+            finite = finite && isfinite(sum[v]);
+        }
+    } else {
+        const double dtvi = dt * a.volInv[c];
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) acc[v] = (first ? 0.0 : Ak * a.dq[v * nc + c]) + dtvi * (double)sum[v];
+    }
+    double qv[NQ];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) qv[v] = a.q[v * nt + c];
+    const double sg = a.sponge[c];
+    if (sg != 0.0) {
+        acc[0] += dt * sg * (a.rhoInf - qv[0]);
+#pragma unroll
+        for (int k = 0; k < D; ++k) acc[k + 1] += dt * sg * (a.rhoInf * a.UInf[k] - qv[k + 1]);
+        acc[D + 1] += dt * sg * (a.rhoInf * a.EInf - qv[D + 1]);
+    }
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) {
+        a.dq[v * nc + c] = acc[v];
+        const double qn = qv[v] + Bk * acc[v];
+        if constexpr (sizeof(T) != sizeof(float)) finite = finite && isfinite(qn);
+        a.q[v * nt + c] = qn;
+        if (RES) a.res[v * nc + c] = (double)sum[v];
+    }
+    if (!finite) atomicOr(a.flag, 1);
+}
+
 }  // namespace dev
 }  // namespace lfm

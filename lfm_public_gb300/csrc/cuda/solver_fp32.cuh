@@ -1,0 +1,407 @@
+// FP32-bulk form of the time step: face fluxes, limiter and residual sums in
+// FP32; the RK registers (q, dq), boundary ghost states, geometry precompute
+// and the dt reduction in FP64.
+//
+// Perturbation form. Every FP32 quantity is a deviation from a constant
+// reference state q_ref = (rho_inf, rho_inf U_inf, rho_inf E_inf):
+//   prep32 forms r' = rho - rho_inf, m' = rho u - rho_inf U_inf and
+//   E' = rho E - rho_inf E_inf in FP64 (differences of nearby numbers, exact
+//   or nearly so), rounds them to FP32 and derives u' = u - U_inf and
+//   R psi' = p/rho - p_ref/rho_inf from expressions whose terms are all
+//   perturbation-sized.
+// Each face rhs is then F(q_f).S - F(q_ref).S. The reference-state flux through
+// the faces of a cell sums to F(q_ref).(sum_f S_f) = 0 because the face vectors
+// of a closed cell cancel, so dropping it leaves every cell residual unchanged
+// while FP32 rounding only ever scales perturbations. Evaluated on absolute
+// values, FP32 would round the pressure (~1e5 Pa) by ~1e-2 Pa per face, the
+// size of an acoustic wave; here the rounding is ~1e-7 of the perturbation.
+//
+// The schemes are those of the FP64 kernels (solver_kernels.cu), which follow
+// the reference (src/cfd_v0.cpp:1896-2822): M1 as the central flux its
+// Kurganov-Tadmor formula reduces to, M2 and M2AUSM as written, with the
+// perfect-gas enthalpy h = e + p/rho = gamma/(gamma-1) R psi.
+#pragma once
+
+#include "solver_device.cuh"
+
+namespace lfm {
+namespace dev {
+
+// Row of the FP32 primitive array (rho', m'[D], u'[D], R psi', c).
+template <int D>
+struct PRow {
+    static constexpr int r = 0, m = 1, u = 1 + D, Rpsi = 1 + 2 * D, c = 2 + 2 * D;
+};
+
+__device__ __forceinline__ float ld(const float* p, int row, size_t nt, int i) { return p[(size_t)row * nt + i]; }
+
+// p - p_ref of a state with perturbations r', R psi':
+// rho R psi - rho_inf R psi_inf = rho_inf R psi' + r' (R psi_inf + R psi').
+__device__ __forceinline__ float pressure_dev(const RefState32& R, float r, float Rpsi) {
+    return R.rho * Rpsi + r * (R.Rpsi + Rpsi);
+}
+
+// ---------------------------------------------------------------------------
+// prep32: ghost states (FP64) and perturbation primitives of cell or ghost t.
+// ---------------------------------------------------------------------------
+template <int D>
+__device__ __forceinline__ void prep32(const Args<float>& a, int t) {
+    constexpr int NQ = D + 2;
+    using P = PRow<D>;
+    double qv[NQ];
+    stage_state<float, D>(a, t, qv);
+    const RefState32& R = a.ref;
+    const size_t nt = (size_t)a.nt;
+    const float r = (float)(qv[0] - a.qRef[0]);
+    float m[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) m[k] = (float)(qv[k + 1] - a.qRef[k + 1]);
+    float u[D], Rpsi;
+    if (t < a.nc) {
+        const float E = (float)(qv[D + 1] - a.qRef[D + 1]);
+        const float rho = R.rho + r;
+        const float rinv = 1.0f / rho;
+        float Uu = 0.0f, uu = 0.0f, U2 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            u[k] = (m[k] - R.U[k] * r) * rinv;   // (rho u - rho_inf U_inf - U_inf r') / rho
+            Uu += R.U[k] * u[k];
+            uu += u[k] * u[k];
+            U2 += R.U[k] * R.U[k];
+        }
+        // kinetic energy: rho|u|^2/2 - rho_inf|U_inf|^2/2 = r'|U_inf|^2/2 + rho (U_inf.u' + |u'|^2/2)
+        const float K = 0.5f * r * U2 + rho * (Uu + 0.5f * uu);
+        const float p = R.gm1 * (E - K);  // p - p_ref
+        Rpsi = (p - R.Rpsi * r) * rinv;         // p/rho - p_ref/rho_inf
+    } else {
+        // A ghost state can lie far from the free stream (a wall mirrors the
+        // momentum, u' = -2 U_inf - u'), where the FP32 kinetic-energy
+        // difference above would cancel; ghosts are few, so theirs is FP64.
+        const double rinv = 1.0 / qv[0];
+        double ke = 0.0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            u[k] = (float)(qv[k + 1] * rinv - a.UInf[k]);
+            ke += qv[k + 1] * qv[k + 1];
+        }
+        const double p = a.gm1 * (qv[D + 1] - 0.5 * ke * rinv);
+        Rpsi = (float)(p * rinv - a.pRef / a.qRef[0]);
+    }
+    a.prim[(size_t)P::r * nt + t] = r;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        a.prim[(size_t)(P::m + k) * nt + t] = m[k];
+        a.prim[(size_t)(P::u + k) * nt + t] = u[k];
+    }
+    a.prim[(size_t)P::Rpsi * nt + t] = Rpsi;
+    a.prim[(size_t)P::c * nt + t] = sqrtf(R.gamma * (R.Rpsi + Rpsi));
+}
+
+// ---------------------------------------------------------------------------
+// grad32: Gauss gradients of rho', p' and u' (those of rho, p and u up to
+// the reference state's closed-cell sum) for M2AUSM's minmod reconstruction.
+// ---------------------------------------------------------------------------
+template <int D>
+__device__ __forceinline__ void grad32(const Args<float>& a, int c) {
+    using P = PRow<D>;
+    const RefState32& R = a.ref;
+    const size_t nt = (size_t)a.nt, nf = (size_t)a.nf;
+    float gr[D], gp[D], gu[D][D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        gr[k] = gp[k] = 0.0f;
+#pragma unroll
+        for (int l = 0; l < D; ++l) gu[k][l] = 0.0f;
+    }
+    const float vi = a.volInv32[c];
+    for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
+        const int code = a.cfList[e];
+        const int f = code >= 0 ? code : ~code;
+        const int i = a.fP[f], j = a.fN[f];
+        const float w = a.w[f];
+        float so[D], uu[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            const float Sk = a.S[(size_t)k * nf + f];
+            so[k] = (code >= 0) ? Sk * vi : -Sk * vi;
+            uu[k] = interp(w, ld(a.prim, P::u + k, nt, i), ld(a.prim, P::u + k, nt, j));
+        }
+        const float ri = ld(a.prim, P::r, nt, i), rj = ld(a.prim, P::r, nt, j);
+        const float pi = pressure_dev(R, ri, ld(a.prim, P::Rpsi, nt, i));
+        const float pj = pressure_dev(R, rj, ld(a.prim, P::Rpsi, nt, j));
+        const float rho = interp(w, ri, rj);
+        const float p = interp(w, pi, pj);
+#pragma unroll
+        for (int x = 0; x < D; ++x) {
+            gp[x] += p * so[x];
+            gr[x] += rho * so[x];
+#pragma unroll
+            for (int b = 0; b < D; ++b) gu[b][x] += uu[b] * so[x];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        a.grad[(size_t)k * nt + c] = gr[k];
+        a.grad[(size_t)(D + k) * nt + c] = gp[k];
+#pragma unroll
+        for (int l = 0; l < D; ++l) a.grad[(size_t)(2 * D + k * D + l) * nt + c] = gu[k][l];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// vis32: dudx and dTdx from u' and T', sigmaU = (U_inf + u') . tau.
+// ---------------------------------------------------------------------------
+template <int D>
+__device__ __forceinline__ void vis32(const Args<float>& a, int c) {
+    using P = PRow<D>;
+    const size_t nt = (size_t)a.nt, nf = (size_t)a.nf;
+    float g[D][D], gT[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        gT[k] = 0.0f;
+#pragma unroll
+        for (int l = 0; l < D; ++l) g[k][l] = 0.0f;
+    }
+    const float vi = a.volInv32[c];
+    const float Rinv = a.ref.Rinv;
+    for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
+        const int code = a.cfList[e];
+        const int f = code >= 0 ? code : ~code;
+        const int i = a.fP[f], j = a.fN[f];
+        const float w = a.w[f];
+        float so[D], fU[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            const float Sk = a.S[(size_t)k * nf + f];
+            so[k] = (code >= 0) ? Sk * vi : -Sk * vi;
+            fU[k] = interp(w, ld(a.prim, P::u + k, nt, i), ld(a.prim, P::u + k, nt, j));
+        }
+        const float fT = interp(w, ld(a.prim, P::Rpsi, nt, i), ld(a.prim, P::Rpsi, nt, j)) * Rinv;
+#pragma unroll
+        for (int x = 0; x < D; ++x) {
+#pragma unroll
+            for (int y = 0; y < D; ++y) g[x][y] += fU[x] * so[y];
+            gT[x] += fT * so[x];
+        }
+    }
+    const float mu = a.ref.mu;
+    float tau[D][D];
+    stress<float, D>(g, mu, tau);
+    float U[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) U[k] = a.ref.U[k] + ld(a.prim, P::u + k, nt, c);
+#pragma unroll
+    for (int x = 0; x < D; ++x) {
+#pragma unroll
+        for (int y = 0; y < D; ++y) a.V[(size_t)(x * D + y) * nt + c] = g[x][y];
+        a.V[(size_t)(D * D + x) * nt + c] = gT[x];
+        a.V[(size_t)(D * D + D + x) * nt + c] = dotv<float, D>(U, tau[x]);
+    }
+}
+
+// d(M) = p5pos(M) - p5neg(M) is, for |M| < 1, the odd polynomial
+// (3M - M^3)/2 + 2 alpha M (1 - M^2)^2. Its divided difference
+// (d(a) - d(b)) / (a - b), so that d(MN) - d(MP) is formed as a product with
+// MN - MP instead of a difference of two O(1) numbers.
+__device__ __forceinline__ float p5diff_dd(float a, float b, float alpha) {
+    const float s2 = a * a + a * b + b * b;                                   // (a^3 - b^3)/(a - b)
+    const float s4 = a * a * a * a + a * a * a * b + a * a * b * b + a * b * b * b + b * b * b * b;
+    return 1.5f - 0.5f * s2 + 2.0f * alpha * (1.0f - 2.0f * s2 + s4);
+}
+
+// ---------------------------------------------------------------------------
+// flux32: perturbation rhs of face f, F(q_f).S - F(q_ref).S, plus the
+// viscous terms (linear in the gradients, so unchanged in form).
+// ---------------------------------------------------------------------------
+template <int D, int SCH>
+__device__ __forceinline__ void flux32(const Args<float>& a, int f) {
+    constexpr int NQ = D + 2;
+    using P = PRow<D>;
+    const RefState32& R = a.ref;
+    const size_t nt = (size_t)a.nt, nf = (size_t)a.nf;
+    const int i = a.fP[f], j = a.fN[f];
+    const float w = a.w[f];
+    float S[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) S[k] = a.S[(size_t)k * nf + f];
+    const float ri = ld(a.prim, P::r, nt, i), rj = ld(a.prim, P::r, nt, j);
+    float mi[D], mj[D], ui[D], uj[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        mi[k] = ld(a.prim, P::m + k, nt, i);
+        mj[k] = ld(a.prim, P::m + k, nt, j);
+        ui[k] = ld(a.prim, P::u + k, nt, i);
+        uj[k] = ld(a.prim, P::u + k, nt, j);
+    }
+    const float Ri = ld(a.prim, P::Rpsi, nt, i), Rj = ld(a.prim, P::Rpsi, nt, j);
+    float rhs[NQ];
+
+    // Face state: linear interpolation for M1, the mid-point for M2 / M2AUSM.
+    const float wf = (SCH == kSchemeM1) ? w : 0.5f;
+    const float rf = interp(wf, ri, rj);
+    const float rinv = 1.0f / (R.rho + rf);
+    float mf[D], uf[D];
+    float mS = 0.0f, ufS = 0.0f, UrS = 0.0f, mrS = 0.0f;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        mf[k] = interp(wf, mi[k], mj[k]);
+        uf[k] = (mf[k] - R.U[k] * rf) * rinv;      // u_f - U_inf with u_f = m_f / rho_f
+        mS += mf[k] * S[k];
+        ufS += uf[k] * S[k];
+        UrS += R.U[k] * S[k];
+        mrS += R.m[k] * S[k];
+    }
+    const float phi = UrS + ufS;                    // u_f . S
+    const float Rf = interp(wf, Ri, Rj);
+    float pf = pressure_dev(R, rf, Rf);             // rho_f R psi_f - p_ref
+    float Hf;                                       // H - H_ref
+    if (SCH == kSchemeM1) {
+        // H_f = e_f + |u_f|^2/2 + R psi_f with e_f = R psi_f / (gamma - 1)
+        float Uu = 0.0f, uu = 0.0f;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            Uu += R.U[k] * uf[k];
+            uu += uf[k] * uf[k];
+        }
+        Hf = R.gh * Rf + Uu + 0.5f * uu;
+    } else {
+        // mean of the cells' H = gamma/(gamma-1) R psi + |u|^2/2
+        float Hi = R.gh * Ri, Hj = R.gh * Rj;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            Hi += R.U[k] * ui[k] + 0.5f * ui[k] * ui[k];
+            Hj += R.U[k] * uj[k] + 0.5f * uj[k] * uj[k];
+        }
+        Hf = 0.5f * (Hi + Hj);
+    }
+    if (SCH == kSchemeAUSM) {
+        // shock sensor, minmod reconstructions and AUSM+ pressure dissipation
+        // (src/cfd_v0.cpp:2288-2339) on the perturbation variables; minmod is
+        // invariant under a common shift of both sides.
+        const float cavg = 0.5f * (ld(a.prim, P::c, nt, i) + ld(a.prim, P::c, nt, j));
+        float d[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) d[k] = a.d[(size_t)k * nf + f];
+        float cdiv = 0.0f, ndiv = 0.0f, ccurl = 0.0f, ncurl = 0.0f, unPos = 0.0f, unNeg = 0.0f, dUn = 0.0f,
+              norm = 0.0f;
+#pragma unroll
+        for (int x = 0; x < D; ++x) {
+            cdiv += a.V[(size_t)(x * D + x) * nt + i];
+            ndiv += a.V[(size_t)(x * D + x) * nt + j];
+#pragma unroll
+            for (int y = x + 1; y < D; ++y) {
+                const float cc = a.V[(size_t)(x * D + y) * nt + i] - a.V[(size_t)(y * D + x) * nt + i];
+                const float nn = a.V[(size_t)(x * D + y) * nt + j] - a.V[(size_t)(y * D + x) * nt + j];
+                ccurl += cc * cc;
+                ncurl += nn * nn;
+            }
+            float gi[D], gj[D];
+#pragma unroll
+            for (int y = 0; y < D; ++y) {
+                gi[y] = a.grad[(size_t)(2 * D + x * D + y) * nt + i];
+                gj[y] = a.grad[(size_t)(2 * D + x * D + y) * nt + j];
+            }
+            const float uP = minmod_interp<float, D>(ui[x], uj[x], gi, d, w, 1.0f);
+            const float uN = minmod_interp<float, D>(ui[x], uj[x], gj, d, w, -1.0f);
+            unPos += (R.U[x] + uP) * S[x];
+            unNeg += (R.U[x] + uN) * S[x];
+            dUn += (uN - uP) * S[x];
+            norm += S[x] * S[x];
+        }
+        float ct = -(cdiv / sqrtf(cdiv * cdiv + ccurl + 4e-2f));
+        ct = (ct < 0.0f) ? 0.0f : ct;
+        float nt_ = -(ndiv / sqrtf(ndiv * ndiv + ncurl + 4e-2f));
+        nt_ = (nt_ < 0.0f) ? 0.0f : nt_;
+        const float theta = 0.5f * (ct + nt_);
+        const float pi = pressure_dev(R, ri, Ri), pj = pressure_dev(R, rj, Rj);
+        float gri[D], grj[D], gpi[D], gpj[D];
+#pragma unroll
+        for (int y = 0; y < D; ++y) {
+            gri[y] = a.grad[(size_t)y * nt + i];
+            grj[y] = a.grad[(size_t)y * nt + j];
+            gpi[y] = a.grad[(size_t)(D + y) * nt + i];
+            gpj[y] = a.grad[(size_t)(D + y) * nt + j];
+        }
+        const float rhoPos = R.rho + minmod_interp<float, D>(ri, rj, gri, d, w, 1.0f);
+        const float rhoNeg = R.rho + minmod_interp<float, D>(ri, rj, grj, d, w, -1.0f);
+        const float pPos = minmod_interp<float, D>(pi, pj, gpi, d, w, 1.0f);    // p - p_ref
+        const float pNeg = minmod_interp<float, D>(pi, pj, gpj, d, w, -1.0f);
+        const float Msq = (unPos * unPos + unNeg * unNeg) / (2.0f * cavg * cavg * norm);
+        const float sc = 1.0f / (sqrtf(norm) * cavg);
+        const float MPos = unPos * sc, MNeg = unNeg * sc;
+        const float Minf = 0.2f;
+        float mm = (Msq < Minf * Minf) ? Minf * Minf : Msq;
+        mm = (mm < 1.0f) ? mm : 1.0f;
+        const float M0 = sqrtf(mm);
+        const float fa = M0 * (2.0f - M0);
+        const float alpha = 3.0f * (5.0f * fa * fa - 4.0f) / 16.0f;
+        const float ppP = p5pos(MPos, alpha), pnP = p5neg(MPos, alpha);
+        const float ppN = p5pos(MNeg, alpha), pnN = p5neg(MNeg, alpha);
+        const float dN = ppN - pnN, dP = ppP - pnP;
+        const float dNdP = (fabsf(MPos) < 1.0f && fabsf(MNeg) < 1.0f) ? dUn * sc * p5diff_dd(MNeg, MPos, alpha)
+                                                                       : dN - dP;
+        // pNeg dN - pPos dP with p = p_ref + p'
+        const float phalf = R.p * dNdP + pNeg * dN - pPos * dP;
+        const float pu = -0.75f * ppP * pnN * (rhoPos + rhoNeg) * cavg * fa * dUn;
+        pf += theta * (pu - 0.5f * phalf);
+    }
+    // F(q_f).S - F(q_ref).S
+    rhs[0] = -mS;
+#pragma unroll
+    for (int k = 0; k < D; ++k) rhs[k + 1] = -(R.m[k] * ufS + mf[k] * phi + pf * S[k]);
+    rhs[D + 1] = -(mS * R.H + (mrS + mS) * Hf);
+
+    // Viscous face terms (src/cfd_v0.cpp:2682-2796), as in the FP64 kernel.
+    const float mu = a.ref.mu;
+    if (mu != 0.0f) {
+        const float Rinv = a.ref.Rinv;
+        const float Ti = Ri * Rinv, Tj = Rj * Rinv;   // T - T_ref
+        const float lapc = a.lapc[f];
+        float Kf[D], g[D][D], gT[D], sU[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) Kf[k] = a.K[(size_t)k * nf + f];
+        if (!a.fGhost[f]) {
+#pragma unroll
+            for (int x = 0; x < D; ++x) {
+#pragma unroll
+                for (int y = 0; y < D; ++y)
+                    g[x][y] = interp(w, a.V[(size_t)(x * D + y) * nt + i], a.V[(size_t)(x * D + y) * nt + j]);
+                gT[x] = interp(w, a.V[(size_t)(D * D + x) * nt + i], a.V[(size_t)(D * D + x) * nt + j]);
+                sU[x] = interp(w, a.V[(size_t)(D * D + D + x) * nt + i], a.V[(size_t)(D * D + D + x) * nt + j]);
+            }
+        } else {
+            const float dinv = a.dinv[f];
+            float dn[D], tau[D][D], Uf[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) dn[k] = a.dnorm[(size_t)k * nf + f];
+#pragma unroll
+            for (int x = 0; x < D; ++x) {
+#pragma unroll
+                for (int y = 0; y < D; ++y) g[x][y] = (uj[x] - ui[x]) * dn[y] * dinv;
+                gT[x] = (Tj - Ti) * dn[x] * dinv;
+                Uf[x] = R.U[x] + interp(w, ui[x], uj[x]);
+            }
+            stress<float, D>(g, mu, tau);
+#pragma unroll
+            for (int x = 0; x < D; ++x) sU[x] = dotv<float, D>(Uf, tau[x]);
+        }
+        float tr = g[0][0];
+#pragma unroll
+        for (int x = 1; x < D; ++x) tr += g[x][x];
+        const float dsum = -(mu * 2.0f / 3.0f) * tr;
+        const float kc = a.ref.kcond;
+#pragma unroll
+        for (int x = 0; x < D; ++x) {
+            float gtS = g[0][x] * S[0];
+#pragma unroll
+            for (int y = 1; y < D; ++y) gtS += g[y][x] * S[y];
+            rhs[x + 1] += mu * gtS + dsum * S[x] + mu * (lapc * (uj[x] - ui[x]) + dotv<float, D>(Kf, g[x]));
+        }
+        rhs[D + 1] += dotv<float, D>(sU, S) + kc * (lapc * (Tj - Ti) + dotv<float, D>(Kf, gT));
+    }
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) a.flux[(size_t)v * nf + f] = rhs[v];
+}
+
+}  // namespace dev
+}  // namespace lfm

@@ -343,55 +343,13 @@ __global__ void __launch_bounds__(128) k_flux(Args<T> a) {
 }
 
 // ---------------------------------------------------------------------------
-// k_update: gather, sponge, RK update.
+// k_update: gather, sponge, RK update (update_cell, solver_device.cuh).
 // ---------------------------------------------------------------------------
-// The face rhs are summed per cell in the flux arithmetic T, in ascending face
-// order (the order in which the reference's scatter reaches the cell); the
-// sum is the cell residual RES. The RK register update is FP64.
 template <typename T, int D, bool RES>
-__global__ void __launch_bounds__(256) k_update(Args<T> a, double Ak, double Bk, double dt, int first) {
+__global__ void __launch_bounds__(256) k_update(const __grid_constant__ Args<T> a, double Ak, double Bk, double dt, int first) {
     const int c = LFM_GLOBAL_ID();
     if (c >= a.nc) return;
-    constexpr int NQ = D + 2;
-    const size_t nt = (size_t)a.nt, nf = (size_t)a.nf, nc = (size_t)a.nc;
-    T sum[NQ];
-#pragma unroll
-    for (int v = 0; v < NQ; ++v) sum[v] = T(0);
-    for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
-        const int code = a.cfList[e];
-        if (code >= 0) {
-#pragma unroll
-            for (int v = 0; v < NQ; ++v) sum[v] += a.flux[v * nf + code];
-        } else {
-            const int f = ~code;
-#pragma unroll
-            for (int v = 0; v < NQ; ++v) sum[v] -= a.flux[v * nf + f];
-        }
-    }
-    const double dtvi = dt * a.volInv[c];
-    double acc[NQ];
-#pragma unroll
-    for (int v = 0; v < NQ; ++v) acc[v] = (first ? 0.0 : Ak * a.dq[v * nc + c]) + dtvi * (double)sum[v];
-    double qv[NQ];
-#pragma unroll
-    for (int v = 0; v < NQ; ++v) qv[v] = a.q[v * nt + c];
-    const double sg = a.sponge[c];
-    if (sg != 0.0) {
-        acc[0] += dt * sg * (a.rhoInf - qv[0]);
-#pragma unroll
-        for (int k = 0; k < D; ++k) acc[k + 1] += dt * sg * (a.rhoInf * a.UInf[k] - qv[k + 1]);
-        acc[D + 1] += dt * sg * (a.rhoInf * a.EInf - qv[D + 1]);
-    }
-    bool finite = true;
-#pragma unroll
-    for (int v = 0; v < NQ; ++v) {
-        a.dq[v * nc + c] = acc[v];
-        const double qn = qv[v] + Bk * acc[v];
-        finite = finite && isfinite(qn);
-        a.q[v * nt + c] = qn;
-        if (RES) a.res[v * nc + c] = (double)sum[v];
-    }
-    if (!finite) atomicOr(a.flag, 1);
+    update_cell<T, D, RES>(a, c, Ak, Bk, dt, first);
 }
 
 // ---------------------------------------------------------------------------

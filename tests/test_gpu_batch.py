@@ -1,0 +1,147 @@
+"""Batch engine: many cases advanced by one persistent kernel per RK stage.
+
+Bar: a case advanced inside a batch -- whatever else is in the batch, whenever
+it joined, whatever launch shape the autotuner picked -- ends bit for bit where
+it ends alone in a batch; it agrees with the single-case FP32-bulk solver to
+1e-6 relative L2 per conserved field (the two are separately compiled kernels,
+so FMA contraction may differ); its acoustic pressure stays within 1e-3
+relative L2 of the FP64 path; the arena admits by footprint."""
+import numpy as np
+import pytest
+
+from lfm_public_gb300 import _native as N, acoustics, cases
+
+pytestmark = pytest.mark.gpu
+
+
+def _single(ch, n, dt, precision=N.LFM_FP32_BULK):
+    s = N.Solver(ch, precision=precision)
+    s.step(n, dt)
+    s.sync()
+    q = s.get_state()
+    s.close()
+    return q
+
+
+def _alone(ch, n, dt, shape=None):
+    b = N.Batch(arena_bytes=N.Batch.case_bytes(ch) + (1 << 20), max_cases=1)
+    if shape:
+        b.set_tuning(*shape)
+    s = b.add(ch, dt)
+    b.step(n)
+    b.sync()
+    q = b.get_state(s)
+    b.close()
+    return q
+
+
+def _mixed_cases():
+    spec = cases.sweep_spec(n_cases=6, seed=11, cells_min=2e3, cells_max=2e4)
+    cs = [cases.sweep_case(x) for x in spec]
+    cs.append(cases.cylinder_case(n_theta=48, n_r=24, r1=15, first=0.02, Ls=4, solver=2, minmod=True, noise=0.02))
+    cs.append(cases.cylinder_case(n_theta=24, n_r=12, r1=8, first=0.04, Ls=3, solver=1, minmod=False, n_span=6,
+                                  noise=0.01))
+    return cs
+
+
+def test_batch_mix_matches_alone_bitwise_and_single_solver():
+    cs = _mixed_cases()
+    chs = [N.CaseHandle.from_case(c) for c in cs]
+    b = N.Batch(arena_bytes=512 << 20)
+    slots = [b.add(ch, c.delta_t) for ch, c in zip(chs, cs)]
+    n = 12
+    b.step(n)
+    b.sync()
+    for s, ch, c in zip(slots, chs, cs):
+        q = b.get_state(s)
+        assert np.array_equal(q, _alone(ch, n, c.delta_t)), c.name
+        q1 = _single(ch, n, c.delta_t)
+        err = np.linalg.norm(q - q1, axis=1) / np.linalg.norm(q1, axis=1)
+        assert np.all(err <= 1e-6), (c.name, err)
+    b.close()
+
+
+def test_batch_join_leave_between_steps():
+    cs = _mixed_cases()[:4]
+    chs = [N.CaseHandle.from_case(c) for c in cs]
+    b = N.Batch(arena_bytes=256 << 20, max_cases=8)
+    s0 = b.add(chs[0], cs[0].delta_t)
+    s1 = b.add(chs[1], cs[1].delta_t)
+    b.step(5)
+    b.remove(s0)
+    s2 = b.add(chs[2], cs[2].delta_t)
+    s3 = b.add(chs[3], cs[3].delta_t)
+    b.step(7)
+    b.sync()
+    assert np.array_equal(b.get_state(s1), _alone(chs[1], 12, cs[1].delta_t))
+    assert np.array_equal(b.get_state(s2), _alone(chs[2], 7, cs[2].delta_t))
+    assert np.array_equal(b.get_state(s3), _alone(chs[3], 7, cs[3].delta_t))
+    b.close()
+
+
+def test_batch_autotune_restores_state_and_keeps_results():
+    cs = _mixed_cases()[:5]
+    chs = [N.CaseHandle.from_case(c) for c in cs]
+    b = N.Batch(arena_bytes=256 << 20)
+    slots = [b.add(ch, c.delta_t) for ch, c in zip(chs, cs)]
+    b.step(3)
+    b.sync()
+    before = [b.get_state(s) for s in slots]
+    t = b.autotune(trial_steps=1)
+    assert t["block"] in (128, 256, 512) and t["items_per_thread"] >= 1
+    for s, q in zip(slots, before):
+        assert np.array_equal(b.get_state(s), q)
+    b.step(4)
+    b.sync()
+    for s, ch, c in zip(slots, chs, cs):
+        assert np.array_equal(b.get_state(s), _alone(ch, 7, c.delta_t)), (c.name, t)
+    b.close()
+
+
+@pytest.mark.parametrize("shape", [(128, 1, 0), (256, 4, 1), (512, 2, 0)])
+def test_batch_launch_shapes_agree(shape):
+    cs = _mixed_cases()[:3]
+    chs = [N.CaseHandle.from_case(c) for c in cs]
+    b = N.Batch(arena_bytes=128 << 20)
+    b.set_tuning(*shape)
+    slots = [b.add(ch, c.delta_t) for ch, c in zip(chs, cs)]
+    b.step(6)
+    b.sync()
+    for s, ch, c in zip(slots, chs, cs):
+        assert np.array_equal(b.get_state(s), _alone(ch, 6, c.delta_t)), (c.name, shape)
+    b.close()
+
+
+def test_batch_admission_by_footprint():
+    c = cases.vortex_case(n=64)
+    ch = N.CaseHandle.from_case(c)
+    need = N.Batch.case_bytes(ch)
+    b = N.Batch(arena_bytes=2 * need + 4096, max_cases=8)
+    s0 = b.add(ch, c.delta_t)
+    s1 = b.add(ch, c.delta_t)
+    with pytest.raises(N.LfmError) as e:
+        b.add(ch, c.delta_t)
+    assert e.value.code == N.LFM_ERR_NOMEM
+    b.remove(s0)
+    assert b.memory()["largest_free"] >= need
+    s2 = b.add(ch, c.delta_t)
+    assert s2 == s0
+    b.step(2)
+    b.sync()
+    assert np.array_equal(b.get_state(s1), b.get_state(s2))
+    b.close()
+
+
+def test_batch_acoustic_pressure_against_fp64():
+    cs = _mixed_cases()
+    chs = [N.CaseHandle.from_case(c) for c in cs]
+    b = N.Batch(arena_bytes=512 << 20)
+    slots = [b.add(ch, c.delta_t) for ch, c in zip(chs, cs)]
+    n = 60
+    b.step(n)
+    b.sync()
+    for s, ch, c in zip(slots, chs, cs):
+        q64 = _single(ch, n, c.delta_t, N.LFM_FP64)
+        err = acoustics.acoustic_rel_l2(b.get_state(s), q64, ch.desc.gamma, c.dim, c.p_inf)
+        assert err <= 1e-3, (c.name, err)
+    b.close()

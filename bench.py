@@ -371,19 +371,172 @@ def run_gpu(args):
     return 0
 
 
+BATCH_DESC = ("64-case batched sweep: quad grids and jittered triangulations of [-10,10]^2, cells log-uniform "
+              "16k-1M, isentropic vortex beta U(1,5), M U(0.1,0.6), M1/M2 at random, rkOrder 5, seed 20261203; "
+              "FP32-bulk, one persistent kernel per RK stage")
+
+
+def _build_sweep(n_cases: int, seed: int):
+    """Cases and handles of the batched sweep, set up in parallel threads (the
+    C++ set-up runs outside the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
+    from lfm_public_gb300 import _native as N, cases
+    spec = cases.sweep_spec(n_cases=n_cases, seed=seed)
+
+    def one(sp):
+        c = cases.sweep_case(sp)
+        return c, N.CaseHandle.from_case(c)
+
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        out = list(ex.map(one, spec))
+    return spec, out
+
+
+def run_batch(args):
+    """The batched form: all sweep cases in one batch, autotuned launch shape."""
+    ws, rank, local, pg = _dist()
+    import numpy as np
+    from lfm_public_gb300 import _native as N, acoustics
+    n_cases = args.batch_cases
+    spec, built = _build_sweep(n_cases, 20261203)
+    cells = sum(ch.desc.n_cells for _, ch in built)
+    need = sum(N.Batch.case_bytes(ch) for _, ch in built)
+    b = N.Batch(device=local, arena_bytes=need + (64 << 20), max_cases=n_cases)
+    slots = [b.add(ch, c.delta_t) for c, ch in built]
+    tuning = b.autotune(trial_steps=2)
+    for _ in range(args.warmup):
+        b.step(1)
+    # timed steps start from the initial states (the reference's central
+    # schemes diverge on some jittered triangulations after a few hundred steps)
+    for (c, ch), s in zip(built, slots):
+        b.set_state(s, ch.q0())
+    if pg:
+        pg.barrier()
+    with ClockSampler(local) as clk:
+        time.sleep(0.3)
+        times = b.bench(args.steps, 512 << 20)
+    nonfinite = [k for k, s in enumerate(slots) if b.case_status(s) != N.LFM_OK]
+    if pg:
+        pg.barrier()
+    total_ms = _allmax(pg, float(times.sum()))
+    stages = 5
+    value = ws * cells * stages * args.steps / (total_ms / 1000.0)
+
+    # end to end through the C ABI: every case's state in from pinned host
+    # memory, one step of the batch, every state back out, each step
+    import torch
+    hosts = [torch.empty((ch.desc.nq, ch.desc.n_cells), dtype=torch.float64, pin_memory=True).numpy()
+             for _, ch in built]
+    for (c, ch), h in zip(built, hosts):
+        h[:] = ch.q0()
+    e2e_steps = max(1, min(args.steps, 20))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for s, h in zip(slots, hosts):
+            b.set_state(s, h)
+        b.step(1)
+        for s, h in zip(slots, hosts):
+            b.get_state(s, out=h)    # synchronous: the step is complete
+    e2e_s = _allmax(pg, time.perf_counter() - t0)
+    e2e_value = ws * cells * stages * e2e_steps / e2e_s
+    io_bytes = sum(h.nbytes for h in hosts)
+    launches = b.launches_per_step()
+    b.close()
+
+    # the plain FP64 path on the same cases, one solver per case in turn
+    k64 = max(1, min(args.steps, 20))
+    ms64 = 0.0
+    for c, ch in built:
+        s = N.Solver(ch, precision=N.LFM_FP64, device=local)
+        s.step(2, c.delta_t)
+        ms64 += float(s.bench(k64, c.delta_t, 0).sum())
+        s.close()
+    v64 = cells * stages * k64 / (ms64 / 1000.0)
+
+    # each case against its own FP64 run
+    accuracy = None
+    if args.accuracy_steps > 0:
+        n_acc = args.accuracy_steps
+        ba = N.Batch(device=local, arena_bytes=need + (64 << 20), max_cases=n_cases)
+        sa = [ba.add(ch, c.delta_t) for c, ch in built]
+        ba.step(n_acc)
+        errs, diverged64, diverged32 = [], [], []
+        for k, ((c, ch), s) in enumerate(zip(built, sa)):
+            s64 = N.Solver(ch, precision=N.LFM_FP64, device=local)
+            s64.step(n_acc, c.delta_t)
+            q64 = s64.get_state()
+            s64.close()
+            q32 = ba.get_state(s)
+            f64, f32 = bool(np.all(np.isfinite(q64))), bool(np.all(np.isfinite(q32)))
+            if not f64:
+                diverged64.append(k)
+            if not f32:
+                diverged32.append(k)
+            if f64 and f32:
+                errs.append(acoustics.acoustic_rel_l2(q32, q64, ch.desc.gamma, c.dim, c.p_inf))
+        ba.close()
+        accuracy = {"acoustic_p_rel_l2_max": max(errs) if errs else None,
+                    "acoustic_p_rel_l2_median": float(np.median(errs)) if errs else None,
+                    "steps": n_acc, "cases_compared": len(errs),
+                    "diverged_fp64": diverged64, "diverged_fp32_bulk": diverged32,
+                    "against": "each case's own FP64 device run (within 1e-12 of the oracle), same steps"}
+
+    if rank != 0:
+        return 0
+    peaks = json.load(open(PEAKS_FILE)) if os.path.exists(PEAKS_FILE) else {}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    step_bytes = 0.0
+    for sp, (c, ch) in zip(spec, built):
+        kb = kernel_bytes(2, 4 if sp["kind"] == "quad" else 3, True, "M1" if sp["solver"] == 0 else "M2", False)
+        step_bytes += sum(kb.values()) * ch.desc.n_cells
+    stage_ms = total_ms / ws / args.steps / stages
+    achieved = step_bytes / (stage_ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32-flux/f64-rk", "data": "synthetic (generated meshes and initial fields)",
+        "config": {"workload": BATCH_DESC, "cases": len(built), "cells": cells, "rk_stages": stages,
+                   "precision": "fp32-bulk", "l2": "512 MB write between timed steps",
+                   "parallelism": f"replicas x{ws}", "tuning": tuning,
+                   "nonfinite_after_timed_steps": nonfinite},
+        "roofline": {"bound": "hbm", "kernel": "k_batch_stage", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                     "traffic": None, "algorithmic_bytes_per_stage": step_bytes, "cells_per_launch": cells},
+        "plain_fp64": {"value": v64, "unit": UNIT, "steps_per_case": k64, "speedup": value / v64,
+                       "how": "one FP64 solver per case, cases in turn, CUDA-event time summed"},
+        "accuracy": accuracy,
+        "cpu_baseline": None,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes},
+        "gpu_launches": launches * args.steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="cylinder2d", choices=sorted(WORKLOAD_DESC))
+    ap.add_argument("--workload", default="cylinder2d", choices=sorted(WORKLOAD_DESC) + ["batch64"])
     ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32"])
-    ap.add_argument("--accuracy-steps", type=int, default=1000)
+    ap.add_argument("--accuracy-steps", type=int, default=None,
+                    help="steps of the FP32-bulk vs FP64 comparison (default 1000; 200 for batch64)")
+    ap.add_argument("--batch-cases", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
+    if args.accuracy_steps is None:
+        args.accuracy_steps = 200 if args.workload == "batch64" else 1000
     if args.impl == "reference":
+        if args.workload == "batch64":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched form; its CPU path is "
+                              "timed per case with --workload cylinder2d / vortex2d"}), flush=True)
+            return 0
         return run_reference(args)
+    if args.workload == "batch64":
+        return run_batch(args)
     return run_gpu(args)
 
 

@@ -164,7 +164,8 @@ typedef struct lfm_solver_opts {
 int lfm_solver_create(const lfm_solver_desc* desc, const lfm_solver_opts* opts, lfm_solver** out);
 void lfm_solver_destroy(lfm_solver* s);
 
-/* Host <-> device state copies ([nq][n_cells], pageable or pinned host memory). */
+/* Host <-> device state copies ([nq][n_cells], pageable or pinned host memory).
+ * set_state also clears the non-finite flag that lfm_solver_sync reports. */
 int lfm_solver_set_state(lfm_solver* s, const double* q);
 int lfm_solver_get_state(lfm_solver* s, double* q);
 
@@ -278,7 +279,8 @@ int lfm_batch_case_bytes(const lfm_solver_desc* desc, size_t* bytes);
 int lfm_batch_add(lfm_batch* b, const lfm_solver_desc* desc, double dt, int* slot);
 /* Removes a case (waits for queued steps) and frees its arena block. */
 int lfm_batch_remove(lfm_batch* b, int slot);
-/* Host <-> device state of one case ([nq][n_cells], solver order); synchronous. */
+/* Host <-> device state of one case ([nq][n_cells], solver order); synchronous.
+ * set_state also clears the case's non-finite flag. */
 int lfm_batch_set_state(lfm_batch* b, int slot, const double* q);
 int lfm_batch_get_state(lfm_batch* b, int slot, double* q);
 /* nsteps time steps of every case in the batch; asynchronous. */
@@ -299,7 +301,9 @@ int lfm_batch_set_tuning(lfm_batch* b, const lfm_batch_tuning* t);
  * keeps the fastest; the cases' states are restored afterwards. */
 int lfm_batch_autotune(lfm_batch* b, int trial_steps, lfm_batch_tuning* chosen);
 /* nsteps steps, each after a write of flush_bytes of scratch (outside its
- * timing), ms[k] = duration of step k (CUDA events on the batch stream). */
+ * timing), ms[k] = duration of step k (CUDA events on the batch stream).
+ * Reports barrier failures; numeric state is left to lfm_batch_sync and
+ * lfm_batch_case_status. */
 int lfm_batch_bench(lfm_batch* b, int nsteps, size_t flush_bytes, float* ms);
 /* Kernel launches per time step (one per RK stage). */
 int lfm_batch_launches_per_step(const lfm_batch* b, int* launches);

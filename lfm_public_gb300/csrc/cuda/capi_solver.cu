@@ -314,6 +314,8 @@ extern "C" void lfm_solver_destroy(lfm_solver* s) {
 extern "C" int lfm_solver_set_state(lfm_solver* s, const double* q) {
     if (!s || !q) return lfm::setError(LFM_ERR_INVALID, "null argument");
     LFM_CUDA(cudaSetDevice(s->device));
+    // a new state starts with a clear non-finite flag
+    LFM_CUDA(cudaMemsetAsync(s->flag, 0, sizeof(int), s->stream));
     for (int v = 0; v < s->nq; ++v)
         LFM_CUDA(cudaMemcpyAsync(s->q + (size_t)v * s->nt, q + (size_t)v * s->nc, (size_t)s->nc * sizeof(double),
                                  cudaMemcpyHostToDevice, s->stream));

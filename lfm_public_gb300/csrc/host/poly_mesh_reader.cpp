@@ -355,13 +355,15 @@ void CPolyMeshReaderOF::initializeSubmesh() {
     m_nSubmeshPointMappingList.assign((size_t)m_nSubmeshCount, {});
     m_nSubmeshFaceMappingList.assign((size_t)m_nSubmeshCount, {});
     m_nSubmeshCellMappingList.assign((size_t)m_nSubmeshCount, {});
+    // The index lists are ascending: appending at the end of each map is
+    // amortised constant time.
+    auto fill = [](std::map<int, int>& m, const std::vector<int>& ids) {
+        for (size_t i = 0; i < ids.size(); ++i) m.emplace_hint(m.end(), ids[i], (int)i);
+    };
     for (int s = 0; s < m_nSubmeshCount; ++s) {
-        const std::vector<int> pts = getSubmeshPointIndexList(s);
-        for (size_t i = 0; i < pts.size(); ++i) m_nSubmeshPointMappingList[(size_t)s].emplace(pts[i], (int)i);
-        const std::vector<int> fcs = getSubmeshFaceIndexList(s);
-        for (size_t i = 0; i < fcs.size(); ++i) m_nSubmeshFaceMappingList[(size_t)s].emplace(fcs[i], (int)i);
-        const std::vector<int> cls = getSubmeshCellIndexList(s);
-        for (size_t i = 0; i < cls.size(); ++i) m_nSubmeshCellMappingList[(size_t)s].emplace(cls[i], (int)i);
+        fill(m_nSubmeshPointMappingList[(size_t)s], getSubmeshPointIndexList(s));
+        fill(m_nSubmeshFaceMappingList[(size_t)s], getSubmeshFaceIndexList(s));
+        fill(m_nSubmeshCellMappingList[(size_t)s], getSubmeshCellIndexList(s));
     }
 }
 

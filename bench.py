@@ -53,6 +53,8 @@ def workload(name: str):
         return cases.cylinder_case(n_theta=768, n_r=512, solver=0, minmod=True)
     if name == "cylinder2d_m2":
         return cases.cylinder_case(n_theta=768, n_r=512, solver=1, minmod=True)
+    if name == "cylinder2d_fine":
+        return cases.cylinder_case(n_theta=1536, n_r=1024, first=0.001, solver=0, minmod=True)
     if name == "vortex2d":
         return cases.vortex_case(n=256, solver=0)
     if name == "cylinder3d":
@@ -66,6 +68,8 @@ WORKLOAD_DESC = {
                        dim=2, scheme="M1", faces_per_cell=4, viscous=True),
     "cylinder2d_m2": dict(workload="2D cylinder O-grid 768x512, M2, minmod on, rkOrder 5, CFL 0.5", cells=393216,
                           dim=2, scheme="M2", faces_per_cell=4, viscous=True),
+    "cylinder2d_fine": dict(workload="2D cylinder O-grid 1536x1024, M1, minmod on, rkOrder 5, CFL 0.5",
+                            cells=1572864, dim=2, scheme="M1", faces_per_cell=4, viscous=True),
     "vortex2d": dict(workload="2D isentropic vortex 256x256, M1, rkOrder 5, CFL 0.5", cells=65536, dim=2,
                      scheme="M1", faces_per_cell=4, viscous=False),
     "cylinder3d": dict(workload="3D cylinder wake 384x256x96, M2, cyclic span, rkOrder 5", cells=9437184, dim=3,
@@ -403,7 +407,12 @@ def run_batch(args):
     need = sum(N.Batch.case_bytes(ch) for _, ch in built)
     b = N.Batch(device=local, arena_bytes=need + (64 << 20), max_cases=n_cases)
     slots = [b.add(ch, c.delta_t) for c, ch in built]
-    tuning = b.autotune(trial_steps=2)
+    if args.tuning:
+        blk, ipt, bps = (int(x) for x in args.tuning.split(","))
+        b.set_tuning(blk, ipt, bps)
+        tuning = b.tuning()
+    else:
+        tuning = b.autotune(trial_steps=2)
     for _ in range(args.warmup):
         b.step(1)
     # timed steps start from the initial states (the reference's central
@@ -525,6 +534,8 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=None,
                     help="steps of the FP32-bulk vs FP64 comparison (default 1000; 200 for batch64)")
     ap.add_argument("--batch-cases", type=int, default=64)
+    ap.add_argument("--tuning", default=None, help="batch launch shape block,items_per_thread,blocks_per_sm "
+                                                   "(default: autotuned)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.accuracy_steps is None:

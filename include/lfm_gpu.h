@@ -308,6 +308,63 @@ int lfm_batch_bench(lfm_batch* b, int nsteps, size_t flush_bytes, float* ms);
 /* Kernel launches per time step (one per RK stage). */
 int lfm_batch_launches_per_step(const lfm_batch* b, int* launches);
 
+/* ---- request server: continuous batching of solve requests ---------------
+ *
+ * No reference counterpart (the reference runs one case per job). A server
+ * owns a batch and one worker thread. lfm_server_submit packs a request (a
+ * case, its dt and step count) on the calling thread and queues it; the worker
+ * admits queued requests in arrival order whenever a case slot and an arena
+ * block of the request's footprint are free (a request that does not fit is
+ * passed over at most max_bypass times before admission waits for it),
+ * advances all admitted requests together in chunks of at most chunk_steps
+ * steps, and retires finished requests (copying their state out and freeing
+ * their slot and block) at chunk boundaries, where newly arrived requests
+ * join. A request's result does not depend on what else runs beside it (the
+ * batch computes every case with the same kernels). All functions are
+ * thread-safe. Times are seconds on a steady clock since lfm_server_create. */
+typedef struct lfm_server lfm_server;
+
+typedef struct lfm_server_opts {
+    int device;
+    int rk_order;             /* RK stages per step of every request */
+    size_t arena_bytes;       /* device memory for admitted requests; 0 = a quarter of free memory */
+    int max_cases;            /* most requests on the device at once; 0 = 256 */
+    int chunk_steps;          /* most steps between admission passes; 0 = 50 */
+    int max_bypass;           /* times the oldest waiting request may be passed over; 0 = 8, < 0 = never */
+    lfm_batch_tuning tuning;  /* launch shape of the stage kernel; block 0 = default */
+} lfm_server_opts;
+
+typedef struct lfm_request_info {
+    int state;                /* 0 queued, 1 running, 2 done */
+    int status;               /* LFM_OK, LFM_ERR_NUMERIC (non-finite state: the result is the state at
+                                 detection), LFM_ERR_NOMEM (larger than the arena), other: server failure */
+    int64_t cells;
+    int steps;
+    double t_submit, t_admit, t_done;   /* -1 when not reached */
+    size_t footprint_bytes;
+} lfm_request_info;
+
+typedef struct lfm_server_stats {
+    int queued, running;
+    int64_t completed;
+    int64_t chunks;           /* chunks of steps run so far */
+    double t_now;
+} lfm_server_stats;
+
+int lfm_server_create(const lfm_server_opts* opts, lfm_server** out);
+/* Stops the worker (queued and running requests are abandoned) and frees the server. */
+void lfm_server_destroy(lfm_server* s);
+/* Queues nsteps steps of the case at time step dt, starting from desc->q0;
+ * the description may be freed when the call returns. */
+int lfm_server_submit(lfm_server* s, const lfm_solver_desc* desc, double dt, int nsteps, int64_t* id);
+int lfm_server_info(lfm_server* s, int64_t id, lfm_request_info* info);
+/* Waits until the request is done or timeout_s passes (< 0: no limit). */
+int lfm_server_wait(lfm_server* s, int64_t id, double timeout_s, int* done);
+/* Final state of a done request ([nq][n_cells], may be NULL) and its info;
+ * releases the request. */
+int lfm_server_result(lfm_server* s, int64_t id, double* q, lfm_request_info* info);
+int lfm_server_get_stats(lfm_server* s, lfm_server_stats* st);
+
 #ifdef __cplusplus
 }
 #endif

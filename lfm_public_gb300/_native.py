@@ -88,6 +88,25 @@ class BatchTuning(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class ServerOpts(C.Structure):
+    _fields_ = [("device", C.c_int), ("rk_order", C.c_int), ("arena_bytes", C.c_size_t), ("max_cases", C.c_int),
+                ("chunk_steps", C.c_int), ("max_bypass", C.c_int), ("tuning", BatchTuning)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("state", C.c_int), ("status", C.c_int), ("cells", C.c_int64), ("steps", C.c_int),
+                ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double),
+                ("footprint_bytes", C.c_size_t)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("queued", C.c_int), ("running", C.c_int), ("completed", C.c_int64), ("chunks", C.c_int64),
+                ("t_now", C.c_double)]
+
+
 class LfmError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"lfm error {code}: {msg}")
@@ -151,6 +170,13 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "lfm_batch_autotune": ([vp, C.c_int, C.POINTER(BatchTuning)], C.c_int),
         "lfm_batch_bench": ([vp, C.c_int, C.c_size_t, C.POINTER(C.c_float)], C.c_int),
         "lfm_batch_launches_per_step": ([vp, C.POINTER(C.c_int)], C.c_int),
+        "lfm_server_create": ([C.POINTER(ServerOpts), C.POINTER(vp)], C.c_int),
+        "lfm_server_destroy": ([vp], None),
+        "lfm_server_submit": ([vp, C.POINTER(SolverDesc), C.c_double, C.c_int, C.POINTER(C.c_int64)], C.c_int),
+        "lfm_server_info": ([vp, C.c_int64, C.POINTER(RequestInfo)], C.c_int),
+        "lfm_server_wait": ([vp, C.c_int64, C.c_double, C.POINTER(C.c_int)], C.c_int),
+        "lfm_server_result": ([vp, C.c_int64, _dp, C.POINTER(RequestInfo)], C.c_int),
+        "lfm_server_get_stats": ([vp, C.POINTER(ServerStats)], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -457,6 +483,64 @@ class Batch:
     def close(self):
         if getattr(self, "_h", None):
             load_library().lfm_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """An lfm_server: continuous batching of solve requests on one GPU
+    (thread-safe; the worker runs in the library)."""
+
+    def __init__(self, device: int = 0, rk_order: int = 5, arena_bytes: int = 0, max_cases: int = 256,
+                 chunk_steps: int = 50, max_bypass: int = 0, tuning: Optional[tuple] = None):
+        t = BatchTuning()
+        if tuning:
+            t.block, t.items_per_thread, t.blocks_per_sm = tuning[:3]
+            t.cooperative = tuning[3] if len(tuning) > 3 else 1
+        opts = ServerOpts(device=device, rk_order=rk_order, arena_bytes=arena_bytes, max_cases=max_cases,
+                          chunk_steps=chunk_steps, max_bypass=max_bypass, tuning=t)
+        h = C.c_void_p()
+        check(load_library().lfm_server_create(C.byref(opts), C.byref(h)))
+        self._h = h
+        self._shape = {}
+
+    def submit(self, case: CaseHandle, dt: float, nsteps: int) -> int:
+        i = C.c_int64()
+        check(load_library().lfm_server_submit(self._h, C.byref(case.desc), dt, nsteps, C.byref(i)))
+        self._shape[i.value] = (case.desc.nq, case.desc.n_cells)
+        return i.value
+
+    def info(self, rid: int) -> dict:
+        r = RequestInfo()
+        check(load_library().lfm_server_info(self._h, rid, C.byref(r)))
+        return r.as_dict()
+
+    def wait(self, rid: int, timeout: float = -1.0) -> bool:
+        d = C.c_int()
+        check(load_library().lfm_server_wait(self._h, rid, timeout, C.byref(d)))
+        return bool(d.value)
+
+    def result(self, rid: int):
+        """(state [nq][n_cells], info dict) of a done request; releases it."""
+        nq, nc = self._shape.pop(rid)
+        q = np.empty((nq, nc), dtype=np.float64)
+        r = RequestInfo()
+        check(load_library().lfm_server_result(self._h, rid, _ptr(q, C.c_double), C.byref(r)))
+        return q, r.as_dict()
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        check(load_library().lfm_server_get_stats(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().lfm_server_destroy(self._h)
             self._h = None
 
     def __del__(self):

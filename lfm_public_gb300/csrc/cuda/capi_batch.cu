@@ -17,6 +17,7 @@
 #include "../host/capi_internal.h"
 #include "args_setup.h"
 #include "batch.cuh"
+#include "batch_internal.h"
 #include "lfm_gpu.h"
 #include "solver_launch.h"
 
@@ -27,11 +28,14 @@ using lfm::dev::BatchCtl;
 using lfm::dev::BatchTile;
 using lfm::dev::kBatchMaxStages;
 using lfm::dev::kBatchPhases;
+using lfm::batch::Arena;
+using lfm::batch::CaseLayout;
+using lfm::batch::PreparedCase;
+using lfm::batch::Slot;
+using lfm::batch::roundUp;
+
 
 namespace {
-
-constexpr size_t kAlign = 256;
-inline size_t roundUp(size_t b) { return (b + kAlign - 1) & ~(kAlign - 1); }
 
 int cudaFail(cudaError_t e, const char* what) {
     return lfm::setError(e == cudaErrorMemoryAllocation ? LFM_ERR_NOMEM : LFM_ERR_CUDA,
@@ -43,108 +47,6 @@ int cudaFail(cudaError_t e, const char* what) {
         cudaError_t e__ = (call);                            \
         if (e__ != cudaSuccess) return cudaFail(e__, #call); \
     } while (0)
-
-// First-fit allocator over [0, size) in 256-byte granules; free ranges are
-// kept sorted by offset and coalesced on release.
-class Arena {
-public:
-    void reset(size_t size) {
-        free_.clear();
-        size_ = size & ~(kAlign - 1);
-        if (size_) free_[0] = size_;
-    }
-    bool alloc(size_t bytes, size_t* off) {
-        bytes = roundUp(bytes);
-        for (auto it = free_.begin(); it != free_.end(); ++it) {
-            if (it->second >= bytes) {
-                *off = it->first;
-                const size_t rest = it->second - bytes;
-                const size_t at = it->first + bytes;
-                free_.erase(it);
-                if (rest) free_[at] = rest;
-                return true;
-            }
-        }
-        return false;
-    }
-    void release(size_t off, size_t bytes) {
-        bytes = roundUp(bytes);
-        auto it = free_.emplace(off, bytes).first;
-        auto nx = std::next(it);
-        if (nx != free_.end() && it->first + it->second == nx->first) {
-            it->second += nx->second;
-            free_.erase(nx);
-        }
-        if (it != free_.begin()) {
-            auto pv = std::prev(it);
-            if (pv->first + pv->second == it->first) {
-                pv->second += it->second;
-                free_.erase(it);
-            }
-        }
-    }
-    size_t largest() const {
-        size_t m = 0;
-        for (auto& kv : free_) m = std::max(m, kv.second);
-        return m;
-    }
-    size_t total() const {
-        size_t m = 0;
-        for (auto& kv : free_) m += kv.second;
-        return m;
-    }
-    size_t size() const { return size_; }
-
-private:
-    std::map<size_t, size_t> free_;
-    size_t size_ = 0;
-};
-
-// Byte offsets of every array of one case inside its arena block.
-struct CaseLayout {
-    size_t total = 0;
-    size_t q, dq, res, prim, V, grad, flux, S, d, w, dinv, dnorm, K, lapc, fP, fN, fGhost, volInv, volInv32,
-        sponge, cfOff, cfList, gCell, gKind, gFace;
-
-    explicit CaseLayout(const lfm_solver_desc* d) {
-        const size_t D = (size_t)d->dim, nq = (size_t)d->nq, nc = (size_t)d->n_cells, ng = (size_t)d->n_ghosts;
-        const size_t nt = nc + ng, nf = (size_t)d->n_faces, ne = (size_t)d->cell_face_offsets[nc];
-        const bool ausm = d->solver == LFM_SOLVER_M2AUSM;
-        q = add(nq * nt * 8);
-        dq = add(nq * nc * 8);
-        res = d->residuals ? add(nq * nc * 8) : npos();
-        prim = add((size_t)lfm::dev::primRows<float>(d->dim) * nt * 4);
-        V = lfm::setup::needVis(d) ? add((D * D + 2 * D) * nt * 4) : npos();
-        grad = ausm ? add((2 * D + D * D) * nt * 4) : npos();
-        flux = add(nq * nf * 4);
-        S = add(D * nf * 4);
-        this->d = add(D * nf * 4);
-        w = add(nf * 4);
-        dinv = add(nf * 4);
-        dnorm = add(D * nf * 4);
-        K = add(D * nf * 4);
-        lapc = add(nf * 4);
-        fP = add(nf * 4);
-        fN = add(nf * 4);
-        fGhost = add(nf);
-        volInv = add(nc * 8);
-        volInv32 = add(nc * 4);
-        sponge = add(nc * 8);
-        cfOff = add((nc + 1) * 4);
-        cfList = add(ne * 4);
-        gCell = add(ng * 4);
-        gKind = add(ng * 4);
-        gFace = add(ng * 4);
-    }
-    static size_t npos() { return ~(size_t)0; }
-
-private:
-    size_t add(size_t bytes) {
-        const size_t at = total;
-        total += roundUp(bytes ? bytes : 1);
-        return at;
-    }
-};
 
 // Host image of a case's arena block: constant arrays and the initial state
 // in their final device layout, scratch zero-filled (the viscous terms and
@@ -186,40 +88,7 @@ std::vector<unsigned char> packCase(const lfm_solver_desc* d, const CaseLayout& 
     return img;
 }
 
-struct Slot {
-    bool used = false;
-    size_t off = 0, bytes = 0;
-    int D = 2, nq = 4, nc = 0, ng = 0, nf = 0, nt = 0;
-    bool needGradVis = false;
-    double* q = nullptr;   // device
-};
-
 }  // namespace
-
-struct lfm_batch {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    int rkOrder = 5;
-    int maxCases = 0;
-    unsigned char* arenaBase = nullptr;
-    Arena arena;
-    BatchCase* dCases = nullptr;
-    int* dFlags = nullptr;
-    int* dError = nullptr;
-    BatchCtl* dCtl = nullptr;
-    BatchTile* dTiles[kBatchPhases] = {};
-    size_t tileCap[kBatchPhases] = {};
-    int* dNTiles = nullptr;
-    std::vector<Slot> slots;
-    int sms = 0;
-    lfm_batch_tuning tune{256, 1, 0, 1};
-    int grid = 0;
-    bool tilesDirty = true;
-    cudaGraphExec_t graph = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    void* scrub = nullptr;
-    size_t scrubBytes = 0;
-};
 
 namespace {
 
@@ -401,15 +270,43 @@ extern "C" void lfm_batch_destroy(lfm_batch* b) {
     delete b;
 }
 
-extern "C" int lfm_batch_add(lfm_batch* b, const lfm_solver_desc* d, double dt, int* slot) {
-    if (!b || !slot) return lfm::setError(LFM_ERR_INVALID, "null argument");
-    *slot = -1;
+namespace lfm {
+namespace batch {
+
+int prepareCase(const lfm_solver_desc* d, double dt, int rkOrder, PreparedCase** out) {
+    *out = nullptr;
     int rc = lfm::setup::validateDesc(d);
     if (rc) return rc;
-    if (d->rk_order != b->rkOrder)
+    if (d->rk_order != rkOrder)
         return lfm::setError(LFM_ERR_INVALID, "case rk_order " + std::to_string(d->rk_order) +
-                                                  " differs from the batch's " + std::to_string(b->rkOrder));
+                                                  " differs from the batch's " + std::to_string(rkOrder));
     if (!(dt > 0.0)) return lfm::setError(LFM_ERR_INVALID, "dt must be positive");
+    PreparedCase* pc = new PreparedCase(d);
+    pc->image = packCase(d, pc->layout);
+    BatchCase& bc = pc->bc;
+    std::memset(&bc, 0, sizeof(bc));
+    lfm::setup::setConstants(bc.a, d);
+    bc.dt = dt;
+    for (int k = 0; k < d->rk_order; ++k) {
+        bc.rkA[k] = d->rkA[k];
+        bc.rkB[k] = d->rkB[k];
+    }
+    bc.scheme = d->solver;
+    bc.needGrad = lfm::setup::needGrad(d) ? 1 : 0;
+    bc.needVis = lfm::setup::needVis(d) ? 1 : 0;
+    bc.residuals = d->residuals ? 1 : 0;
+    pc->D = d->dim;
+    pc->nq = d->nq;
+    pc->nc = (int)d->n_cells;
+    pc->ng = (int)d->n_ghosts;
+    pc->nf = (int)d->n_faces;
+    pc->needGradVis = bc.needGrad || bc.needVis;
+    *out = pc;
+    return LFM_OK;
+}
+
+int commitCase(lfm_batch* b, const PreparedCase& pc, int* slot) {
+    *slot = -1;
     int s = -1;
     for (int k = 0; k < (int)b->slots.size(); ++k)
         if (!b->slots[(size_t)k].used) {
@@ -417,19 +314,16 @@ extern "C" int lfm_batch_add(lfm_batch* b, const lfm_solver_desc* d, double dt, 
             break;
         }
     if (s < 0) return lfm::setError(LFM_ERR_NOMEM, "batch has no free case slot");
-    const CaseLayout L(d);
+    const CaseLayout& L = pc.layout;
     size_t off = 0;
     if (!b->arena.alloc(L.total, &off))
         return lfm::setError(LFM_ERR_NOMEM, "case needs " + std::to_string(L.total) + " bytes; largest free arena block " +
                                                 std::to_string(b->arena.largest()));
     LFM_CUDA(cudaSetDevice(b->device));
-    std::vector<unsigned char> img = packCase(d, L);
     unsigned char* base = b->arenaBase + off;
-    cudaError_t e = cudaMemcpyAsync(base, img.data(), img.size(), cudaMemcpyHostToDevice, b->stream);
-    BatchCase bc;
-    std::memset(&bc, 0, sizeof(bc));
+    cudaError_t e = cudaMemcpyAsync(base, pc.image.data(), pc.image.size(), cudaMemcpyHostToDevice, b->stream);
+    BatchCase bc = pc.bc;
     Args<float>& a = bc.a;
-    lfm::setup::setConstants(a, d);
     auto P = [&](size_t o) -> unsigned char* { return o == CaseLayout::npos() ? nullptr : base + o; };
     a.q = reinterpret_cast<double*>(P(L.q));
     a.dq = reinterpret_cast<double*>(P(L.dq));
@@ -457,19 +351,10 @@ extern "C" int lfm_batch_add(lfm_batch* b, const lfm_solver_desc* d, double dt, 
     a.gKind = reinterpret_cast<const int*>(P(L.gKind));
     a.gFace = reinterpret_cast<const int*>(P(L.gFace));
     a.flag = b->dFlags + s;
-    bc.dt = dt;
-    for (int k = 0; k < d->rk_order; ++k) {
-        bc.rkA[k] = d->rkA[k];
-        bc.rkB[k] = d->rkB[k];
-    }
-    bc.scheme = d->solver;
-    bc.needGrad = lfm::setup::needGrad(d) ? 1 : 0;
-    bc.needVis = lfm::setup::needVis(d) ? 1 : 0;
-    bc.residuals = d->residuals ? 1 : 0;
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(b->dCases + s, &bc, sizeof(bc), cudaMemcpyHostToDevice, b->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->dFlags + s, 0, sizeof(int), b->stream);
-    // img and bc are host temporaries: the copies must finish before they go
+    // bc is a host temporary: the copies must finish before it goes
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
     if (e != cudaSuccess) {
         b->arena.release(off, L.total);
@@ -479,17 +364,31 @@ extern "C" int lfm_batch_add(lfm_batch* b, const lfm_solver_desc* d, double dt, 
     sl.used = true;
     sl.off = off;
     sl.bytes = L.total;
-    sl.D = d->dim;
-    sl.nq = d->nq;
-    sl.nc = (int)d->n_cells;
-    sl.ng = (int)d->n_ghosts;
-    sl.nf = (int)d->n_faces;
-    sl.nt = sl.nc + sl.ng;
-    sl.needGradVis = bc.needGrad || bc.needVis;
+    sl.D = pc.D;
+    sl.nq = pc.nq;
+    sl.nc = pc.nc;
+    sl.ng = pc.ng;
+    sl.nf = pc.nf;
+    sl.nt = pc.nc + pc.ng;
+    sl.needGradVis = pc.needGradVis;
     sl.q = a.q;
     b->tilesDirty = true;
     *slot = s;
     return LFM_OK;
+}
+
+}  // namespace batch
+}  // namespace lfm
+
+extern "C" int lfm_batch_add(lfm_batch* b, const lfm_solver_desc* d, double dt, int* slot) {
+    if (!b || !slot) return lfm::setError(LFM_ERR_INVALID, "null argument");
+    *slot = -1;
+    PreparedCase* pc = nullptr;
+    int rc = lfm::batch::prepareCase(d, dt, b->rkOrder, &pc);
+    if (rc) return rc;
+    rc = lfm::batch::commitCase(b, *pc, slot);
+    delete pc;
+    return rc;
 }
 
 extern "C" int lfm_batch_remove(lfm_batch* b, int slot) {

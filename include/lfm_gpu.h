@@ -240,6 +240,12 @@ int lfm_solver_launches_per_step(const lfm_solver* s, int* launches);
 int lfm_solver_profile_step(lfm_solver* s, double dt, int n, float* ms);
 const char* lfm_solver_kernel_name(int i);
 
+/* Diagnostic: runs the FP32-bulk kernels' integer-pipe binary32 <-> binary64
+ * conversions on the device over n bit patterns (host arrays) and returns
+ * their results, for comparison with IEEE 754 conversions. */
+int lfm_selftest_fp_convert(int64_t n, const uint32_t* f32_bits, const uint64_t* f64_bits, uint64_t* f64_of_f32,
+                            uint32_t* f32_of_f64);
+
 /* ---- batch engine: many cases, one persistent kernel per RK stage ---------
  *
  * No single reference call corresponds: the reference advances one case per

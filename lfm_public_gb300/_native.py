@@ -153,6 +153,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "lfm_solver_bench": ([vp, C.c_int, C.c_double, C.c_size_t, C.POINTER(C.c_float)], C.c_int),
         "lfm_solver_profile_step": ([vp, C.c_double, C.c_int, C.POINTER(C.c_float)], C.c_int),
         "lfm_solver_kernel_name": ([C.c_int], C.c_char_p),
+        "lfm_selftest_fp_convert": ([C.c_int64, C.POINTER(C.c_uint32), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+                                     C.POINTER(C.c_uint32)], C.c_int),
         "lfm_batch_create": ([C.POINTER(BatchOpts), C.POINTER(vp)], C.c_int),
         "lfm_batch_destroy": ([vp], None),
         "lfm_batch_case_bytes": ([C.POINTER(SolverDesc), C.POINTER(C.c_size_t)], C.c_int),
@@ -548,6 +550,22 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def selftest_fp_convert(f32_bits: np.ndarray, f64_bits: np.ndarray):
+    """Device integer-pipe conversions of the FP32-bulk kernels over bit
+    patterns: (binary64 bits of each binary32, binary32 bits of each binary64)."""
+    a = np.ascontiguousarray(f32_bits, dtype=np.uint32)
+    b = np.ascontiguousarray(f64_bits, dtype=np.uint64)
+    if a.size != b.size:
+        raise ValueError("both inputs need the same length")
+    o64 = np.empty(a.size, dtype=np.uint64)
+    o32 = np.empty(a.size, dtype=np.uint32)
+    rc = load_library().lfm_selftest_fp_convert(a.size, _ptr(a, C.c_uint32), _ptr(b, C.c_uint64),
+                                                _ptr(o64, C.c_uint64), _ptr(o32, C.c_uint32))
+    if rc != 0:
+        raise LfmError(rc, "conversion self-test failed to run")
+    return o64, o32
 
 
 def port_run(case: CaseHandle, q: np.ndarray, nsteps: int, dt: float, residual: bool = False):

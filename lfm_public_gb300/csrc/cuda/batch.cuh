@@ -3,11 +3,12 @@
 //
 // Every case lives in its own block of a device arena, with the FP32-bulk
 // arrays of a single-case solver (Args<float>). A stage is four phases over
-// all cases -- ghost states and primitives; gradients and viscous terms;
-// face fluxes; gather and RK update -- separated by grid-wide barriers. Work
+// all cases -- ghost states and primitives (of every cell too, right after a
+// case's state was set); gradients and viscous terms; face fluxes; gather, RK
+// update and the cells' next primitives -- separated by grid-wide barriers. Work
 // is a flat list of tiles per phase (a tile is a run of consecutive cells or
-// faces of one case), taken from a per-phase atomic counter, so uneven cases
-// load-balance at tile granularity. The tile lists and case table are read
+// faces of one case); each block takes an equal contiguous range of it, so
+// uneven cases load-balance at tile granularity. The tile lists and case table are read
 // from device memory at run time: cases join and leave between time steps
 // without recapturing the CUDA graph of a step.
 #pragma once
@@ -28,6 +29,7 @@ constexpr int kBatchPhases = 4;   // prep, grad+vis, flux, update
 struct __align__(16) BatchCase {
     Args<float> a;
     double dt;
+    float dt32;
     double rkA[kBatchMaxStages], rkB[kBatchMaxStages];
     int scheme, needGrad, needVis, residuals;
 };
@@ -37,11 +39,9 @@ struct __align__(16) BatchTile {
     int slot, start, count, pad;
 };
 
-// Zeroed before every time step: grid-barrier arrival counters and the
-// per-phase tile counters of each stage.
+// Zeroed before every time step: the grid-barrier arrival counter of each stage.
 struct BatchCtl {
     unsigned barrier[kBatchMaxStages];
-    unsigned next[kBatchMaxStages][kBatchPhases];
 };
 
 struct BatchArgs {

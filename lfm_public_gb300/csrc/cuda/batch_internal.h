@@ -127,6 +127,8 @@ struct Slot {
     size_t off = 0, bytes = 0;
     int D = 2, nq = 4, nc = 0, ng = 0, nf = 0, nt = 0;
     bool needGradVis = false;
+    bool primsValid = false;   // cells' primitives current (kept so by the update phase)
+    double qRef[5] = {0, 0, 0, 0, 0};   // the device state is q - qRef
     double* q = nullptr;   // device
 };
 
@@ -174,4 +176,6 @@ struct lfm_batch {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     void* scrub = nullptr;
     size_t scrubBytes = 0;
+    double* dStage = nullptr;   // a case's absolute state in transit to or from the host
+    size_t stageBytes = 0;
 };

@@ -38,8 +38,9 @@ __device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target,
     return sOk != 0;
 }
 
-// One item of a phase: a cell or ghost (prep), a cell (grad + vis, update) or
-// a face (flux) of the case in shared memory.
+// One item of a phase: a cell or ghost (prep; the tiles of a case whose cell
+// primitives are current cover its ghosts only), a cell (grad + vis, update)
+// or a face (flux) of the case in shared memory.
 template <int PH, int D>
 __device__ __forceinline__ void item(const BatchCase& bc, int stage, int i) {
     const Args<float>& a = bc.a;
@@ -58,9 +59,9 @@ __device__ __forceinline__ void item(const BatchCase& bc, int stage, int i) {
     } else {
         const int first = stage == 0;
         if (bc.residuals && first)
-            update_cell<float, D, true>(a, i, bc.rkA[stage], bc.rkB[stage], bc.dt, first);
+            update32<D, true>(a, i, bc.rkA[stage], bc.rkB[stage], bc.dt, bc.dt32, first);
         else
-            update_cell<float, D, false>(a, i, bc.rkA[stage], bc.rkB[stage], bc.dt, first);
+            update32<D, false>(a, i, bc.rkA[stage], bc.rkB[stage], bc.dt, bc.dt32, first);
     }
 }
 

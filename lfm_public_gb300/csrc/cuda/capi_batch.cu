@@ -49,9 +49,9 @@ int cudaFail(cudaError_t e, const char* what) {
     } while (0)
 
 // Host image of a case's arena block: constant arrays and the initial state
-// in their final device layout, scratch zero-filled (the viscous terms and
-// gradients of ghosts are read as zeros).
-std::vector<unsigned char> packCase(const lfm_solver_desc* d, const CaseLayout& L) {
+// (as q - qRef) in their final device layout, scratch zero-filled (the viscous
+// terms and gradients of ghosts are read as zeros).
+std::vector<unsigned char> packCase(const lfm_solver_desc* d, const CaseLayout& L, const double* qRef) {
     std::vector<unsigned char> img(L.total, 0);
     const size_t D = (size_t)d->dim, nq = (size_t)d->nq, nc = (size_t)d->n_cells, ng = (size_t)d->n_ghosts;
     const size_t nt = nc + ng, nf = (size_t)d->n_faces;
@@ -62,8 +62,10 @@ std::vector<unsigned char> packCase(const lfm_solver_desc* d, const CaseLayout& 
         float* p = f32(off);
         for (size_t k = 0; k < n; ++k) p[k] = (float)src[k];
     };
-    if (d->q0)
-        for (size_t v = 0; v < nq; ++v) std::memcpy(f64(L.q) + v * nt, d->q0 + v * nc, nc * 8);
+    for (size_t v = 0; v < nq; ++v) {
+        double* row = f64(L.q) + v * nt;
+        for (size_t c = 0; c < nc; ++c) row[c] = (d->q0 ? d->q0[v * nc + c] : 0.0) - qRef[v];
+    }
     conv(L.S, d->S, D * nf);
     conv(L.d, d->d, D * nf);
     conv(L.w, d->w, nf);
@@ -98,10 +100,13 @@ int rebuildTiles(lfm_batch* b) {
     for (int s = 0; s < (int)b->slots.size(); ++s) {
         const Slot& sl = b->slots[(size_t)s];
         if (!sl.used) continue;
-        const int counts[kBatchPhases] = {sl.nt, sl.needGradVis ? sl.nc : 0, sl.nf, sl.nc};
+        // preparation covers the ghosts only while the update phase keeps the
+        // cells' primitives current
+        const int first[kBatchPhases] = {sl.primsValid ? sl.nc : 0, 0, 0, 0};
+        const int end[kBatchPhases] = {sl.nt, sl.needGradVis ? sl.nc : 0, sl.nf, sl.nc};
         for (int ph = 0; ph < kBatchPhases; ++ph)
-            for (int st = 0; st < counts[ph]; st += tileSize)
-                tl[ph].push_back(BatchTile{s, st, std::min(tileSize, counts[ph] - st), 0});
+            for (int st = first[ph]; st < end[ph]; st += tileSize)
+                tl[ph].push_back(BatchTile{s, st, std::min(tileSize, end[ph] - st), 0});
     }
     int n[kBatchPhases];
     bool realloc = false;
@@ -188,6 +193,18 @@ int ensureGraph(lfm_batch* b) {
     return rc;
 }
 
+// Device buffer for a case's absolute state in transit to or from the host.
+int ensureStage(lfm_batch* b, size_t bytes) {
+    if (bytes <= b->stageBytes) return LFM_OK;
+    LFM_CUDA(cudaStreamSynchronize(b->stream));
+    if (b->dStage) cudaFree(b->dStage);
+    b->dStage = nullptr;
+    b->stageBytes = 0;
+    LFM_CUDA(cudaMalloc(&b->dStage, bytes));
+    b->stageBytes = bytes;
+    return LFM_OK;
+}
+
 int checkSlot(const lfm_batch* b, int slot) {
     if (!b) return lfm::setError(LFM_ERR_INVALID, "null batch");
     if (slot < 0 || slot >= (int)b->slots.size() || !b->slots[(size_t)slot].used)
@@ -263,6 +280,7 @@ extern "C" void lfm_batch_destroy(lfm_batch* b) {
     cudaFree(b->dError);
     cudaFree(b->dCtl);
     cudaFree(b->dNTiles);
+    if (b->dStage) cudaFree(b->dStage);
     if (b->scrub) cudaFree(b->scrub);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
@@ -282,11 +300,12 @@ int prepareCase(const lfm_solver_desc* d, double dt, int rkOrder, PreparedCase**
                                                   " differs from the batch's " + std::to_string(rkOrder));
     if (!(dt > 0.0)) return lfm::setError(LFM_ERR_INVALID, "dt must be positive");
     PreparedCase* pc = new PreparedCase(d);
-    pc->image = packCase(d, pc->layout);
     BatchCase& bc = pc->bc;
     std::memset(&bc, 0, sizeof(bc));
     lfm::setup::setConstants(bc.a, d);
+    pc->image = packCase(d, pc->layout, bc.a.qRef);
     bc.dt = dt;
+    bc.dt32 = (float)dt;
     for (int k = 0; k < d->rk_order; ++k) {
         bc.rkA[k] = d->rkA[k];
         bc.rkB[k] = d->rkB[k];
@@ -371,6 +390,8 @@ int commitCase(lfm_batch* b, const PreparedCase& pc, int* slot) {
     sl.nf = pc.nf;
     sl.nt = pc.nc + pc.ng;
     sl.needGradVis = pc.needGradVis;
+    sl.primsValid = false;
+    for (int v = 0; v < 5; ++v) sl.qRef[v] = pc.bc.a.qRef[v];
     sl.q = a.q;
     b->tilesDirty = true;
     *slot = s;
@@ -408,14 +429,20 @@ extern "C" int lfm_batch_set_state(lfm_batch* b, int slot, const double* q) {
     int rc = checkSlot(b, slot);
     if (rc) return rc;
     if (!q) return lfm::setError(LFM_ERR_INVALID, "null state");
-    const Slot& sl = b->slots[(size_t)slot];
+    Slot& sl = b->slots[(size_t)slot];
     LFM_CUDA(cudaSetDevice(b->device));
     // a new state starts with a clear non-finite flag
     LFM_CUDA(cudaMemsetAsync(b->dFlags + slot, 0, sizeof(int), b->stream));
-    for (int v = 0; v < sl.nq; ++v)
-        LFM_CUDA(cudaMemcpyAsync(sl.q + (size_t)v * sl.nt, q + (size_t)v * sl.nc, (size_t)sl.nc * sizeof(double),
-                                 cudaMemcpyHostToDevice, b->stream));
+    const size_t bytes = (size_t)sl.nq * sl.nc * sizeof(double);
+    if ((rc = ensureStage(b, bytes))) return rc;
+    LFM_CUDA(cudaMemcpyAsync(b->dStage, q, bytes, cudaMemcpyHostToDevice, b->stream));
+    lfm::dev::QOffset qo;   // stored as q - qRef
+    for (int v = 0; v < 5; ++v) qo.v[v] = sl.qRef[v];
+    lfm::dev::launch_offset_rows(sl.q, sl.nt, b->dStage, sl.nc, sl.nc, sl.nq, qo, -1.0, b->stream);
+    LFM_CUDA(cudaGetLastError());
     LFM_CUDA(cudaStreamSynchronize(b->stream));
+    sl.primsValid = false;
+    b->tilesDirty = true;
     return LFM_OK;
 }
 
@@ -425,9 +452,13 @@ extern "C" int lfm_batch_get_state(lfm_batch* b, int slot, double* q) {
     if (!q) return lfm::setError(LFM_ERR_INVALID, "null state");
     const Slot& sl = b->slots[(size_t)slot];
     LFM_CUDA(cudaSetDevice(b->device));
-    for (int v = 0; v < sl.nq; ++v)
-        LFM_CUDA(cudaMemcpyAsync(q + (size_t)v * sl.nc, sl.q + (size_t)v * sl.nt, (size_t)sl.nc * sizeof(double),
-                                 cudaMemcpyDeviceToHost, b->stream));
+    const size_t bytes = (size_t)sl.nq * sl.nc * sizeof(double);
+    if ((rc = ensureStage(b, bytes))) return rc;
+    lfm::dev::QOffset qo;   // stored as q - qRef
+    for (int v = 0; v < 5; ++v) qo.v[v] = sl.qRef[v];
+    lfm::dev::launch_offset_rows(b->dStage, sl.nc, sl.q, sl.nt, sl.nc, sl.nq, qo, 1.0, b->stream);
+    LFM_CUDA(cudaGetLastError());
+    LFM_CUDA(cudaMemcpyAsync(q, b->dStage, bytes, cudaMemcpyDeviceToHost, b->stream));
     LFM_CUDA(cudaStreamSynchronize(b->stream));
     return LFM_OK;
 }
@@ -438,7 +469,22 @@ extern "C" int lfm_batch_step(lfm_batch* b, int nsteps) {
     LFM_CUDA(cudaSetDevice(b->device));
     int rc = ensureGraph(b);
     if (rc) return rc;
-    for (int k = 0; k < nsteps; ++k) LFM_CUDA(cudaGraphLaunch(b->graph, b->stream));
+    if (nsteps == 0) return LFM_OK;
+    // Cases whose state was just set prepare all their cells in the first
+    // step; after it the update phase keeps their primitives current and the
+    // tile lists shrink to their ghosts.
+    bool stale = false;
+    for (Slot& sl : b->slots)
+        if (sl.used && !sl.primsValid) {
+            stale = true;
+            sl.primsValid = true;
+        }
+    LFM_CUDA(cudaGraphLaunch(b->graph, b->stream));
+    if (stale) {
+        b->tilesDirty = true;
+        if ((rc = ensureGraph(b))) return rc;
+    }
+    for (int k = 1; k < nsteps; ++k) LFM_CUDA(cudaGraphLaunch(b->graph, b->stream));
     return LFM_OK;
 }
 
@@ -539,11 +585,21 @@ extern "C" int lfm_batch_bench(lfm_batch* b, int nsteps, size_t flush_bytes, flo
     if (rc) return rc;
     std::vector<cudaEvent_t> ev(2 * (size_t)nsteps);
     for (auto& e : ev) LFM_CUDA(cudaEventCreate(&e));
+    bool stale = false;   // as in lfm_batch_step: stale cases prepare all cells in the first step
+    for (Slot& sl : b->slots)
+        if (sl.used && !sl.primsValid) {
+            stale = true;
+            sl.primsValid = true;
+        }
     for (int k = 0; k < nsteps; ++k) {
         if ((rc = flushL2(b, flush_bytes))) break;
         cudaEventRecord(ev[2 * (size_t)k], b->stream);
         cudaGraphLaunch(b->graph, b->stream);
         cudaEventRecord(ev[2 * (size_t)k + 1], b->stream);
+        if (k == 0 && stale) {
+            b->tilesDirty = true;
+            if ((rc = ensureGraph(b))) break;
+        }
     }
     cudaError_t e = cudaStreamSynchronize(b->stream);
     for (int k = 0; k < nsteps && e == cudaSuccess; ++k)
@@ -614,6 +670,8 @@ extern "C" int lfm_batch_autotune(lfm_batch* b, int trial_steps, lfm_batch_tunin
     }
     if (e == cudaSuccess) e = copyStates(false);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->dFlags, 0, sizeof(int) * (size_t)b->maxCases, b->stream);
+    for (Slot& sl : b->slots) sl.primsValid = false;   // restored states: primitives are stale
+    b->tilesDirty = true;
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
     if (snap) cudaFree(snap);
     if (rc) return rc;

@@ -47,6 +47,11 @@ struct lfm_solver {
     double* volInv = nullptr;
     cudaGraphExec_t graph = nullptr;
     double graphDt = 0;
+    // FP32-bulk: q holds q - q_ref, and the update kernel keeps the cells'
+    // primitives current; they are stale after a new state is set.
+    bool primsValid = false;
+    double qRef[5] = {0, 0, 0, 0, 0};
+    double* stage = nullptr;   // FP32-bulk: absolute state [nq][nc] in transit to or from the host
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     void* scrub = nullptr;
     size_t scrubBytes = 0;
@@ -162,20 +167,35 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
     return LFM_OK;
 }
 
+StageConfig stageConfig(const lfm_solver* s, int k, double dt) {
+    StageConfig c;
+    c.scheme = s->scheme;
+    c.needGrad = s->needGrad;
+    c.needVis = s->needVis;
+    c.A = s->rkA[(size_t)k];
+    c.B = s->rkB[(size_t)k];
+    c.dt = dt;
+    c.first = (k == 0);
+    c.withRes = (s->residuals && k == 0) ? 1 : 0;
+    c.fullPrep = false;   // FP32-bulk: cells' primitives come from the previous update
+    return c;
+}
+
 template <typename T>
 void stageAll(lfm_solver* s, const Args<T>& a, double dt) {
-    for (int k = 0; k < s->rkOrder; ++k) {
-        StageConfig c;
-        c.scheme = s->scheme;
-        c.needGrad = s->needGrad;
-        c.needVis = s->needVis;
-        c.A = s->rkA[(size_t)k];
-        c.B = s->rkB[(size_t)k];
-        c.dt = dt;
-        c.first = (k == 0);
-        c.withRes = (s->residuals && k == 0) ? 1 : 0;
-        lfm::dev::launch_stage<T>(a, c, s->stream);
-    }
+    for (int k = 0; k < s->rkOrder; ++k) lfm::dev::launch_stage<T>(a, stageConfig(s, k, dt), s->stream);
+}
+
+// FP32-bulk: primitives of every cell from the stored state, once after a
+// new state (the update kernels keep them current afterwards).
+int ensurePrims(lfm_solver* s) {
+    if (s->precision != LFM_FP32_BULK || s->primsValid) return LFM_OK;
+    StageConfig c;
+    c.fullPrep = true;
+    lfm::dev::launch_kernel<float>(s->a32, c, 0, s->stream);
+    LFM_CUDA(cudaGetLastError());
+    s->primsValid = true;
+    return LFM_OK;
 }
 
 void launchStep(lfm_solver* s, double dt) {
@@ -287,11 +307,13 @@ extern "C" int lfm_solver_create(const lfm_solver_desc* d, const lfm_solver_opts
     else
         rc = buildArgs<double>(s, d, s->a64, dP, dN, dG, dOff, dList, dGC, dGK, dGF, sponge);
     if (rc) return fail(rc);
+    if (s->precision == LFM_FP32_BULK) {
+        for (int v = 0; v < s->nq; ++v) s->qRef[v] = s->a32.qRef[v];
+        if ((rc = devAlloc(s, &s->stage, nq * nc))) return fail(rc);
+    }
     if (d->q0) {
-        for (size_t v = 0; v < nq; ++v)
-            if ((e = cudaMemcpyAsync(s->q + v * nt, d->q0 + v * nc, nc * sizeof(double), cudaMemcpyHostToDevice,
-                                     s->stream)) != cudaSuccess)
-                return fail(cudaFail(e, "cudaMemcpyAsync q0"));
+        if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return fail(cudaFail(e, "create"));
+        if ((rc = lfm_solver_set_state(s, d->q0))) return fail(rc);
     }
     if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return fail(cudaFail(e, "create"));
     *out = s;
@@ -316,19 +338,39 @@ extern "C" int lfm_solver_set_state(lfm_solver* s, const double* q) {
     LFM_CUDA(cudaSetDevice(s->device));
     // a new state starts with a clear non-finite flag
     LFM_CUDA(cudaMemsetAsync(s->flag, 0, sizeof(int), s->stream));
-    for (int v = 0; v < s->nq; ++v)
-        LFM_CUDA(cudaMemcpyAsync(s->q + (size_t)v * s->nt, q + (size_t)v * s->nc, (size_t)s->nc * sizeof(double),
-                                 cudaMemcpyHostToDevice, s->stream));
+    const size_t nc = (size_t)s->nc;
+    if (s->precision == LFM_FP32_BULK) {   // stored as q - q_ref
+        LFM_CUDA(cudaMemcpyAsync(s->stage, q, (size_t)s->nq * nc * sizeof(double), cudaMemcpyHostToDevice,
+                                 s->stream));
+        lfm::dev::QOffset qo;
+        for (int v = 0; v < 5; ++v) qo.v[v] = s->qRef[v];
+        lfm::dev::launch_offset_rows(s->q, s->nt, s->stage, s->nc, s->nc, s->nq, qo, -1.0, s->stream);
+        LFM_CUDA(cudaGetLastError());
+    } else {
+        for (int v = 0; v < s->nq; ++v)
+            LFM_CUDA(cudaMemcpyAsync(s->q + (size_t)v * s->nt, q + (size_t)v * nc, nc * sizeof(double),
+                                     cudaMemcpyHostToDevice, s->stream));
+    }
     LFM_CUDA(cudaStreamSynchronize(s->stream));
+    s->primsValid = false;
     return LFM_OK;
 }
 
 extern "C" int lfm_solver_get_state(lfm_solver* s, double* q) {
     if (!s || !q) return lfm::setError(LFM_ERR_INVALID, "null argument");
     LFM_CUDA(cudaSetDevice(s->device));
-    for (int v = 0; v < s->nq; ++v)
-        LFM_CUDA(cudaMemcpyAsync(q + (size_t)v * s->nc, s->q + (size_t)v * s->nt, (size_t)s->nc * sizeof(double),
-                                 cudaMemcpyDeviceToHost, s->stream));
+    if (s->precision == LFM_FP32_BULK) {   // stored as q - q_ref
+        lfm::dev::QOffset qo;
+        for (int v = 0; v < 5; ++v) qo.v[v] = s->qRef[v];
+        lfm::dev::launch_offset_rows(s->stage, s->nc, s->q, s->nt, s->nc, s->nq, qo, 1.0, s->stream);
+        LFM_CUDA(cudaGetLastError());
+        LFM_CUDA(cudaMemcpyAsync(q, s->stage, (size_t)s->nq * s->nc * sizeof(double), cudaMemcpyDeviceToHost,
+                                 s->stream));
+    } else {
+        for (int v = 0; v < s->nq; ++v)
+            LFM_CUDA(cudaMemcpyAsync(q + (size_t)v * s->nc, s->q + (size_t)v * s->nt, (size_t)s->nc * sizeof(double),
+                                     cudaMemcpyDeviceToHost, s->stream));
+    }
     LFM_CUDA(cudaStreamSynchronize(s->stream));
     return LFM_OK;
 }
@@ -337,15 +379,9 @@ extern "C" int lfm_solver_stage(lfm_solver* s, int rk, double dt) {
     if (!s) return lfm::setError(LFM_ERR_INVALID, "null solver");
     if (rk < 0 || rk >= s->rkOrder) return lfm::setError(LFM_ERR_INVALID, "stage index out of range");
     LFM_CUDA(cudaSetDevice(s->device));
-    StageConfig c;
-    c.scheme = s->scheme;
-    c.needGrad = s->needGrad;
-    c.needVis = s->needVis;
-    c.A = s->rkA[(size_t)rk];
-    c.B = s->rkB[(size_t)rk];
-    c.dt = dt;
-    c.first = (rk == 0);
-    c.withRes = (s->residuals && rk == 0) ? 1 : 0;
+    int rc = ensurePrims(s);
+    if (rc) return rc;
+    const StageConfig c = stageConfig(s, rk, dt);
     if (s->precision == LFM_FP32_BULK)
         lfm::dev::launch_stage<float>(s->a32, c, s->stream);
     else
@@ -360,6 +396,7 @@ extern "C" int lfm_solver_step(lfm_solver* s, int nsteps, double dt) {
     LFM_CUDA(cudaSetDevice(s->device));
     int rc = ensureGraph(s, dt);
     if (rc) return rc;
+    if ((rc = ensurePrims(s))) return rc;
     for (int k = 0; k < nsteps; ++k) LFM_CUDA(cudaGraphLaunch(s->graph, s->stream));
     return LFM_OK;
 }
@@ -380,7 +417,9 @@ extern "C" int lfm_solver_step_timed(lfm_solver* s, int nsteps, double dt, float
 
 static int reduceScalar(lfm_solver* s, double dt, int mode, double maxCo, double* out) {
     LFM_CUDA(cudaSetDevice(s->device));
-    lfm::dev::launch_cfl(s->D, s->q, s->nt, s->nc, s->volInv, s->sOff, s->cellS, dt, mode, maxCo, s->partial,
+    lfm::dev::QOffset qo;
+    for (int v = 0; v < 5; ++v) qo.v[v] = s->qRef[v];
+    lfm::dev::launch_cfl(s->D, s->q, qo, s->nt, s->nc, s->volInv, s->sOff, s->cellS, dt, mode, maxCo, s->partial,
                          s->scalar, s->stream);
     LFM_CUDA(cudaGetLastError());
     LFM_CUDA(cudaMemcpyAsync(out, s->scalar, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
@@ -499,9 +538,14 @@ int residualNoalloc(const lfm_solver* s, const Args<T>& base, const double* q, i
     // gradients of the ghosts are read as zeros, so clear both blocks.
     LFM_CUDA(cudaMemsetAsync(a.V, 0, bV, st));
     if (ausm) LFM_CUDA(cudaMemsetAsync(a.grad, 0, bGrad, st));
-    for (size_t v = 0; v < nq; ++v)
-        LFM_CUDA(cudaMemcpyAsync(a.q + v * nt, q + (size_t)v * (size_t)qStride, (size_t)s->nc * sizeof(double),
-                                 cudaMemcpyDeviceToDevice, st));
+    if constexpr (sizeof(T) == sizeof(float)) {
+        // the FP32-bulk kernels read the state as q - q_ref
+        lfm::dev::launch_to_perturbation(a, q, qStride, st);
+    } else {
+        for (size_t v = 0; v < nq; ++v)
+            LFM_CUDA(cudaMemcpyAsync(a.q + v * nt, q + (size_t)v * (size_t)qStride, (size_t)s->nc * sizeof(double),
+                                     cudaMemcpyDeviceToDevice, st));
+    }
     StageConfig c;
     c.scheme = s->scheme;
     c.needGrad = s->needGrad;
@@ -558,6 +602,7 @@ extern "C" int lfm_solver_bench(lfm_solver* s, int nsteps, double dt, size_t flu
     LFM_CUDA(cudaSetDevice(s->device));
     int rc = ensureGraph(s, dt);
     if (rc) return rc;
+    if ((rc = ensurePrims(s))) return rc;
     if (flush_bytes > s->scrubBytes) {
         if (s->scrub) cudaFree(s->scrub);
         s->scrub = nullptr;
@@ -591,18 +636,12 @@ extern "C" int lfm_solver_profile_step(lfm_solver* s, double dt, int n, float* m
     if (!s || !ms || n < lfm::dev::kKernelsPerStage) return lfm::setError(LFM_ERR_INVALID, "bad argument");
     LFM_CUDA(cudaSetDevice(s->device));
     for (int k = 0; k < n; ++k) ms[k] = 0.f;
+    int rc = ensurePrims(s);
+    if (rc) return rc;
     std::vector<cudaEvent_t> ev(2 * (size_t)s->rkOrder * lfm::dev::kKernelsPerStage);
     for (auto& x : ev) LFM_CUDA(cudaEventCreate(&x));
     for (int k = 0; k < s->rkOrder; ++k) {
-        StageConfig c;
-        c.scheme = s->scheme;
-        c.needGrad = s->needGrad;
-        c.needVis = s->needVis;
-        c.A = s->rkA[(size_t)k];
-        c.B = s->rkB[(size_t)k];
-        c.dt = dt;
-        c.first = (k == 0);
-        c.withRes = (s->residuals && k == 0) ? 1 : 0;
+        const StageConfig c = stageConfig(s, k, dt);
         for (int w = 0; w < lfm::dev::kKernelsPerStage; ++w) {
             const size_t base = 2 * ((size_t)k * lfm::dev::kKernelsPerStage + (size_t)w);
             cudaEventRecord(ev[base], s->stream);

@@ -75,23 +75,13 @@ __device__ __forceinline__ T p5neg(T M, T alpha) {
     return T(0.5) * (M - fabs(M)) / M;
 }
 
-// Conservative state of cell or ghost t in FP64. For a ghost the boundary
-// condition of set_boundary_conditions (src/cfd_v0.cpp:1009-1221) is applied
-// to its interior cell and the result stored into q.
+// Ghost state qv of ghost g from the conservative state qi of its interior
+// cell (FP64): the boundary condition of set_boundary_conditions
+// (src/cfd_v0.cpp:1009-1221).
 template <typename T, int D>
-__device__ __forceinline__ void stage_state(const Args<T>& a, int t, double* qv) {
+__device__ __forceinline__ void ghost_bc(const Args<T>& a, int g, const double* qi, double* qv) {
     constexpr int NQ = D + 2;
-    if (t < a.nc) {
-#pragma unroll
-        for (int v = 0; v < NQ; ++v) qv[v] = a.q[(size_t)v * a.nt + t];
-        return;
-    }
-    const int g = t - a.nc;
-    const int in = a.gCell[g];
     const int kind = a.gKind[g];
-    double qi[NQ];
-#pragma unroll
-    for (int v = 0; v < NQ; ++v) qi[v] = a.q[(size_t)v * a.nt + in];
     if (kind == 1) {  // wall: mirror the momentum
         qv[0] = qi[0];
 #pragma unroll
@@ -133,16 +123,33 @@ __device__ __forceinline__ void stage_state(const Args<T>& a, int t, double* qv)
 #pragma unroll
         for (int v = 0; v < NQ; ++v) qv[v] = 0.0;
     }
+}
+
+// Conservative state of cell or ghost t in FP64 (FP64 path: q holds the
+// state itself). A ghost's state is computed from its interior cell and
+// stored into q.
+template <typename T, int D>
+__device__ __forceinline__ void stage_state(const Args<T>& a, int t, double* qv) {
+    constexpr int NQ = D + 2;
+    if (t < a.nc) {
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) qv[v] = a.q[(size_t)v * a.nt + t];
+        return;
+    }
+    const int g = t - a.nc;
+    const int in = a.gCell[g];
+    double qi[NQ];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) qi[v] = a.q[(size_t)v * a.nt + in];
+    ghost_bc<T, D>(a, g, qi, qv);
 #pragma unroll
     for (int v = 0; v < NQ; ++v) a.q[(size_t)v * a.nt + t] = qv[v];
 }
 
-// Gather of the face rhs of cell c, sponge source and low-storage RK update
-// (src/cfd_v0.cpp:2800-2822). The rhs are summed in the flux arithmetic T in
-// ascending face order (the order in which the reference's scatter reaches
-// the cell); the sum is the cell residual RES. The RK registers are FP64. In
-// the FP32-bulk form the increment dt/V * RES is formed in FP32 (its error is
-// that of the FP32 rhs) and only the accumulation runs in FP64.
+// FP64 path: gather of the face rhs of cell c, sponge source and low-storage
+// RK update (src/cfd_v0.cpp:2800-2822). The rhs are summed in ascending face
+// order (the order in which the reference's scatter reaches the cell); the
+// sum is the cell residual RES.
 template <typename T, int D, bool RES>
 __device__ __forceinline__ void update_cell(const Args<T>& a, int c, double Ak, double Bk, double dt, int first) {
     constexpr int NQ = D + 2;
@@ -163,19 +170,9 @@ __device__ __forceinline__ void update_cell(const Args<T>& a, int c, double Ak, 
     }
     double acc[NQ];
     bool finite = true;
-    if constexpr (sizeof(T) == sizeof(float)) {
-        const float dtvi = (float)dt * a.volInv32[c];
+    const double dtvi = dt * a.volInv[c];
 #pragma unroll
-        for (int v = 0; v < NQ; ++v) {
-            const double inc = (double)(dtvi * sum[v]);
-            acc[v] = first ? inc : fma(Ak, a.dq[v * nc + c], inc);
-            finite = finite && isfinite(sum[v]);
-        }
-    } else {
-        const double dtvi = dt * a.volInv[c];
-#pragma unroll
-        for (int v = 0; v < NQ; ++v) acc[v] = (first ? 0.0 : Ak * a.dq[v * nc + c]) + dtvi * (double)sum[v];
-    }
+    for (int v = 0; v < NQ; ++v) acc[v] = (first ? 0.0 : Ak * a.dq[v * nc + c]) + dtvi * (double)sum[v];
     double qv[NQ];
 #pragma unroll
     for (int v = 0; v < NQ; ++v) qv[v] = a.q[v * nt + c];
@@ -190,7 +187,7 @@ __device__ __forceinline__ void update_cell(const Args<T>& a, int c, double Ak, 
     for (int v = 0; v < NQ; ++v) {
         a.dq[v * nc + c] = acc[v];
         const double qn = qv[v] + Bk * acc[v];
-        if constexpr (sizeof(T) != sizeof(float)) finite = finite && isfinite(qn);
+        finite = finite && isfinite(qn);
         a.q[v * nt + c] = qn;
         if (RES) a.res[v * nc + c] = (double)sum[v];
     }

@@ -2,19 +2,27 @@
 // FP32; the RK registers (q, dq), boundary ghost states, geometry precompute
 // and the dt reduction in FP64.
 //
-// Perturbation form. Every FP32 quantity is a deviation from a constant
-// reference state q_ref = (rho_inf, rho_inf U_inf, rho_inf E_inf):
-//   prep32 forms r' = rho - rho_inf, m' = rho u - rho_inf U_inf and
-//   E' = rho E - rho_inf E_inf in FP64 (differences of nearby numbers, exact
-//   or nearly so), rounds them to FP32 and derives u' = u - U_inf and
-//   R psi' = p/rho - p_ref/rho_inf from expressions whose terms are all
-//   perturbation-sized.
-// Each face rhs is then F(q_f).S - F(q_ref).S. The reference-state flux through
-// the faces of a cell sums to F(q_ref).(sum_f S_f) = 0 because the face vectors
-// of a closed cell cancel, so dropping it leaves every cell residual unchanged
-// while FP32 rounding only ever scales perturbations. Evaluated on absolute
-// values, FP32 would round the pressure (~1e5 Pa) by ~1e-2 Pa per face, the
-// size of an acoustic wave; here the rounding is ~1e-7 of the perturbation.
+// Perturbation form. The FP64 state is stored as its deviation from a
+// constant reference state q_ref = (rho_inf, rho_inf U_inf, rho_inf E_inf):
+// q' = q - q_ref (exact differences of nearby numbers, and no cancellation
+// when it is rounded to FP32). Every FP32 quantity is a perturbation too:
+// r' = rho - rho_inf, m' = rho u - rho_inf U_inf, u' = u - U_inf and
+// R psi' = p/rho - p_ref/rho_inf, derived by expressions whose terms are all
+// perturbation-sized. Each face rhs is F(q_f).S - F(q_ref).S. The
+// reference-state flux through the faces of a cell sums to
+// F(q_ref).(sum_f S_f) = 0 because the face vectors of a closed cell cancel,
+// so dropping it leaves every cell residual unchanged while FP32 rounding only
+// ever scales perturbations. Evaluated on absolute values, FP32 would round
+// the pressure (~1e5 Pa) by ~1e-2 Pa per face, the size of an acoustic wave;
+// here the rounding is ~1e-7 of the perturbation.
+//
+// GB300 runs FP64 instructions (conversions included) at about two per clock
+// per SM, so the FP64 work is kept to the two FMAs per component of the
+// low-storage accumulation: conversions between FP32 and FP64 run on the
+// integer pipes (fp_convert.cuh), and the update kernel derives the next
+// stage's primitives from the new state while it holds it in registers
+// (prims32), so a stage reads q' once. The primitive formulas use explicitly
+// rounded operations, so they give the same bits wherever they are inlined.
 //
 // The schemes are those of the FP64 kernels (solver_kernels.cu), which follow
 // the reference (src/cfd_v0.cpp:1896-2822): M1 as the central flux its
@@ -22,6 +30,7 @@
 // perfect-gas enthalpy h = e + p/rho = gamma/(gamma-1) R psi.
 #pragma once
 
+#include "fp_convert.cuh"
 #include "solver_device.cuh"
 
 namespace lfm {
@@ -42,51 +51,34 @@ __device__ __forceinline__ float pressure_dev(const RefState32& R, float r, floa
 }
 
 // ---------------------------------------------------------------------------
-// prep32: ghost states (FP64) and perturbation primitives of cell or ghost t.
+// prims32: FP32 primitives of interior cell t from its FP64 perturbation state
+// qp = q - q_ref. Explicitly rounded operations only (no contraction), so the
+// preparation and update kernels produce identical bits.
 // ---------------------------------------------------------------------------
 template <int D>
-__device__ __forceinline__ void prep32(const Args<float>& a, int t) {
-    constexpr int NQ = D + 2;
+__device__ __forceinline__ void prims32(const Args<float>& a, int t, const double* qp) {
     using P = PRow<D>;
-    double qv[NQ];
-    stage_state<float, D>(a, t, qv);
     const RefState32& R = a.ref;
     const size_t nt = (size_t)a.nt;
-    const float r = (float)(qv[0] - a.qRef[0]);
+    const float r = f64_to_f32(qp[0]);
     float m[D];
 #pragma unroll
-    for (int k = 0; k < D; ++k) m[k] = (float)(qv[k + 1] - a.qRef[k + 1]);
-    float u[D], Rpsi;
-    if (t < a.nc) {
-        const float E = (float)(qv[D + 1] - a.qRef[D + 1]);
-        const float rho = R.rho + r;
-        const float rinv = 1.0f / rho;
-        float Uu = 0.0f, uu = 0.0f, U2 = 0.0f;
+    for (int k = 0; k < D; ++k) m[k] = f64_to_f32(qp[k + 1]);
+    const float E = f64_to_f32(qp[D + 1]);
+    const float rho = __fadd_rn(R.rho, r);
+    const float rinv = __frcp_rn(rho);
+    float u[D], Uu = 0.0f, uu = 0.0f, U2 = 0.0f;
 #pragma unroll
-        for (int k = 0; k < D; ++k) {
-            u[k] = (m[k] - R.U[k] * r) * rinv;   // (rho u - rho_inf U_inf - U_inf r') / rho
-            Uu += R.U[k] * u[k];
-            uu += u[k] * u[k];
-            U2 += R.U[k] * R.U[k];
-        }
-        // kinetic energy: rho|u|^2/2 - rho_inf|U_inf|^2/2 = r'|U_inf|^2/2 + rho (U_inf.u' + |u'|^2/2)
-        const float K = 0.5f * r * U2 + rho * (Uu + 0.5f * uu);
-        const float p = R.gm1 * (E - K);  // p - p_ref
-        Rpsi = (p - R.Rpsi * r) * rinv;         // p/rho - p_ref/rho_inf
-    } else {
-        // A ghost state can lie far from the free stream (a wall mirrors the
-        // momentum, u' = -2 U_inf - u'), where the FP32 kinetic-energy
-        // difference above would cancel; ghosts are few, so theirs is FP64.
-        const double rinv = 1.0 / qv[0];
-        double ke = 0.0;
-#pragma unroll
-        for (int k = 0; k < D; ++k) {
-            u[k] = (float)(qv[k + 1] * rinv - a.UInf[k]);
-            ke += qv[k + 1] * qv[k + 1];
-        }
-        const double p = a.gm1 * (qv[D + 1] - 0.5 * ke * rinv);
-        Rpsi = (float)(p * rinv - a.pRef / a.qRef[0]);
+    for (int k = 0; k < D; ++k) {
+        u[k] = __fmul_rn(__fmaf_rn(-R.U[k], r, m[k]), rinv);   // (m' - U_inf r') / rho
+        Uu = __fmaf_rn(R.U[k], u[k], Uu);
+        uu = __fmaf_rn(u[k], u[k], uu);
+        U2 = __fmaf_rn(R.U[k], R.U[k], U2);
     }
+    // kinetic energy: rho|u|^2/2 - rho_inf|U_inf|^2/2 = r'|U_inf|^2/2 + rho (U_inf.u' + |u'|^2/2)
+    const float K = __fmaf_rn(rho, __fmaf_rn(0.5f, uu, Uu), __fmul_rn(__fmul_rn(0.5f, r), U2));
+    const float p = __fmul_rn(R.gm1, __fsub_rn(E, K));            // p - p_ref
+    const float Rpsi = __fmul_rn(__fmaf_rn(-R.Rpsi, r, p), rinv);  // p/rho - p_ref/rho_inf
     a.prim[(size_t)P::r * nt + t] = r;
 #pragma unroll
     for (int k = 0; k < D; ++k) {
@@ -94,7 +86,104 @@ __device__ __forceinline__ void prep32(const Args<float>& a, int t) {
         a.prim[(size_t)(P::u + k) * nt + t] = u[k];
     }
     a.prim[(size_t)P::Rpsi * nt + t] = Rpsi;
-    a.prim[(size_t)P::c * nt + t] = sqrtf(R.gamma * (R.Rpsi + Rpsi));
+    a.prim[(size_t)P::c * nt + t] = __fsqrt_rn(__fmul_rn(R.gamma, __fadd_rn(R.Rpsi, Rpsi)));
+}
+
+// ---------------------------------------------------------------------------
+// prep32: primitives of cell t from the stored perturbation state, or, for a
+// ghost, its boundary state (FP64, from the interior cell) and primitives.
+// ---------------------------------------------------------------------------
+template <int D>
+__device__ __forceinline__ void prep32(const Args<float>& a, int t) {
+    constexpr int NQ = D + 2;
+    using P = PRow<D>;
+    const size_t nt = (size_t)a.nt;
+    if (t < a.nc) {
+        double qp[NQ];
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) qp[v] = a.q[(size_t)v * nt + t];
+        prims32<D>(a, t, qp);
+        return;
+    }
+    // A ghost state can lie far from the free stream (a wall mirrors the
+    // momentum, u' = -2 U_inf - u'), where the FP32 kinetic-energy difference
+    // of prims32 would cancel; ghosts are few, so theirs is FP64.
+    const int g = t - a.nc;
+    const int in = a.gCell[g];
+    double qi[NQ], qv[NQ];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) qi[v] = a.q[(size_t)v * nt + in] + a.qRef[v];
+    ghost_bc<float, D>(a, g, qi, qv);
+    const double rinv = 1.0 / qv[0];
+    double ke = 0.0;
+    a.prim[(size_t)P::r * nt + t] = (float)(qv[0] - a.qRef[0]);
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        a.prim[(size_t)(P::m + k) * nt + t] = (float)(qv[k + 1] - a.qRef[k + 1]);
+        a.prim[(size_t)(P::u + k) * nt + t] = (float)(qv[k + 1] * rinv - a.UInf[k]);
+        ke += qv[k + 1] * qv[k + 1];
+    }
+    const double p = a.gm1 * (qv[D + 1] - 0.5 * ke * rinv);
+    const float Rpsi = (float)(p * rinv - a.pRef / a.qRef[0]);
+    a.prim[(size_t)P::Rpsi * nt + t] = Rpsi;
+    a.prim[(size_t)P::c * nt + t] = sqrtf(a.ref.gamma * (a.ref.Rpsi + Rpsi));
+}
+
+// ---------------------------------------------------------------------------
+// update32: gather of the face rhs of cell c in ascending face order (the
+// reference's scatter order; the sum is the cell residual RES), sponge source
+// and low-storage RK update of the FP64 perturbation state
+// (src/cfd_v0.cpp:2800-2822), then the next stage's primitives of the cell.
+// The increment dt/V RES is formed in FP32 (its error is that of the FP32
+// rhs); dq and q' accumulate in FP64. The sponge pulls q towards q_ref:
+// dt sigma (q_ref - q) = -dt sigma q'.
+// ---------------------------------------------------------------------------
+template <int D, bool RES>
+__device__ __forceinline__ void update32(const Args<float>& a, int c, double Ak, double Bk, double dt,
+                                         float dt32, int first) {
+    constexpr int NQ = D + 2;
+    const size_t nt = (size_t)a.nt, nf = (size_t)a.nf, nc = (size_t)a.nc;
+    float sum[NQ];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) sum[v] = 0.0f;
+    for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
+        const int code = a.cfList[e];
+        if (code >= 0) {
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) sum[v] += a.flux[v * nf + code];
+        } else {
+            const int f = ~code;
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) sum[v] -= a.flux[v * nf + f];
+        }
+    }
+    const float dtvi = __fmul_rn(dt32, a.volInv32[c]);
+    const double sg = a.sponge[c];
+    const double dts = sg != 0.0 ? -dt * sg : 0.0;
+    double qn[NQ];
+    bool finite = true;
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) {
+        const double inc = f32_to_f64(__fmul_rn(dtvi, sum[v]));
+        double acc = first ? inc : fma(Ak, a.dq[v * nc + c], inc);
+        const double qp = a.q[v * nt + c];
+        if (sg != 0.0) acc = fma(dts, qp, acc);
+        a.dq[v * nc + c] = acc;
+        qn[v] = fma(Bk, acc, qp);
+        a.q[v * nt + c] = qn[v];
+        finite = finite && isfinite(sum[v]);
+        if (RES) a.res[v * nc + c] = f32_to_f64(sum[v]);
+    }
+    if (!finite) atomicOr(a.flag, 1);
+    prims32<D>(a, c, qn);
+}
+
+// Perturbation state q' = q - q_ref of cells [0, n) from a caller's absolute
+// state q ([nq][stride] doubles).
+template <int D>
+__device__ __forceinline__ void to_perturbation(const Args<float>& a, const double* q, int64_t stride, int c) {
+#pragma unroll
+    for (int v = 0; v < D + 2; ++v) a.q[(size_t)v * a.nt + c] = q[(size_t)v * stride + c] - a.qRef[v];
 }
 
 // ---------------------------------------------------------------------------

@@ -358,18 +358,19 @@ __global__ void __launch_bounds__(256) k_update(const __grid_constant__ Args<T> 
 // finishes; both levels use a fixed tree, so results are reproducible.
 // ---------------------------------------------------------------------------
 template <int D>
-__global__ void __launch_bounds__(256) k_cfl(const double* q, int nt, int nc, const double* volInv, const int* sOff,
-                                             const double* cellS, double dt, int mode, double maxCo, double* partial) {
+__global__ void __launch_bounds__(256) k_cfl(const double* q, QOffset qo, int nt, int nc, const double* volInv,
+                                             const int* sOff, const double* cellS, double dt, int mode, double maxCo,
+                                             double* partial) {
     __shared__ double sh[256];
     const int c = LFM_GLOBAL_ID();
     double v = (mode == 0) ? 0.0 : 100.0;
     if (c < nc) {
-        const double rho = q[c];
+        const double rho = q[c] + qo.v[0];
         if (mode == 0) {
             double cfl = 0;
             for (int e = sOff[c]; e < sOff[c + 1]; ++e) {
                 double flux = 0.;
-                for (int k = 0; k < D; ++k) flux += q[(size_t)(k + 1) * nt + c] * cellS[(size_t)e * D + k];
+                for (int k = 0; k < D; ++k) flux += (q[(size_t)(k + 1) * nt + c] + qo.v[k + 1]) * cellS[(size_t)e * D + k];
                 cfl += fabs(flux);
             }
             v = cfl * ((1.0 / rho) * volInv[c] * dt);
@@ -381,7 +382,7 @@ __global__ void __launch_bounds__(256) k_cfl(const double* q, int nt, int nc, co
                 for (int k = 0; k < D; ++k) sMag += S[k] * S[k];
                 sMag = sqrt(sMag);
                 double flux = 0.;
-                for (int k = 0; k < D; ++k) flux += q[(size_t)(k + 1) * nt + c] * S[k] / sMag;
+                for (int k = 0; k < D; ++k) flux += (q[(size_t)(k + 1) * nt + c] + qo.v[k + 1]) * S[k] / sMag;
                 sumFlux += fabs(flux);
             }
             v = maxCo * rho * 2.0 * (1.0 / volInv[c]) / sumFlux;
@@ -518,25 +519,13 @@ void launch_kernel<float>(const Args<float>& a, const StageConfig& s, int which,
     launch_kernel_fp32(a, s, which, st);
 }
 
-// The FP32-bulk form shares k_update: FP32 sums of the face rhs, FP64 update.
-void launch_update_fp32(const Args<float>& a, const StageConfig& s, cudaStream_t st) {
-    const unsigned nb = blocks(a.nc, 256);
-    if (a.D == 2) {
-        if (s.withRes) k_update<float, 2, true><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
-        else k_update<float, 2, false><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
-    } else {
-        if (s.withRes) k_update<float, 3, true><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
-        else k_update<float, 3, false><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
-    }
-}
-
-void launch_cfl(int D, const double* q, int nt, int nc, const double* volInv, const int* sOff, const double* cellS,
+void launch_cfl(int D, const double* q, QOffset qo, int nt, int nc, const double* volInv, const int* sOff, const double* cellS,
                 double dt, int mode, double maxCo, double* partial, double* out, cudaStream_t st) {
     const unsigned nb = blocks(nc, 256);
     if (D == 2)
-        k_cfl<2><<<nb, 256, 0, st>>>(q, nt, nc, volInv, sOff, cellS, dt, mode, maxCo, partial);
+        k_cfl<2><<<nb, 256, 0, st>>>(q, qo, nt, nc, volInv, sOff, cellS, dt, mode, maxCo, partial);
     else
-        k_cfl<3><<<nb, 256, 0, st>>>(q, nt, nc, volInv, sOff, cellS, dt, mode, maxCo, partial);
+        k_cfl<3><<<nb, 256, 0, st>>>(q, qo, nt, nc, volInv, sOff, cellS, dt, mode, maxCo, partial);
     k_reduce_final<<<1, 256, 0, st>>>(partial, (int)nb, mode, out);
 }
 
@@ -547,6 +536,20 @@ void launch_res_sum(const double* res, int nc, double* partial, double* out, cud
 }
 
 void launch_set_flag(int* flag, int v, cudaStream_t st) { k_set_flag<<<1, 1, 0, st>>>(flag, v); }
+
+// dst[v][c] = src[v][c] + sign * off[v] for nq rows of n cells (converts
+// between the FP32-bulk form's stored q - q_ref and the absolute state).
+__global__ void __launch_bounds__(256) k_offset_rows(double* dst, int64_t dstStride, const double* src,
+                                                     int64_t srcStride, int n, int nq, QOffset off, double sign) {
+    const int c = LFM_GLOBAL_ID();
+    if (c >= n) return;
+    for (int v = 0; v < nq; ++v) dst[(size_t)v * dstStride + c] = src[(size_t)v * srcStride + c] + sign * off.v[v];
+}
+
+void launch_offset_rows(double* dst, int64_t dstStride, const double* src, int64_t srcStride, int n, int nq,
+                        QOffset off, double sign, cudaStream_t st) {
+    if (n > 0) k_offset_rows<<<blocks(n, 256), 256, 0, st>>>(dst, dstStride, src, srcStride, n, nq, off, sign);
+}
 
 }  // namespace dev
 }  // namespace lfm

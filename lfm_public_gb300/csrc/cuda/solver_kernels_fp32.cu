@@ -7,9 +7,11 @@
 namespace lfm {
 namespace dev {
 
+// Primitives of cells and ghosts [first, a.nt): first = 0 after a new state,
+// first = nc (ghosts only) once the update kernels keep the cells' current.
 template <int D>
-__global__ void __launch_bounds__(256) k_prep32(const __grid_constant__ Args<float> a) {
-    const int t = LFM_GLOBAL_ID();
+__global__ void __launch_bounds__(256) k_prep32(const __grid_constant__ Args<float> a, int first) {
+    const int t = first + LFM_GLOBAL_ID();
     if (t < a.nt) prep32<D>(a, t);
 }
 
@@ -31,6 +33,20 @@ __global__ void __launch_bounds__(256) k_flux32(const __grid_constant__ Args<flo
     if (f < a.nf) flux32<D, SCH>(a, f);
 }
 
+template <int D, bool RES>
+__global__ void __launch_bounds__(256) k_update32(const __grid_constant__ Args<float> a, double Ak, double Bk,
+                                                  double dt, float dt32, int first) {
+    const int c = LFM_GLOBAL_ID();
+    if (c < a.nc) update32<D, RES>(a, c, Ak, Bk, dt, dt32, first);
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) k_to_perturbation(const __grid_constant__ Args<float> a, const double* q,
+                                                         int64_t stride) {
+    const int c = LFM_GLOBAL_ID();
+    if (c < a.nc) to_perturbation<D>(a, q, stride, c);
+}
+
 // ---------------------------------------------------------------------------
 // Launchers.
 // ---------------------------------------------------------------------------
@@ -39,7 +55,11 @@ static inline unsigned nblocks(int n, int b) { return (unsigned)((n + b - 1) / b
 template <int D>
 void launch_fp32(const Args<float>& a, const StageConfig& s, int which, cudaStream_t st) {
     switch (which) {
-        case 0: k_prep32<D><<<nblocks(a.nt, 256), 256, 0, st>>>(a); break;
+        case 0: {
+            const int first = s.fullPrep ? 0 : a.nc;
+            if (a.nt > first) k_prep32<D><<<nblocks(a.nt - first, 256), 256, 0, st>>>(a, first);
+            break;
+        }
         case 1:
             if (s.needGrad) k_grad32<D><<<nblocks(a.nc, 256), 256, 0, st>>>(a);
             break;
@@ -51,7 +71,12 @@ void launch_fp32(const Args<float>& a, const StageConfig& s, int which, cudaStre
             else if (s.scheme == kSchemeM2) k_flux32<D, kSchemeM2><<<nblocks(a.nf, 256), 256, 0, st>>>(a);
             else k_flux32<D, kSchemeAUSM><<<nblocks(a.nf, 256), 256, 0, st>>>(a);
             break;
-        case 4: launch_update_fp32(a, s, st); break;
+        case 4:
+            if (s.withRes)
+                k_update32<D, true><<<nblocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, (float)s.dt, s.first);
+            else
+                k_update32<D, false><<<nblocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, (float)s.dt, s.first);
+            break;
         default: break;
     }
 }
@@ -63,5 +88,51 @@ void launch_kernel_fp32(const Args<float>& a, const StageConfig& s, int which, c
         launch_fp32<3>(a, s, which, st);
 }
 
+void launch_to_perturbation(const Args<float>& a, const double* q, int64_t stride, cudaStream_t st) {
+    if (a.D == 2)
+        k_to_perturbation<2><<<nblocks(a.nc, 256), 256, 0, st>>>(a, q, stride);
+    else
+        k_to_perturbation<3><<<nblocks(a.nc, 256), 256, 0, st>>>(a, q, stride);
+}
+
 }  // namespace dev
 }  // namespace lfm
+
+// ---------------------------------------------------------------------------
+// Self-test of the integer-pipe conversions (lfm_selftest_fp_convert).
+// ---------------------------------------------------------------------------
+namespace {
+
+__global__ void k_convert_selftest(int64_t n, const unsigned* f32, const unsigned long long* f64,
+                                   unsigned long long* f64_of_f32, unsigned* f32_of_f64) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    f64_of_f32[i] = (unsigned long long)__double_as_longlong(lfm::dev::f32_to_f64(__uint_as_float(f32[i])));
+    f32_of_f64[i] = __float_as_uint(lfm::dev::f64_to_f32(__longlong_as_double((long long)f64[i])));
+}
+
+}  // namespace
+
+extern "C" int lfm_selftest_fp_convert(int64_t n, const uint32_t* f32_bits, const uint64_t* f64_bits,
+                                       uint64_t* f64_of_f32, uint32_t* f32_of_f64) {
+    if (n <= 0 || !f32_bits || !f64_bits || !f64_of_f32 || !f32_of_f64) return -1;
+    unsigned *d32 = nullptr, *o32 = nullptr;
+    unsigned long long *d64 = nullptr, *o64 = nullptr;
+    cudaError_t e = cudaMalloc(&d32, (size_t)n * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&o32, (size_t)n * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&d64, (size_t)n * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&o64, (size_t)n * 8);
+    if (e == cudaSuccess) e = cudaMemcpy(d32, f32_bits, (size_t)n * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d64, f64_bits, (size_t)n * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        k_convert_selftest<<<(unsigned)((n + 255) / 256), 256>>>(n, d32, d64, o64, o32);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(f64_of_f32, o64, (size_t)n * 8, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(f32_of_f64, o32, (size_t)n * 4, cudaMemcpyDeviceToHost);
+    cudaFree(d32);
+    cudaFree(o32);
+    cudaFree(d64);
+    cudaFree(o64);
+    return e == cudaSuccess ? 0 : -3;
+}

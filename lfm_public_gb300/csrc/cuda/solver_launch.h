@@ -17,6 +17,10 @@ struct StageConfig {
     double dt = 0;
     int first = 0;        // stage 0: dq starts from zero (prepare_for_timestep)
     int withRes = 0;      // record the stage-0 residual
+    // FP32-bulk: the update writes the next stage's cell primitives, so the
+    // preparation pass covers the ghosts only unless the cell primitives are
+    // stale (a new state was set).
+    bool fullPrep = true;
 };
 
 template <typename T>
@@ -27,9 +31,11 @@ template <>
 void launch_stage<float>(const Args<float>& a, const StageConfig& s, cudaStream_t st);
 template <>
 void launch_kernel<float>(const Args<float>& a, const StageConfig& s, int which, cudaStream_t st);
-// FP32-bulk kernels (perturbation form) and their shared RK update.
+// FP32-bulk kernels (perturbation form).
 void launch_kernel_fp32(const Args<float>& a, const StageConfig& s, int which, cudaStream_t st);
-void launch_update_fp32(const Args<float>& a, const StageConfig& s, cudaStream_t st);
+// q' = q - q_ref for the cells of an FP32-bulk solver from an absolute state
+// [nq][stride] on the device.
+void launch_to_perturbation(const Args<float>& a, const double* q, int64_t stride, cudaStream_t st);
 
 // Rows of the per-cell primitive array: FP64 keeps 1/rho, u[D], R psi, c;
 // the FP32 perturbation form keeps rho', m'[D], u'[D], R psi', c.
@@ -37,11 +43,19 @@ template <typename T>
 constexpr int primRows(int D) {
     return sizeof(T) == sizeof(double) ? D + 3 : 2 * D + 3;
 }
+// Offset added to the stored state before use (the FP32-bulk form stores
+// q - q_ref; zero for the FP64 path).
+struct QOffset {
+    double v[5];
+};
 // mode 0: max CFL, mode 1: min dt
-void launch_cfl(int D, const double* q, int nt, int nc, const double* volInv, const int* sOff, const double* cellS,
+void launch_cfl(int D, const double* q, QOffset qo, int nt, int nc, const double* volInv, const int* sOff, const double* cellS,
                 double dt, int mode, double maxCo, double* partial, double* out, cudaStream_t st);
 void launch_res_sum(const double* res, int nc, double* partial, double* out, cudaStream_t st);
 void launch_set_flag(int* flag, int v, cudaStream_t st);
+// dst[v][c] = src[v][c] + sign * off.v[v], v < nq, c < n (row strides in elements).
+void launch_offset_rows(double* dst, int64_t dstStride, const double* src, int64_t srcStride, int n, int nq,
+                        QOffset off, double sign, cudaStream_t st);
 
 constexpr int kKernelsPerStage = 5;  // prep, grad, vis, flux, update
 inline const char* kernelName(int i) {

@@ -105,3 +105,34 @@ def test_fp32_bulk_residual_and_cell_residual():
     assert np.max(np.abs(r32 - r64) / scale) < 1e-4
     s64.close()
     s32.close()
+
+
+def _conversion_inputs():
+    rng = np.random.default_rng(1)
+    f32 = rng.integers(0, 2 ** 32, size=100000, dtype=np.uint64).astype(np.uint32)
+    edge32 = np.array([0, 0x80000000, 1, 0x80000001, 0x7fffff, 0x800000, 0x7f7fffff, 0x7f800000, 0xff800000,
+                       0x7fc00000, 0x3f800000], dtype=np.uint32)
+    f32 = np.concatenate([f32, edge32])
+    bits = rng.integers(0, 2 ** 63, size=40000, dtype=np.uint64)
+    vals = (rng.standard_normal(40000) * np.exp(rng.uniform(-100, 100, 40000))).view(np.uint64)
+    fl = rng.standard_normal(20000).astype(np.float32)
+    ties = (fl.astype(np.float64) + np.spacing(fl).astype(np.float64) / 2).view(np.uint64)   # halfway cases
+    sub = rng.uniform(0, 2e-38, 11).view(np.uint64)                                           # binary32 subnormals
+    f64 = np.concatenate([bits, vals, ties, sub])[:f32.size]
+    return f32, f64
+
+
+def test_integer_pipe_conversions_match_ieee():
+    # The FP32-bulk kernels convert between FP32 and FP64 with integer
+    # operations; they must equal IEEE 754 conversions bit for bit (NaNs: any NaN).
+    f32, f64 = _conversion_inputs()
+    o64, o32 = N.selftest_fp_convert(f32, f64)
+    with np.errstate(invalid="ignore", over="ignore"):
+        r64 = f32.view(np.float32).astype(np.float64).view(np.uint64)
+        r32 = f64.view(np.float64).astype(np.float32).view(np.uint32)
+    nan64 = np.isnan(r64.view(np.float64))
+    assert np.array_equal(o64[~nan64], r64[~nan64])
+    assert np.all(np.isnan(o64[nan64].view(np.float64)))
+    nan32 = np.isnan(r32.view(np.float32))
+    assert np.array_equal(o32[~nan32], r32[~nan32])
+    assert np.all(np.isnan(o32[nan32].view(np.float32)))

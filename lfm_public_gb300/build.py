@@ -31,6 +31,11 @@ HOST_SOURCES = ["foam_io.cpp", "foam_case.cpp", "dict_reader.cpp", "poly_mesh_re
 CUDA_SOURCES = ["solver_kernels.cu", "solver_kernels_fp32.cu", "batch_kernels.cu", "capi_solver.cu", "capi_batch.cu",
                 "capi_server.cu"]
 CLI_SOURCES = ["gpu_mesh.cpp", "lfm_solve_gpu.cpp"]
+# The FP32-bulk kernels are compiled without implicit FMA contraction (explicit
+# fmaf/fma calls stay fused): every kernel that inlines the same device
+# function then rounds identically, so a case gives the same bits in the
+# single-case solver, in any batch-kernel variant and in any mix of cases.
+CUDA_FLAGS = {"solver_kernels_fp32.cu": ["-fmad=false"], "batch_kernels.cu": ["-fmad=false"]}
 
 LIB = os.path.join(PKG, "liblfm_gpu.so")
 CLI = os.path.join(PKG, "lfm_solve_gpu")
@@ -60,7 +65,7 @@ def _newer(target: str, deps) -> bool:
 
 
 def _headers():
-    out = []
+    out = [os.path.abspath(__file__)]   # flags live here: a change rebuilds everything
     for d in INCLUDES:
         for n in os.listdir(d):
             if n.endswith((".h", ".cuh")):
@@ -86,8 +91,8 @@ def build_library(verbose: bool = False) -> str:
         obj = os.path.join(BUILD, s + ".o")
         objs.append(obj)
         if not _newer(obj, [src] + hdrs):
-            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *inc, "-c", src,
-                         "-o", obj])
+            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", *CUDA_FLAGS.get(s, []), "-Xcompiler", "-fPIC",
+                         *inc, "-c", src, "-o", obj])
     with cf.ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
         for r in ex.map(_run, jobs):
             if verbose and (r.stdout or r.stderr):

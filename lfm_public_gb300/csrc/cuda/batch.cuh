@@ -53,12 +53,18 @@ struct BatchArgs {
     int itemsPerThread;
 };
 
+// Kernel variants, chosen from the cases in the batch: compiling out what no
+// case needs lowers the kernel's register count and raises its occupancy.
+constexpr int kBatchVariant2DInviscid = 0;   // 2D, M1/M2, mu = 0
+constexpr int kBatchVariant2D = 1;           // 2D, any scheme, viscous
+constexpr int kBatchVariantGeneral = 2;      // 2D and 3D, any scheme, viscous
+
 // Launches stage `stage` of every case as one persistent (cooperative when
 // `cooperative`) kernel of `grid` blocks of `block` threads (128, 256 or 512).
-cudaError_t launch_batch_stage(const BatchArgs& b, int stage, int block, int grid, bool cooperative,
+cudaError_t launch_batch_stage(const BatchArgs& b, int stage, int block, int variant, int grid, bool cooperative,
                                cudaStream_t st);
 // Resident blocks per SM of the stage kernel at `block` threads.
-int batch_blocks_per_sm(int block);
+int batch_blocks_per_sm(int block, int variant);
 
 }  // namespace dev
 }  // namespace lfm

@@ -40,22 +40,27 @@ __device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target,
 
 // One item of a phase: a cell or ghost (prep; the tiles of a case whose cell
 // primitives are current cover its ghosts only), a cell (grad + vis, update)
-// or a face (flux) of the case in shared memory.
-template <int PH, int D>
+// or a face (flux) of the case in shared memory. FULL = false is the variant
+// for batches of M1/M2 cases without viscosity: no gradient or viscous code
+// is compiled in, which keeps the kernel's register count (and so its
+// occupancy) down.
+template <int PH, int D, bool FULL>
 __device__ __forceinline__ void item(const BatchCase& bc, int stage, int i) {
     const Args<float>& a = bc.a;
     if (PH == 0) {
         prep32<D>(a, i);
     } else if (PH == 1) {
-        if (bc.needGrad) grad32<D>(a, i);
-        if (bc.needVis) vis32<D>(a, i);
+        if (FULL) {
+            if (bc.needGrad) grad32<D>(a, i);
+            if (bc.needVis) vis32<D>(a, i);
+        }
     } else if (PH == 2) {
         if (bc.scheme == kSchemeM1)
-            flux32<D, kSchemeM1>(a, i);
-        else if (bc.scheme == kSchemeM2)
-            flux32<D, kSchemeM2>(a, i);
+            flux32<D, kSchemeM1, FULL>(a, i);
+        else if (!FULL || bc.scheme == kSchemeM2)
+            flux32<D, kSchemeM2, FULL>(a, i);
         else
-            flux32<D, kSchemeAUSM>(a, i);
+            flux32<D, kSchemeAUSM, FULL>(a, i);
     } else {
         const int first = stage == 0;
         if (bc.residuals && first)
@@ -69,7 +74,7 @@ __device__ __forceinline__ void item(const BatchCase& bc, int stage, int i) {
 // phase's tile list (neighbouring tiles of a case share cached neighbours).
 // The block keeps the current tile's case in shared memory and reloads it when
 // the case changes.
-template <int PH, int BLOCK>
+template <int PH, int BLOCK, int DIMS, bool FULL>
 __device__ __forceinline__ void phase_tiles(const BatchArgs& b, int stage, BatchCase& sc, int& sSlot) {
     const int nT = b.nTiles[PH];
     const long long t0 = (long long)nT * blockIdx.x / gridDim.x;
@@ -91,10 +96,10 @@ __device__ __forceinline__ void phase_tiles(const BatchArgs& b, int stage, Batch
         for (int k = 0; k < b.itemsPerThread; ++k) {
             const int i = td.start + (int)threadIdx.x + k * BLOCK;
             if (i < end) {
-                if (sc.a.D == 2)
-                    item<PH, 2>(sc, stage, i);
+                if (DIMS == 2 || sc.a.D == 2)
+                    item<PH, 2, FULL>(sc, stage, i);
                 else
-                    item<PH, 3>(sc, stage, i);
+                    item<PH, 3, FULL>(sc, stage, i);
             }
         }
     }
@@ -104,7 +109,8 @@ __device__ __forceinline__ void phase_tiles(const BatchArgs& b, int stage, Batch
 // barrier between phases (none after the last). Within the launch every array
 // is written by one phase and read only by later ones, so no block reads a
 // line it cached before another block rewrote it.
-template <int BLOCK>
+// DIMS = 2: every case is 2D; DIMS = 0: 2D and 3D cases. FULL: see item().
+template <int BLOCK, int DIMS, bool FULL>
 __global__ void __launch_bounds__(BLOCK) k_batch_stage(const __grid_constant__ BatchArgs b, int stage) {
     __shared__ BatchCase sc;
     __shared__ int sSlot;
@@ -112,21 +118,31 @@ __global__ void __launch_bounds__(BLOCK) k_batch_stage(const __grid_constant__ B
     __syncthreads();
     unsigned* counter = &b.ctl->barrier[stage];
     unsigned target = gridDim.x;
-    phase_tiles<0, BLOCK>(b, stage, sc, sSlot);
+    phase_tiles<0, BLOCK, DIMS, FULL>(b, stage, sc, sSlot);
     if (!grid_barrier(counter, target, b.error)) return;
-    if (b.nTiles[1] > 0) {
-        phase_tiles<1, BLOCK>(b, stage, sc, sSlot);
+    if (FULL && b.nTiles[1] > 0) {
+        phase_tiles<1, BLOCK, DIMS, FULL>(b, stage, sc, sSlot);
         target += gridDim.x;
         if (!grid_barrier(counter, target, b.error)) return;
     }
-    phase_tiles<2, BLOCK>(b, stage, sc, sSlot);
+    phase_tiles<2, BLOCK, DIMS, FULL>(b, stage, sc, sSlot);
     target += gridDim.x;
     if (!grid_barrier(counter, target, b.error)) return;
-    phase_tiles<3, BLOCK>(b, stage, sc, sSlot);
+    phase_tiles<3, BLOCK, DIMS, FULL>(b, stage, sc, sSlot);
+}
+
+// Kernel of a launch shape and variant (kBatchVariant*).
+template <int BLOCK>
+auto kernel_of(int variant) -> void (*)(BatchArgs, int) {
+    switch (variant) {
+        case kBatchVariant2DInviscid: return k_batch_stage<BLOCK, 2, false>;
+        case kBatchVariant2D: return k_batch_stage<BLOCK, 2, true>;
+        default: return k_batch_stage<BLOCK, 0, true>;
+    }
 }
 
 template <int BLOCK>
-cudaError_t launch_block(const BatchArgs& b, int stage, int grid, bool cooperative, cudaStream_t st) {
+cudaError_t launch_block(const BatchArgs& b, int stage, int variant, int grid, bool cooperative, cudaStream_t st) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
     cfg.blockDim = dim3(BLOCK);
@@ -137,27 +153,27 @@ cudaError_t launch_block(const BatchArgs& b, int stage, int grid, bool cooperati
     attr[0].val.cooperative = 1;
     cfg.attrs = cooperative ? attr : nullptr;
     cfg.numAttrs = cooperative ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, k_batch_stage<BLOCK>, b, stage);
+    return cudaLaunchKernelEx(&cfg, kernel_of<BLOCK>(variant), b, stage);
 }
 
 }  // namespace
 
-cudaError_t launch_batch_stage(const BatchArgs& b, int stage, int block, int grid, bool cooperative,
+cudaError_t launch_batch_stage(const BatchArgs& b, int stage, int block, int variant, int grid, bool cooperative,
                                cudaStream_t st) {
     switch (block) {
-        case 128: return launch_block<128>(b, stage, grid, cooperative, st);
-        case 512: return launch_block<512>(b, stage, grid, cooperative, st);
-        default: return launch_block<256>(b, stage, grid, cooperative, st);
+        case 128: return launch_block<128>(b, stage, variant, grid, cooperative, st);
+        case 512: return launch_block<512>(b, stage, variant, grid, cooperative, st);
+        default: return launch_block<256>(b, stage, variant, grid, cooperative, st);
     }
 }
 
-int batch_blocks_per_sm(int block) {
+int batch_blocks_per_sm(int block, int variant) {
     int n = 0;
     cudaError_t e;
     switch (block) {
-        case 128: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_stage<128>, 128, 0); break;
-        case 512: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_stage<512>, 512, 0); break;
-        default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_stage<256>, 256, 0); break;
+        case 128: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel_of<128>(variant), 128, 0); break;
+        case 512: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel_of<512>(variant), 512, 0); break;
+        default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel_of<256>(variant), 256, 0); break;
     }
     return e == cudaSuccess ? n : 0;
 }

@@ -94,6 +94,18 @@ std::vector<unsigned char> packCase(const lfm_solver_desc* d, const CaseLayout& 
 
 namespace {
 
+// The stage-kernel variant that covers every case in the batch.
+int currentVariant(const lfm_batch* b) {
+    bool d3 = false, full = false;
+    for (const Slot& sl : b->slots) {
+        if (!sl.used) continue;
+        d3 = d3 || sl.D == 3;
+        full = full || sl.needGradVis;
+    }
+    if (d3) return lfm::dev::kBatchVariantGeneral;
+    return full ? lfm::dev::kBatchVariant2D : lfm::dev::kBatchVariant2DInviscid;
+}
+
 int rebuildTiles(lfm_batch* b) {
     const int tileSize = b->tune.block * b->tune.items_per_thread;
     std::vector<BatchTile> tl[kBatchPhases];
@@ -128,10 +140,12 @@ int rebuildTiles(lfm_batch* b) {
     LFM_CUDA(cudaMemcpyAsync(b->dNTiles, n, sizeof(n), cudaMemcpyHostToDevice, b->stream));
     // the host vectors die here: wait for the copies out of them
     LFM_CUDA(cudaStreamSynchronize(b->stream));
-    if (realloc && b->graph) {
+    const int variant = currentVariant(b);
+    if ((realloc || variant != b->variant) && b->graph) {
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
     }
+    b->variant = variant;
     b->tilesDirty = false;
     return LFM_OK;
 }
@@ -153,7 +167,7 @@ int captureStep(lfm_batch* b, bool cooperative, cudaGraphExec_t* out) {
     LFM_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t le = cudaMemsetAsync(b->dCtl, 0, sizeof(BatchCtl), b->stream);
     for (int k = 0; k < b->rkOrder && le == cudaSuccess; ++k)
-        le = lfm::dev::launch_batch_stage(args, k, b->tune.block, b->grid, cooperative, b->stream);
+        le = lfm::dev::launch_batch_stage(args, k, b->tune.block, b->variant, b->grid, cooperative, b->stream);
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (le != cudaSuccess || e != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
@@ -178,7 +192,7 @@ int ensureGraph(lfm_batch* b) {
         if (rc) return rc;
     }
     if (b->graph) return LFM_OK;
-    const int fit = lfm::dev::batch_blocks_per_sm(b->tune.block);
+    const int fit = lfm::dev::batch_blocks_per_sm(b->tune.block, b->variant);
     if (fit <= 0) return lfm::setError(LFM_ERR_UNSUPPORTED, "batch kernel does not fit on an SM");
     const int bps = b->tune.blocks_per_sm > 0 ? std::min(b->tune.blocks_per_sm, fit) : fit;
     b->grid = bps * b->sms;
@@ -649,7 +663,7 @@ extern "C" int lfm_batch_autotune(lfm_batch* b, int trial_steps, lfm_batch_tunin
     const int ipts[3] = {1, 2, 4};
     int rc = LFM_OK;
     for (int bi = 0; bi < 3 && e == cudaSuccess && rc == LFM_OK; ++bi) {
-        const int fit = lfm::dev::batch_blocks_per_sm(blocks[bi]);
+        const int fit = lfm::dev::batch_blocks_per_sm(blocks[bi], currentVariant(b));
         for (int ii = 0; ii < 3 && rc == LFM_OK; ++ii) {
             for (int bps = 1; bps <= fit && rc == LFM_OK; ++bps) {
                 lfm_batch_tuning t{blocks[bi], ipts[ii], bps, start.cooperative};

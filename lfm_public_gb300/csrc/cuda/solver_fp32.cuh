@@ -302,7 +302,8 @@ __device__ __forceinline__ float p5diff_dd(float a, float b, float alpha) {
 // flux32: perturbation rhs of face f, F(q_f).S - F(q_ref).S, plus the
 // viscous terms (linear in the gradients, so unchanged in form).
 // ---------------------------------------------------------------------------
-template <int D, int SCH>
+// VIS = false compiles the viscous terms out (for callers that know mu = 0).
+template <int D, int SCH, bool VIS = true>
 __device__ __forceinline__ void flux32(const Args<float>& a, int f) {
     constexpr int NQ = D + 2;
     using P = PRow<D>;
@@ -442,7 +443,7 @@ __device__ __forceinline__ void flux32(const Args<float>& a, int f) {
 
     // Viscous face terms (src/cfd_v0.cpp:2682-2796), as in the FP64 kernel.
     const float mu = a.ref.mu;
-    if (mu != 0.0f) {
+    if (VIS && mu != 0.0f) {
         const float Rinv = a.ref.Rinv;
         const float Ti = Ri * Rinv, Tj = Rj * Rinv;   // T - T_ref
         const float lapc = a.lapc[f];

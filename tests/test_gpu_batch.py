@@ -1,11 +1,10 @@
 """Batch engine: many cases advanced by one persistent kernel per RK stage.
 
-Bar: a case advanced inside a batch -- whatever else is in the batch, whenever
-it joined, whatever launch shape the autotuner picked -- ends bit for bit where
-it ends alone in a batch; it agrees with the single-case FP32-bulk solver to
-1e-6 relative L2 per conserved field (the two are separately compiled kernels,
-so FMA contraction may differ); its acoustic pressure stays within 1e-3
-relative L2 of the FP64 path; the arena admits by footprint."""
+Bar: a case advanced inside a batch -- whatever else is in the batch (and so
+whichever stage-kernel variant runs), whenever it joined, whatever launch
+shape the autotuner picked -- ends bit for bit where it ends alone in a batch
+and where the single-case FP32-bulk solver ends; its acoustic pressure stays
+within 1e-3 relative L2 of the FP64 path; the arena admits by footprint."""
 import numpy as np
 import pytest
 
@@ -44,7 +43,7 @@ def _mixed_cases():
     return cs
 
 
-def test_batch_mix_matches_alone_bitwise_and_single_solver():
+def test_batch_mix_matches_alone_and_single_solver_bitwise():
     cs = _mixed_cases()
     chs = [N.CaseHandle.from_case(c) for c in cs]
     b = N.Batch(arena_bytes=512 << 20)
@@ -55,9 +54,9 @@ def test_batch_mix_matches_alone_bitwise_and_single_solver():
     for s, ch, c in zip(slots, chs, cs):
         q = b.get_state(s)
         assert np.array_equal(q, _alone(ch, n, c.delta_t)), c.name
-        q1 = _single(ch, n, c.delta_t)
-        err = np.linalg.norm(q - q1, axis=1) / np.linalg.norm(q1, axis=1)
-        assert np.all(err <= 1e-6), (c.name, err)
+        # the FP32-bulk kernels are compiled without implicit FMA contraction,
+        # so the single-case solver's kernels round exactly as the batch's
+        assert np.array_equal(q, _single(ch, n, c.delta_t)), c.name
     b.close()
 
 

@@ -56,7 +56,8 @@ typedef enum lfm_status {
  * CFDv0_solver::initialize + reorder_faces (src/cfd_v0.cpp:83-339, 759-967),
  * flattened. Faces are the "owned" cell-faces in the reference's processing
  * order (cell by cell, slot by slot); P is the processing cell, N the other
- * side (N >= n_cells: boundary ghost N - n_cells). Geometry is seen from P. */
+ * side (N >= n_cells: boundary ghost N - n_cells, then processor-face halo
+ * N - n_cells - n_ghosts). Geometry is seen from P. */
 typedef struct lfm_solver_desc {
     int dim;                 /* 2 or 3 */
     int nq;                  /* dim + 2 */
@@ -89,6 +90,14 @@ typedef struct lfm_solver_desc {
     double gamma, Rgas, rhoInf, EInf, pInf, TInf, UInf[3], mu, Cp, PrInv;
     const double* rkA;       /* [rk_order] */
     const double* rkB;
+    /* Processor-face halos of one partition of a decomposed case (0 for a
+     * whole case): halo h is the neighbour slot N = n_cells + n_ghosts + h of
+     * a processor face; each stage it takes the state of cell
+     * halo_src_cell[h] of partition halo_src_part[h] (the reference receives
+     * it over MPI, src/cfd_v0.cpp:3283-3374). */
+    int64_t n_halos;
+    const int64_t* halo_src_part;  /* [n_halos] */
+    const int64_t* halo_src_cell;  /* [n_halos] solver-order cell of that partition */
 } lfm_solver_desc;
 
 typedef struct lfm_case lfm_case;
@@ -239,6 +248,44 @@ int lfm_solver_launches_per_step(const lfm_solver* s, int* launches);
  * lfm_solver_kernel_name). Synchronizes. */
 int lfm_solver_profile_step(lfm_solver* s, double dt, int n, float* ms);
 const char* lfm_solver_kernel_name(int i);
+
+/* ---- decomposed cases on one GPU ------------------------------------------
+ *
+ * The reference runs a decomposed case (processor0..N-1, decomposePar) as one
+ * MPI rank per partition, exchanging halo cells over MPI (MPI_env,
+ * src/mpi_env.cpp:406-463; CFDv0_solver::mpi_communication/mpi_wait,
+ * src/cfd_v0.cpp:3546-3603). Here all partitions run on one GPU: each
+ * processor face's neighbour is a halo slot, and the exchange is an on-device
+ * copy from the source partition -- conserved state before each stage,
+ * viscous terms before the fluxes -- with no collective. */
+typedef struct lfm_pcase lfm_pcase;
+typedef struct lfm_partitioned lfm_partitioned;
+
+/* Reads <root>/processor0..nparts-1 (polyMesh with processor patches and
+ * faceProcAddressing / cellProcAddressing, fields at the start time) and the
+ * dictionaries of <root>; builds every partition's description with its
+ * halos resolved. */
+int lfm_pcase_open(const char* root, int nparts, lfm_pcase** out);
+int lfm_pcase_parts(const lfm_pcase* pc, int* nparts);
+/* Partition part's description (pointers valid until lfm_pcase_free). */
+int lfm_pcase_describe(const lfm_pcase* pc, int part, lfm_solver_desc* out);
+/* Global cell (cellProcAddressing) of each solver-order cell of a partition. */
+int lfm_pcase_cell_global(const lfm_pcase* pc, int part, int64_t* out);
+int lfm_pcase_time(const lfm_pcase* pc, double* delta_t, double* start_time, double* end_time,
+                   int* adjust_time_step, double* max_co);
+void lfm_pcase_free(lfm_pcase* pc);
+
+/* One solver per partition on a shared stream; descs[p] carries partition
+ * p's halos (halo_src_part, halo_src_cell). */
+int lfm_partitioned_create(const lfm_solver_desc* const* descs, int nparts, const lfm_solver_opts* opts,
+                           lfm_partitioned** out);
+void lfm_partitioned_destroy(lfm_partitioned* P);
+/* State of one partition ([nq][n_cells] of that partition, solver order). */
+int lfm_partitioned_set_state(lfm_partitioned* P, int part, const double* q);
+int lfm_partitioned_get_state(lfm_partitioned* P, int part, double* q);
+/* nsteps time steps of every partition (one CUDA graph per step); asynchronous. */
+int lfm_partitioned_step(lfm_partitioned* P, int nsteps, double dt);
+int lfm_partitioned_sync(lfm_partitioned* P);
 
 /* Diagnostic: runs the FP32-bulk kernels' integer-pipe binary32 <-> binary64
  * conversions on the device over n bit patterns (host arrays) and returns

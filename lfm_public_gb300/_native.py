@@ -46,6 +46,7 @@ class SolverDesc(C.Structure):
         ("gamma", C.c_double), ("Rgas", C.c_double), ("rhoInf", C.c_double), ("EInf", C.c_double),
         ("pInf", C.c_double), ("TInf", C.c_double), ("UInf", C.c_double * 3), ("mu", C.c_double), ("Cp", C.c_double),
         ("PrInv", C.c_double), ("rkA", _dp), ("rkB", _dp),
+        ("n_halos", C.c_int64), ("halo_src_part", _i64p), ("halo_src_cell", _i64p),
     ]
 
 
@@ -153,6 +154,19 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "lfm_solver_bench": ([vp, C.c_int, C.c_double, C.c_size_t, C.POINTER(C.c_float)], C.c_int),
         "lfm_solver_profile_step": ([vp, C.c_double, C.c_int, C.POINTER(C.c_float)], C.c_int),
         "lfm_solver_kernel_name": ([C.c_int], C.c_char_p),
+        "lfm_pcase_open": ([C.c_char_p, C.c_int, C.POINTER(vp)], C.c_int),
+        "lfm_pcase_parts": ([vp, C.POINTER(C.c_int)], C.c_int),
+        "lfm_pcase_describe": ([vp, C.c_int, C.POINTER(SolverDesc)], C.c_int),
+        "lfm_pcase_cell_global": ([vp, C.c_int, _i64p], C.c_int),
+        "lfm_pcase_time": ([vp, _dp, _dp, _dp, C.POINTER(C.c_int), _dp], C.c_int),
+        "lfm_pcase_free": ([vp], None),
+        "lfm_partitioned_create": ([C.POINTER(C.POINTER(SolverDesc)), C.c_int, C.POINTER(SolverOpts), C.POINTER(vp)],
+                                   C.c_int),
+        "lfm_partitioned_destroy": ([vp], None),
+        "lfm_partitioned_set_state": ([vp, C.c_int, _dp], C.c_int),
+        "lfm_partitioned_get_state": ([vp, C.c_int, _dp], C.c_int),
+        "lfm_partitioned_step": ([vp, C.c_int, C.c_double], C.c_int),
+        "lfm_partitioned_sync": ([vp], C.c_int),
         "lfm_selftest_fp_convert": ([C.c_int64, C.POINTER(C.c_uint32), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                      C.POINTER(C.c_uint32)], C.c_int),
         "lfm_batch_create": ([C.POINTER(BatchOpts), C.POINTER(vp)], C.c_int),
@@ -388,6 +402,97 @@ class Solver:
     def close(self):
         if getattr(self, "_h", None):
             load_library().lfm_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PartitionedCase:
+    """An lfm_pcase: every partition (processor0..N-1) of a decomposed case."""
+
+    def __init__(self, root: str, nparts: int):
+        lib = load_library()
+        h = C.c_void_p()
+        check(lib.lfm_pcase_open(root.encode(), nparts, C.byref(h)))
+        self._h = h
+        self.nparts = nparts
+        self.descs = []
+        for p in range(nparts):
+            d = SolverDesc()
+            check(lib.lfm_pcase_describe(h, p, C.byref(d)))
+            self.descs.append(d)
+
+    def cell_global(self, part: int) -> np.ndarray:
+        out = np.empty(self.descs[part].n_cells, dtype=np.int64)
+        check(load_library().lfm_pcase_cell_global(self._h, part, _ptr(out, C.c_int64)))
+        return out
+
+    def delta_t(self) -> float:
+        v = C.c_double()
+        check(load_library().lfm_pcase_time(self._h, C.byref(v), None, None, None, None))
+        return v.value
+
+    def q0(self, part: int) -> np.ndarray:
+        d = self.descs[part]
+        return np.ctypeslib.as_array(d.q0, shape=(d.nq * d.n_cells,)).reshape(d.nq, d.n_cells).copy()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().lfm_pcase_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Partitioned:
+    """An lfm_partitioned: every partition of a decomposed case on one GPU,
+    halos exchanged by on-device copies."""
+
+    def __init__(self, pcase: PartitionedCase, precision: int = LFM_FP64, device: int = 0):
+        lib = load_library()
+        self.pcase = pcase
+        arr = (C.POINTER(SolverDesc) * pcase.nparts)(*[C.pointer(d) for d in pcase.descs])
+        opts = SolverOpts(precision=precision, device=device, block=0)
+        h = C.c_void_p()
+        check(lib.lfm_partitioned_create(arr, pcase.nparts, C.byref(opts), C.byref(h)))
+        self._h = h
+
+    def step(self, nsteps: int, dt: float):
+        check(load_library().lfm_partitioned_step(self._h, nsteps, dt))
+
+    def sync(self):
+        check(load_library().lfm_partitioned_sync(self._h))
+
+    def set_state(self, part: int, q: np.ndarray):
+        d = self.pcase.descs[part]
+        q = np.ascontiguousarray(q, dtype=np.float64).reshape(d.nq, d.n_cells)
+        check(load_library().lfm_partitioned_set_state(self._h, part, _ptr(q, C.c_double)))
+
+    def get_state(self, part: int) -> np.ndarray:
+        d = self.pcase.descs[part]
+        out = np.empty((d.nq, d.n_cells), dtype=np.float64)
+        check(load_library().lfm_partitioned_get_state(self._h, part, _ptr(out, C.c_double)))
+        return out
+
+    def global_state(self, n_global: int) -> np.ndarray:
+        """State of the whole case [nq][n_global] by global (undecomposed) cell."""
+        nq = self.pcase.descs[0].nq
+        out = np.full((nq, n_global), np.nan)
+        for p in range(self.pcase.nparts):
+            out[:, self.pcase.cell_global(p)] = self.get_state(p)
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().lfm_partitioned_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -40,6 +40,8 @@ class Patch:
     start: int
     size: int
     neighbour: Optional[str] = None
+    my_proc: Optional[int] = None          # processor patches (decomposed cases)
+    neighb_proc: Optional[int] = None
 
 
 @dataclass
@@ -593,6 +595,8 @@ def write_polymesh(case: Case, d: str) -> None:
             f.write(f"    {p.name}\n    {{\n        type            {p.type};\n")
             if p.neighbour:
                 f.write(f"        neighbourPatch  {p.neighbour};\n")
+            if p.neighb_proc is not None:
+                f.write(f"        myProcNo        {p.my_proc};\n        neighbProcNo    {p.neighb_proc};\n")
             f.write(f"        nFaces          {p.size};\n        startFace       {p.start};\n    }}\n")
         f.write(")\n")
 
@@ -600,7 +604,7 @@ def write_polymesh(case: Case, d: str) -> None:
 def _boundary_block(case: Case) -> str:
     out = "\n"
     for p in case.patches:
-        t = p.type if p.type in ("empty", "cyclic") else "zeroGradient"
+        t = p.type if p.type in ("empty", "cyclic", "processor") else "zeroGradient"
         out += f"    {p.name}\n    {{\n        type            {t};\n    }}\n"
     return out
 
@@ -702,3 +706,127 @@ def _read_internal_field(path: str) -> np.ndarray:
         vals = np.array(body.replace("(", " ").replace(")", " ").split()[:3 * n], dtype=np.float64)
         return vals.reshape(n, 3)
     return np.array(body.split()[:n], dtype=np.float64)
+
+
+# ---------------------------------------------------------------------------
+# decomposition into processor partitions (what decomposePar writes)
+# ---------------------------------------------------------------------------
+def partition_cells(case: Case, nparts: int, method: str = "x", seed: int = 0) -> np.ndarray:
+    """Partition of every cell: slabs along x ("x"), contiguous index ranges
+    ("index") or a seeded random assignment ("random", many processor faces)."""
+    n = case.n_cells
+    if method == "x":
+        # cells with the same x (to 1e-9) share a partition, so that an
+        # extruded case keeps each spanwise column - and its cyclic pair - whole
+        xs, inv, counts = np.unique(np.round(case.cell_centres[:, 0], 9), return_inverse=True, return_counts=True)
+        first = np.cumsum(counts) - counts
+        return (first[inv] * nparts // n).astype(np.int64)
+    if method == "index":
+        return np.arange(n) * nparts // n
+    if method == "random":
+        return np.random.default_rng(seed).integers(0, nparts, size=n)
+    raise ValueError(f"unknown partition method {method}")
+
+
+def _write_label_list(path: str, obj: str, values) -> None:
+    with open(path, "w") as f:
+        f.write(_header("labelList", obj, "constant/polyMesh"))
+        f.write(f"{len(values)}\n(\n" + "\n".join(str(int(v)) for v in values) + "\n)\n")
+
+
+def decompose_case(case: Case, root: str, nparts: int, method: str = "x", seed: int = 0, **kw) -> np.ndarray:
+    """Writes ``case`` under ``root`` (dictionaries and the whole mesh) and its
+    decomposition into ``root``/processor0..nparts-1, as decomposePar does:
+    each partition's cells and points renumbered in global order, its internal
+    faces, the original patches restricted to its cells, and one processor
+    patch per neighbouring partition (faces in global order on both sides; the
+    side that does not own a face globally stores it flipped, with a negative
+    faceProcAddressing), plus cell/face/point/boundaryProcAddressing and the
+    initial fields. A cyclic pair must join cells of one partition (the "x"
+    method keeps spanwise columns whole); processorCyclic patches are not
+    written. Returns the partition of every cell."""
+    part = partition_cells(case, nparts, method, seed)
+    byname = {pt.name: pt for pt in case.patches}
+    for pt in case.patches:
+        if pt.type != "cyclic":
+            continue
+        nb = byname[pt.neighbour]
+        a = part[case.owner[pt.start:pt.start + pt.size]]
+        b = part[case.owner[nb.start:nb.start + nb.size]]
+        if not np.array_equal(a, b):
+            raise ValueError(f"cyclic patch {pt.name} pairs cells of different partitions "
+                             "(processorCyclic patches are not supported)")
+    write_case(case, root, **kw)
+    fo, fp = case.face_offsets, case.face_points
+    owner, nbr = case.owner, case.neighbour
+    n_int = nbr.shape[0]
+    for p in range(nparts):
+        cells = np.nonzero(part == p)[0]
+        lcell = np.full(case.n_cells, -1, dtype=np.int64)
+        lcell[cells] = np.arange(cells.size)
+        faces, flip, fown, fnbr = [], [], [], []
+        # internal faces of the partition (global order is upper-triangular and
+        # the renumbering is monotone, so the order stays valid)
+        inner = np.nonzero((part[owner[:n_int]] == p) & (part[nbr] == p))[0]
+        faces += inner.tolist()
+        flip += [False] * inner.size
+        fown += lcell[owner[inner]].tolist()
+        fnbr += lcell[nbr[inner]].tolist()
+        patches = []
+        bmap = []
+        for bi, pt in enumerate(case.patches):
+            gf = np.arange(pt.start, pt.start + pt.size)
+            gf = gf[part[owner[gf]] == p]
+            patches.append(Patch(pt.name, pt.type, len(faces), int(gf.size), neighbour=pt.neighbour))
+            bmap.append(bi)
+            faces += gf.tolist()
+            flip += [False] * gf.size
+            fown += lcell[owner[gf]].tolist()
+        gi = np.arange(n_int)
+        po, pn = part[owner[:n_int]], part[nbr]
+        for q in range(nparts):
+            if q == p:
+                continue
+            mine = gi[(po == p) & (pn == q)]
+            theirs = gi[(po == q) & (pn == p)]
+            gf = np.sort(np.concatenate([mine, theirs]))
+            if gf.size == 0:
+                continue
+            patches.append(Patch(f"procBoundary{p}to{q}", "processor", len(faces), int(gf.size), my_proc=p,
+                                 neighb_proc=q))
+            bmap.append(-1)
+            own_side = po[gf] == p
+            faces += gf.tolist()
+            flip += (~own_side).tolist()
+            fown += np.where(own_side, lcell[owner[gf]], lcell[nbr[gf]]).tolist()
+        # points in global order
+        used = np.unique(np.concatenate([fp[fo[f]:fo[f + 1]] for f in faces]))
+        lpt = np.full(case.points.shape[0], -1, dtype=np.int64)
+        lpt[used] = np.arange(used.size)
+        offs, pts = [0], []
+        for f, fl in zip(faces, flip):
+            v = fp[fo[f]:fo[f + 1]]
+            if fl:   # reversed orientation, first point kept (OpenFOAM's face::reverseFace)
+                v = np.concatenate([v[:1], v[1:][::-1]])
+            pts.append(lpt[v])
+            offs.append(offs[-1] + v.size)
+        local = Case(name=f"{case.name}.p{p}", dim=case.dim, points=case.points[used],
+                     face_offsets=np.array(offs, dtype=np.int64), face_points=np.concatenate(pts).astype(np.int64),
+                     owner=np.array(fown, dtype=np.int64), neighbour=np.array(fnbr, dtype=np.int64), patches=patches,
+                     n_cells=int(cells.size), cell_centres=case.cell_centres[cells])
+        pdir = os.path.join(root, f"processor{p}")
+        mesh = os.path.join(pdir, "constant", "polyMesh")
+        write_polymesh(local, mesh)
+        _write_label_list(os.path.join(mesh, "cellProcAddressing"), "cellProcAddressing", cells)
+        fpa = [(-(f + 1) if fl else (f + 1)) for f, fl in zip(faces, flip)]
+        _write_label_list(os.path.join(mesh, "faceProcAddressing"), "faceProcAddressing", fpa)
+        _write_label_list(os.path.join(mesh, "pointProcAddressing"), "pointProcAddressing", used)
+        _write_label_list(os.path.join(mesh, "boundaryProcAddressing"), "boundaryProcAddressing", bmap)
+        z = os.path.join(pdir, "0")
+        os.makedirs(z, exist_ok=True)
+        write_field(local, z, "p", case.fields["p"][cells], "[1 -1 -2 0 0 0 0]")
+        write_field(local, z, "T", case.fields["T"][cells], "[0 0 0 1 0 0 0]")
+        write_field(local, z, "U", case.fields["U"][cells], "[0 1 -1 0 0 0 0]")
+        if "alpha" in case.fields:
+            write_field(local, z, "alpha", case.fields["alpha"][cells], "[0 1 0 0 0 0 0]")
+    return part

@@ -21,15 +21,17 @@ inline int validateDesc(const lfm_solver_desc* d) {
     if (d->solver < 0 || d->solver > 2) return lfm::setError(LFM_ERR_INVALID, "unknown solver");
     if (d->n_cells <= 0 || d->n_faces <= 0 || d->n_ghosts < 0)
         return lfm::setError(LFM_ERR_INVALID, "empty mesh");
-    if (d->n_cells + d->n_ghosts > 0x7fffffffLL / 32 || d->n_faces > 0x7fffffffLL / 8)
+    if (d->n_cells + d->n_ghosts + d->n_halos > 0x7fffffffLL / 32 || d->n_faces > 0x7fffffffLL / 8)
         return lfm::setError(LFM_ERR_UNSUPPORTED, "mesh too large for 32-bit device indexing");
     if (!d->face_p || !d->face_n || !d->face_ghost || !d->S || !d->d || !d->w || !d->smag || !d->dmag_inv ||
         !d->dnorm || !d->delta_mag || !d->K || !d->vol_inv || !d->sponge || !d->cell_face_offsets ||
         !d->cell_faces || !d->cell_face_sign || !d->cell_s_offsets || !d->cell_s || !d->rkA || !d->rkB ||
-        (d->n_ghosts > 0 && (!d->ghost_cell || !d->ghost_kind)))
+        (d->n_ghosts > 0 && (!d->ghost_cell || !d->ghost_kind)) ||
+        (d->n_halos > 0 && (!d->halo_src_part || !d->halo_src_cell)))
         return lfm::setError(LFM_ERR_INVALID, "incomplete solver description");
+    if (d->n_halos < 0) return lfm::setError(LFM_ERR_INVALID, "negative halo count");
     if (d->rk_order < 1 || d->rk_order > 8) return lfm::setError(LFM_ERR_INVALID, "rk_order out of range");
-    const int64_t nt = d->n_cells + d->n_ghosts;
+    const int64_t nt = d->n_cells + d->n_ghosts + d->n_halos;
     for (int64_t f = 0; f < d->n_faces; ++f) {
         if (d->face_p[f] < 0 || d->face_p[f] >= d->n_cells || d->face_n[f] < 0 || d->face_n[f] >= nt)
             return lfm::setError(LFM_ERR_INVALID, "face index out of range at face " + std::to_string(f));
@@ -83,8 +85,8 @@ struct DescIndex {
             gCell[g] = (int)d->ghost_cell[g];
             gKind[g] = d->ghost_kind[g];
         }
-        for (size_t f = 0; f < nf; ++f)
-            if (fN[f] >= (int)nc) gFace[(size_t)fN[f] - nc] = (int)f;
+        for (size_t f = 0; f < nf; ++f)   // ghosts only (halos follow them)
+            if (fN[f] >= (int)nc && fN[f] < (int)(nc + ng)) gFace[(size_t)fN[f] - nc] = (int)f;
     }
 };
 
@@ -97,7 +99,8 @@ void setConstants(dev::Args<T>& a, const lfm_solver_desc* d) {
     a.nc = (int)d->n_cells;
     a.ng = (int)d->n_ghosts;
     a.nf = (int)d->n_faces;
-    a.nt = a.nc + a.ng;
+    a.nh = (int)d->n_halos;
+    a.nt = a.nc + a.ng + a.nh;
     a.gamma = d->gamma;
     a.gm1 = d->gamma - 1.0;
     a.Rinv = 1.0 / d->Rgas;

@@ -52,6 +52,8 @@ struct lfm_solver {
     bool primsValid = false;
     double qRef[5] = {0, 0, 0, 0, 0};
     double* stage = nullptr;   // FP32-bulk: absolute state [nq][nc] in transit to or from the host
+    int nh = 0;                // processor-face halos (partitions of a decomposed case)
+    bool ownStream = true;     // false for the partitions of an lfm_partitioned
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     void* scrub = nullptr;
     size_t scrubBytes = 0;
@@ -225,11 +227,17 @@ int ensureGraph(lfm_solver* s, double dt) {
 
 }  // namespace
 
-extern "C" int lfm_solver_create(const lfm_solver_desc* d, const lfm_solver_opts* opts, lfm_solver** out) {
+namespace {
+
+// Creates a solver; `stream` (not owned) is shared by the partitions of a
+// decomposed case, which alone may carry processor-face halos.
+int createSolver(const lfm_solver_desc* d, const lfm_solver_opts* opts, cudaStream_t stream, lfm_solver** out) {
     if (!out) return lfm::setError(LFM_ERR_INVALID, "null output handle");
     *out = nullptr;
     int rc = lfm::setup::validateDesc(d);
     if (rc) return rc;
+    if (d->n_halos > 0 && !stream)
+        return lfm::setError(LFM_ERR_INVALID, "a partition with processor-face halos runs in an lfm_partitioned");
     lfm_solver* s = new lfm_solver;
     s->precision = opts ? opts->precision : LFM_FP64;
     s->device = opts ? opts->device : 0;
@@ -246,8 +254,10 @@ extern "C" int lfm_solver_create(const lfm_solver_desc* d, const lfm_solver_opts
         delete s;
         return cudaFail(e, "cudaSetDevice");
     }
-    e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) {
+    if (stream) {
+        s->stream = stream;
+        s->ownStream = false;
+    } else if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess) {
         delete s;
         return cudaFail(e, "cudaStreamCreate");
     }
@@ -258,7 +268,8 @@ extern "C" int lfm_solver_create(const lfm_solver_desc* d, const lfm_solver_opts
     s->nc = (int)d->n_cells;
     s->ng = (int)d->n_ghosts;
     s->nf = (int)d->n_faces;
-    s->nt = s->nc + s->ng;
+    s->nh = (int)d->n_halos;
+    s->nt = s->nc + s->ng + s->nh;
     s->scheme = d->solver;
     s->rkOrder = d->rk_order;
     s->rkA.assign(d->rkA, d->rkA + d->rk_order);
@@ -287,8 +298,8 @@ extern "C" int lfm_solver_create(const lfm_solver_desc* d, const lfm_solver_opts
         cfList[k] = d->cell_face_sign[k] > 0 ? (int)d->cell_faces[k] : ~(int)d->cell_faces[k];
     std::vector<int> gCell = toInt(d->ghost_cell, (size_t)s->ng), gKind((size_t)s->ng), gFace((size_t)s->ng, 0);
     for (int g = 0; g < s->ng; ++g) gKind[(size_t)g] = d->ghost_kind[g];
-    for (int f = 0; f < s->nf; ++f)
-        if (fN[(size_t)f] >= s->nc) gFace[(size_t)(fN[(size_t)f] - s->nc)] = f;
+    for (int f = 0; f < s->nf; ++f)   // ghosts only (halos follow them)
+        if (fN[(size_t)f] >= s->nc && fN[(size_t)f] < s->nc + s->ng) gFace[(size_t)(fN[(size_t)f] - s->nc)] = f;
     std::vector<int> sOff = toInt(d->cell_s_offsets, nc + 1);
     int *dP, *dN, *dOff, *dList, *dGC, *dGK, *dGF;
     uint8_t* dG;
@@ -320,6 +331,12 @@ extern "C" int lfm_solver_create(const lfm_solver_desc* d, const lfm_solver_opts
     return LFM_OK;
 }
 
+}  // namespace
+
+extern "C" int lfm_solver_create(const lfm_solver_desc* d, const lfm_solver_opts* opts, lfm_solver** out) {
+    return createSolver(d, opts, nullptr, out);
+}
+
 extern "C" void lfm_solver_destroy(lfm_solver* s) {
     if (!s) return;
     cudaSetDevice(s->device);
@@ -329,7 +346,7 @@ extern "C" void lfm_solver_destroy(lfm_solver* s) {
     if (s->scrub) cudaFree(s->scrub);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
-    if (s->stream) cudaStreamDestroy(s->stream);
+    if (s->stream && s->ownStream) cudaStreamDestroy(s->stream);
     delete s;
 }
 
@@ -662,5 +679,208 @@ extern "C" int lfm_solver_profile_step(lfm_solver* s, double dt, int n, float* m
         }
     for (auto& x : ev) cudaEventDestroy(x);
     LFM_CUDA(cudaGetLastError());
+    return LFM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Decomposed cases: every partition on the same GPU (lfm_partitioned_*).
+//
+// The reference runs one partition per MPI rank and exchanges halo cells
+// after each stage's update (conserved state) and after calc_VIS (viscous
+// terms) (src/mesh_solver.cpp:500-672). Here every partition is a solver on
+// one shared stream, and the exchange is a gather kernel per partition that
+// copies the source cells into the halo slots: state before each stage's
+// preparation, viscous terms between the viscous pass and the fluxes.
+// Gradients are not exchanged (the reference exchanges none: its halos'
+// gradients stay zero, and M2AUSM with minmod reads zero gradients there).
+// ---------------------------------------------------------------------------
+struct lfm_partitioned {
+    int device = 0;
+    int precision = LFM_FP64;
+    cudaStream_t stream = nullptr;
+    std::vector<lfm_solver*> parts;
+    std::vector<int*> haloPart, haloCell;   // device lists per partition
+    double** dQ = nullptr;                  // per-partition state base pointers
+    void** dV = nullptr;                    // per-partition viscous-term base pointers
+    int* dNt = nullptr;                     // per-partition row strides
+    cudaGraphExec_t graph = nullptr;
+    double graphDt = 0;
+};
+
+namespace {
+
+template <typename T>
+void partitionedStages(lfm_partitioned* P, double dt) {
+    const size_t np = P->parts.size();
+    auto args = [&](size_t p) -> const Args<T>& {
+        if constexpr (sizeof(T) == sizeof(float)) return P->parts[p]->a32;
+        else return P->parts[p]->a64;
+    };
+    lfm_solver* s0 = P->parts[0];
+    for (int k = 0; k < s0->rkOrder; ++k) {
+        const StageConfig c = stageConfig(s0, k, dt);
+        for (size_t p = 0; p < np; ++p) {
+            const lfm_solver* s = P->parts[p];
+            lfm::dev::launch_halo_gather<double>(s->q, s->nt, s->nc + s->ng, s->nq, s->nh, P->haloPart[p],
+                                                 P->haloCell[p], P->dQ, P->dNt, P->stream);
+        }
+        for (int w = 0; w < 3; ++w)   // preparation, gradients, viscous terms
+            for (size_t p = 0; p < np; ++p) lfm::dev::launch_kernel<T>(args(p), c, w, P->stream);
+        if (s0->needVis)
+            for (size_t p = 0; p < np; ++p) {
+                const lfm_solver* s = P->parts[p];
+                const int rows = s->D * s->D + 2 * s->D;
+                lfm::dev::launch_halo_gather<T>(args(p).V, s->nt, s->nc + s->ng, rows, s->nh, P->haloPart[p],
+                                                P->haloCell[p], reinterpret_cast<T* const*>(P->dV), P->dNt,
+                                                P->stream);
+            }
+        for (int w = 3; w < 5; ++w)   // fluxes, update
+            for (size_t p = 0; p < np; ++p) lfm::dev::launch_kernel<T>(args(p), c, w, P->stream);
+    }
+}
+
+int partitionedGraph(lfm_partitioned* P, double dt) {
+    if (P->graph && P->graphDt == dt) return LFM_OK;
+    if (P->graph) {
+        cudaGraphExecDestroy(P->graph);
+        P->graph = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    LFM_CUDA(cudaStreamBeginCapture(P->stream, cudaStreamCaptureModeThreadLocal));
+    if (P->precision == LFM_FP32_BULK)
+        partitionedStages<float>(P, dt);
+    else
+        partitionedStages<double>(P, dt);
+    cudaError_t e = cudaStreamEndCapture(P->stream, &g);
+    if (e != cudaSuccess) return cudaFail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&P->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cudaFail(e, "cudaGraphInstantiate");
+    P->graphDt = dt;
+    return LFM_OK;
+}
+
+int checkPart(const lfm_partitioned* P, int part) {
+    if (!P) return lfm::setError(LFM_ERR_INVALID, "null partitioned solver");
+    if (part < 0 || part >= (int)P->parts.size())
+        return lfm::setError(LFM_ERR_INVALID, "no partition " + std::to_string(part));
+    return LFM_OK;
+}
+
+}  // namespace
+
+extern "C" void lfm_partitioned_destroy(lfm_partitioned* P) {
+    if (!P) return;
+    cudaSetDevice(P->device);
+    if (P->stream) cudaStreamSynchronize(P->stream);
+    if (P->graph) cudaGraphExecDestroy(P->graph);
+    for (lfm_solver* s : P->parts) lfm_solver_destroy(s);
+    for (int* p : P->haloPart) cudaFree(p);
+    for (int* p : P->haloCell) cudaFree(p);
+    cudaFree(P->dQ);
+    cudaFree(P->dV);
+    cudaFree(P->dNt);
+    if (P->stream) cudaStreamDestroy(P->stream);
+    delete P;
+}
+
+extern "C" int lfm_partitioned_create(const lfm_solver_desc* const* descs, int nparts, const lfm_solver_opts* opts,
+                                      lfm_partitioned** out) {
+    if (!descs || !out || nparts < 1) return lfm::setError(LFM_ERR_INVALID, "lfm_partitioned_create: bad argument");
+    *out = nullptr;
+    for (int p = 0; p < nparts; ++p) {
+        int rc = lfm::setup::validateDesc(descs[p]);
+        if (rc) return rc;
+        const lfm_solver_desc* d = descs[p];
+        const lfm_solver_desc* d0 = descs[0];
+        if (d->dim != d0->dim || d->solver != d0->solver || d->rk_order != d0->rk_order || d->mu != d0->mu ||
+            d->minmod != d0->minmod)
+            return lfm::setError(LFM_ERR_INVALID, "partitions of one case must share dim, scheme, rk_order and mu");
+        for (int64_t h = 0; h < d->n_halos; ++h) {
+            const int64_t q = d->halo_src_part[h];
+            if (q < 0 || q >= nparts || d->halo_src_cell[h] < 0 || d->halo_src_cell[h] >= descs[q]->n_cells)
+                return lfm::setError(LFM_ERR_INVALID, "halo " + std::to_string(h) + " of partition " +
+                                                          std::to_string(p) + " has no valid source cell");
+        }
+    }
+    lfm_partitioned* P = new lfm_partitioned;
+    P->device = opts ? opts->device : 0;
+    P->precision = opts ? opts->precision : LFM_FP64;
+    auto fail = [&](int rc) {
+        lfm_partitioned_destroy(P);
+        return rc;
+    };
+    cudaError_t e = cudaSetDevice(P->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return fail(cudaFail(e, "partitioned stream"));
+    for (int p = 0; p < nparts; ++p) {
+        lfm_solver* s = nullptr;
+        int rc = createSolver(descs[p], opts, P->stream, &s);
+        if (rc) return fail(rc);
+        P->parts.push_back(s);
+        std::vector<int> hp((size_t)s->nh), hc((size_t)s->nh);
+        for (int h = 0; h < s->nh; ++h) {
+            hp[(size_t)h] = (int)descs[p]->halo_src_part[h];
+            hc[(size_t)h] = (int)descs[p]->halo_src_cell[h];
+        }
+        int *dp = nullptr, *dc = nullptr;
+        const size_t n = std::max<size_t>(1, hp.size());
+        if ((e = cudaMalloc(&dp, n * sizeof(int))) != cudaSuccess || (e = cudaMalloc(&dc, n * sizeof(int))) != cudaSuccess)
+            return fail(cudaFail(e, "halo lists"));
+        P->haloPart.push_back(dp);
+        P->haloCell.push_back(dc);
+        if (!hp.empty() &&
+            ((e = cudaMemcpy(dp, hp.data(), hp.size() * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess ||
+             (e = cudaMemcpy(dc, hc.data(), hc.size() * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess))
+            return fail(cudaFail(e, "halo lists"));
+    }
+    std::vector<double*> q((size_t)nparts);
+    std::vector<void*> v((size_t)nparts);
+    std::vector<int> nt((size_t)nparts);
+    for (int p = 0; p < nparts; ++p) {
+        const lfm_solver* s = P->parts[(size_t)p];
+        q[(size_t)p] = s->q;
+        v[(size_t)p] = P->precision == LFM_FP32_BULK ? (void*)s->a32.V : (void*)s->a64.V;
+        nt[(size_t)p] = s->nt;
+    }
+    if ((e = cudaMalloc(&P->dQ, nparts * sizeof(double*))) != cudaSuccess ||
+        (e = cudaMalloc(&P->dV, nparts * sizeof(void*))) != cudaSuccess ||
+        (e = cudaMalloc(&P->dNt, nparts * sizeof(int))) != cudaSuccess ||
+        (e = cudaMemcpy(P->dQ, q.data(), nparts * sizeof(double*), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(P->dV, v.data(), nparts * sizeof(void*), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(P->dNt, nt.data(), nparts * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return fail(cudaFail(e, "partition tables"));
+    *out = P;
+    return LFM_OK;
+}
+
+extern "C" int lfm_partitioned_set_state(lfm_partitioned* P, int part, const double* q) {
+    int rc = checkPart(P, part);
+    return rc ? rc : lfm_solver_set_state(P->parts[(size_t)part], q);
+}
+
+extern "C" int lfm_partitioned_get_state(lfm_partitioned* P, int part, double* q) {
+    int rc = checkPart(P, part);
+    return rc ? rc : lfm_solver_get_state(P->parts[(size_t)part], q);
+}
+
+extern "C" int lfm_partitioned_step(lfm_partitioned* P, int nsteps, double dt) {
+    if (!P || nsteps < 0) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    if (nsteps == 0) return LFM_OK;
+    LFM_CUDA(cudaSetDevice(P->device));
+    int rc = partitionedGraph(P, dt);
+    if (rc) return rc;
+    for (lfm_solver* s : P->parts)
+        if ((rc = ensurePrims(s))) return rc;
+    for (int k = 0; k < nsteps; ++k) LFM_CUDA(cudaGraphLaunch(P->graph, P->stream));
+    return LFM_OK;
+}
+
+extern "C" int lfm_partitioned_sync(lfm_partitioned* P) {
+    if (!P) return lfm::setError(LFM_ERR_INVALID, "null partitioned solver");
+    for (lfm_solver* s : P->parts) {
+        int rc = lfm_solver_sync(s);
+        if (rc) return rc;
+    }
     return LFM_OK;
 }

@@ -125,13 +125,13 @@ __device__ __forceinline__ void ghost_bc(const Args<T>& a, int g, const double* 
     }
 }
 
-// Conservative state of cell or ghost t in FP64 (FP64 path: q holds the
+// Conservative state of cell, ghost or halo t in FP64 (FP64 path: q holds the
 // state itself). A ghost's state is computed from its interior cell and
-// stored into q.
+// stored into q; a halo's was copied in from its partition.
 template <typename T, int D>
 __device__ __forceinline__ void stage_state(const Args<T>& a, int t, double* qv) {
     constexpr int NQ = D + 2;
-    if (t < a.nc) {
+    if (t < a.nc || t >= a.nc + a.ng) {
 #pragma unroll
         for (int v = 0; v < NQ; ++v) qv[v] = a.q[(size_t)v * a.nt + t];
         return;

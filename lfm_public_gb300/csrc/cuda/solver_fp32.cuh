@@ -90,15 +90,15 @@ __device__ __forceinline__ void prims32(const Args<float>& a, int t, const doubl
 }
 
 // ---------------------------------------------------------------------------
-// prep32: primitives of cell t from the stored perturbation state, or, for a
-// ghost, its boundary state (FP64, from the interior cell) and primitives.
+// prep32: primitives of cell or halo t from the stored perturbation state, or,
+// for a ghost, its boundary state (FP64, from the interior cell) and primitives.
 // ---------------------------------------------------------------------------
 template <int D>
 __device__ __forceinline__ void prep32(const Args<float>& a, int t) {
     constexpr int NQ = D + 2;
     using P = PRow<D>;
     const size_t nt = (size_t)a.nt;
-    if (t < a.nc) {
+    if (t < a.nc || t >= a.nc + a.ng) {
         double qp[NQ];
 #pragma unroll
         for (int v = 0; v < NQ; ++v) qp[v] = a.q[(size_t)v * nt + t];

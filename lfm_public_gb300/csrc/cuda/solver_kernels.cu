@@ -551,5 +551,33 @@ void launch_offset_rows(double* dst, int64_t dstStride, const double* src, int64
     if (n > 0) k_offset_rows<<<blocks(n, 256), 256, 0, st>>>(dst, dstStride, src, srcStride, n, nq, off, sign);
 }
 
+// Halo copies between the partitions of a decomposed case: halo slot h (index
+// first + h of the destination) takes `rows` values of cell srcCell[h] of
+// partition srcPart[h] -- the on-device form of the reference's MPI halo
+// exchange (src/cfd_v0.cpp:3283-3374, 3607-3692).
+template <typename X>
+__global__ void __launch_bounds__(256) k_halo_gather(X* dst, int dstNt, int first, int rows, int nh,
+                                                     const int* srcPart, const int* srcCell, X* const* srcBase,
+                                                     const int* srcNt) {
+    const int h = LFM_GLOBAL_ID();
+    if (h >= nh) return;
+    const int p = srcPart[h], c = srcCell[h];
+    const X* src = srcBase[p];
+    const size_t snt = (size_t)srcNt[p];
+    for (int r = 0; r < rows; ++r) dst[(size_t)r * dstNt + first + h] = src[(size_t)r * snt + c];
+}
+
+template <typename X>
+void launch_halo_gather(X* dst, int dstNt, int first, int rows, int nh, const int* srcPart, const int* srcCell,
+                        X* const* srcBase, const int* srcNt, cudaStream_t st) {
+    if (nh > 0)
+        k_halo_gather<X><<<blocks(nh, 256), 256, 0, st>>>(dst, dstNt, first, rows, nh, srcPart, srcCell, srcBase,
+                                                          srcNt);
+}
+template void launch_halo_gather<double>(double*, int, int, int, int, const int*, const int*, double* const*,
+                                         const int*, cudaStream_t);
+template void launch_halo_gather<float>(float*, int, int, int, int, const int*, const int*, float* const*,
+                                        const int*, cudaStream_t);
+
 }  // namespace dev
 }  // namespace lfm

@@ -52,7 +52,8 @@ struct RefState32 {
 template <typename T>
 struct Args {
     int D, nq;
-    int nc, ng, nf, nt;       // cells, ghosts, flux faces, cells + ghosts
+    int nc, ng, nf, nt;       // cells, ghosts, flux faces, cells + ghosts + halos
+    int nh;                   // processor-face halos (after the ghosts; filled by copies)
     // state (FP64 RK registers)
     double* q;                // nq x nt
     double* dq;               // nq x nc

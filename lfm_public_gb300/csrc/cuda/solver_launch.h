@@ -56,6 +56,11 @@ void launch_set_flag(int* flag, int v, cudaStream_t st);
 // dst[v][c] = src[v][c] + sign * off.v[v], v < nq, c < n (row strides in elements).
 void launch_offset_rows(double* dst, int64_t dstStride, const double* src, int64_t srcStride, int n, int nq,
                         QOffset off, double sign, cudaStream_t st);
+// Halo slots [first, first + nh) of dst (row stride dstNt) take `rows` values
+// of cell srcCell[h] of partition srcPart[h] (base srcBase[p], stride srcNt[p]).
+template <typename X>
+void launch_halo_gather(X* dst, int dstNt, int first, int rows, int nh, const int* srcPart, const int* srcCell,
+                        X* const* srcBase, const int* srcNt, cudaStream_t st);
 
 constexpr int kKernelsPerStage = 5;  // prep, grad, vis, flux, update
 inline const char* kernelName(int i) {

@@ -1,9 +1,13 @@
 // C ABI, case half: case input and the flattened solver description
 // (declarations and the reference interfaces they replace: include/lfm_gpu.h).
+#include <array>
 #include <cstring>
 #include <exception>
+#include <map>
 #include <memory>
 #include <string>
+#include <tuple>
+#include <vector>
 
 #include "capi_internal.h"
 #include "case_setup.h"
@@ -193,3 +197,117 @@ extern "C" int lfm_case_cell_ids(const lfm_case* c, int64_t* out) {
 }
 
 extern "C" void lfm_case_free(lfm_case* c) { delete c; }
+
+// ---- decomposed cases: all processor partitions of a case at once ----------
+
+struct lfm_pcase {
+    std::vector<lfm::SolverCase> parts;
+    double deltaT = 0, startTime = 0, endTime = 0, maxCo = 1;
+    bool adjust = false;
+};
+
+namespace {
+
+// Offsets (cell centre - face centre) of the processor faces of every
+// partition, keyed by (partition, partition across, face id): what each rank
+// of the reference sends its neighbours (src/mesh_reader.cpp:520-552).
+class OffsetTable : public lfm::HaloLookup {
+public:
+    std::map<std::tuple<int, int, int64_t>, std::array<double, 3>> offsets;
+    int self = 0;
+    bool neighbourOffset(int nbr, int64_t faceId, double* x) const override {
+        auto it = offsets.find(std::make_tuple(nbr, self, faceId));
+        if (it == offsets.end()) return false;
+        for (int k = 0; k < 3; ++k) x[k] = it->second[(size_t)k];
+        return true;
+    }
+};
+
+}  // namespace
+
+extern "C" int lfm_pcase_open(const char* root, int nparts, lfm_pcase** out) {
+    if (!root || !out || nparts < 1) return lfm::setError(LFM_ERR_INVALID, "lfm_pcase_open: bad argument");
+    *out = nullptr;
+    try {
+        CInputReader in;
+        in.readCase(root);
+        lfm::CaseParams prm = paramsFromInput(in);
+        int rc = validateParams(prm);
+        if (rc) return rc;
+        std::vector<std::unique_ptr<lfm::FoamTime>> rts;
+        std::vector<std::unique_ptr<CPolyMeshReaderOF>> readers;
+        OffsetTable table;
+        for (int p = 0; p < nparts; ++p) {
+            rts.emplace_back(lfm::newFoamTime(root, "processor" + std::to_string(p)));
+            readers.emplace_back(new CPolyMeshReaderOF(rts.back().get()));
+            CPolyMeshReaderOF& r = *readers.back();
+            for (int b = 0; b < r.getBoundaryCount(); ++b) {
+                const int q = r.getBoundaryProcessorRank(b);
+                if (q < 0) continue;
+                for (int f = r.getBoundaryFaceStart(b); f <= r.getBoundaryFaceEnd(b); ++f) {
+                    double xc[3], xf[3];
+                    r.getCellCenter(r.getFaceOwner(f), xc);
+                    r.getFaceCenter(f, xf);
+                    table.offsets[std::make_tuple(p, q, (int64_t)r.getFaceId(f))] = {xc[0] - xf[0], xc[1] - xf[1],
+                                                                                      xc[2] - xf[2]};
+                }
+            }
+        }
+        std::unique_ptr<lfm_pcase> pc(new lfm_pcase);
+        for (int p = 0; p < nparts; ++p) {
+            table.self = p;
+            pc->parts.push_back(lfm::buildSolverCase(*readers[(size_t)p], prm, &table));
+            lfm::SolverCase& sc = pc->parts.back();
+            sc.cellGlobal.resize(sc.cellId.size());
+            for (size_t c = 0; c < sc.cellId.size(); ++c)
+                sc.cellGlobal[c] = readers[(size_t)p]->getCellProcAddressing((int)sc.cellId[c]);
+        }
+        lfm::resolveHalos(pc->parts);
+        pc->deltaT = rts[0]->deltaT;
+        pc->startTime = rts[0]->startTime;
+        pc->endTime = rts[0]->endTime;
+        pc->adjust = rts[0]->adjustTimeStep;
+        pc->maxCo = in.m_dCFLMax;
+        readers.clear();
+        *out = pc.release();
+        return LFM_OK;
+    } catch (const lfm::foam::FoamError& e) {
+        return lfm::setError(LFM_ERR_IO, e.what());
+    } catch (const std::exception& e) {
+        return lfm::setError(LFM_ERR_INVALID, e.what());
+    }
+}
+
+extern "C" int lfm_pcase_parts(const lfm_pcase* pc, int* nparts) {
+    if (!pc || !nparts) return lfm::setError(LFM_ERR_INVALID, "lfm_pcase_parts: null argument");
+    *nparts = (int)pc->parts.size();
+    return LFM_OK;
+}
+
+extern "C" int lfm_pcase_describe(const lfm_pcase* pc, int part, lfm_solver_desc* d) {
+    if (!pc || !d || part < 0 || part >= (int)pc->parts.size())
+        return lfm::setError(LFM_ERR_INVALID, "lfm_pcase_describe: bad argument");
+    lfm::describeSolverCase(pc->parts[(size_t)part], d);
+    return LFM_OK;
+}
+
+extern "C" int lfm_pcase_cell_global(const lfm_pcase* pc, int part, int64_t* out) {
+    if (!pc || !out || part < 0 || part >= (int)pc->parts.size())
+        return lfm::setError(LFM_ERR_INVALID, "lfm_pcase_cell_global: bad argument");
+    const lfm::SolverCase& sc = pc->parts[(size_t)part];
+    std::memcpy(out, sc.cellGlobal.data(), sc.cellGlobal.size() * sizeof(int64_t));
+    return LFM_OK;
+}
+
+extern "C" int lfm_pcase_time(const lfm_pcase* pc, double* delta_t, double* start_time, double* end_time,
+                              int* adjust_time_step, double* max_co) {
+    if (!pc) return lfm::setError(LFM_ERR_INVALID, "lfm_pcase_time: null case");
+    if (delta_t) *delta_t = pc->deltaT;
+    if (start_time) *start_time = pc->startTime;
+    if (end_time) *end_time = pc->endTime;
+    if (adjust_time_step) *adjust_time_step = pc->adjust ? 1 : 0;
+    if (max_co) *max_co = pc->maxCo;
+    return LFM_OK;
+}
+
+extern "C" void lfm_pcase_free(lfm_pcase* pc) { delete pc; }

@@ -45,18 +45,20 @@ namespace {
 
 struct Slot {            // one valid face of a cell, as the reference stores it
     int64_t face;        // polyMesh face label
-    int nbType;          // 0 regular / submesh cell, 1 boundary ghost, 2 processor (unsupported)
+    int nbType;          // 0 regular / submesh cell, 1 boundary ghost, 2 processor halo
     int64_t nbSolver;    // solver index of the neighbour cell (nbType 0)
     int nbSm;            // neighbour submesh (nbType 0)
     int64_t nbLocal;     // neighbour index inside its submesh (nbType 0)
     int bound;           // patch of a boundary face
+    int nbProc;          // neighbouring partition (nbType 2)
+    int64_t faceId;      // global face id (nbType 2)
     double S[3], d[3], w;
     bool owned;
 };
 
 }  // namespace
 
-SolverCase buildSolverCase(IMeshReader& r, const CaseParams& prm) {
+SolverCase buildSolverCase(IMeshReader& r, const CaseParams& prm, const HaloLookup* halos) {
     const int D = prm.dimension;
     if (D != 2 && D != 3) throw std::runtime_error("invalid dimension " + std::to_string(D));
     SolverCase sc;
@@ -114,7 +116,12 @@ SolverCase buildSolverCase(IMeshReader& r, const CaseParams& prm) {
             } else if (r.getBoundaryProcessorRank(sl.bound) == -1) {
                 sl.nbType = 1;
             } else {
-                throw std::runtime_error("processor patches are not supported: one case is one partition");
+                if (!halos)
+                    throw std::runtime_error("a processor patch needs its neighbouring partitions: open the "
+                                             "decomposed case as a whole");
+                sl.nbType = 2;
+                sl.nbProc = r.getBoundaryProcessorRank(sl.bound);
+                sl.faceId = r.getFaceId(f);
             }
             const double sign = (own == cell) ? 1.0 : -1.0;
             double an[3], xf[3];
@@ -123,7 +130,16 @@ SolverCase buildSolverCase(IMeshReader& r, const CaseParams& prm) {
             for (int dd = 0; dd < D; ++dd) sl.S[dd] = sign * an[dd];
             double dP[3];
             for (int dd = 0; dd < D; ++dd) dP[dd] = xc[dd] - xf[dd];
-            if (sl.nbType == 1) {
+            if (sl.nbType == 2) {
+                // neighbour centre from the other partition: its cell centre
+                // relative to its face centre, plus this face's centre
+                // relative to this cell (src/mesh_reader.cpp:548-601)
+                double x[3] = {0, 0, 0};
+                if (!halos->neighbourOffset(sl.nbProc, sl.faceId, x))
+                    throw std::runtime_error("processor face " + std::to_string(sl.faceId) +
+                                             " has no partner in partition " + std::to_string(sl.nbProc));
+                for (int dd = 0; dd < D; ++dd) sl.d[dd] = sign * (x[dd] + xf[dd] - xc[dd]);
+            } else if (sl.nbType == 1) {
                 double smag2 = 0.0, dps = 0.0;
                 for (int dd = 0; dd < D; ++dd) smag2 += sl.S[dd] * sl.S[dd];
                 for (int dd = 0; dd < D; ++dd) dps += dP[dd] * sl.S[dd];
@@ -152,8 +168,9 @@ SolverCase buildSolverCase(IMeshReader& r, const CaseParams& prm) {
                 wden += (-sl.S[dd] * dP[dd] + sl.S[dd] * dN[dd]);
             }
             sl.w = wnum / wden;
-            // Ownership (src/cfd_v0.cpp:295-305): ghosts rank above every cell.
-            if (sl.nbType == 1) {
+            // Ownership (src/cfd_v0.cpp:295-305): boundary ghosts and MPI halos
+            // rank above every cell (sm_id = MAX_MPI_RANKS, :428, :514).
+            if (sl.nbType != 0) {
                 sl.owned = true;
             } else {
                 const int mySm = (int)smOf[(size_t)cell];
@@ -206,7 +223,14 @@ SolverCase buildSolverCase(IMeshReader& r, const CaseParams& prm) {
         for (const Slot& sl : slots[(size_t)ci]) {
             if (!sl.owned) continue;
             sc.faceP[(size_t)fi] = ci;
-            if (sl.nbType == 1) {
+            if (sl.nbType == 2) {
+                // halos follow the ghosts: N fixed up once the ghosts are counted
+                sc.faceN[(size_t)fi] = -1 - (int64_t)sc.haloFace.size();
+                sc.haloFace.push_back(fi);
+                sc.haloProc.push_back(sl.nbProc);
+                sc.haloFaceId.push_back(sl.faceId);
+                sc.haloCell.push_back(ci);
+            } else if (sl.nbType == 1) {
                 const int64_t g = (int64_t)sc.ghostCell.size();
                 sc.ghostCell.push_back(ci);
                 sc.ghostKind.push_back(patchKind[(size_t)sl.bound]);
@@ -246,6 +270,8 @@ SolverCase buildSolverCase(IMeshReader& r, const CaseParams& prm) {
         }
     }
     sc.nGhosts = (int64_t)sc.ghostCell.size();
+    sc.nHalos = (int64_t)sc.haloFace.size();
+    for (int64_t h = 0; h < sc.nHalos; ++h) sc.faceN[(size_t)sc.haloFace[(size_t)h]] = nc + sc.nGhosts + h;
 
     // -- cell -> face incidence (ascending face index) --------------------------
     std::vector<int64_t> cnt((size_t)nc, 0);
@@ -342,6 +368,31 @@ SolverCase buildSolverCase(IMeshReader& r, const CaseParams& prm) {
 }
 
 
+void resolveHalos(std::vector<SolverCase>& parts) {
+    // (partition across, face id) -> halo index, per partition
+    std::vector<std::map<std::pair<int, int64_t>, int64_t>> index(parts.size());
+    for (size_t p = 0; p < parts.size(); ++p)
+        for (int64_t h = 0; h < parts[p].nHalos; ++h)
+            index[p][{parts[p].haloProc[(size_t)h], parts[p].haloFaceId[(size_t)h]}] = h;
+    for (size_t p = 0; p < parts.size(); ++p) {
+        SolverCase& sc = parts[p];
+        sc.haloSrcPart.assign((size_t)sc.nHalos, -1);
+        sc.haloSrcCell.assign((size_t)sc.nHalos, -1);
+        for (int64_t h = 0; h < sc.nHalos; ++h) {
+            const int q = sc.haloProc[(size_t)h];
+            if (q < 0 || q >= (int)parts.size())
+                throw std::runtime_error("processor patch refers to partition " + std::to_string(q) + " of " +
+                                         std::to_string(parts.size()));
+            auto it = index[(size_t)q].find({(int)p, sc.haloFaceId[(size_t)h]});
+            if (it == index[(size_t)q].end())
+                throw std::runtime_error("processor face " + std::to_string(sc.haloFaceId[(size_t)h]) + " of partition " +
+                                         std::to_string(p) + " has no partner in partition " + std::to_string(q));
+            sc.haloSrcPart[(size_t)h] = q;
+            sc.haloSrcCell[(size_t)h] = parts[(size_t)q].haloCell[(size_t)it->second];
+        }
+    }
+}
+
 void describeSolverCase(const SolverCase& s, lfm_solver_desc* d) {
     std::memset(d, 0, sizeof(*d));
     d->dim = s.dim;
@@ -387,6 +438,9 @@ void describeSolverCase(const SolverCase& s, lfm_solver_desc* d) {
     d->PrInv = s.PrInv;
     d->rkA = s.rkA.data();
     d->rkB = s.rkB.data();
-    }
+    d->n_halos = s.nHalos;
+    d->halo_src_part = s.haloSrcPart.empty() ? nullptr : s.haloSrcPart.data();
+    d->halo_src_cell = s.haloSrcCell.empty() ? nullptr : s.haloSrcCell.data();
+}
 
 }  // namespace lfm

@@ -39,12 +39,23 @@ struct CaseParams {
     double Cp = 0, molWeight = 0, mu = 0, Pr = 1;
 };
 
+// Other side of a processor face, for a partition built alongside its
+// neighbours (the reference exchanges these over MPI, src/mesh_reader.cpp:481-611):
+// the neighbour's cell centre relative to its face centre, keyed by the
+// face's global id (getFaceId).
+class HaloLookup {
+public:
+    virtual ~HaloLookup() = default;
+    virtual bool neighbourOffset(int nbrProc, int64_t faceId, double* x) const = 0;
+};
+
 struct SolverCase {
     int dim = 2;
     int nq = 4;                  // dim + 2 conserved variables
     int64_t nCells = 0;          // interior cells, submesh 0 first then submesh 1
     int64_t nCells0 = 0;         // cells of submesh 0
     int64_t nGhosts = 0;         // boundary ghosts, stored after the cells
+    int64_t nHalos = 0;          // processor-face halos, stored after the ghosts
     int64_t nFaces = 0;          // flux faces, in the reference's processing order
     int maxFacesPerCell = 0;
 
@@ -59,8 +70,20 @@ struct SolverCase {
     std::vector<int64_t> ghostFace;      // flux face of the ghost
     std::vector<int> ghostPatch;
 
+    // processor-face halos (partitioned cases) ------------------------------------
+    // Halo h is the N side of flux face haloFace[h]: the cell across a processor
+    // patch, owned by partition haloProc[h]; it is matched to that partition's
+    // copy of the face by haloFaceId[h], and its source cell there (solver
+    // order) is filled in by resolveHalos.
+    std::vector<int64_t> haloFace;
+    std::vector<int> haloProc;
+    std::vector<int64_t> haloFaceId;
+    std::vector<int64_t> haloCell;       // the local cell P of the face
+    std::vector<int64_t> haloSrcPart, haloSrcCell;
+    std::vector<int64_t> cellGlobal;     // cellProcAddressing of each solver cell (partitioned cases)
+
     // flux faces (owner side = reference processing side) ------------------------
-    std::vector<int64_t> faceP, faceN;   // N >= nCells: ghost N - nCells
+    std::vector<int64_t> faceP, faceN;   // N >= nCells: ghost N - nCells, halo N - nCells - nGhosts
     std::vector<uint8_t> faceGhost;      // neighbour is a boundary ghost
     std::vector<double> S, d;            // dim x nFaces (SoA)
     std::vector<double> w;               // linear weight of P
@@ -87,7 +110,12 @@ struct SolverCase {
 
 // Builds the case from a mesh reader that already holds the fields p, T, U and
 // (when Ls > 0) alpha at the start time. Throws std::runtime_error on bad input.
-SolverCase buildSolverCase(IMeshReader& reader, const CaseParams& params);
+// Processor patches need `halos` (the neighbouring partitions' geometry).
+SolverCase buildSolverCase(IMeshReader& reader, const CaseParams& params, const HaloLookup* halos = nullptr);
+
+// Matches every halo of every partition to its source cell in the partition
+// across the processor face (by face id). Throws when a face has no partner.
+void resolveHalos(std::vector<SolverCase>& parts);
 
 // Fills the flattened C description with pointers into `sc` (valid while sc lives).
 void describeSolverCase(const SolverCase& sc, lfm_solver_desc* out);

@@ -17,8 +17,8 @@ workload on the host cores (the oracle port: one process per core, each on
 the full mesh, aggregate throughput).
 
 The default precision is the FP32-bulk form (FP32 fluxes, limiter and
-residual sums on perturbations from the free stream; FP64 RK registers,
-ghost states and geometry). The same run also times the plain FP64 path
+residual sums and the RK increment register on perturbations from the free
+stream; FP64 accumulation of the conserved state, ghost states and geometry). The same run also times the plain FP64 path
 (``plain_fp64``: value and speed-up) and states the acoustic-pressure error of
 the FP32-bulk state against the FP64 state after --accuracy-steps time steps
 (``accuracy``: over all cells and on 72 probes at r = 50 D).
@@ -54,7 +54,7 @@ def workload(name: str):
     if name == "cylinder2d_m2":
         return cases.cylinder_case(n_theta=768, n_r=512, solver=1, minmod=True)
     if name == "cylinder2d_fine":
-        return cases.cylinder_case(n_theta=1536, n_r=1024, first=0.001, solver=0, minmod=True)
+        return cases.cylinder_case(n_theta=1536, n_r=1024, first=0.002, solver=0, minmod=True)
     if name == "vortex2d":
         return cases.vortex_case(n=256, solver=0)
     if name == "cylinder3d":
@@ -91,7 +91,10 @@ def kernel_bytes(dim: int, faces_per_cell: int, fp32: bool, scheme: str, viscous
     csr = 4 + 4 * faces_per_cell          # cell -> face offsets and list
     face_basic = 8 + (dim + 1) * w        # fP, fN, S, w
     b = {}
-    b["k_prep"] = nq * 8 + prim * w
+    # FP32-bulk: the update writes the next stage's primitives of its cell and
+    # of its boundary ghosts, so the preparation pass only covers processor
+    # halos (none in a single-partition case)
+    b["k_prep"] = 0.0 if fp32 else nq * 8 + prim * w
     b["k_grad"] = (prim * w + fpc * face_basic + csr + ng * w) if scheme == "M2AUSM" else 0.0
     b["k_vis"] = ((dim + 1) * w + fpc * face_basic + csr + nv * w) if (viscous or scheme == "M2AUSM") else 0.0
     flux_cell = (prim - 1) * w + (0 if fp32 else nq * 8)   # FP64 also reads q
@@ -101,7 +104,10 @@ def kernel_bytes(dim: int, faces_per_cell: int, fp32: bool, scheme: str, viscous
         flux_cell += ng * w + w
     flux_face = face_basic + 1 + nq * w + ((dim + 1) * w if viscous else 0) + (dim * w if scheme == "M2AUSM" else 0)
     b["k_flux"] = flux_cell + fpc * flux_face
-    b["k_update"] = csr + fpc * nq * w + 4 * nq * 8 + 16
+    if fp32:   # q' read + written (FP64), dq read + written (FP32), 1/V, sigma, primitives out
+        b["k_update"] = csr + fpc * nq * w + 2 * nq * 8 + 2 * nq * 4 + 8 + prim * 4
+    else:      # q and dq read + written, 1/V, sigma
+        b["k_update"] = csr + fpc * nq * w + 4 * nq * 8 + 16
     return b
 
 

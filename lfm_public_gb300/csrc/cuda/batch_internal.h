@@ -87,7 +87,7 @@ struct CaseLayout {
         const size_t nt = nc + ng, nf = (size_t)d->n_faces, ne = (size_t)d->cell_face_offsets[nc];
         const bool ausm = d->solver == LFM_SOLVER_M2AUSM;
         q = add(nq * nt * 8);
-        dq = add(nq * nc * 8);
+        dq = add(nq * nc * 4);
         res = d->residuals ? add(nq * nc * 8) : npos();
         prim = add((size_t)lfm::dev::primRows<float>(d->dim) * nt * 4);
         V = lfm::setup::needVis(d) ? add((D * D + 2 * D) * nt * 4) : npos();
@@ -105,7 +105,7 @@ struct CaseLayout {
         fGhost = add(nf);
         volInv = add(nc * 8);
         volInv32 = add(nc * 4);
-        sponge = add(nc * 8);
+        sponge = add(nc * 4);
         cfOff = add((nc + 1) * 4);
         cfList = add(ne * 4);
         gCell = add(ng * 4);

@@ -79,7 +79,7 @@ std::vector<unsigned char> packCase(const lfm_solver_desc* d, const CaseLayout& 
     std::memcpy(img.data() + L.fGhost, d->face_ghost, nf);
     std::memcpy(f64(L.volInv), d->vol_inv, nc * 8);
     conv(L.volInv32, d->vol_inv, nc);
-    std::memcpy(f64(L.sponge), d->sponge, nc * 8);
+    conv(L.sponge, d->sponge, nc);
     std::memcpy(i32(L.cfOff), ix.cfOff.data(), (nc + 1) * 4);
     std::memcpy(i32(L.cfList), ix.cfList.data(), ix.cfList.size() * 4);
     if (ng) {
@@ -359,7 +359,7 @@ int commitCase(lfm_batch* b, const PreparedCase& pc, int* slot) {
     Args<float>& a = bc.a;
     auto P = [&](size_t o) -> unsigned char* { return o == CaseLayout::npos() ? nullptr : base + o; };
     a.q = reinterpret_cast<double*>(P(L.q));
-    a.dq = reinterpret_cast<double*>(P(L.dq));
+    a.dq = reinterpret_cast<float*>(P(L.dq));
     a.res = reinterpret_cast<double*>(P(L.res));
     a.prim = reinterpret_cast<float*>(P(L.prim));
     a.V = reinterpret_cast<float*>(P(L.V));
@@ -377,9 +377,10 @@ int commitCase(lfm_batch* b, const PreparedCase& pc, int* slot) {
     a.fGhost = reinterpret_cast<const uint8_t*>(P(L.fGhost));
     a.volInv = reinterpret_cast<const double*>(P(L.volInv));
     a.volInv32 = reinterpret_cast<const float*>(P(L.volInv32));
-    a.sponge = reinterpret_cast<const double*>(P(L.sponge));
+    a.sponge = reinterpret_cast<const float*>(P(L.sponge));
     a.cfOff = reinterpret_cast<const int*>(P(L.cfOff));
     a.cfList = reinterpret_cast<const int*>(P(L.cfList));
+    a.cellGhosts = nullptr;   // the batch's preparation phase writes the ghosts
     a.gCell = reinterpret_cast<const int*>(P(L.gCell));
     a.gKind = reinterpret_cast<const int*>(P(L.gKind));
     a.gFace = reinterpret_cast<const int*>(P(L.gFace));

@@ -113,7 +113,7 @@ std::vector<int> toInt(const int64_t* p, size_t n) {
 template <typename T>
 int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP, const int* fN,
               const uint8_t* fGhost, const int* cfOff, const int* cfList, const int* gCell, const int* gKind,
-              const int* gFace, const double* sponge) {
+              const int* gFace) {
     lfm::setup::setConstants(a, d);
     a.q = s->q;
     a.res = s->res;
@@ -121,13 +121,13 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
     a.fN = fN;
     a.fGhost = fGhost;
     a.volInv = s->volInv;
-    a.sponge = sponge;
     a.cfOff = cfOff;
     a.cfList = cfList;
     a.gCell = gCell;
     a.gKind = gKind;
     a.gFace = gFace;
     a.flag = s->flag;
+    a.cellGhosts = nullptr;
     const size_t nt = (size_t)s->nt, nf = (size_t)s->nf, D = (size_t)s->D;
     int rc;
     if ((rc = devAlloc(s, &a.dq, (size_t)s->nq * s->nc))) return rc;
@@ -154,6 +154,8 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
     a.dmag = p;
     if ((rc = uploadAs<T>(s, &p, d->K, D * nf))) return rc;
     a.K = p;
+    if ((rc = uploadAs<T>(s, &p, d->sponge, (size_t)s->nc))) return rc;
+    a.sponge = p;
     {
         std::vector<double> lapc(nf);
         for (size_t f = 0; f < nf; ++f) lapc[f] = d->delta_mag[f] * d->dmag_inv[f];
@@ -286,8 +288,6 @@ int createSolver(const lfm_solver_desc* d, const lfm_solver_opts* opts, cudaStre
     if ((rc = devAlloc(s, &s->scalar, 16))) return fail(rc);
     if ((rc = devAlloc(s, &s->flag, 1))) return fail(rc);
     if ((rc = upload(s, &s->volInv, d->vol_inv, nc))) return fail(rc);
-    double* sponge = nullptr;
-    if ((rc = upload(s, &sponge, d->sponge, nc))) return fail(rc);
 
     // connectivity as 32-bit indices
     std::vector<int> fP = toInt(d->face_p, nf), fN = toInt(d->face_n, nf);
@@ -314,11 +314,18 @@ int createSolver(const lfm_solver_desc* d, const lfm_solver_opts* opts, cudaStre
     if ((rc = upload(s, &s->sOff, sOff.data(), nc + 1))) return fail(rc);
     if ((rc = upload(s, &s->cellS, d->cell_s, (size_t)d->cell_s_offsets[nc] * (size_t)s->D))) return fail(rc);
     if (s->precision == LFM_FP32_BULK)
-        rc = buildArgs<float>(s, d, s->a32, dP, dN, dG, dOff, dList, dGC, dGK, dGF, sponge);
+        rc = buildArgs<float>(s, d, s->a32, dP, dN, dG, dOff, dList, dGC, dGK, dGF);
     else
-        rc = buildArgs<double>(s, d, s->a64, dP, dN, dG, dOff, dList, dGC, dGK, dGF, sponge);
+        rc = buildArgs<double>(s, d, s->a64, dP, dN, dG, dOff, dList, dGC, dGK, dGF);
     if (rc) return fail(rc);
     if (s->precision == LFM_FP32_BULK) {
+        // cells with boundary faces: their update writes the ghosts' next state
+        std::vector<uint8_t> cg(nc, 0);
+        for (size_t f = 0; f < nf; ++f)
+            if (fN[f] >= s->nc && fN[f] < s->nc + s->ng) cg[(size_t)fP[f]] = 1;
+        uint8_t* dCG = nullptr;
+        if ((rc = upload(s, &dCG, cg.data(), nc))) return fail(rc);
+        s->a32.cellGhosts = dCG;
         for (int v = 0; v < s->nq; ++v) s->qRef[v] = s->a32.qRef[v];
         if ((rc = devAlloc(s, &s->stage, nq * nc))) return fail(rc);
     }

@@ -1,6 +1,7 @@
-// FP32-bulk form of the time step: face fluxes, limiter and residual sums in
-// FP32; the RK registers (q, dq), boundary ghost states, geometry precompute
-// and the dt reduction in FP64.
+// FP32-bulk form of the time step: face fluxes, limiter, residual sums and
+// the RK increment register dq in FP32; the accumulation of the conserved
+// state, boundary ghost states, geometry precompute and the dt reduction in
+// FP64.
 //
 // Perturbation form. The FP64 state is stored as its deviation from a
 // constant reference state q_ref = (rho_inf, rho_inf U_inf, rho_inf E_inf):
@@ -17,8 +18,8 @@
 // here the rounding is ~1e-7 of the perturbation.
 //
 // GB300 runs FP64 instructions (conversions included) at about two per clock
-// per SM, so the FP64 work is kept to the two FMAs per component of the
-// low-storage accumulation: conversions between FP32 and FP64 run on the
+// per SM, so the FP64 work is kept to one FMA per component, the
+// accumulation of the conserved state: conversions between FP32 and FP64 run on the
 // integer pipes (fp_convert.cuh), and the update kernel derives the next
 // stage's primitives from the new state while it holds it in registers
 // (prims32), so a stage reads q' once. The primitive formulas use explicitly
@@ -90,29 +91,19 @@ __device__ __forceinline__ void prims32(const Args<float>& a, int t, const doubl
 }
 
 // ---------------------------------------------------------------------------
-// prep32: primitives of cell or halo t from the stored perturbation state, or,
-// for a ghost, its boundary state (FP64, from the interior cell) and primitives.
+// ghost32: boundary state of ghost g (FP64) from the absolute state qi of its
+// interior cell, and its FP32 primitives. A ghost state can lie far from the
+// free stream (a wall mirrors the momentum, u' = -2 U_inf - u'), where the
+// FP32 kinetic-energy difference of prims32 would cancel; ghosts are few, so
+// theirs is FP64.
 // ---------------------------------------------------------------------------
 template <int D>
-__device__ __forceinline__ void prep32(const Args<float>& a, int t) {
+__device__ __forceinline__ void ghost32(const Args<float>& a, int g, const double* qi) {
     constexpr int NQ = D + 2;
     using P = PRow<D>;
     const size_t nt = (size_t)a.nt;
-    if (t < a.nc || t >= a.nc + a.ng) {
-        double qp[NQ];
-#pragma unroll
-        for (int v = 0; v < NQ; ++v) qp[v] = a.q[(size_t)v * nt + t];
-        prims32<D>(a, t, qp);
-        return;
-    }
-    // A ghost state can lie far from the free stream (a wall mirrors the
-    // momentum, u' = -2 U_inf - u'), where the FP32 kinetic-energy difference
-    // of prims32 would cancel; ghosts are few, so theirs is FP64.
-    const int g = t - a.nc;
-    const int in = a.gCell[g];
-    double qi[NQ], qv[NQ];
-#pragma unroll
-    for (int v = 0; v < NQ; ++v) qi[v] = a.q[(size_t)v * nt + in] + a.qRef[v];
+    const int t = a.nc + g;
+    double qv[NQ];
     ghost_bc<float, D>(a, g, qi, qv);
     const double rinv = 1.0 / qv[0];
     double ke = 0.0;
@@ -130,15 +121,46 @@ __device__ __forceinline__ void prep32(const Args<float>& a, int t) {
 }
 
 // ---------------------------------------------------------------------------
+// prep32: primitives of cell or halo t from the stored perturbation state, or,
+// for a ghost, its boundary state (FP64, from the interior cell) and primitives.
+// ---------------------------------------------------------------------------
+template <int D>
+__device__ __forceinline__ void prep32(const Args<float>& a, int t) {
+    constexpr int NQ = D + 2;
+    using P = PRow<D>;
+    const size_t nt = (size_t)a.nt;
+    if (t < a.nc || t >= a.nc + a.ng) {
+        double qp[NQ];
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) qp[v] = a.q[(size_t)v * nt + t];
+        prims32<D>(a, t, qp);
+        return;
+    }
+    const int g = t - a.nc;
+    const int in = a.gCell[g];
+    double qi[NQ];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) qi[v] = a.q[(size_t)v * nt + in] + a.qRef[v];
+    ghost32<D>(a, g, qi);
+}
+
+// ---------------------------------------------------------------------------
 // update32: gather of the face rhs of cell c in ascending face order (the
 // reference's scatter order; the sum is the cell residual RES), sponge source
 // and low-storage RK update of the FP64 perturbation state
 // (src/cfd_v0.cpp:2800-2822), then the next stage's primitives of the cell.
-// The increment dt/V RES is formed in FP32 (its error is that of the FP32
-// rhs); dq and q' accumulate in FP64. The sponge pulls q towards q_ref:
+// The increment dt/V RES, the sponge source and the RK register
+// dq = A dq + increment are FP32: dq restarts at every step (A = 0 in stage
+// 0) and holds only that step's increments, so its rounding is that of the
+// FP32 rhs it sums. The conserved state accumulates in FP64,
+// q' = q' + B dq (one FP64 FMA per component), so rounding does not build up
+// over the steps. The sponge pulls q towards q_ref:
 // dt sigma (q_ref - q) = -dt sigma q'.
+// GH: the cell also writes the next stage's state of its boundary ghosts
+// (a ghost depends on its interior cell only), so no preparation pass over
+// the ghosts is needed; the values are those prep32 computes.
 // ---------------------------------------------------------------------------
-template <int D, bool RES>
+template <int D, bool RES, bool GH = false>
 __device__ __forceinline__ void update32(const Args<float>& a, int c, double Ak, double Bk, double dt,
                                          float dt32, int first) {
     constexpr int NQ = D + 2;
@@ -158,24 +180,36 @@ __device__ __forceinline__ void update32(const Args<float>& a, int c, double Ak,
         }
     }
     const float dtvi = __fmul_rn(dt32, a.volInv32[c]);
-    const double sg = a.sponge[c];
-    const double dts = sg != 0.0 ? -dt * sg : 0.0;
+    const float sg = a.sponge[c];
+    const float dts = -__fmul_rn(dt32, sg);
+    const float A32 = __double2float_rn(Ak);
     double qn[NQ];
     bool finite = true;
 #pragma unroll
     for (int v = 0; v < NQ; ++v) {
-        const double inc = f32_to_f64(__fmul_rn(dtvi, sum[v]));
-        double acc = first ? inc : fma(Ak, a.dq[v * nc + c], inc);
+        const float inc = __fmul_rn(dtvi, sum[v]);
+        float acc = first ? inc : __fmaf_rn(A32, a.dq[v * nc + c], inc);
         const double qp = a.q[v * nt + c];
-        if (sg != 0.0) acc = fma(dts, qp, acc);
+        if (sg != 0.0f) acc = __fmaf_rn(dts, f64_to_f32(qp), acc);
         a.dq[v * nc + c] = acc;
-        qn[v] = fma(Bk, acc, qp);
+        qn[v] = fma(Bk, f32_to_f64(acc), qp);
         a.q[v * nt + c] = qn[v];
         finite = finite && isfinite(sum[v]);
         if (RES) a.res[v * nc + c] = f32_to_f64(sum[v]);
     }
     if (!finite) atomicOr(a.flag, 1);
     prims32<D>(a, c, qn);
+    if (GH && a.cellGhosts[c]) {
+        double qa[NQ];
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) qa[v] = qn[v] + a.qRef[v];
+        for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
+            const int code = a.cfList[e];
+            if (code < 0) continue;
+            const int j = a.fN[code];
+            if (j >= a.nc && j < a.nc + a.ng) ghost32<D>(a, j - a.nc, qa);
+        }
+    }
 }
 
 // Perturbation state q' = q - q_ref of cells [0, n) from a caller's absolute

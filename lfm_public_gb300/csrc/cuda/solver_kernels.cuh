@@ -56,7 +56,8 @@ struct Args {
     int nh;                   // processor-face halos (after the ghosts; filled by copies)
     // state (FP64 RK registers)
     double* q;                // nq x nt
-    double* dq;               // nq x nc
+    T* dq;                    // nq x nc RK register: FP64, or FP32 in the FP32-bulk form
+                              // (it holds one step's increments and restarts every step)
     // per cell + ghost, computed every stage
     T* prim;                  // FP64: (D + 3) x nt: 1/rho, u[D], R psi, c
                               // FP32: (2D + 3) x nt: rho', m'[D], u'[D], R psi', c
@@ -80,9 +81,11 @@ struct Args {
     // cells
     const double* volInv;
     const float* volInv32;    // FP32 copy (FP32-bulk gradient kernels)
-    const double* sponge;
+    const T* sponge;          // sponge coefficient sigma per cell
     const int* cfOff;         // nc + 1
     const int* cfList;        // face index, negative (~f) when the cell is N
+    const uint8_t* cellGhosts;  // FP32-bulk single case: boundary faces of each cell
+                                // (its update writes their ghosts' primitives), or null
     // ghosts
     const int* gCell;
     const int* gKind;

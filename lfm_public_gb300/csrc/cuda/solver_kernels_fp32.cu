@@ -7,8 +7,9 @@
 namespace lfm {
 namespace dev {
 
-// Primitives of cells and ghosts [first, a.nt): first = 0 after a new state,
-// first = nc (ghosts only) once the update kernels keep the cells' current.
+// Primitives of cells, ghosts and halos [first, a.nt): first = 0 after a new
+// state; once the update kernels keep the cells' current, first = nc (ghosts
+// and halos), or nc + ng (halos only) when the update also writes the ghosts.
 template <int D>
 __global__ void __launch_bounds__(256) k_prep32(const __grid_constant__ Args<float> a, int first) {
     const int t = first + LFM_GLOBAL_ID();
@@ -33,11 +34,11 @@ __global__ void __launch_bounds__(256) k_flux32(const __grid_constant__ Args<flo
     if (f < a.nf) flux32<D, SCH>(a, f);
 }
 
-template <int D, bool RES>
+template <int D, bool RES, bool GH>
 __global__ void __launch_bounds__(256) k_update32(const __grid_constant__ Args<float> a, double Ak, double Bk,
                                                   double dt, float dt32, int first) {
     const int c = LFM_GLOBAL_ID();
-    if (c < a.nc) update32<D, RES>(a, c, Ak, Bk, dt, dt32, first);
+    if (c < a.nc) update32<D, RES, GH>(a, c, Ak, Bk, dt, dt32, first);
 }
 
 template <int D>
@@ -56,7 +57,7 @@ template <int D>
 void launch_fp32(const Args<float>& a, const StageConfig& s, int which, cudaStream_t st) {
     switch (which) {
         case 0: {
-            const int first = s.fullPrep ? 0 : a.nc;
+            const int first = s.fullPrep ? 0 : (a.cellGhosts ? a.nc + a.ng : a.nc);
             if (a.nt > first) k_prep32<D><<<nblocks(a.nt - first, 256), 256, 0, st>>>(a, first);
             break;
         }
@@ -71,12 +72,18 @@ void launch_fp32(const Args<float>& a, const StageConfig& s, int which, cudaStre
             else if (s.scheme == kSchemeM2) k_flux32<D, kSchemeM2><<<nblocks(a.nf, 256), 256, 0, st>>>(a);
             else k_flux32<D, kSchemeAUSM><<<nblocks(a.nf, 256), 256, 0, st>>>(a);
             break;
-        case 4:
-            if (s.withRes)
-                k_update32<D, true><<<nblocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, (float)s.dt, s.first);
-            else
-                k_update32<D, false><<<nblocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, (float)s.dt, s.first);
+        case 4: {
+            const unsigned nb = nblocks(a.nc, 256);
+            const float dt32 = (float)s.dt;
+            if (a.cellGhosts) {
+                if (s.withRes) k_update32<D, true, true><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, dt32, s.first);
+                else k_update32<D, false, true><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, dt32, s.first);
+            } else {
+                if (s.withRes) k_update32<D, true, false><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, dt32, s.first);
+                else k_update32<D, false, false><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, dt32, s.first);
+            }
             break;
+        }
         default: break;
     }
 }

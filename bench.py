@@ -54,7 +54,7 @@ def workload(name: str):
     if name == "cylinder2d_m2":
         return cases.cylinder_case(n_theta=768, n_r=512, solver=1, minmod=True)
     if name == "cylinder2d_fine":
-        return cases.cylinder_case(n_theta=1536, n_r=1024, first=0.002, solver=0, minmod=True)
+        return cases.cylinder_case(n_theta=1536, n_r=1024, first=0.004, solver=0, minmod=True)
     if name == "vortex2d":
         return cases.vortex_case(n=256, solver=0)
     if name == "cylinder3d":
@@ -68,7 +68,7 @@ WORKLOAD_DESC = {
                        dim=2, scheme="M1", faces_per_cell=4, viscous=True),
     "cylinder2d_m2": dict(workload="2D cylinder O-grid 768x512, M2, minmod on, rkOrder 5, CFL 0.5", cells=393216,
                           dim=2, scheme="M2", faces_per_cell=4, viscous=True),
-    "cylinder2d_fine": dict(workload="2D cylinder O-grid 1536x1024, M1, minmod on, rkOrder 5, CFL 0.5",
+    "cylinder2d_fine": dict(workload="2D cylinder O-grid 1536x1024 (first cell 0.004 D), M1, minmod on, rkOrder 5, CFL 0.5",
                             cells=1572864, dim=2, scheme="M1", faces_per_cell=4, viscous=True),
     "vortex2d": dict(workload="2D isentropic vortex 256x256, M1, rkOrder 5, CFL 0.5", cells=65536, dim=2,
                      scheme="M1", faces_per_cell=4, viscous=False),

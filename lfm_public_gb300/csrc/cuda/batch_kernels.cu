@@ -38,9 +38,10 @@ __device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target,
     return sOk != 0;
 }
 
-// One item of a phase: a cell or ghost (prep; the tiles of a case whose cell
-// primitives are current cover its ghosts only), a cell (grad + vis, update)
-// or a face (flux) of the case in shared memory. FULL = false is the variant
+// One item of a phase: a cell or ghost (prep, only in a case's first step
+// after a new state: afterwards the update writes the next stage's primitives
+// of each cell and of its boundary ghosts), a cell (grad + vis, update) or a
+// face (flux) of the case in shared memory. FULL = false is the variant
 // for batches of M1/M2 cases without viscosity: no gradient or viscous code
 // is compiled in, which keeps the kernel's register count (and so its
 // occupancy) down.
@@ -64,9 +65,9 @@ __device__ __forceinline__ void item(const BatchCase& bc, int stage, int i) {
     } else {
         const int first = stage == 0;
         if (bc.residuals && first)
-            update32<D, true>(a, i, bc.rkA[stage], bc.rkB[stage], bc.dt, bc.dt32, first);
+            update32<D, true, true>(a, i, bc.rkA[stage], bc.rkB[stage], bc.dt, bc.dt32, first);
         else
-            update32<D, false>(a, i, bc.rkA[stage], bc.rkB[stage], bc.dt, bc.dt32, first);
+            update32<D, false, true>(a, i, bc.rkA[stage], bc.rkB[stage], bc.dt, bc.dt32, first);
     }
 }
 
@@ -105,8 +106,9 @@ __device__ __forceinline__ void phase_tiles(const BatchArgs& b, int stage, Batch
     }
 }
 
-// Stage `stage` of every case: prep | grad + vis | flux | update, with a grid
-// barrier between phases (none after the last). Within the launch every array
+// Stage `stage` of every case: [prep] | [grad + vis] | flux | update, with a
+// grid barrier between phases (none after the last; the bracketed phases and
+// their barriers only when they have tiles). Within the launch every array
 // is written by one phase and read only by later ones, so no block reads a
 // line it cached before another block rewrote it.
 // DIMS = 2: every case is 2D; DIMS = 0: 2D and 3D cases. FULL: see item().
@@ -117,9 +119,12 @@ __global__ void __launch_bounds__(BLOCK) k_batch_stage(const __grid_constant__ B
     if (threadIdx.x == 0) sSlot = -1;
     __syncthreads();
     unsigned* counter = &b.ctl->barrier[stage];
-    unsigned target = gridDim.x;
-    phase_tiles<0, BLOCK, DIMS, FULL>(b, stage, sc, sSlot);
-    if (!grid_barrier(counter, target, b.error)) return;
+    unsigned target = 0;
+    if (b.nTiles[0] > 0) {
+        phase_tiles<0, BLOCK, DIMS, FULL>(b, stage, sc, sSlot);
+        target += gridDim.x;
+        if (!grid_barrier(counter, target, b.error)) return;
+    }
     if (FULL && b.nTiles[1] > 0) {
         phase_tiles<1, BLOCK, DIMS, FULL>(b, stage, sc, sSlot);
         target += gridDim.x;

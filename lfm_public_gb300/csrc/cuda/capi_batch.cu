@@ -82,6 +82,9 @@ std::vector<unsigned char> packCase(const lfm_solver_desc* d, const CaseLayout& 
     conv(L.sponge, d->sponge, nc);
     std::memcpy(i32(L.cfOff), ix.cfOff.data(), (nc + 1) * 4);
     std::memcpy(i32(L.cfList), ix.cfList.data(), ix.cfList.size() * 4);
+    unsigned char* cg = img.data() + L.cellGhosts;   // cells whose update writes ghosts
+    for (size_t f = 0; f < nf; ++f)
+        if (ix.fN[f] >= (int)nc && ix.fN[f] < (int)(nc + ng)) cg[(size_t)ix.fP[f]] = 1;
     if (ng) {
         std::memcpy(i32(L.gCell), ix.gCell.data(), ng * 4);
         std::memcpy(i32(L.gKind), ix.gKind.data(), ng * 4);
@@ -112,10 +115,10 @@ int rebuildTiles(lfm_batch* b) {
     for (int s = 0; s < (int)b->slots.size(); ++s) {
         const Slot& sl = b->slots[(size_t)s];
         if (!sl.used) continue;
-        // preparation covers the ghosts only while the update phase keeps the
-        // cells' primitives current
-        const int first[kBatchPhases] = {sl.primsValid ? sl.nc : 0, 0, 0, 0};
-        const int end[kBatchPhases] = {sl.nt, sl.needGradVis ? sl.nc : 0, sl.nf, sl.nc};
+        // the update phase keeps the primitives of the cells and ghosts
+        // current: preparation runs only in a case's first step after a new state
+        const int first[kBatchPhases] = {0, 0, 0, 0};
+        const int end[kBatchPhases] = {sl.primsValid ? 0 : sl.nt, sl.needGradVis ? sl.nc : 0, sl.nf, sl.nc};
         for (int ph = 0; ph < kBatchPhases; ++ph)
             for (int st = first[ph]; st < end[ph]; st += tileSize)
                 tl[ph].push_back(BatchTile{s, st, std::min(tileSize, end[ph] - st), 0});
@@ -380,7 +383,7 @@ int commitCase(lfm_batch* b, const PreparedCase& pc, int* slot) {
     a.sponge = reinterpret_cast<const float*>(P(L.sponge));
     a.cfOff = reinterpret_cast<const int*>(P(L.cfOff));
     a.cfList = reinterpret_cast<const int*>(P(L.cfList));
-    a.cellGhosts = nullptr;   // the batch's preparation phase writes the ghosts
+    a.cellGhosts = reinterpret_cast<const uint8_t*>(P(L.cellGhosts));
     a.gCell = reinterpret_cast<const int*>(P(L.gCell));
     a.gKind = reinterpret_cast<const int*>(P(L.gKind));
     a.gFace = reinterpret_cast<const int*>(P(L.gFace));

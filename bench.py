@@ -77,6 +77,44 @@ WORKLOAD_DESC = {
 }
 
 
+# DRAM bytes (read + write) of one launch of the dominant kernel, from one ncu
+# capture of this bench's own command (cold L2: ncu flushes the caches before
+# each captured launch). Keyed by (workload, precision, kernel).
+# profiles/fp32_kernels_cylinder768x512.md
+DRAM_TRAFFIC = {
+    ("cylinder2d", "fp32", "k_update"): 42934272 + 166912,
+    ("cylinder2d", "fp64", "k_flux"): 95860992 + 7875328,
+}
+
+# FP64 pipe thread-instructions per cell of one launch of each kernel of the
+# plain FP64 path (DFMA, DMUL, DADD and the FP64 parts of divisions and square
+# roots), counted by ncu (sm__thread_inst_executed_pipe_fp64_pred_on.sum /
+# cells) on the 768x512 cylinder, M1, viscous. profiles/fp64_pipe_cylinder768x512.md
+FP64_INST_PER_CELL = {
+    "cylinder2d": {"k_prep": 22.19, "k_grad": 0.0, "k_vis": 85.00, "k_flux": 202.26, "k_update": 34.31},
+}
+# FP64 pipe instruction rate: the measured DFMA rate (FP64_PEAK_TFLOPS counts
+# an FMA as two operations) in instructions per second.
+FP64_PIPE_PEAK_GINST = FP64_PEAK_TFLOPS * 1e3 / 2.0
+
+
+def fp64_pipe_roofline(workload: str, cells: int, stages: int, ms_per_step: float, kernels_ms_per_step: dict):
+    """The plain FP64 path is bound by GB300's FP64 pipe, not by HBM: FP64
+    instructions executed per second against the measured DFMA rate, for the
+    whole step and for its dominant kernel."""
+    per = FP64_INST_PER_CELL.get(workload)
+    if per is None:
+        return None
+    step_inst = sum(per.values()) * cells * stages
+    dom = max(kernels_ms_per_step, key=kernels_ms_per_step.get)
+    dom_ginst = per[dom] * cells * stages / (kernels_ms_per_step[dom] * 1e-3) / 1e9
+    achieved = step_inst / (ms_per_step * 1e-3) / 1e9
+    return {"bound": "fp64-pipe", "achieved": achieved, "peak": FP64_PIPE_PEAK_GINST, "unit": "G FP64 inst/s",
+            "frac": achieved / FP64_PIPE_PEAK_GINST, "kernel": dom, "kernel_achieved": dom_ginst,
+            "kernel_frac": dom_ginst / FP64_PIPE_PEAK_GINST, "fp64_inst_per_cell_stage": sum(per.values()),
+            "peak_source": "measured DFMA rate"}
+
+
 def kernel_bytes(dim: int, faces_per_cell: int, fp32: bool, scheme: str, viscous: bool):
     """Algorithmic bytes per cell of one launch of each kernel: every array
     element the kernel must touch, once (face arrays once per face, cell arrays
@@ -321,7 +359,8 @@ def run_gpu(args):
         s64.close()
         v64 = ws * nc * stages * args.steps / (ms64 / 1000.0)
         plain = {"value": v64, "unit": UNIT, "ms_per_step": ms64 / args.steps, "kernels_ms_per_step": prof64,
-                 "speedup": value / v64}
+                 "speedup": value / v64,
+                 "roofline": fp64_pipe_roofline(args.workload, nc, stages, ms64 / args.steps, prof64)}
         n_acc = args.accuracy_steps
         if n_acc > 0:
             qs = []
@@ -366,11 +405,13 @@ def run_gpu(args):
                    "precision": "fp32-bulk" if fp32 else "fp64", "l2": "512 MB write between timed steps",
                    "parallelism": f"replicas x{ws}"},
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "peak_source": peak_src, "traffic": None,
+                     "frac": achieved / hbm, "peak_source": peak_src,
+                     "traffic": DRAM_TRAFFIC.get((args.workload, args.precision, dominant)),
                      "algorithmic_bytes_per_cell": kb[dominant], "cells_per_launch": nc,
                      "step_achieved": step_achieved, "step_frac": step_achieved / hbm,
                      "step_algorithmic_bytes_per_cell_stage": step_bytes},
         "kernels_ms_per_step": prof, "dominant_kernel": dominant,
+        "fp64_pipe": None if fp32 else fp64_pipe_roofline(args.workload, nc, stages, total_ms / args.steps, prof),
         "plain_fp64": plain, "accuracy": accuracy,
         "cpu_baseline": base,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nq * nc * 8, "d2h_bytes_per_step": nq * nc * 8},

@@ -7,6 +7,8 @@
 #ifndef LFM_GPU_MESH_H
 #define LFM_GPU_MESH_H
 
+#include <vector>
+
 #include "fastmesh.h"
 #include "meshReader.h"
 
@@ -40,6 +42,13 @@ public:
 
 private:
     void updateSolution();
+    // haveForces: wall patches (type "wall", in patch order, as the
+    // reference's m_nWallBCList) and the records not yet written
+    void recordForces(double time);
+    void writeForces(bool header);
+    std::vector<int> m_wallPatches;
+    std::vector<double> m_forceTimes;
+    std::vector<std::vector<double>> m_forceRows;   // per record: [patch][Fp D, Fv D]
     lfm::SolverCase* m_pCase = nullptr;
     lfm_solver* m_pSolver = nullptr;
     int m_nPrecision = 0;

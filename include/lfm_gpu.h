@@ -98,6 +98,10 @@ typedef struct lfm_solver_desc {
     int64_t n_halos;
     const int64_t* halo_src_part;  /* [n_halos] */
     const int64_t* halo_src_cell;  /* [n_halos] solver-order cell of that partition */
+    /* Boundary patch (index in the mesh's patch list) of each ghost, for the
+     * wall-force post-processing (may be NULL: lfm_solver_forces is then
+     * unavailable). */
+    const int32_t* ghost_patch;    /* [n_ghosts] */
 } lfm_solver_desc;
 
 typedef struct lfm_case lfm_case;
@@ -227,6 +231,39 @@ int lfm_solver_cell_residual(lfm_solver* s, double* res);
  * overlaps on the GPU race with each other. */
 #define LFM_NOALLOC_SCRATCH_BYTES (32u << 20)
 int lfm_solver_residual_noalloc(const lfm_solver* s, const double* q, int64_t q_stride, double* res, void* stream);
+
+/* ---- post-processing on the device ------------------------------------- */
+
+/* Pressure statistics (haveAverage; postProcAverage and updateAverageField,
+ * src/cfd_v0.cpp:3083-3104, 2966-2970). reset zeroes the per-cell sums;
+ * accumulate(n) adds, from the current state, pAVG += p and
+ * pRMS += (p - pAVG / n)^2 in every cell (nothing when n < 1: the reference
+ * passes the step count since tStartAverage); get(n) returns
+ * p_avg = pAVG * (1/n) and p_rms = sqrt(pRMS * (1/n)) per cell ([n_cells],
+ * solver order). Asynchronous on the solver stream, except get. */
+int lfm_solver_stats_reset(lfm_solver* s);
+int lfm_solver_stats_accumulate(lfm_solver* s, int n);
+int lfm_solver_stats_get(lfm_solver* s, int n, double* p_avg, double* p_rms);
+
+/* Pressure and viscous forces on boundary patches (haveForces;
+ * postProcForces, src/cfd_v0.cpp:3169-3250): for patch patches[i] (index in
+ * the mesh's patch list, see desc->ghost_patch),
+ *   f_pressure[i*dim + k] = sum over its faces of S_k (p - p_inf),
+ *   f_viscous[i*dim + k]  = - sum over its faces of (tau . S)_k,
+ * tau from the wall-normal velocity difference between the cell and its
+ * ghost, summed in the reference's face order. The ghost state is, as the
+ * reference's ghost cells hold after a step, the boundary state of the last
+ * stage's starting state (the FP32-bulk path recovers that state from the
+ * last update, q' - B dq); before any stage, that of the current state.
+ * Synchronous. */
+int lfm_solver_forces(lfm_solver* s, int n_patches, const int32_t* patches, double* f_pressure, double* f_viscous);
+
+/* Pressure probes: p - p_inf of the listed cells (solver order), appended to
+ * a device history by each record call (up to `capacity` records), read
+ * back in one copy ([n_records][n]). */
+int lfm_solver_probes_set(lfm_solver* s, int n, const int64_t* cells, int capacity);
+int lfm_solver_probes_record(lfm_solver* s);
+int lfm_solver_probes_read(lfm_solver* s, double* out, int* n_records);
 
 /* Blocks until all work on the solver stream has finished and reports the
  * first CUDA or numeric error. */

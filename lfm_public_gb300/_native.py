@@ -47,6 +47,7 @@ class SolverDesc(C.Structure):
         ("pInf", C.c_double), ("TInf", C.c_double), ("UInf", C.c_double * 3), ("mu", C.c_double), ("Cp", C.c_double),
         ("PrInv", C.c_double), ("rkA", _dp), ("rkB", _dp),
         ("n_halos", C.c_int64), ("halo_src_part", _i64p), ("halo_src_cell", _i64p),
+        ("ghost_patch", C.POINTER(C.c_int32)),
     ]
 
 
@@ -129,6 +130,12 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     vp = C.c_void_p
     sig = {
         "lfm_last_error": ([], C.c_char_p), "lfm_version": ([], C.c_char_p),
+        "lfm_solver_stats_reset": ([vp], C.c_int), "lfm_solver_stats_accumulate": ([vp, C.c_int], C.c_int),
+        "lfm_solver_stats_get": ([vp, C.c_int, _dp, _dp], C.c_int),
+        "lfm_solver_forces": ([vp, C.c_int, C.POINTER(C.c_int32), _dp, _dp], C.c_int),
+        "lfm_solver_probes_set": ([vp, C.c_int, C.POINTER(C.c_int64), C.c_int], C.c_int),
+        "lfm_solver_probes_record": ([vp], C.c_int),
+        "lfm_solver_probes_read": ([vp, _dp, C.POINTER(C.c_int)], C.c_int),
         "lfm_case_open": ([C.c_char_p, C.c_int, C.POINTER(vp)], C.c_int),
         "lfm_case_from_polymesh": ([C.POINTER(PolyMesh), C.POINTER(Params), C.POINTER(Fields), C.POINTER(vp)],
                                    C.c_int),
@@ -387,6 +394,45 @@ class Solver:
         check(load_library().lfm_solver_cell_residual(self._h, _ptr(out, C.c_double)))
         return out
 
+    # post-processing ------------------------------------------------------
+    def stats_reset(self):
+        check(load_library().lfm_solver_stats_reset(self._h))
+
+    def stats_accumulate(self, n: int):
+        check(load_library().lfm_solver_stats_accumulate(self._h, n))
+
+    def stats_get(self, n: int):
+        """(p_avg, p_rms) per cell, solver order."""
+        a = np.empty(self.n_cells)
+        r = np.empty(self.n_cells)
+        check(load_library().lfm_solver_stats_get(self._h, n, _ptr(a, C.c_double), _ptr(r, C.c_double)))
+        return a, r
+
+    def forces(self, patches) -> tuple:
+        """(pressure, viscous) force [len(patches)][dim] on the given patches."""
+        p = np.ascontiguousarray(patches, dtype=np.int32)
+        D = self.case.desc.dim
+        fp = np.empty((len(p), D))
+        fv = np.empty((len(p), D))
+        check(load_library().lfm_solver_forces(self._h, len(p), _ptr(p, C.c_int32), _ptr(fp, C.c_double),
+                                               _ptr(fv, C.c_double)))
+        return fp, fv
+
+    def probes_set(self, cells, capacity: int):
+        c = np.ascontiguousarray(cells, dtype=np.int64)
+        self._nprobes = len(c)
+        self._probe_cap = capacity
+        check(load_library().lfm_solver_probes_set(self._h, len(c), _ptr(c, C.c_int64), capacity))
+
+    def probes_record(self):
+        check(load_library().lfm_solver_probes_record(self._h))
+
+    def probes_read(self) -> np.ndarray:
+        out = np.empty((max(self._probe_cap, 1), self._nprobes))
+        n = C.c_int()
+        check(load_library().lfm_solver_probes_read(self._h, _ptr(out, C.c_double), C.byref(n)))
+        return out[:n.value]
+
     def launches_per_step(self) -> int:
         v = C.c_int()
         check(load_library().lfm_solver_launches_per_step(self._h, C.byref(v)))
@@ -581,6 +627,45 @@ class Batch:
         ms = (C.c_float * nsteps)()
         check(load_library().lfm_batch_bench(self._h, nsteps, flush_bytes, ms))
         return np.array(ms[:], dtype=np.float64)
+
+    # post-processing ------------------------------------------------------
+    def stats_reset(self):
+        check(load_library().lfm_solver_stats_reset(self._h))
+
+    def stats_accumulate(self, n: int):
+        check(load_library().lfm_solver_stats_accumulate(self._h, n))
+
+    def stats_get(self, n: int):
+        """(p_avg, p_rms) per cell, solver order."""
+        a = np.empty(self.n_cells)
+        r = np.empty(self.n_cells)
+        check(load_library().lfm_solver_stats_get(self._h, n, _ptr(a, C.c_double), _ptr(r, C.c_double)))
+        return a, r
+
+    def forces(self, patches) -> tuple:
+        """(pressure, viscous) force [len(patches)][dim] on the given patches."""
+        p = np.ascontiguousarray(patches, dtype=np.int32)
+        D = self.case.desc.dim
+        fp = np.empty((len(p), D))
+        fv = np.empty((len(p), D))
+        check(load_library().lfm_solver_forces(self._h, len(p), _ptr(p, C.c_int32), _ptr(fp, C.c_double),
+                                               _ptr(fv, C.c_double)))
+        return fp, fv
+
+    def probes_set(self, cells, capacity: int):
+        c = np.ascontiguousarray(cells, dtype=np.int64)
+        self._nprobes = len(c)
+        self._probe_cap = capacity
+        check(load_library().lfm_solver_probes_set(self._h, len(c), _ptr(c, C.c_int64), capacity))
+
+    def probes_record(self):
+        check(load_library().lfm_solver_probes_record(self._h))
+
+    def probes_read(self) -> np.ndarray:
+        out = np.empty((max(self._probe_cap, 1), self._nprobes))
+        n = C.c_int()
+        check(load_library().lfm_solver_probes_read(self._h, _ptr(out, C.c_double), C.byref(n)))
+        return out[:n.value]
 
     def launches_per_step(self) -> int:
         v = C.c_int()

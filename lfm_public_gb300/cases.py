@@ -623,8 +623,16 @@ def write_field(case: Case, d: str, name: str, values: np.ndarray, dims: str) ->
         f.write("\n)\n;\n\nboundaryField\n{" + _boundary_block(case) + "}\n")
 
 
-def write_case(case: Case, root: str, n_steps: Optional[int] = None, write_interval: Optional[int] = None) -> str:
-    """Writes ``case`` as an OpenFOAM case directory under ``root``."""
+def write_case(case: Case, root: str, n_steps: Optional[int] = None, write_interval: Optional[int] = None,
+               post: Optional[dict] = None) -> str:
+    """Writes ``case`` as an OpenFOAM case directory under ``root``. ``post``
+    sets lfm/post entries of controlDict (haveAverage, tStartAverage,
+    haveForces, saveForcesStep, printInfoFreq, ...)."""
+    pe = {"haveProbes": "false", "haveSampling": "false", "haveAverage": "false", "haveForces": "false",
+          "haveResiduals": "true" if case.residuals else "false", "printInfoFreq": str(case.print_freq),
+          "saveResiduals": "false", "saveBlendFactor": "false"}
+    for k, v in (post or {}).items():
+        pe[k] = ("true" if v else "false") if isinstance(v, bool) else (_fmt(v) if isinstance(v, float) else str(v))
     n_steps = case.n_steps if n_steps is None else n_steps
     wi = n_steps if write_interval is None else write_interval
     os.makedirs(root, exist_ok=True)
@@ -641,11 +649,7 @@ def write_case(case: Case, root: str, n_steps: Optional[int] = None, write_inter
     with open(os.path.join(root, "system", "controlDict"), "w") as f:
         f.write(_header("dictionary", "controlDict", "system"))
         f.write("lfm\n{\n    commType        2;\n    haloCommType    1;\n    doublePrecision true;\n"
-                "    post\n    {\n        haveProbes      false;\n        haveSampling    false;\n"
-                "        haveAverage     false;\n        haveForces      false;\n"
-                f"        haveResiduals   {'true' if case.residuals else 'false'};\n"
-                f"        printInfoFreq   {case.print_freq};\n        saveResiduals   false;\n"
-                "        saveBlendFactor false;\n    }\n}\n\n")
+                "    post\n    {\n" + "".join(f"        {k:<15} {v};\n" for k, v in pe.items()) + "    }\n}\n\n")
         f.write(f"startFrom       startTime;\nstartTime       0;\nstopAt          endTime;\n"
                 f"endTime         {_fmt(end)};\ndeltaT          {_fmt(case.delta_t)};\n"
                 f"writeControl    timeStep;\nwriteInterval   {wi};\nwriteFormat     ascii;\n"

@@ -3,6 +3,8 @@
 // A solver owns its device arrays and one CUDA stream. A full time step
 // (rk_order stages of 3-5 kernels) is captured once into a CUDA graph and
 // replayed; the graph is captured again only when dt changes.
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -57,6 +59,21 @@ struct lfm_solver {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     void* scrub = nullptr;
     size_t scrubBytes = 0;
+    // post-processing
+    double* gS = nullptr;        // [D][ng] FP64 face vector of each ghost's face
+    double* gD = nullptr;        // [D][ng] FP64 cell-to-ghost vector
+    int* gPatch = nullptr;       // [ng] boundary patch of each ghost (null: not described)
+    bool ghostRowsValid = false; // a stage ran since the last set_state (FP64: ghost states stored)
+    double lastStageB = 0;       // B coefficient of the last stage run
+    double* statAvg = nullptr;   // [nc] sum of p
+    double* statRms = nullptr;   // [nc] sum of (p - mean)^2
+    double* forceTerms = nullptr;   // [D + D*D][ng]
+    int* dPatches = nullptr;
+    double* dForces = nullptr;      // [2][patch capacity * D]
+    int patchCap = 0;
+    int* probeCells = nullptr;
+    double* probeHist = nullptr;
+    int nProbes = 0, probeCap = 0, probeRecords = 0;
 };
 
 namespace {
@@ -190,9 +207,12 @@ void stageAll(lfm_solver* s, const Args<T>& a, double dt) {
     for (int k = 0; k < s->rkOrder; ++k) lfm::dev::launch_stage<T>(a, stageConfig(s, k, dt), s->stream);
 }
 
-// FP32-bulk: primitives of every cell from the stored state, once after a
-// new state (the update kernels keep them current afterwards).
+// Called before stages are launched. FP32-bulk: primitives of every cell from
+// the stored state, once after a new state (the update kernels keep them
+// current afterwards). FP64: the stages that follow store the ghosts' states.
 int ensurePrims(lfm_solver* s) {
+    s->ghostRowsValid = true;
+    s->lastStageB = s->rkB.empty() ? 0.0 : s->rkB.back();
     if (s->precision != LFM_FP32_BULK || s->primsValid) return LFM_OK;
     StageConfig c;
     c.fullPrep = true;
@@ -336,6 +356,22 @@ int createSolver(const lfm_solver_desc* d, const lfm_solver_opts* opts, cudaStre
         if ((rc = upload(s, &dCG, cg.data(), nc))) return fail(rc);
         s->a32.cellGhosts = dCG;
     }
+    {   // ghost face geometry in FP64 and patch ids (post-processing)
+        const size_t ng = (size_t)s->ng, D = (size_t)s->D;
+        std::vector<double> gs(D * ng), gd(D * ng);
+        for (size_t g = 0; g < ng; ++g)
+            for (size_t k = 0; k < D; ++k) {
+                gs[k * ng + g] = d->S[k * nf + (size_t)gFace[g]];
+                gd[k * ng + g] = d->d[k * nf + (size_t)gFace[g]];
+            }
+        if ((rc = upload(s, &s->gS, gs.data(), D * ng))) return fail(rc);
+        if ((rc = upload(s, &s->gD, gd.data(), D * ng))) return fail(rc);
+        if (d->ghost_patch) {
+            std::vector<int> gp(ng);
+            for (size_t g = 0; g < ng; ++g) gp[g] = (int)d->ghost_patch[g];
+            if ((rc = upload(s, &s->gPatch, gp.data(), ng))) return fail(rc);
+        }
+    }
     if (s->precision == LFM_FP32_BULK) {
         for (int v = 0; v < s->nq; ++v) s->qRef[v] = s->a32.qRef[v];
         if ((rc = devAlloc(s, &s->stage, nq * nc))) return fail(rc);
@@ -362,6 +398,10 @@ extern "C" void lfm_solver_destroy(lfm_solver* s) {
     if (s->graph) cudaGraphExecDestroy(s->graph);
     for (void* p : s->allocations) cudaFree(p);
     if (s->scrub) cudaFree(s->scrub);
+    if (s->dPatches) cudaFree(s->dPatches);
+    if (s->dForces) cudaFree(s->dForces);
+    if (s->probeCells) cudaFree(s->probeCells);
+    if (s->probeHist) cudaFree(s->probeHist);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     if (s->stream && s->ownStream) cudaStreamDestroy(s->stream);
@@ -388,6 +428,7 @@ extern "C" int lfm_solver_set_state(lfm_solver* s, const double* q) {
     }
     LFM_CUDA(cudaStreamSynchronize(s->stream));
     s->primsValid = false;
+    s->ghostRowsValid = false;
     return LFM_OK;
 }
 
@@ -416,6 +457,7 @@ extern "C" int lfm_solver_stage(lfm_solver* s, int rk, double dt) {
     LFM_CUDA(cudaSetDevice(s->device));
     int rc = ensurePrims(s);
     if (rc) return rc;
+    s->lastStageB = s->rkB[(size_t)rk];
     const StageConfig c = stageConfig(s, rk, dt);
     if (s->precision == LFM_FP32_BULK)
         lfm::dev::launch_stage<float>(s->a32, c, s->stream);
@@ -605,6 +647,153 @@ extern "C" int lfm_solver_residual_noalloc(const lfm_solver* s, const double* q,
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (s->precision == LFM_FP32_BULK) return residualNoalloc<float>(s, s->a32, q, q_stride, res, st);
     return residualNoalloc<double>(s, s->a64, q, q_stride, res, st);
+}
+
+// ---------------------------------------------------------------------------
+// Post-processing (post_kernels.cu).
+// ---------------------------------------------------------------------------
+namespace {
+
+lfm::dev::QOffset stateOffset(const lfm_solver* s) {
+    lfm::dev::QOffset qo;
+    for (int v = 0; v < 5; ++v) qo.v[v] = s->precision == LFM_FP32_BULK ? s->qRef[v] : 0.0;
+    return qo;
+}
+
+double gammaMinusOne(const lfm_solver* s) { return s->precision == LFM_FP32_BULK ? s->a32.gm1 : s->a64.gm1; }
+double pInfOf(const lfm_solver* s) { return s->precision == LFM_FP32_BULK ? s->a32.pInf : s->a64.pInf; }
+
+}  // namespace
+
+extern "C" int lfm_solver_stats_reset(lfm_solver* s) {
+    if (!s) return lfm::setError(LFM_ERR_INVALID, "null solver");
+    LFM_CUDA(cudaSetDevice(s->device));
+    int rc;
+    if (!s->statAvg && ((rc = devAlloc(s, &s->statAvg, (size_t)s->nc)) || (rc = devAlloc(s, &s->statRms, (size_t)s->nc))))
+        return rc;
+    LFM_CUDA(cudaMemsetAsync(s->statAvg, 0, (size_t)s->nc * sizeof(double), s->stream));
+    LFM_CUDA(cudaMemsetAsync(s->statRms, 0, (size_t)s->nc * sizeof(double), s->stream));
+    return LFM_OK;
+}
+
+extern "C" int lfm_solver_stats_accumulate(lfm_solver* s, int n) {
+    if (!s) return lfm::setError(LFM_ERR_INVALID, "null solver");
+    if (!s->statAvg) return lfm::setError(LFM_ERR_INVALID, "lfm_solver_stats_reset was not called");
+    if (n < 1) return LFM_OK;
+    LFM_CUDA(cudaSetDevice(s->device));
+    lfm::dev::launch_stats(s->D, s->q, s->nt, stateOffset(s), s->nc, gammaMinusOne(s), n, s->statAvg, s->statRms,
+                           s->stream);
+    LFM_CUDA(cudaGetLastError());
+    return LFM_OK;
+}
+
+extern "C" int lfm_solver_stats_get(lfm_solver* s, int n, double* p_avg, double* p_rms) {
+    if (!s || !p_avg || !p_rms || n < 1) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    if (!s->statAvg) return lfm::setError(LFM_ERR_INVALID, "lfm_solver_stats_reset was not called");
+    LFM_CUDA(cudaSetDevice(s->device));
+    const size_t nc = (size_t)s->nc;
+    LFM_CUDA(cudaMemcpyAsync(p_avg, s->statAvg, nc * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    LFM_CUDA(cudaMemcpyAsync(p_rms, s->statRms, nc * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    LFM_CUDA(cudaStreamSynchronize(s->stream));
+    // updateAverageField: factor 1/n, square root of the RMS sum
+    // (updateScalarField / updateScalarFieldSqrt of the mesh reader)
+    const double f = 1.0 / n;
+    for (size_t c = 0; c < nc; ++c) {
+        p_avg[c] = p_avg[c] * f;
+        p_rms[c] = std::sqrt(p_rms[c] * f);
+    }
+    return LFM_OK;
+}
+
+extern "C" int lfm_solver_forces(lfm_solver* s, int n_patches, const int32_t* patches, double* f_pressure,
+                                 double* f_viscous) {
+    if (!s || n_patches < 0 || (n_patches > 0 && (!patches || !f_pressure || !f_viscous)))
+        return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    if (!s->gPatch && s->ng > 0)
+        return lfm::setError(LFM_ERR_INVALID, "the solver description has no ghost_patch: forces unavailable");
+    if (n_patches == 0) return LFM_OK;
+    LFM_CUDA(cudaSetDevice(s->device));
+    int rc;
+    if (!s->forceTerms && s->ng > 0 &&
+        (rc = devAlloc(s, &s->forceTerms, (size_t)(s->D + s->D * s->D) * (size_t)s->ng)))
+        return rc;
+    if (n_patches > s->patchCap) {
+        if (s->dPatches) cudaFree(s->dPatches);
+        if (s->dForces) cudaFree(s->dForces);
+        s->dPatches = nullptr;
+        s->dForces = nullptr;
+        s->patchCap = 0;
+        LFM_CUDA(cudaMalloc(&s->dPatches, (size_t)n_patches * sizeof(int)));
+        LFM_CUDA(cudaMalloc(&s->dForces, 2 * (size_t)n_patches * (size_t)s->D * sizeof(double)));
+        s->patchCap = n_patches;
+    }
+    const size_t nv = (size_t)n_patches * (size_t)s->D;
+    std::vector<int> pl(patches, patches + n_patches);
+    LFM_CUDA(cudaMemcpyAsync(s->dPatches, pl.data(), pl.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    LFM_CUDA(cudaMemsetAsync(s->dForces, 0, 2 * nv * sizeof(double), s->stream));
+    // ghost states of the last stage's start, as the reference's ghost cells
+    // hold after a step: stored on the FP64 path, recovered from the last
+    // update on the FP32-bulk path; the current state's before any stage
+    const int mode = !s->ghostRowsValid ? lfm::dev::kGhostFresh
+                     : s->precision == LFM_FP64 ? lfm::dev::kGhostStored : lfm::dev::kGhostUndo;
+    if (s->precision == LFM_FP32_BULK)
+        lfm::dev::launch_forces<float>(s->a32, stateOffset(s), s->gS, s->gD, s->gPatch, mode, s->lastStageB,
+                                       s->dPatches, n_patches, s->forceTerms, s->dForces, s->dForces + nv, s->stream);
+    else
+        lfm::dev::launch_forces<double>(s->a64, stateOffset(s), s->gS, s->gD, s->gPatch, mode, s->lastStageB,
+                                        s->dPatches, n_patches, s->forceTerms, s->dForces, s->dForces + nv,
+                                        s->stream);
+    LFM_CUDA(cudaGetLastError());
+    LFM_CUDA(cudaMemcpyAsync(f_pressure, s->dForces, nv * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    LFM_CUDA(cudaMemcpyAsync(f_viscous, s->dForces + nv, nv * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    LFM_CUDA(cudaStreamSynchronize(s->stream));
+    return LFM_OK;
+}
+
+extern "C" int lfm_solver_probes_set(lfm_solver* s, int n, const int64_t* cells, int capacity) {
+    if (!s || n < 0 || capacity < 0 || (n > 0 && !cells)) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    for (int i = 0; i < n; ++i)
+        if (cells[i] < 0 || cells[i] >= s->nc) return lfm::setError(LFM_ERR_INVALID, "probe cell out of range");
+    LFM_CUDA(cudaSetDevice(s->device));
+    LFM_CUDA(cudaStreamSynchronize(s->stream));
+    if (s->probeCells) cudaFree(s->probeCells);
+    if (s->probeHist) cudaFree(s->probeHist);
+    s->probeCells = nullptr;
+    s->probeHist = nullptr;
+    s->nProbes = s->probeCap = s->probeRecords = 0;
+    if (n == 0) return LFM_OK;
+    std::vector<int> c32(cells, cells + n);
+    LFM_CUDA(cudaMalloc(&s->probeCells, (size_t)n * sizeof(int)));
+    LFM_CUDA(cudaMalloc(&s->probeHist, (size_t)n * (size_t)std::max(capacity, 1) * sizeof(double)));
+    LFM_CUDA(cudaMemcpy(s->probeCells, c32.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice));
+    s->nProbes = n;
+    s->probeCap = capacity;
+    return LFM_OK;
+}
+
+extern "C" int lfm_solver_probes_record(lfm_solver* s) {
+    if (!s) return lfm::setError(LFM_ERR_INVALID, "null solver");
+    if (s->nProbes == 0) return lfm::setError(LFM_ERR_INVALID, "no probes set");
+    if (s->probeRecords >= s->probeCap) return lfm::setError(LFM_ERR_NOMEM, "probe history is full");
+    LFM_CUDA(cudaSetDevice(s->device));
+    lfm::dev::launch_probe(s->D, s->q, s->nt, stateOffset(s), s->probeCells, s->nProbes, gammaMinusOne(s), pInfOf(s),
+                           s->probeHist + (size_t)s->probeRecords * (size_t)s->nProbes, s->stream);
+    LFM_CUDA(cudaGetLastError());
+    ++s->probeRecords;
+    return LFM_OK;
+}
+
+extern "C" int lfm_solver_probes_read(lfm_solver* s, double* out, int* n_records) {
+    if (!s || !n_records) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    LFM_CUDA(cudaSetDevice(s->device));
+    *n_records = s->probeRecords;
+    if (s->probeRecords > 0) {
+        if (!out) return lfm::setError(LFM_ERR_INVALID, "null output");
+        LFM_CUDA(cudaMemcpyAsync(out, s->probeHist, (size_t)s->probeRecords * (size_t)s->nProbes * sizeof(double),
+                                 cudaMemcpyDeviceToHost, s->stream));
+    }
+    LFM_CUDA(cudaStreamSynchronize(s->stream));
+    return LFM_OK;
 }
 
 extern "C" int lfm_solver_sync(lfm_solver* s) {

@@ -62,6 +62,17 @@ template <typename X>
 void launch_halo_gather(X* dst, int dstNt, int first, int rows, int nh, const int* srcPart, const int* srcCell,
                         X* const* srcBase, const int* srcNt, cudaStream_t st);
 
+// Post-processing (post_kernels.cu).
+void launch_stats(int D, const double* q, int64_t nt, QOffset qo, int nc, double gm1, int n, double* avg,
+                  double* rms, cudaStream_t st);
+void launch_probe(int D, const double* q, int64_t nt, QOffset qo, const int* cells, int n, double gm1, double pInf,
+                  double* out, cudaStream_t st);
+enum { kGhostStored = 0, kGhostFresh = 1, kGhostUndo = 2 };
+template <typename T>
+void launch_forces(const Args<T>& a, QOffset qo, const double* gS, const double* gD, const int* gPatch, int mode,
+                   double Blast, const int* patches, int nPatches, double* terms, double* fp, double* fv,
+                   cudaStream_t st);
+
 constexpr int kKernelsPerStage = 5;  // prep, grad, vis, flux, update
 inline const char* kernelName(int i) {
     static const char* names[] = {"k_prep", "k_grad", "k_vis", "k_flux", "k_update"};

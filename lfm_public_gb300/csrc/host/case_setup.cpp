@@ -441,6 +441,7 @@ void describeSolverCase(const SolverCase& s, lfm_solver_desc* d) {
     d->n_halos = s.nHalos;
     d->halo_src_part = s.haloSrcPart.empty() ? nullptr : s.haloSrcPart.data();
     d->halo_src_cell = s.haloSrcCell.empty() ? nullptr : s.haloSrcCell.data();
+    d->ghost_patch = s.ghostPatch.data();
 }
 
 }  // namespace lfm

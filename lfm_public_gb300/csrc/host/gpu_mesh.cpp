@@ -7,13 +7,24 @@
 // step, time, CFL / dt (and residuals) are printed; at write times rho, E, p, U
 // are stored into the reader's fields (updateSolutionPrimitives,
 // src/cfd_v0.cpp:2999-3033) and all AUTO_WRITE fields are written. T and alpha
-// are written as read, as the reference does.
+// are written as read, as the reference does. Post-processing runs on the
+// device: haveAverage accumulates pAvg / pRMS after every step from
+// tStartAverage on and writes them as fields; haveForces records the wall
+// forces at the start and every saveForcesStep steps and appends them to
+// ./output/postProcess_Forces_<k> at write times (src/mesh_solver.cpp:253-360,
+// 740-756, 828-838, 1081-1123).
 #include "gpuMesh.h"
 
+#include <sys/stat.h>
+
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <fstream>
+#include <iomanip>
 #include <iostream>
+#include <sstream>
 #include <stdexcept>
 #include <vector>
 
@@ -106,6 +117,54 @@ void GpuMesh::updateSolution() {
     }
 }
 
+void GpuMesh::recordForces(double time) {
+    const int D = m_pCase->dim;
+    const size_t nw = m_wallPatches.size();
+    std::vector<double> fp(nw * (size_t)D), fv(nw * (size_t)D);
+    if (lfm_solver_forces(m_pSolver, (int)nw, m_wallPatches.data(), fp.data(), fv.data()) != LFM_OK)
+        throw std::runtime_error(std::string("forces: ") + lfm_last_error());
+    std::vector<double> row;
+    for (size_t i = 0; i < nw; ++i) {
+        for (int k = 0; k < D; ++k) row.push_back(fp[i * (size_t)D + (size_t)k]);
+        for (int k = 0; k < D; ++k) row.push_back(fv[i * (size_t)D + (size_t)k]);
+    }
+    m_forceTimes.push_back(time);
+    m_forceRows.push_back(row);
+}
+
+// output_Forces / postProcForcesOutput (src/mesh_solver.cpp:1081-1123,
+// src/cfd_v0.cpp:3254-3275): one file per wall patch.
+void GpuMesh::writeForces(bool header) {
+    const int D = m_pCase->dim;
+    static const char xyz[3] = {'x', 'y', 'z'};
+    for (size_t i = 0; i < m_wallPatches.size(); ++i) {
+        std::ostringstream name;
+        name << "./output/postProcess_Forces_" << i + 1;
+        std::ofstream f(name.str(), header ? std::ios::out : std::ios::app);
+        if (header) {
+            f << std::setw(25) << "time";
+            for (int k = 0; k < D; ++k) f << std::setw(25) << "Fp," << xyz[k];
+            for (int k = 0; k < D; ++k) f << std::setw(25) << "Fv," << xyz[k];
+            for (int k = 0; k < D; ++k) f << std::setw(25) << "Fp," << xyz[k] << " + Fv," << xyz[k];
+            f << std::endl;
+            continue;
+        }
+        for (size_t r = 0; r < m_forceTimes.size(); ++r) {
+            const double* v = m_forceRows[r].data() + i * 2 * (size_t)D;
+            f << std::scientific << std::setprecision(16);
+            f << std::setw(25) << m_forceTimes[r];
+            for (int k = 0; k < D; ++k) f << std::setw(25) << v[k];
+            for (int k = 0; k < D; ++k) f << std::setw(25) << v[D + k];
+            for (int k = 0; k < D; ++k) f << std::setw(25) << v[k] + v[D + k];
+            f << std::endl;
+        }
+    }
+    if (!header) {
+        m_forceTimes.clear();
+        m_forceRows.clear();
+    }
+}
+
 void GpuMesh::solve() {
     if (!m_pSolver) throw std::runtime_error("GpuMesh::solve before initializeSolver");
     const lfm::SolverCase& c = *m_pCase;
@@ -145,6 +204,28 @@ void GpuMesh::solve() {
     double dt = m_pRunTime->getDeltaTime();
     double time = m_pRunTime->getCurrentTime();
     const double tEnd = m_pRunTime->getEndTime();
+    // pressure statistics from tStartAverage on (src/mesh_solver.cpp:253-270)
+    const bool average = m_pInput->m_bHaveAverage;
+    const int indexStartAverage = (int)((m_pInput->m_tStartAverage - time) / dt);
+    if (average) {
+        std::cout << "Statistics will start being computed at t = " << m_pInput->m_tStartAverage
+                  << ", at iteration " << indexStartAverage << std::endl;
+        m_pMeshReader->createScalarField("pAvg");
+        m_pMeshReader->createScalarField("pRMS");
+        if (lfm_solver_stats_reset(m_pSolver) != LFM_OK) throw std::runtime_error(lfm_last_error());
+    }
+    // wall forces: header if the first file is new, then the start record
+    // (src/mesh_solver.cpp:341-358, 428)
+    const bool forces = m_pInput->m_bHaveForces;
+    if (forces) {
+        m_wallPatches.clear();
+        for (int b = 0; b < m_pMeshReader->getBoundaryCount(); ++b)
+            if (m_pMeshReader->getBoundaryType(b) == "wall") m_wallPatches.push_back(b);
+        struct stat st;
+        if (stat("./output/postProcess_Forces_1", &st) != 0) writeForces(true);
+        recordForces(m_pRunTime->getCurrentTime());
+    }
+    const int saveForces = std::max(1, m_pInput->m_nSaveForcesSteps);
     double cflMax = m_pInput->m_dCFLMax;
     int timeStep = 0;
     double rkLoop = 0.0, outputTime = 0.0;
@@ -169,6 +250,9 @@ void GpuMesh::solve() {
         m_pRunTime->advanceTime();
         time += dt;
         ++timeStep;
+        if (average && lfm_solver_stats_accumulate(m_pSolver, timeStep - indexStartAverage) != LFM_OK)
+            throw std::runtime_error(lfm_last_error());
+        if (forces && timeStep % saveForces == 0) recordForces(time);
         if (print) {
             std::printf("Time step: %d     Time: %.10g", timeStep, time);
             if (m_pRunTime->isAdjustDeltaTime())
@@ -201,6 +285,20 @@ void GpuMesh::solve() {
                 }
             }
             updateSolution();
+            const int nAvg = timeStep - indexStartAverage;
+            if (average && nAvg >= 1) {   // updateAverages (src/cfd_v0.cpp:2966-2970)
+                const size_t nc = (size_t)c.nCells;
+                std::vector<double> pa(nc), pr(nc);
+                if (lfm_solver_stats_get(m_pSolver, nAvg, pa.data(), pr.data()) != LFM_OK)
+                    throw std::runtime_error(lfm_last_error());
+                const int iA = m_pMeshReader->getScalarFieldIndex("pAvg");
+                const int iR = m_pMeshReader->getScalarFieldIndex("pRMS");
+                for (size_t i = 0; i < nc; ++i) {
+                    m_pMeshReader->updateScalarField(iA, pa[i], (int)c.cellId[i]);
+                    m_pMeshReader->updateScalarField(iR, pr[i], (int)c.cellId[i]);
+                }
+            }
+            if (forces) writeForces(false);
             m_pRunTime->writeResults();
             outputTime += std::chrono::duration<double>(std::chrono::steady_clock::now() - b).count();
         }

@@ -4,8 +4,9 @@ Each fixture is a small synthetic case (mesh, initial fields, dictionary
 values) together with the fields the reference solver wrote after n_steps
 time steps: rho, U, E, p per polyMesh cell, and the CFL it printed. The
 reference is built from its own sources by oracle/Makefile (oracle/_ref/
-lfm_oracle); this script only runs where those sources exist. Run from the
-repository root:
+lfm_oracle); this script only runs where those sources exist. The post_*
+fixtures also hold the reference's pAvg / pRMS fields and its wall-force
+records (haveAverage, haveForces). Run from the repository root:
 
     python tests/golden/make_golden.py
 """
@@ -108,9 +109,60 @@ def run_reference(case: cases.Case, n_steps: int, workdir: str):
     return fields, cfl, r.stdout
 
 
+# Post-processing fixtures: the same runs with haveAverage (pAvg, pRMS fields)
+# and haveForces (output/postProcess_Forces_1) switched on.
+# name -> (generator, kwargs, n_steps, averaging start step, saveForcesStep)
+POST_FIXTURES = {
+    "post_cyl24x12_m2": (cases.cylinder_case, dict(n_theta=24, n_r=12, r1=10, first=0.05, Ls=3, solver=1,
+                                                   minmod=False, noise=0.02), 20, 5, 5),
+    "post_cyl16x8x4_ausm_3d": (cases.cylinder_case, dict(n_theta=16, n_r=8, r1=10, first=0.05, Ls=3, solver=2,
+                                                         n_span=4, noise=0.01), 10, 3, 2),
+}
+
+
+def read_forces(path: str) -> np.ndarray:
+    """Rows of a postProcess_Forces file: time, Fp[D], Fv[D], Fp + Fv[D]."""
+    rows = [ln.split() for ln in open(path).read().splitlines()[1:] if ln.strip()]
+    return np.array(rows, dtype=np.float64)
+
+
+def run_reference_post(case: cases.Case, n_steps: int, start: int, save_step: int, workdir: str):
+    post = dict(haveAverage=True, tStartAverage=case.delta_t * start, haveForces=True, saveForcesStep=save_step,
+                printInfoFreq=n_steps)
+    cases.write_case(case, workdir, n_steps=n_steps, post=post)
+    os.makedirs(os.path.join(workdir, "output"), exist_ok=True)
+    r = subprocess.run([ORACLE], cwd=workdir, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference run failed:\n" + r.stdout[-3000:] + r.stderr[-3000:])
+    m = re.findall(r"CFL:\s*([0-9eE+\-.]+)", r.stdout)
+    fields = cases.read_result_fields(workdir, names=("rho", "E", "p", "U", "pAvg", "pRMS"))
+    forces = read_forces(os.path.join(workdir, "output", "postProcess_Forces_1"))
+    return fields, forces, float(m[-1]) if m else float("nan")
+
+
+def main_post():
+    for name, (gen, kw, n, start, save) in POST_FIXTURES.items():
+        case = gen(n_steps=n, **kw)
+        tmp = tempfile.mkdtemp(prefix="lfm_golden_")
+        try:
+            res, forces, cfl = run_reference_post(case, n, start, save, tmp)
+        finally:
+            shutil.rmtree(tmp, ignore_errors=True)
+        arrs = case_to_arrays(case)
+        arrs.update({f"ref_{k}": v for k, v in res.items()})
+        arrs["ref_forces"] = forces
+        arrs["ref_cfl"] = np.float64(cfl)
+        arrs["n_steps"] = np.int64(n)
+        arrs["average_start"] = np.int64(start)
+        arrs["save_forces_step"] = np.int64(save)
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrs)
+        print(f"{name}: {case.n_cells} cells, {n} steps, {forces.shape[0]} force records")
+
+
 def main():
     if not os.path.exists(ORACLE):
         raise SystemExit(f"{ORACLE} is missing: run `make -C oracle` where the reference sources exist")
+    main_post()
     for name, (gen, kw, n) in FIXTURES.items():
         case = gen(n_steps=n, **kw)
         if name.endswith("_res"):

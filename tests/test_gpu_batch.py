@@ -60,6 +60,18 @@ def test_batch_mix_matches_alone_and_single_solver_bitwise():
     b.close()
 
 
+def test_single_solver_ghost_pass_variants_bitwise():
+    """Above a size threshold the single-case solver prepares its ghosts in a
+    separate kernel instead of inside the update; both give the batch's bits
+    (the batch always writes ghosts from the update)."""
+    case = cases.cylinder_case(n_theta=96, n_r=48, r1=12, first=0.03, Ls=3, solver=1, minmod=False, n_span=64,
+                               noise=0.01)   # 294,912 cells: above the 3D threshold
+    ch = N.CaseHandle.from_case(case)
+    assert ch.desc.n_cells > (1 << 18)
+    n = 8
+    assert np.array_equal(_single(ch, n, case.delta_t), _alone(ch, n, case.delta_t))
+
+
 def test_batch_join_leave_between_steps():
     cs = _mixed_cases()[:4]
     chs = [N.CaseHandle.from_case(c) for c in cs]

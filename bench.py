@@ -57,6 +57,12 @@ def workload(name: str):
         return cases.cylinder_case(n_theta=1536, n_r=1024, first=0.004, solver=0, minmod=True)
     if name == "vortex2d":
         return cases.vortex_case(n=256, solver=0)
+    if name == "cylinder2d_shuffled":
+        # the 768x512 O-grid with its cells numbered at random, as an
+        # unstructured mesh generator may leave them (renumbering test)
+        import numpy as np
+        c = cases.cylinder_case(n_theta=768, n_r=512, solver=0, minmod=True)
+        return cases.renumber_cells(c, np.random.default_rng(768512).permutation(c.n_cells))
     if name == "cylinder3d":
         return cases.cylinder_case(n_theta=384, n_r=256, n_span=96, solver=1, reynolds=3900.0, noise=0.01, seed=3900,
                                    minmod=False)
@@ -70,6 +76,8 @@ WORKLOAD_DESC = {
                           dim=2, scheme="M2", faces_per_cell=4, viscous=True),
     "cylinder2d_fine": dict(workload="2D cylinder O-grid 1536x1024 (first cell 0.004 D), M1, minmod on, rkOrder 5, CFL 0.5",
                             cells=1572864, dim=2, scheme="M1", faces_per_cell=4, viscous=True),
+    "cylinder2d_shuffled": dict(workload="2D cylinder O-grid 768x512 with randomly numbered cells, M1, minmod on, "
+                                "rkOrder 5, CFL 0.5", cells=393216, dim=2, scheme="M1", faces_per_cell=4, viscous=True),
     "vortex2d": dict(workload="2D isentropic vortex 256x256, M1, rkOrder 5, CFL 0.5", cells=65536, dim=2,
                      scheme="M1", faces_per_cell=4, viscous=False),
     "cylinder3d": dict(workload="3D cylinder wake 384x256x96, M2, cyclic span, rkOrder 5", cells=9437184, dim=3,
@@ -322,7 +330,7 @@ def run_gpu(args):
                 "sample": f"1 time step (5 RK stages) of the full {desc['cells']}-cell mesh, single thread, {t:.1f} s"}
 
     case = workload(args.workload)
-    ch = N.CaseHandle.from_case(case)
+    ch = N.CaseHandle.from_case(case, renumber={"none": 0, "rcm": 1, "hilbert": 2}[args.renumber])
     nc, nq, stages = ch.desc.n_cells, ch.desc.nq, ch.desc.rk_order
     dt = case.delta_t
     prec = N.LFM_FP32_BULK if fp32 else N.LFM_FP64
@@ -403,6 +411,7 @@ def run_gpu(args):
         "dtype": "f32-flux/f64-rk" if fp32 else "f64", "data": "synthetic (generated mesh and initial field)",
         "config": {"workload": desc["workload"], "cells": nc, "rk_stages": stages,
                    "precision": "fp32-bulk" if fp32 else "fp64", "l2": "512 MB write between timed steps",
+                   "renumber": args.renumber,
                    "parallelism": f"replicas x{ws}"},
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_source": peak_src,
@@ -724,6 +733,8 @@ def main():
     ap.add_argument("--serve-arena-gb", type=float, default=4.0)
     ap.add_argument("--serve-chunk", type=int, default=25)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--renumber", default="none", choices=["none", "rcm", "hilbert"],
+                    help="solver order of the cells (single-case workloads)")
     args = ap.parse_args()
     if args.accuracy_steps is None:
         args.accuracy_steps = 200 if args.workload == "batch64" else 1000

@@ -145,7 +145,17 @@ typedef struct lfm_params {
     int solver, dimension, rk_order, minmod, laminar, residuals;
     double p_inf, T_inf, U_inf[3], Ls, mach, k_sponge;
     double Cp, mol_weight, mu, Pr;
+    /* Solver order of the cells inside each submesh, for locality of the
+     * device gathers: LFM_RENUMBER_NONE (polyMesh order, the reference's),
+     * _RCM (reverse Cuthill-McKee) or _HILBERT (Hilbert curve through the
+     * cell centres). lfm_case_open reads it from controlDict lfm/renumber
+     * (none | rcm | hilbert). Written fields keep the polyMesh numbering. */
+    int renumber;
 } lfm_params;
+
+#define LFM_RENUMBER_NONE 0
+#define LFM_RENUMBER_RCM 1
+#define LFM_RENUMBER_HILBERT 2
 
 typedef struct lfm_fields {
     const double* p;      /* [n_cells] */

@@ -19,6 +19,7 @@ PORT_PATH = os.path.join(ROOT, "oracle", "port", "liblfm_port.so")
 
 LFM_FP64 = 0
 LFM_FP32_BULK = 1
+LFM_RENUMBER_NONE, LFM_RENUMBER_RCM, LFM_RENUMBER_HILBERT = 0, 1, 2
 # lfm_status codes (include/lfm_gpu.h)
 LFM_OK = 0
 LFM_ERR_INVALID = -1
@@ -66,7 +67,7 @@ class Params(C.Structure):
         ("solver", C.c_int), ("dimension", C.c_int), ("rk_order", C.c_int), ("minmod", C.c_int), ("laminar", C.c_int),
         ("residuals", C.c_int), ("p_inf", C.c_double), ("T_inf", C.c_double), ("U_inf", C.c_double * 3),
         ("Ls", C.c_double), ("mach", C.c_double), ("k_sponge", C.c_double), ("Cp", C.c_double),
-        ("mol_weight", C.c_double), ("mu", C.c_double), ("Pr", C.c_double),
+        ("mol_weight", C.c_double), ("mu", C.c_double), ("Pr", C.c_double), ("renumber", C.c_int),
     ]
 
 
@@ -256,8 +257,9 @@ class CaseHandle:
         return cls(h)
 
     @classmethod
-    def from_case(cls, case) -> "CaseHandle":
-        """From an in-memory lfm_public_gb300.cases.Case."""
+    def from_case(cls, case, renumber: int = 0) -> "CaseHandle":
+        """From an in-memory lfm_public_gb300.cases.Case; ``renumber``: solver
+        order inside each submesh (LFM_RENUMBER_NONE / _RCM / _HILBERT)."""
         lib = load_library()
         pts = np.ascontiguousarray(case.points, dtype=np.float64)
         fo = np.ascontiguousarray(case.face_offsets, dtype=np.int64)
@@ -280,7 +282,7 @@ class CaseHandle:
         prm = Params(solver=pr["solver"], dimension=pr["dimension"], rk_order=pr["rk_order"], minmod=pr["minmod"],
                      laminar=1, residuals=pr["residuals"], p_inf=pr["p_inf"], T_inf=pr["T_inf"],
                      U_inf=(C.c_double * 3)(*pr["U_inf"]), Ls=pr["Ls"], mach=pr["mach"], k_sponge=pr["k_sponge"],
-                     Cp=pr["Cp"], mol_weight=pr["mol_weight"], mu=pr["mu"], Pr=pr["Pr"])
+                     Cp=pr["Cp"], mol_weight=pr["mol_weight"], mu=pr["mu"], Pr=pr["Pr"], renumber=renumber)
         p = np.ascontiguousarray(case.fields["p"], dtype=np.float64)
         T = np.ascontiguousarray(case.fields["T"], dtype=np.float64)
         U = np.ascontiguousarray(case.fields["U"], dtype=np.float64)

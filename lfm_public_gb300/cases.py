@@ -713,6 +713,48 @@ def _read_internal_field(path: str) -> np.ndarray:
 
 
 # ---------------------------------------------------------------------------
+# cell renumbering of a polyMesh (what renumberMesh writes)
+# ---------------------------------------------------------------------------
+def renumber_cells(case: Case, order: np.ndarray) -> Case:
+    """The same case with its cells renumbered: new cell i is old cell
+    ``order[i]``. Internal faces are flipped where the new owner label would
+    exceed the neighbour's (point order reversed, first point kept) and
+    sorted upper-triangular; boundary faces keep their patches and order."""
+    import copy
+    order = np.asarray(order, dtype=np.int64)
+    n = case.n_cells
+    if sorted(order.tolist()) != list(range(n)):
+        raise ValueError("order is not a permutation of the cells")
+    inv = np.empty(n, dtype=np.int64)
+    inv[order] = np.arange(n)
+    n_int = case.neighbour.shape[0]
+    fo, fp = case.face_offsets, case.face_points
+    own = inv[case.owner]
+    nbr = inv[case.neighbour]
+    flip = own[:n_int] > nbr
+    lo = np.where(flip, nbr, own[:n_int])
+    hi = np.where(flip, own[:n_int], nbr)
+    perm = np.lexsort((hi, lo))
+    faces = [(int(f), bool(flip[f])) for f in perm] + [(f, False) for f in range(n_int, case.n_faces)]
+    offs, pts = [0], []
+    for f, fl in faces:
+        v = fp[fo[f]:fo[f + 1]]
+        if fl:
+            v = np.concatenate([v[:1], v[1:][::-1]])
+        pts.append(v)
+        offs.append(offs[-1] + v.size)
+    out = copy.copy(case)
+    out.face_offsets = np.array(offs, dtype=np.int64)
+    out.face_points = np.concatenate(pts).astype(np.int64)
+    out.owner = np.concatenate([lo[perm], own[n_int:]]).astype(np.int64)
+    out.neighbour = hi[perm].astype(np.int64)
+    out.cell_centres = case.cell_centres[order]
+    out.fields = {k: v[order] for k, v in case.fields.items()}
+    out.name = case.name + ".renumbered"
+    return out
+
+
+# ---------------------------------------------------------------------------
 # decomposition into processor partitions (what decomposePar writes)
 # ---------------------------------------------------------------------------
 def partition_cells(case: Case, nparts: int, method: str = "x", seed: int = 0) -> np.ndarray:

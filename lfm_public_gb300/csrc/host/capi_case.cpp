@@ -14,7 +14,9 @@
 #include "foam_case.h"
 #include "inputReader.h"
 #include "lfm_gpu.h"
+#include "dictReaderOF.h"
 #include "polyMeshReaderOF.h"
+#include "renumber.h"
 
 struct lfm_case {
     lfm::SolverCase sc;
@@ -54,6 +56,13 @@ static lfm::CaseParams paramsFromInput(const CInputReader& in) {
     return p;
 }
 
+// controlDict lfm/renumber (none | rcm | hilbert): an extension of the
+// reference's controlDict, which the reference ignores.
+static int renumberOption(const std::string& root) {
+    CDictReaderOF controlDict("controlDict", root + "/system");
+    return lfm::renumberFromName(controlDict.readDictWord("renumber", "lfm", "none", true));
+}
+
 static int validateParams(const lfm::CaseParams& p) {
     if (p.solver < 0 || p.solver > 2) return lfm::setError(LFM_ERR_INVALID, "unknown solver type " + std::to_string(p.solver));
     if (p.dimension != 2 && p.dimension != 3)
@@ -63,6 +72,8 @@ static int validateParams(const lfm::CaseParams& p) {
                              "turbulenceProperties simulationType must be laminar (the Smagorinsky viscous pass is "
                              "not part of this build)");
     if (p.rkOrder < 0 || p.rkOrder > 5) return lfm::setError(LFM_ERR_INVALID, "rkOrder must be 0..5");
+    if (p.renumber < LFM_RENUMBER_NONE || p.renumber > LFM_RENUMBER_HILBERT)
+        return lfm::setError(LFM_ERR_INVALID, "unknown renumbering (none, rcm or hilbert)");
     return LFM_OK;
 }
 
@@ -73,6 +84,7 @@ extern "C" int lfm_case_open(const char* root, int rank, lfm_case** out) {
         CInputReader in;
         in.readCase(root);
         lfm::CaseParams prm = paramsFromInput(in);
+        prm.renumber = renumberOption(root);
         int rc = validateParams(prm);
         if (rc) return rc;
         const std::string caseName = rank >= 0 ? "processor" + std::to_string(rank) : ".";
@@ -118,6 +130,7 @@ extern "C" int lfm_case_from_polymesh(const lfm_polymesh* mesh, const lfm_params
         prm.molWeight = params->mol_weight;
         prm.mu = params->mu;
         prm.Pr = params->Pr;
+        prm.renumber = params->renumber;
         int rc = validateParams(prm);
         if (rc) return rc;
         if (mesh->n_faces <= 0 || mesh->n_cells <= 0 || !mesh->points || !mesh->face_offsets || !mesh->face_points ||
@@ -232,6 +245,7 @@ extern "C" int lfm_pcase_open(const char* root, int nparts, lfm_pcase** out) {
         CInputReader in;
         in.readCase(root);
         lfm::CaseParams prm = paramsFromInput(in);
+        prm.renumber = renumberOption(root);
         int rc = validateParams(prm);
         if (rc) return rc;
         std::vector<std::unique_ptr<lfm::FoamTime>> rts;

@@ -1,6 +1,8 @@
 // Solver setup restated from the reference (file:line ranges in case_setup.h).
 #include "case_setup.h"
 
+#include "renumber.h"
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -75,6 +77,9 @@ SolverCase buildSolverCase(IMeshReader& r, const CaseParams& prm, const HaloLook
     }
     const int64_t nc = subOffset.back();
     if (nc != r.getCellCount()) throw std::runtime_error("submesh split does not cover every cell");
+    // locality order of the cells inside each submesh (the polyMesh keeps its own)
+    if (prm.renumber != RENUMBER_NONE)
+        for (int s = 0; s < nSub; ++s) renumberCells(r, subCells[(size_t)s], prm.renumber, D);
     sc.nCells = nc;
     sc.nCells0 = nSub > 0 ? (int64_t)subCells[0].size() : 0;
     std::vector<int64_t> solverOf((size_t)nc), smOf((size_t)nc), localOf((size_t)nc);

@@ -37,6 +37,7 @@ struct CaseParams {
     double pInf = 0, TInf = 0, UInf[3] = {0, 0, 0};
     double Ls = 0, mach = 0, kSponge = 4.34294481903252e-01;
     double Cp = 0, molWeight = 0, mu = 0, Pr = 1;
+    int renumber = 0;          // solver order inside each submesh: Renumber (renumber.h)
 };
 
 // Other side of a processor face, for a partition built alongside its

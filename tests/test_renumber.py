@@ -1,0 +1,102 @@
+"""Cell renumbering (reverse Cuthill-McKee, Hilbert) of the solver order.
+
+The polyMesh keeps its numbering; only the solver's cell order inside each
+submesh changes, so results are those of the polyMesh order up to the
+summation order of each cell's faces (FP64 within 1e-12 of the oracle run on
+the unrenumbered case)."""
+import numpy as np
+import pytest
+
+from lfm_public_gb300 import _native as N, cases
+
+
+def _order_stats(ch):
+    d = ch.desc
+    nf, nc, n0 = d.n_faces, d.n_cells, d.n_cells0
+    fp = np.ctypeslib.as_array(d.face_p, shape=(nf,))
+    fn = np.ctypeslib.as_array(d.face_n, shape=(nf,))
+    m = (fn < nc) & (fp >= n0) & (fn >= n0)   # faces inside the interior submesh
+    dist = np.abs(fp[m] - fn[m])
+    return int(dist.max()), float(dist.mean())
+
+
+@pytest.fixture(scope="module")
+def shuffled():
+    c = cases.cylinder_case(n_theta=48, n_r=24, r1=10, first=0.03, Ls=3, solver=1, noise=0.02)
+    perm = np.random.default_rng(1).permutation(c.n_cells)
+    return c, cases.renumber_cells(c, perm), perm
+
+
+def test_renumber_cells_is_a_relabelling(shuffled):
+    c, cs, perm = shuffled
+    a = N.CaseHandle.from_case(c)
+    b = N.CaseHandle.from_case(cs)
+    assert a.desc.n_faces == b.desc.n_faces and a.desc.n_ghosts == b.desc.n_ghosts
+    # the same geometry per cell, in the new labels
+    va = np.ctypeslib.as_array(a.desc.vol_inv, shape=(c.n_cells,))[np.argsort(a.cell_ids())]
+    vb = np.ctypeslib.as_array(b.desc.vol_inv, shape=(c.n_cells,))[np.argsort(b.cell_ids())]
+    np.testing.assert_allclose(vb, va[perm], rtol=1e-12)
+
+
+@pytest.mark.parametrize("method", [N.LFM_RENUMBER_RCM, N.LFM_RENUMBER_HILBERT])
+def test_renumbering_restores_locality(shuffled, method):
+    c, cs, _ = shuffled
+    base = _order_stats(N.CaseHandle.from_case(cs))
+    ch = N.CaseHandle.from_case(cs, renumber=method)
+    ids = ch.cell_ids()
+    assert sorted(ids.tolist()) == list(range(c.n_cells))
+    bw, mean = _order_stats(ch)
+    assert mean < base[1] / 5, (mean, base)
+    if method == N.LFM_RENUMBER_RCM:
+        assert bw <= 2 * 48, bw   # about one ring of the O-grid
+
+
+@pytest.mark.parametrize("method", [N.LFM_RENUMBER_RCM, N.LFM_RENUMBER_HILBERT])
+def test_renumbered_case_matches_oracle(shuffled, method):
+    c, cs, _ = shuffled
+    n = 10
+    a = N.CaseHandle.from_case(cs)
+    qa, _ = N.port_run(a, a.q0(), n, c.delta_t)
+    b = N.CaseHandle.from_case(cs, renumber=method)
+    qb, _ = N.port_run(b, b.q0(), n, c.delta_t)
+    ga = np.empty_like(qa)
+    ga[:, a.cell_ids()] = qa
+    gb = np.empty_like(qb)
+    gb[:, b.cell_ids()] = qb
+    err = np.linalg.norm(gb - ga, axis=1) / np.linalg.norm(ga, axis=1)
+    assert np.all(err <= 1e-12), err
+
+
+def test_controldict_renumber_option(tmp_path, shuffled):
+    _, cs, _ = shuffled
+    root = str(tmp_path / "c")
+    cases.write_case(cs, root, n_steps=2)
+    cd = tmp_path / "c" / "system" / "controlDict"
+    cd.write_text(cd.read_text().replace("    doublePrecision true;", "    doublePrecision true;\n    renumber        rcm;"))
+    ch = N.CaseHandle.open(root)
+    assert _order_stats(ch)[0] <= 2 * 48
+    cd.write_text(cd.read_text().replace("renumber        rcm;", "renumber        bogus;"))
+    with pytest.raises(N.LfmError):
+        N.CaseHandle.open(root)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method", [N.LFM_RENUMBER_RCM, N.LFM_RENUMBER_HILBERT])
+def test_renumbered_device_run_matches_oracle(shuffled, method):
+    c, cs, _ = shuffled
+    n = 10
+    a = N.CaseHandle.from_case(cs)
+    qa, _ = N.port_run(a, a.q0(), n, c.delta_t)
+    ga = np.empty_like(qa)
+    ga[:, a.cell_ids()] = qa
+    b = N.CaseHandle.from_case(cs, renumber=method)
+    for prec, tol in ((N.LFM_FP64, 1e-12), (N.LFM_FP32_BULK, 1e-5)):
+        s = N.Solver(b, precision=prec)
+        s.step(n, c.delta_t)
+        s.sync()
+        q = s.get_state()
+        s.close()
+        g = np.empty_like(q)
+        g[:, b.cell_ids()] = q
+        err = np.linalg.norm(g - ga, axis=1) / np.linalg.norm(ga, axis=1)
+        assert np.all(err <= tol), (prec, err)

@@ -291,8 +291,11 @@ int lfm_solver_bench(lfm_solver* s, int nsteps, double dt, size_t flush_bytes, f
 /* Device kernels launched per time step (for launch accounting). */
 int lfm_solver_launches_per_step(const lfm_solver* s, int* launches);
 
-/* Per-kernel timing of one time step ([n] entries, names in
- * lfm_solver_kernel_name). Synchronizes. */
+/* Per-kernel times of one time step ([n] entries, ms summed over the RK
+ * stages, names in lfm_solver_kernel_name), measured with event nodes around
+ * every kernel in a captured step graph (no host gaps), averaged over a few
+ * launches that each start from an evicted L2 when lfm_solver_bench has
+ * allocated its scrub buffer. Synchronizes. */
 int lfm_solver_profile_step(lfm_solver* s, double dt, int n, float* ms);
 const char* lfm_solver_kernel_name(int i);
 
@@ -333,6 +336,12 @@ int lfm_partitioned_get_state(lfm_partitioned* P, int part, double* q);
 /* nsteps time steps of every partition (one CUDA graph per step); asynchronous. */
 int lfm_partitioned_step(lfm_partitioned* P, int nsteps, double dt);
 int lfm_partitioned_sync(lfm_partitioned* P);
+/* The solver of one partition (owned by P, valid until lfm_partitioned_destroy),
+ * for its per-partition queries: lfm_solver_cfl / _min_dt / _residual /
+ * _cell_residual / _stats_* / _forces / _probes_*. Advance partitions only
+ * through lfm_partitioned_step: a partition stepped on its own would not
+ * refresh its halos. */
+int lfm_partitioned_solver(lfm_partitioned* P, int part, lfm_solver** out);
 
 /* Diagnostic: runs the FP32-bulk kernels' integer-pipe binary32 <-> binary64
  * conversions on the device over n bit patterns (host arrays) and returns

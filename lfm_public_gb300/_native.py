@@ -137,6 +137,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "lfm_solver_probes_set": ([vp, C.c_int, C.POINTER(C.c_int64), C.c_int], C.c_int),
         "lfm_solver_probes_record": ([vp], C.c_int),
         "lfm_solver_probes_read": ([vp, _dp, C.POINTER(C.c_int)], C.c_int),
+        "lfm_partitioned_solver": ([vp, C.c_int, C.POINTER(vp)], C.c_int),
         "lfm_case_open": ([C.c_char_p, C.c_int, C.POINTER(vp)], C.c_int),
         "lfm_case_from_polymesh": ([C.POINTER(PolyMesh), C.POINTER(Params), C.POINTER(Fields), C.POINTER(vp)],
                                    C.c_int),

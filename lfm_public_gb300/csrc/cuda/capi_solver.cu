@@ -859,36 +859,65 @@ extern "C" int lfm_solver_launches_per_step(const lfm_solver* s, int* launches) 
 
 extern "C" const char* lfm_solver_kernel_name(int i) { return lfm::dev::kernelName(i); }
 
+// Per-kernel times of a time step as it runs in the step's CUDA graph: one
+// step captured with an event record node on each side of every kernel (no
+// host launch gaps between them), launched a few times, each after the L2
+// scrub of the benchmark loop when one exists; times averaged over launches.
+// Each stage also records an empty pair of event nodes: its time, the cost
+// of a pair of event nodes alone, is taken off every kernel's.
 extern "C" int lfm_solver_profile_step(lfm_solver* s, double dt, int n, float* ms) {
     if (!s || !ms || n < lfm::dev::kKernelsPerStage) return lfm::setError(LFM_ERR_INVALID, "bad argument");
     LFM_CUDA(cudaSetDevice(s->device));
     for (int k = 0; k < n; ++k) ms[k] = 0.f;
     int rc = ensurePrims(s);
     if (rc) return rc;
-    std::vector<cudaEvent_t> ev(2 * (size_t)s->rkOrder * lfm::dev::kKernelsPerStage);
+    const int K = lfm::dev::kKernelsPerStage;
+    const int K1 = K + 1;   // slot K: the empty calibration pair
+    std::vector<cudaEvent_t> ev(2 * (size_t)s->rkOrder * (size_t)K1);
     for (auto& x : ev) LFM_CUDA(cudaEventCreate(&x));
-    for (int k = 0; k < s->rkOrder; ++k) {
+    auto destroy = [&]() {
+        for (auto& x : ev) cudaEventDestroy(x);
+    };
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
+    for (int k = 0; k < s->rkOrder && e == cudaSuccess; ++k) {
         const StageConfig c = stageConfig(s, k, dt);
-        for (int w = 0; w < lfm::dev::kKernelsPerStage; ++w) {
-            const size_t base = 2 * ((size_t)k * lfm::dev::kKernelsPerStage + (size_t)w);
-            cudaEventRecord(ev[base], s->stream);
-            if (s->precision == LFM_FP32_BULK)
+        for (int w = 0; w < K1 && e == cudaSuccess; ++w) {
+            const size_t base = 2 * ((size_t)k * (size_t)K1 + (size_t)w);
+            e = cudaEventRecordWithFlags(ev[base], s->stream, cudaEventRecordExternal);
+            if (w < K && s->precision == LFM_FP32_BULK)
                 lfm::dev::launch_kernel<float>(s->a32, c, w, s->stream);
-            else
+            else if (w < K)
                 lfm::dev::launch_kernel<double>(s->a64, c, w, s->stream);
-            cudaEventRecord(ev[base + 1], s->stream);
+            if (e == cudaSuccess) e = cudaEventRecordWithFlags(ev[base + 1], s->stream, cudaEventRecordExternal);
         }
     }
-    LFM_CUDA(cudaStreamSynchronize(s->stream));
-    for (int k = 0; k < s->rkOrder; ++k)
-        for (int w = 0; w < lfm::dev::kKernelsPerStage; ++w) {
-            const size_t base = 2 * ((size_t)k * lfm::dev::kKernelsPerStage + (size_t)w);
-            float t = 0;
-            cudaEventElapsedTime(&t, ev[base], ev[base + 1]);
-            ms[w] += t;
+    const cudaError_t ec = cudaStreamEndCapture(s->stream, &g);
+    if (e == cudaSuccess) e = ec;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        destroy();
+        return cudaFail(e, "profile graph");
+    }
+    constexpr int kReps = 5;
+    for (int r = 0; r < kReps && e == cudaSuccess; ++r) {
+        if (s->scrub) e = cudaMemsetAsync(s->scrub, 0x5a + (r & 1), s->scrubBytes, s->stream);
+        if (e == cudaSuccess) e = cudaGraphLaunch(ge, s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        for (int k = 0; k < s->rkOrder && e == cudaSuccess; ++k) {
+            float t[16] = {0};
+            for (int w = 0; w < K1 && e == cudaSuccess; ++w) {
+                const size_t base = 2 * ((size_t)k * (size_t)K1 + (size_t)w);
+                e = cudaEventElapsedTime(&t[w], ev[base], ev[base + 1]);
+            }
+            for (int w = 0; w < K && e == cudaSuccess; ++w) ms[w] += std::max(0.f, t[w] - t[K]) / kReps;
         }
-    for (auto& x : ev) cudaEventDestroy(x);
-    LFM_CUDA(cudaGetLastError());
+    }
+    cudaGraphExecDestroy(ge);
+    destroy();
+    if (e != cudaSuccess) return cudaFail(e, "profile step");
     return LFM_OK;
 }
 
@@ -1083,6 +1112,14 @@ extern "C" int lfm_partitioned_step(lfm_partitioned* P, int nsteps, double dt) {
     for (lfm_solver* s : P->parts)
         if ((rc = ensurePrims(s))) return rc;
     for (int k = 0; k < nsteps; ++k) LFM_CUDA(cudaGraphLaunch(P->graph, P->stream));
+    return LFM_OK;
+}
+
+extern "C" int lfm_partitioned_solver(lfm_partitioned* P, int part, lfm_solver** out) {
+    int rc = checkPart(P, part);
+    if (rc) return rc;
+    if (!out) return lfm::setError(LFM_ERR_INVALID, "null output handle");
+    *out = P->parts[(size_t)part];
     return LFM_OK;
 }
 

@@ -219,25 +219,6 @@ struct lfm_pcase {
     bool adjust = false;
 };
 
-namespace {
-
-// Offsets (cell centre - face centre) of the processor faces of every
-// partition, keyed by (partition, partition across, face id): what each rank
-// of the reference sends its neighbours (src/mesh_reader.cpp:520-552).
-class OffsetTable : public lfm::HaloLookup {
-public:
-    std::map<std::tuple<int, int, int64_t>, std::array<double, 3>> offsets;
-    int self = 0;
-    bool neighbourOffset(int nbr, int64_t faceId, double* x) const override {
-        auto it = offsets.find(std::make_tuple(nbr, self, faceId));
-        if (it == offsets.end()) return false;
-        for (int k = 0; k < 3; ++k) x[k] = it->second[(size_t)k];
-        return true;
-    }
-};
-
-}  // namespace
-
 extern "C" int lfm_pcase_open(const char* root, int nparts, lfm_pcase** out) {
     if (!root || !out || nparts < 1) return lfm::setError(LFM_ERR_INVALID, "lfm_pcase_open: bad argument");
     *out = nullptr;
@@ -250,33 +231,14 @@ extern "C" int lfm_pcase_open(const char* root, int nparts, lfm_pcase** out) {
         if (rc) return rc;
         std::vector<std::unique_ptr<lfm::FoamTime>> rts;
         std::vector<std::unique_ptr<CPolyMeshReaderOF>> readers;
-        OffsetTable table;
+        std::vector<IMeshReader*> rs;
         for (int p = 0; p < nparts; ++p) {
             rts.emplace_back(lfm::newFoamTime(root, "processor" + std::to_string(p)));
             readers.emplace_back(new CPolyMeshReaderOF(rts.back().get()));
-            CPolyMeshReaderOF& r = *readers.back();
-            for (int b = 0; b < r.getBoundaryCount(); ++b) {
-                const int q = r.getBoundaryProcessorRank(b);
-                if (q < 0) continue;
-                for (int f = r.getBoundaryFaceStart(b); f <= r.getBoundaryFaceEnd(b); ++f) {
-                    double xc[3], xf[3];
-                    r.getCellCenter(r.getFaceOwner(f), xc);
-                    r.getFaceCenter(f, xf);
-                    table.offsets[std::make_tuple(p, q, (int64_t)r.getFaceId(f))] = {xc[0] - xf[0], xc[1] - xf[1],
-                                                                                      xc[2] - xf[2]};
-                }
-            }
+            rs.push_back(readers.back().get());
         }
         std::unique_ptr<lfm_pcase> pc(new lfm_pcase);
-        for (int p = 0; p < nparts; ++p) {
-            table.self = p;
-            pc->parts.push_back(lfm::buildSolverCase(*readers[(size_t)p], prm, &table));
-            lfm::SolverCase& sc = pc->parts.back();
-            sc.cellGlobal.resize(sc.cellId.size());
-            for (size_t c = 0; c < sc.cellId.size(); ++c)
-                sc.cellGlobal[c] = readers[(size_t)p]->getCellProcAddressing((int)sc.cellId[c]);
-        }
-        lfm::resolveHalos(pc->parts);
+        pc->parts = lfm::buildPartitionCases(rs, prm);
         pc->deltaT = rts[0]->deltaT;
         pc->startTime = rts[0]->startTime;
         pc->endTime = rts[0]->endTime;

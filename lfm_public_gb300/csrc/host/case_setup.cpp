@@ -4,6 +4,8 @@
 #include "renumber.h"
 
 #include <algorithm>
+#include <tuple>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -447,6 +449,52 @@ void describeSolverCase(const SolverCase& s, lfm_solver_desc* d) {
     d->halo_src_part = s.haloSrcPart.empty() ? nullptr : s.haloSrcPart.data();
     d->halo_src_cell = s.haloSrcCell.empty() ? nullptr : s.haloSrcCell.data();
     d->ghost_patch = s.ghostPatch.data();
+}
+
+namespace {
+
+// Offsets (cell centre - face centre) of the processor faces of every
+// partition, keyed by (partition, partition across, face id).
+class OffsetTable : public HaloLookup {
+public:
+    std::map<std::tuple<int, int, int64_t>, std::array<double, 3>> offsets;
+    int self = 0;
+    bool neighbourOffset(int nbr, int64_t faceId, double* x) const override {
+        auto it = offsets.find(std::make_tuple(nbr, self, faceId));
+        if (it == offsets.end()) return false;
+        for (int k = 0; k < 3; ++k) x[k] = it->second[(size_t)k];
+        return true;
+    }
+};
+
+}  // namespace
+
+std::vector<SolverCase> buildPartitionCases(const std::vector<IMeshReader*>& readers, const CaseParams& prm) {
+    OffsetTable table;
+    for (size_t p = 0; p < readers.size(); ++p) {
+        IMeshReader& r = *readers[p];
+        for (int b = 0; b < r.getBoundaryCount(); ++b) {
+            const int q = r.getBoundaryProcessorRank(b);
+            if (q < 0) continue;
+            for (int f = r.getBoundaryFaceStart(b); f <= r.getBoundaryFaceEnd(b); ++f) {
+                double xc[3], xf[3];
+                r.getCellCenter(r.getFaceOwner(f), xc);
+                r.getFaceCenter(f, xf);
+                table.offsets[std::make_tuple((int)p, q, (int64_t)r.getFaceId(f))] = {xc[0] - xf[0], xc[1] - xf[1],
+                                                                                       xc[2] - xf[2]};
+            }
+        }
+    }
+    std::vector<SolverCase> parts;
+    for (size_t p = 0; p < readers.size(); ++p) {
+        table.self = (int)p;
+        parts.push_back(buildSolverCase(*readers[p], prm, &table));
+        SolverCase& sc = parts.back();
+        sc.cellGlobal.resize(sc.cellId.size());
+        for (size_t c = 0; c < sc.cellId.size(); ++c) sc.cellGlobal[c] = readers[p]->getCellProcAddressing((int)sc.cellId[c]);
+    }
+    resolveHalos(parts);
+    return parts;
 }
 
 }  // namespace lfm

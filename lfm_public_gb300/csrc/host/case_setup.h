@@ -118,6 +118,13 @@ SolverCase buildSolverCase(IMeshReader& reader, const CaseParams& params, const 
 // across the processor face (by face id). Throws when a face has no partner.
 void resolveHalos(std::vector<SolverCase>& parts);
 
+// Every partition of a decomposed case from its readers (processor0..N-1):
+// the processor faces' neighbour offsets exchanged between the readers (what
+// each rank of the reference sends its neighbours, src/mesh_reader.cpp:520-552),
+// each partition's solver case with its halos, cellGlobal from
+// cellProcAddressing, and the halos matched to their source cells.
+std::vector<SolverCase> buildPartitionCases(const std::vector<IMeshReader*>& readers, const CaseParams& params);
+
 // Fills the flattened C description with pointers into `sc` (valid while sc lives).
 void describeSolverCase(const SolverCase& sc, lfm_solver_desc* out);
 

@@ -3,10 +3,15 @@
 // (-h, -p/--parallel, -c/--comm_type); invalid input prints a message and
 // returns 0, as the reference does. controlDict lfm/doublePrecision false
 // selects the FP32-bulk form (FP32 flux, FP64 RK registers) instead of the
-// reference's single-precision build. With -p the case is processor<LFM_RANK>.
+// reference's single-precision build. With -p every partition processor0..N-1
+// runs in this process on one GPU (LFM_RANK=<r>: partition r alone).
+#include <sys/stat.h>
+
 #include <cstdlib>
 #include <exception>
 #include <iostream>
+#include <memory>
+#include <string>
 
 #include "gpuMesh.h"
 #include "inputReader.h"
@@ -37,15 +42,33 @@ int main(int argc, char* argv[]) {
         std::cerr << "invalid halo communication type: " << input.m_nHaloCommType << std::endl;
         return 0;
     }
-    int rank = -1;
+    // -p: the decomposed case. The reference runs it as one MPI rank per
+    // partition (mpirun -np N lfm_solve -p); here one process runs every
+    // partition processor0..N-1 on the GPU, or, with LFM_RANK set, that
+    // partition alone (which must then have no processor patches).
+    int rank = -1, partitions = 0;
     if (input.m_bParallel) {
         const char* r = std::getenv("LFM_RANK");
-        rank = r ? std::atoi(r) : 0;
+        if (r) {
+            rank = std::atoi(r);
+        } else {
+            struct stat st;
+            while (stat(("processor" + std::to_string(partitions)).c_str(), &st) == 0) ++partitions;
+            if (partitions == 0) {
+                std::cerr << "-p: no processor0 directory in the case" << std::endl;
+                return 1;
+            }
+        }
     }
     try {
-        CRunTimeManagerOF runTime(rank);
+        std::unique_ptr<CRunTimeManagerOF> runTime;
         fastmesh::GpuMesh mesh;
-        mesh.setRunTimeManager(&runTime);
+        if (partitions > 0) {
+            mesh.setPartitionCount(partitions);
+        } else {
+            runTime.reset(new CRunTimeManagerOF(rank));
+            mesh.setRunTimeManager(runTime.get());
+        }
         mesh.setInputReader(&input);
         mesh.setPrecision(input.m_bIsDoublePrecision ? LFM_FP64 : LFM_FP32_BULK);
         const char* dev = std::getenv("LFM_DEVICE");

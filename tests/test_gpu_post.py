@@ -141,3 +141,32 @@ def test_driver_writes_reference_post_processing(tmp_path, name):
     assert rel_l2(f["pRMS"][None], z["ref_pRMS"][None])[0] <= 1e-8
     assert rel_l2(f["rho"][None], z["ref_rho"][None])[0] <= 1e-12
     shutil.rmtree(root, ignore_errors=True)
+
+
+@pytest.mark.parametrize("name,nparts,method", [("post_cyl24x12_m2", 3, "random"), ("post_cyl24x12_m2", 2, "x")])
+def test_driver_runs_decomposed_case(tmp_path, name, nparts, method):
+    """`lfm_solve_gpu -p` on processor0..N-1 (the reference's
+    `mpirun -np N lfm_solve -p`): every partition in one process on the GPU,
+    each writing its processor directory; reassembled fields, statistics and
+    the summed wall forces match the reference's undecomposed run."""
+    case, z = load_golden(name)
+    n, start, save = int(z["n_steps"]), int(z["average_start"]), int(z["save_forces_step"])
+    root = str(tmp_path / "case")
+    part = cases.decompose_case(case, root, nparts, method=method, seed=4, n_steps=n,
+                                post=dict(haveAverage=True, tStartAverage=case.delta_t * start, haveForces=True,
+                                          saveForcesStep=save, printInfoFreq=n))
+    os.makedirs(os.path.join(root, "output"))
+    r = subprocess.run([CLI, "-p"], cwd=root, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    assert "partitions   : %d" % nparts in r.stdout
+    glob = {k: np.full(case.n_cells, np.nan) for k in ("rho", "p", "pAvg", "pRMS")}
+    for p in range(nparts):
+        f = cases.read_result_fields(os.path.join(root, f"processor{p}"), names=tuple(glob))
+        cells = np.nonzero(part == p)[0]
+        for k in glob:
+            glob[k][cells] = f[k]
+    for k, tol in (("rho", 1e-12), ("p", 1e-12), ("pAvg", 1e-12), ("pRMS", 1e-8)):
+        assert np.all(np.isfinite(glob[k])), k
+        assert rel_l2(glob[k][None], z["ref_" + k][None])[0] <= tol, k
+    rows = read_forces(os.path.join(root, "output", "postProcess_Forces_1"))
+    _check_forces(rows, z["ref_forces"], case.dim)

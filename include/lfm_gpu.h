@@ -343,6 +343,14 @@ int lfm_partitioned_sync(lfm_partitioned* P);
  * refresh its halos. */
 int lfm_partitioned_solver(lfm_partitioned* P, int part, lfm_solver** out);
 
+/* Diagnostic: the tiles of the fused FP32-bulk stage kernel for a
+ * description (host only, no device): runs of up to tile_cells cells, halved
+ * while their local cells exceed max_local; out = {tiles, largest local cell
+ * count, largest local face count, local cells summed over the tiles, flux
+ * faces summed over the tiles}. LFM_ERR_INVALID when the tiles cannot be
+ * built (processor halos) or an index check fails. */
+int lfm_tiles_stats(const lfm_solver_desc* d, int tile_cells, int max_local, int64_t* out);
+
 /* Diagnostic: runs the FP32-bulk kernels' integer-pipe binary32 <-> binary64
  * conversions on the device over n bit patterns (host arrays) and returns
  * their results, for comparison with IEEE 754 conversions. */

@@ -138,6 +138,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "lfm_solver_probes_record": ([vp], C.c_int),
         "lfm_solver_probes_read": ([vp, _dp, C.POINTER(C.c_int)], C.c_int),
         "lfm_partitioned_solver": ([vp, C.c_int, C.POINTER(vp)], C.c_int),
+        "lfm_tiles_stats": ([C.POINTER(SolverDesc), C.c_int, C.c_int, C.POINTER(C.c_int64)], C.c_int),
         "lfm_case_open": ([C.c_char_p, C.c_int, C.POINTER(vp)], C.c_int),
         "lfm_case_from_polymesh": ([C.POINTER(PolyMesh), C.POINTER(Params), C.POINTER(Fields), C.POINTER(vp)],
                                    C.c_int),
@@ -442,11 +443,15 @@ class Solver:
         return v.value
 
     def profile_step(self, dt: float) -> dict:
+        """ms per time step of each kernel; kernels that did not run are left out."""
         lib = load_library()
-        n = 5
+        n = 6
         ms = (C.c_float * n)()
         check(lib.lfm_solver_profile_step(self._h, dt, n, ms))
-        return {lib.lfm_solver_kernel_name(i).decode(): ms[i] for i in range(n)}
+        names = [lib.lfm_solver_kernel_name(i).decode() for i in range(n)]
+        if ms[5] > 0:   # fused tile stages
+            return {names[5]: ms[5]}
+        return {names[i]: ms[i] for i in range(5)}
 
     def close(self):
         if getattr(self, "_h", None):

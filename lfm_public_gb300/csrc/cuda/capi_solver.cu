@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -13,6 +14,7 @@
 
 #include "../host/capi_internal.h"
 #include "lfm_gpu.h"
+#include "../host/tiles.h"
 #include "args_setup.h"
 #include "solver_launch.h"
 
@@ -74,6 +76,14 @@ struct lfm_solver {
     int* probeCells = nullptr;
     double* probeHist = nullptr;
     int nProbes = 0, probeCap = 0, probeRecords = 0;
+    // fused tile stages (FP32-bulk without halos, tile_kernels.cu): the tiles
+    // on the device, a second primitive buffer, and which of the two holds
+    // the current primitives (0: a32.prim)
+    bool tiled = false;
+    lfm::dev::TileArgs tile{};
+    float* prim1 = nullptr;
+    int primParity = 0;
+    cudaGraphExec_t graphOdd = nullptr;   // the step graph starting from prim1
 };
 
 namespace {
@@ -207,6 +217,28 @@ void stageAll(lfm_solver* s, const Args<T>& a, double dt) {
     for (int k = 0; k < s->rkOrder; ++k) lfm::dev::launch_stage<T>(a, stageConfig(s, k, dt), s->stream);
 }
 
+// Fused tile stage k of a step that starts from primitive buffer `parity`:
+// reads buffer (parity + k) % 2, writes the other.
+void tileStage(lfm_solver* s, int k, double dt, int parity) {
+    float* buf[2] = {s->a32.prim, s->prim1};
+    const int in = (parity + k) & 1;
+    Args<float> g = s->a32;
+    g.prim = buf[in ^ 1];
+    lfm::dev::TileArgs t = s->tile;
+    t.primIn = buf[in];
+    lfm::dev::launch_tile_stage(g, t, stageConfig(s, k, dt), s->stream);
+}
+
+// The tile stages keep the current primitives in either buffer; the other
+// kernels read a32.prim. Before those run, the primitives are rebuilt there
+// from the state when they sit in the other buffer.
+void untile(lfm_solver* s) {
+    if (s->tiled && s->primParity != 0) {
+        s->primsValid = false;
+        s->primParity = 0;
+    }
+}
+
 // Called before stages are launched. FP32-bulk: primitives of every cell from
 // the stored state, once after a new state (the update kernels keep them
 // current afterwards). FP64: the stages that follow store the ghosts' states.
@@ -214,6 +246,7 @@ int ensurePrims(lfm_solver* s) {
     s->ghostRowsValid = true;
     s->lastStageB = s->rkB.empty() ? 0.0 : s->rkB.back();
     if (s->precision != LFM_FP32_BULK || s->primsValid) return LFM_OK;
+    s->primParity = 0;   // rebuilt into a32.prim
     StageConfig c;
     c.fullPrep = true;
     lfm::dev::launch_kernel<float>(s->a32, c, 0, s->stream);
@@ -222,29 +255,46 @@ int ensurePrims(lfm_solver* s) {
     return LFM_OK;
 }
 
-void launchStep(lfm_solver* s, double dt) {
-    if (s->precision == LFM_FP32_BULK)
+void launchStep(lfm_solver* s, double dt, int parity) {
+    if (s->tiled)
+        for (int k = 0; k < s->rkOrder; ++k) tileStage(s, k, dt, parity);
+    else if (s->precision == LFM_FP32_BULK)
         stageAll<float>(s, s->a32, dt);
     else
         stageAll<double>(s, s->a64, dt);
 }
 
-int ensureGraph(lfm_solver* s, double dt) {
-    if (s->graph && s->graphDt == dt) return LFM_OK;
-    if (s->graph) {
-        cudaGraphExecDestroy(s->graph);
-        s->graph = nullptr;
-    }
+int captureStep(lfm_solver* s, double dt, int parity, cudaGraphExec_t* out) {
     cudaGraph_t g = nullptr;
     LFM_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-    launchStep(s, dt);
+    launchStep(s, dt, parity);
     cudaError_t e = cudaStreamEndCapture(s->stream, &g);
     if (e != cudaSuccess) return cudaFail(e, "cudaStreamEndCapture");
-    e = cudaGraphInstantiate(&s->graph, g, 0);
+    e = cudaGraphInstantiate(out, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return cudaFail(e, "cudaGraphInstantiate");
+    return LFM_OK;
+}
+
+// One graph per time step; with tile stages a second one for steps that
+// start from prim1 (an odd stage count swaps the buffers every step).
+int ensureGraph(lfm_solver* s, double dt) {
+    if (s->graph && s->graphDt == dt) return LFM_OK;
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    if (s->graphOdd) cudaGraphExecDestroy(s->graphOdd);
+    s->graph = s->graphOdd = nullptr;
+    int rc = captureStep(s, dt, 0, &s->graph);
+    if (!rc && s->tiled) rc = captureStep(s, dt, 1, &s->graphOdd);
+    if (rc) return rc;
     s->graphDt = dt;
     return LFM_OK;
+}
+
+// Launches the step graph matching the current primitive buffer.
+cudaError_t launchStepGraph(lfm_solver* s) {
+    const cudaError_t e = cudaGraphLaunch(s->tiled && s->primParity ? s->graphOdd : s->graph, s->stream);
+    if (s->tiled) s->primParity ^= (s->rkOrder & 1);
+    return e;
 }
 
 }  // namespace
@@ -259,6 +309,32 @@ namespace {
 // against 0.826) and for a 9.4M-cell 3D case (8.65 against 7.75 ms).
 constexpr int kFuseGhostCells2D = 1 << 20;
 constexpr int kFuseGhostCells3D = 1 << 18;
+
+// Fused tile stages (tile_kernels.cu): cells per tile, 0 = off. Off by
+// default: measured on GB300 (768x512 cylinder, Hilbert order, FP32-bulk M1)
+// a step took 0.352 ms in 256-cell tiles against 0.226 ms with the separate
+// kernels - each block runs its load, viscous, flux and update phases one
+// after another at 3-4 resident blocks per SM, which hides less latency
+// than the separate kernels at full occupancy. LFM_TILE_CELLS=<n> in the
+// environment turns them on for a solver created afterwards.
+constexpr int kTileCells = 0;
+constexpr int kTileMaxLocal2D = 600;   // a tile's cells with their two rings
+constexpr int kTileMaxLocal3D = 360;
+constexpr size_t kMaxTileSmem = 96 * 1024;
+// Cells staged per cell (tile cells and their rings) above which the separate
+// kernels are used instead: a cell order whose runs are strips rather than
+// patches (renumbering fixes that, lfm_params.renumber).
+constexpr double kMaxTileStaging = 2.5;
+
+// Arrays the flux reads: viscous terms when they are computed or M2AUSM
+// reads them (its shock sensor), gradients for M2AUSM (zero without minmod).
+bool tileHaveV(const lfm_solver* s) { return s->needVis || s->scheme == LFM_SOLVER_M2AUSM; }
+bool tileHaveGrad(const lfm_solver* s) { return s->scheme == LFM_SOLVER_M2AUSM; }
+
+int tileCellsOption() {
+    const char* e = getenv("LFM_TILE_CELLS");
+    return e ? atoi(e) : kTileCells;
+}
 
 // Creates a solver; `stream` (not owned) is shared by the partitions of a
 // decomposed case, which alone may carry processor-face halos.
@@ -347,7 +423,25 @@ int createSolver(const lfm_solver_desc* d, const lfm_solver_opts* opts, cudaStre
     else
         rc = buildArgs<double>(s, d, s->a64, dP, dN, dG, dOff, dList, dGC, dGK, dGF);
     if (rc) return fail(rc);
-    if (s->precision == LFM_FP32_BULK && s->nc <= (s->D == 2 ? kFuseGhostCells2D : kFuseGhostCells3D)) {
+    // fused tile stages: FP32-bulk without halos, when a block's tile fits
+    lfm::TileSet tiles;
+    bool tiled = false;
+    if (s->precision == LFM_FP32_BULK && s->nh == 0) {
+        const int tc = tileCellsOption();
+        if (tc > 0) {
+            try {
+                tiles = lfm::buildTiles(d, tc, s->D == 2 ? kTileMaxLocal2D : kTileMaxLocal3D);
+                tiled = lfm::dev::tile_smem_bytes(s->D, tiles.maxL, tiles.maxLF, tileHaveV(s), tileHaveGrad(s)) <=
+                            kMaxTileSmem &&
+                        (double)tiles.localCells <= kMaxTileStaging * (double)s->nc;
+            } catch (const std::exception&) {
+                tiled = false;
+            }
+        }
+    }
+    // the tile stages need the update to write the ghosts
+    if (s->precision == LFM_FP32_BULK &&
+        (tiled || s->nc <= (s->D == 2 ? kFuseGhostCells2D : kFuseGhostCells3D))) {
         // cells with boundary faces: their update writes the ghosts' next state
         std::vector<uint8_t> cg(nc, 0);
         for (size_t f = 0; f < nf; ++f)
@@ -371,6 +465,29 @@ int createSolver(const lfm_solver_desc* d, const lfm_solver_opts* opts, cudaStre
             for (size_t g = 0; g < ng; ++g) gp[g] = (int)d->ghost_patch[g];
             if ((rc = upload(s, &s->gPatch, gp.data(), ng))) return fail(rc);
         }
+    }
+    if (tiled) {
+        lfm::TileDesc* dT = nullptr;
+        int* dI = nullptr;
+        float* dF = nullptr;
+        uint8_t* dB = nullptr;
+        if ((rc = upload(s, &dT, tiles.tiles.data(), tiles.tiles.size()))) return fail(rc);
+        if ((rc = upload(s, &dI, tiles.ints.data(), tiles.ints.size()))) return fail(rc);
+        if ((rc = upload(s, &dF, tiles.floats.data(), tiles.floats.size()))) return fail(rc);
+        if ((rc = upload(s, &dB, tiles.bytes.data(), tiles.bytes.size()))) return fail(rc);
+        if ((rc = devAlloc(s, &s->prim1, (size_t)lfm::dev::primRows<float>(s->D) * nt))) return fail(rc);
+        s->tile.tiles = dT;
+        s->tile.ints = dI;
+        s->tile.floats = dF;
+        s->tile.bytes = dB;
+        s->tile.nTiles = (int)tiles.tiles.size();
+        s->tile.smemBytes = lfm::dev::tile_smem_bytes(s->D, tiles.maxL, tiles.maxLF, tileHaveV(s), tileHaveGrad(s));
+        s->tile.needGrad = s->needGrad ? 1 : 0;
+        s->tile.needVis = s->needVis ? 1 : 0;
+        s->tile.haveV = tileHaveV(s) ? 1 : 0;
+        s->tile.haveGrad = tileHaveGrad(s) ? 1 : 0;
+        s->tile.block = tiles.tileCells <= 128 ? 128 : 256;
+        s->tiled = true;
     }
     if (s->precision == LFM_FP32_BULK) {
         for (int v = 0; v < s->nq; ++v) s->qRef[v] = s->a32.qRef[v];
@@ -396,6 +513,7 @@ extern "C" void lfm_solver_destroy(lfm_solver* s) {
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
     if (s->graph) cudaGraphExecDestroy(s->graph);
+    if (s->graphOdd) cudaGraphExecDestroy(s->graphOdd);
     for (void* p : s->allocations) cudaFree(p);
     if (s->scrub) cudaFree(s->scrub);
     if (s->dPatches) cudaFree(s->dPatches);
@@ -428,6 +546,7 @@ extern "C" int lfm_solver_set_state(lfm_solver* s, const double* q) {
     }
     LFM_CUDA(cudaStreamSynchronize(s->stream));
     s->primsValid = false;
+    s->primParity = 0;
     s->ghostRowsValid = false;
     return LFM_OK;
 }
@@ -455,6 +574,7 @@ extern "C" int lfm_solver_stage(lfm_solver* s, int rk, double dt) {
     if (!s) return lfm::setError(LFM_ERR_INVALID, "null solver");
     if (rk < 0 || rk >= s->rkOrder) return lfm::setError(LFM_ERR_INVALID, "stage index out of range");
     LFM_CUDA(cudaSetDevice(s->device));
+    untile(s);
     int rc = ensurePrims(s);
     if (rc) return rc;
     s->lastStageB = s->rkB[(size_t)rk];
@@ -474,7 +594,7 @@ extern "C" int lfm_solver_step(lfm_solver* s, int nsteps, double dt) {
     int rc = ensureGraph(s, dt);
     if (rc) return rc;
     if ((rc = ensurePrims(s))) return rc;
-    for (int k = 0; k < nsteps; ++k) LFM_CUDA(cudaGraphLaunch(s->graph, s->stream));
+    for (int k = 0; k < nsteps; ++k) LFM_CUDA(launchStepGraph(s));
     return LFM_OK;
 }
 
@@ -839,7 +959,7 @@ extern "C" int lfm_solver_bench(lfm_solver* s, int nsteps, double dt, size_t flu
     for (int k = 0; k < nsteps; ++k) {
         if (flush_bytes) LFM_CUDA(cudaMemsetAsync(s->scrub, 0x5a + (k & 1), flush_bytes, s->stream));
         LFM_CUDA(cudaEventRecord(ev[2 * (size_t)k], s->stream));
-        LFM_CUDA(cudaGraphLaunch(s->graph, s->stream));
+        LFM_CUDA(launchStepGraph(s));
         LFM_CUDA(cudaEventRecord(ev[2 * (size_t)k + 1], s->stream));
     }
     LFM_CUDA(cudaStreamSynchronize(s->stream));
@@ -853,7 +973,7 @@ extern "C" int lfm_solver_launches_per_step(const lfm_solver* s, int* launches) 
     // preparation: every stage on the FP64 path; on the FP32-bulk path the
     // update writes the cells' and ghosts' primitives, so only halos remain
     const bool prep = s->precision != LFM_FP32_BULK || !s->a32.cellGhosts || s->nh > 0;
-    *launches = s->rkOrder * ((prep ? 1 : 0) + 2 + (s->needGrad ? 1 : 0) + (s->needVis ? 1 : 0));
+    *launches = s->tiled ? s->rkOrder : s->rkOrder * ((prep ? 1 : 0) + 2 + (s->needGrad ? 1 : 0) + (s->needVis ? 1 : 0));
     return LFM_OK;
 }
 
@@ -864,16 +984,21 @@ extern "C" const char* lfm_solver_kernel_name(int i) { return lfm::dev::kernelNa
 // host launch gaps between them), launched a few times, each after the L2
 // scrub of the benchmark loop when one exists; times averaged over launches.
 // Each stage also records an empty pair of event nodes: its time, the cost
-// of a pair of event nodes alone, is taken off every kernel's.
+// of a pair of event nodes alone, is taken off every kernel's. With tile
+// stages the graph holds two steps (so that it starts and ends on the same
+// primitive buffer) and the fused kernel's time goes to slot
+// kKernelsPerStage ("k_tile_stage").
 extern "C" int lfm_solver_profile_step(lfm_solver* s, double dt, int n, float* ms) {
-    if (!s || !ms || n < lfm::dev::kKernelsPerStage) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    if (!s || !ms || n < lfm::dev::kKernelSlots) return lfm::setError(LFM_ERR_INVALID, "bad argument");
     LFM_CUDA(cudaSetDevice(s->device));
     for (int k = 0; k < n; ++k) ms[k] = 0.f;
     int rc = ensurePrims(s);
     if (rc) return rc;
     const int K = lfm::dev::kKernelsPerStage;
     const int K1 = K + 1;   // slot K: the empty calibration pair
-    std::vector<cudaEvent_t> ev(2 * (size_t)s->rkOrder * (size_t)K1);
+    const int steps = s->tiled ? 2 : 1;
+    const int nStages = steps * s->rkOrder;
+    std::vector<cudaEvent_t> ev(2 * (size_t)nStages * (size_t)K1);
     for (auto& x : ev) LFM_CUDA(cudaEventCreate(&x));
     auto destroy = [&]() {
         for (auto& x : ev) cudaEventDestroy(x);
@@ -881,15 +1006,19 @@ extern "C" int lfm_solver_profile_step(lfm_solver* s, double dt, int n, float* m
     cudaGraph_t g = nullptr;
     cudaGraphExec_t ge = nullptr;
     cudaError_t e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
-    for (int k = 0; k < s->rkOrder && e == cudaSuccess; ++k) {
+    for (int kk = 0; kk < nStages && e == cudaSuccess; ++kk) {
+        const int k = kk % s->rkOrder;
         const StageConfig c = stageConfig(s, k, dt);
         for (int w = 0; w < K1 && e == cudaSuccess; ++w) {
-            const size_t base = 2 * ((size_t)k * (size_t)K1 + (size_t)w);
+            const size_t base = 2 * ((size_t)kk * (size_t)K1 + (size_t)w);
             e = cudaEventRecordWithFlags(ev[base], s->stream, cudaEventRecordExternal);
-            if (w < K && s->precision == LFM_FP32_BULK)
+            if (s->tiled) {
+                if (w == 0) tileStage(s, kk, dt, s->primParity);
+            } else if (w < K && s->precision == LFM_FP32_BULK) {
                 lfm::dev::launch_kernel<float>(s->a32, c, w, s->stream);
-            else if (w < K)
+            } else if (w < K) {
                 lfm::dev::launch_kernel<double>(s->a64, c, w, s->stream);
+            }
             if (e == cudaSuccess) e = cudaEventRecordWithFlags(ev[base + 1], s->stream, cudaEventRecordExternal);
         }
     }
@@ -906,13 +1035,17 @@ extern "C" int lfm_solver_profile_step(lfm_solver* s, double dt, int n, float* m
         if (s->scrub) e = cudaMemsetAsync(s->scrub, 0x5a + (r & 1), s->scrubBytes, s->stream);
         if (e == cudaSuccess) e = cudaGraphLaunch(ge, s->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-        for (int k = 0; k < s->rkOrder && e == cudaSuccess; ++k) {
+        for (int kk = 0; kk < nStages && e == cudaSuccess; ++kk) {
             float t[16] = {0};
             for (int w = 0; w < K1 && e == cudaSuccess; ++w) {
-                const size_t base = 2 * ((size_t)k * (size_t)K1 + (size_t)w);
+                const size_t base = 2 * ((size_t)kk * (size_t)K1 + (size_t)w);
                 e = cudaEventElapsedTime(&t[w], ev[base], ev[base + 1]);
             }
-            for (int w = 0; w < K && e == cudaSuccess; ++w) ms[w] += std::max(0.f, t[w] - t[K]) / kReps;
+            const float scale = 1.0f / (kReps * steps);
+            if (s->tiled)
+                ms[K] += std::max(0.f, t[0] - t[K]) * scale;
+            else
+                for (int w = 0; w < K && e == cudaSuccess; ++w) ms[w] += std::max(0.f, t[w] - t[K]) * scale;
         }
     }
     cudaGraphExecDestroy(ge);

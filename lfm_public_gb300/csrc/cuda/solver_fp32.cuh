@@ -160,12 +160,11 @@ __device__ __forceinline__ void prep32(const Args<float>& a, int t) {
 // (a ghost depends on its interior cell only), so no preparation pass over
 // the ghosts is needed; the values are those prep32 computes.
 // ---------------------------------------------------------------------------
-template <int D, bool RES, bool GH = false>
-__device__ __forceinline__ void update32(const Args<float>& a, int c, double Ak, double Bk, double dt,
-                                         float dt32, int first) {
+// gather32: the face rhs sum of cell c (ascending face order).
+template <int D>
+__device__ __forceinline__ void gather32(const Args<float>& a, int c, float* sum) {
     constexpr int NQ = D + 2;
-    const size_t nt = (size_t)a.nt, nf = (size_t)a.nf, nc = (size_t)a.nc;
-    float sum[NQ];
+    const size_t nf = (size_t)a.nf;
 #pragma unroll
     for (int v = 0; v < NQ; ++v) sum[v] = 0.0f;
     for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
@@ -179,6 +178,14 @@ __device__ __forceinline__ void update32(const Args<float>& a, int c, double Ak,
             for (int v = 0; v < NQ; ++v) sum[v] -= a.flux[v * nf + f];
         }
     }
+}
+
+// apply32: the update of cell c from its rhs sum (see update32).
+template <int D, bool RES, bool GH>
+__device__ __forceinline__ void apply32(const Args<float>& a, int c, const float* sum, double Ak, double Bk,
+                                        double dt, float dt32, int first) {
+    constexpr int NQ = D + 2;
+    const size_t nt = (size_t)a.nt, nc = (size_t)a.nc;
     const float dtvi = __fmul_rn(dt32, a.volInv32[c]);
     const float sg = a.sponge[c];
     const float dts = -__fmul_rn(dt32, sg);
@@ -210,6 +217,14 @@ __device__ __forceinline__ void update32(const Args<float>& a, int c, double Ak,
             if (j >= a.nc && j < a.nc + a.ng) ghost32<D>(a, j - a.nc, qa);
         }
     }
+}
+
+template <int D, bool RES, bool GH = false>
+__device__ __forceinline__ void update32(const Args<float>& a, int c, double Ak, double Bk, double dt,
+                                         float dt32, int first) {
+    float sum[D + 2];
+    gather32<D>(a, c, sum);
+    apply32<D, RES, GH>(a, c, sum, Ak, Bk, dt, dt32, first);
 }
 
 // Perturbation state q' = q - q_ref of cells [0, n) from a caller's absolute

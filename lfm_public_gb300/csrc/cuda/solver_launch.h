@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "solver_kernels.cuh"
+#include "tile_desc.h"
 
 namespace lfm {
 namespace dev {
@@ -73,10 +74,30 @@ void launch_forces(const Args<T>& a, QOffset qo, const double* gS, const double*
                    double Blast, const int* patches, int nPatches, double* terms, double* fp, double* fv,
                    cudaStream_t st);
 
+// Fused FP32-bulk stage over tiles (tile_kernels.cu).
+struct TileArgs {
+    const TileDesc* tiles;
+    const int* ints;
+    const float* floats;
+    const uint8_t* bytes;
+    const float* primIn;   // primitives at the stage start (the update writes the other buffer)
+    int nTiles;
+    int block;             // threads of a block
+    size_t smemBytes;      // dynamic shared memory of a block
+    int needGrad, needVis; // passes to run
+    int haveV, haveGrad;   // arrays the fluxes read (zero where not computed)
+};
+size_t tile_smem_bytes(int D, int maxL, int maxLF, bool haveV, bool haveGrad);
+// g: the solver's arguments with prim = the output primitive buffer.
+cudaError_t launch_tile_stage(const Args<float>& g, const TileArgs& t, const StageConfig& s, cudaStream_t st);
+
 constexpr int kKernelsPerStage = 5;  // prep, grad, vis, flux, update
+// Timing slots of lfm_solver_profile_step: the five kernels, then the fused
+// tile stage (which does the work of the five).
+constexpr int kKernelSlots = 6;
 inline const char* kernelName(int i) {
-    static const char* names[] = {"k_prep", "k_grad", "k_vis", "k_flux", "k_update"};
-    return (i >= 0 && i < kKernelsPerStage) ? names[i] : "";
+    static const char* names[] = {"k_prep", "k_grad", "k_vis", "k_flux", "k_update", "k_tile_stage"};
+    return (i >= 0 && i < kKernelSlots) ? names[i] : "";
 }
 
 }  // namespace dev

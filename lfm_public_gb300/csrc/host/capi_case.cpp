@@ -17,6 +17,7 @@
 #include "dictReaderOF.h"
 #include "polyMeshReaderOF.h"
 #include "renumber.h"
+#include "tiles.h"
 
 struct lfm_case {
     lfm::SolverCase sc;
@@ -210,6 +211,21 @@ extern "C" int lfm_case_cell_ids(const lfm_case* c, int64_t* out) {
 }
 
 extern "C" void lfm_case_free(lfm_case* c) { delete c; }
+
+extern "C" int lfm_tiles_stats(const lfm_solver_desc* d, int tile_cells, int max_local, int64_t* out) {
+    if (!d || !out) return lfm::setError(LFM_ERR_INVALID, "lfm_tiles_stats: null argument");
+    try {
+        const lfm::TileSet ts = lfm::buildTiles(d, tile_cells, max_local);
+        out[0] = (int64_t)ts.tiles.size();
+        out[1] = ts.maxL;
+        out[2] = ts.maxLF;
+        out[3] = ts.localCells;
+        out[4] = ts.fluxFaces;
+        return LFM_OK;
+    } catch (const std::exception& e) {
+        return lfm::setError(LFM_ERR_INVALID, e.what());
+    }
+}
 
 // ---- decomposed cases: all processor partitions of a case at once ----------
 

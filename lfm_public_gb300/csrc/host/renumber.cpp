@@ -187,8 +187,8 @@ std::vector<int> hilbertOrder(IMeshReader& r, const std::vector<int>& cells, int
             hi[k] = std::max(hi[k], xc[3 * i + (size_t)k]);
         }
     }
-    const int bits = dim == 2 ? 16 : 21;
-    const double top = (double)((1u << bits) - 1);
+    const int bits = dim == 2 ? 31 : 21;   // 62- and 63-bit keys: fine enough for stretched meshes
+    const double top = (double)((1ull << bits) - 1);
     std::vector<uint64_t> key(n);
     for (size_t i = 0; i < n; ++i) {
         uint32_t u[3];

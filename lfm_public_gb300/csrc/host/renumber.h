@@ -28,7 +28,7 @@ int renumberFromName(const std::string& name);
 //        (George-Liu), neighbours visited in increasing degree; minimises
 //        the bandwidth max |i - j| over faces.
 //   Hilbert: cells sorted along a Hilbert curve through their centres (2D
-//        on a 2^16 grid of the bounding box, 3D on 2^21 per axis).
+//        on a 2^31 grid of the bounding box, 3D on 2^21 per axis).
 void renumberCells(IMeshReader& r, std::vector<int>& cells, int method, int dim);
 
 // Bandwidth of an order: max |pos(a) - pos(b)| over faces between cells of

@@ -136,3 +136,35 @@ def test_integer_pipe_conversions_match_ieee():
     nan32 = np.isnan(r32.view(np.float32))
     assert np.array_equal(o32[~nan32], r32[~nan32])
     assert np.all(np.isnan(o32[nan32].view(np.float32)))
+
+
+@pytest.mark.parametrize("make,tiled", [
+    (lambda: cases.cylinder_case(n_theta=96, n_r=64, r1=30, first=0.01, Ls=8, solver=0, minmod=True, noise=0.02),
+     True),
+    (lambda: cases.cylinder_case(n_theta=64, n_r=32, r1=20, first=0.02, Ls=5, solver=2, minmod=True, noise=0.02),
+     True),
+    (lambda: cases.tri_case(n=40, seed=9, solver=1, beta=4.0), True),
+    # a small 3D mesh stages over 8 cells per tile cell: the solver keeps the
+    # separate kernels
+    (lambda: cases.cylinder_case(n_theta=24, n_r=12, r1=8, first=0.04, Ls=3, solver=1, n_span=6, noise=0.01),
+     False),
+])
+def test_fused_tile_stages_are_bitwise_the_separate_kernels(make, tiled, monkeypatch):
+    """The fused tile stage (one kernel per stage, tile data staged in shared
+    memory; opt-in) gives the bits of the separate kernels."""
+    case = make()
+    ch = N.CaseHandle.from_case(case, renumber=N.LFM_RENUMBER_HILBERT)
+    n = 7   # odd: the run ends on the second primitive buffer
+    monkeypatch.setenv("LFM_TILE_CELLS", "0")
+    q0 = _run(ch, n, case.delta_t, N.LFM_FP32_BULK)
+    monkeypatch.setenv("LFM_TILE_CELLS", "128")
+    s = N.Solver(ch, precision=N.LFM_FP32_BULK)
+    assert (s.launches_per_step() == ch.desc.rk_order) == tiled   # one fused kernel per stage
+    s.step(n, case.delta_t)
+    s.sync()
+    q1 = s.get_state()
+    # stepping on after a single-stage call (primitives rebuilt in buffer 0)
+    s.stage(0, case.delta_t)
+    s.sync()
+    s.close()
+    assert np.array_equal(q0, q1)

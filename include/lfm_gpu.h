@@ -102,6 +102,10 @@ typedef struct lfm_solver_desc {
      * wall-force post-processing (may be NULL: lfm_solver_forces is then
      * unavailable). */
     const int32_t* ghost_patch;    /* [n_ghosts] */
+    /* Smagorinsky LES (turbulenceProperties simulationType other than
+     * laminar; calc_VIS_Smagorinsky, src/cfd_v0.cpp:1573-1737): each cell's
+     * model constant -2 (0.16 (1/vol_inv)^(1/3))^2, or NULL for laminar. */
+    const double* smag_c;          /* [n_cells] */
 } lfm_solver_desc;
 
 typedef struct lfm_case lfm_case;

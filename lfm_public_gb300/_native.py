@@ -48,7 +48,7 @@ class SolverDesc(C.Structure):
         ("pInf", C.c_double), ("TInf", C.c_double), ("UInf", C.c_double * 3), ("mu", C.c_double), ("Cp", C.c_double),
         ("PrInv", C.c_double), ("rkA", _dp), ("rkB", _dp),
         ("n_halos", C.c_int64), ("halo_src_part", _i64p), ("halo_src_cell", _i64p),
-        ("ghost_patch", C.POINTER(C.c_int32)),
+        ("ghost_patch", C.POINTER(C.c_int32)), ("smag_c", _dp),
     ]
 
 
@@ -282,7 +282,7 @@ class CaseHandle:
                      n_cells=case.n_cells)
         pr = case.params()
         prm = Params(solver=pr["solver"], dimension=pr["dimension"], rk_order=pr["rk_order"], minmod=pr["minmod"],
-                     laminar=1, residuals=pr["residuals"], p_inf=pr["p_inf"], T_inf=pr["T_inf"],
+                     laminar=pr["laminar"], residuals=pr["residuals"], p_inf=pr["p_inf"], T_inf=pr["T_inf"],
                      U_inf=(C.c_double * 3)(*pr["U_inf"]), Ls=pr["Ls"], mach=pr["mach"], k_sponge=pr["k_sponge"],
                      Cp=pr["Cp"], mol_weight=pr["mol_weight"], mu=pr["mu"], Pr=pr["Pr"], renumber=renumber)
         p = np.ascontiguousarray(case.fields["p"], dtype=np.float64)

@@ -62,6 +62,7 @@ class Case:
     rk_order: int = 5
     minmod: bool = False
     residuals: bool = False
+    laminar: bool = True          # False: Smagorinsky LES viscous terms (turbulenceProperties LES)
     p_inf: float = 101325.0
     T_inf: float = 300.0
     U_inf: Tuple[float, float, float] = (0.0, 0.0, 0.0)
@@ -95,7 +96,7 @@ class Case:
 
     def params(self) -> dict:
         return dict(solver=self.solver, dimension=self.dim, rk_order=self.rk_order, minmod=int(self.minmod),
-                    laminar=1, residuals=int(self.residuals), p_inf=self.p_inf, T_inf=self.T_inf,
+                    laminar=int(self.laminar), residuals=int(self.residuals), p_inf=self.p_inf, T_inf=self.T_inf,
                     U_inf=tuple(self.U_inf), Ls=self.Ls, mach=self.mach, k_sponge=self.k_sponge, Cp=self.Cp,
                     mol_weight=self.mol_weight, mu=self.mu, Pr=self.Pr)
 
@@ -674,7 +675,7 @@ def write_case(case: Case, root: str, n_steps: Optional[int] = None, write_inter
                 f"        Pr              {_fmt(case.Pr)};\n    }}\n}}\n")
     with open(os.path.join(root, "constant", "turbulenceProperties"), "w") as f:
         f.write(_header("dictionary", "turbulenceProperties", "constant"))
-        f.write("simulationType  laminar;\n")
+        f.write("simulationType  " + ("laminar" if case.laminar else "LES") + ";\n")
     return root
 
 

@@ -316,6 +316,10 @@ int prepareCase(const lfm_solver_desc* d, double dt, int rkOrder, PreparedCase**
         return lfm::setError(LFM_ERR_INVALID, "case rk_order " + std::to_string(d->rk_order) +
                                                   " differs from the batch's " + std::to_string(rkOrder));
     if (!(dt > 0.0)) return lfm::setError(LFM_ERR_INVALID, "dt must be positive");
+    if (d->smag_c)
+        return lfm::setError(LFM_ERR_UNSUPPORTED, "Smagorinsky LES cases run in the single-case solver, not in a batch");
+    if (d->n_halos > 0)
+        return lfm::setError(LFM_ERR_UNSUPPORTED, "partitions of a decomposed case run in an lfm_partitioned");
     PreparedCase* pc = new PreparedCase(d);
     BatchCase& bc = pc->bc;
     std::memset(&bc, 0, sizeof(bc));
@@ -384,6 +388,7 @@ int commitCase(lfm_batch* b, const PreparedCase& pc, int* slot) {
     a.cfOff = reinterpret_cast<const int*>(P(L.cfOff));
     a.cfList = reinterpret_cast<const int*>(P(L.cfList));
     a.cellGhosts = reinterpret_cast<const uint8_t*>(P(L.cellGhosts));
+    a.smagC = nullptr;
     a.gCell = reinterpret_cast<const int*>(P(L.gCell));
     a.gKind = reinterpret_cast<const int*>(P(L.gKind));
     a.gFace = reinterpret_cast<const int*>(P(L.gFace));

@@ -155,11 +155,12 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
     a.gFace = gFace;
     a.flag = s->flag;
     a.cellGhosts = nullptr;
+    a.smagC = nullptr;
     const size_t nt = (size_t)s->nt, nf = (size_t)s->nf, D = (size_t)s->D;
     int rc;
     if ((rc = devAlloc(s, &a.dq, (size_t)s->nq * s->nc))) return rc;
     if ((rc = devAlloc(s, &a.prim, (size_t)lfm::dev::primRows<T>(s->D) * nt))) return rc;
-    if ((rc = devAlloc(s, &a.V, (D * D + 2 * D) * nt))) return rc;
+    if ((rc = devAlloc(s, &a.V, (D * D + 2 * D + (d->smag_c ? D * D : 0)) * nt))) return rc;
     // M2AUSM always reads the gradients (all zero when minmod is off, as in the
     // reference, whose prepare_for_RKstep zeroes them every stage).
     if ((rc = devAlloc(s, &a.grad, (2 * D + D * D) * (s->scheme == LFM_SOLVER_M2AUSM ? nt : 1)))) return rc;
@@ -183,6 +184,21 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
     a.K = p;
     if ((rc = uploadAs<T>(s, &p, d->sponge, (size_t)s->nc))) return rc;
     a.sponge = p;
+    if (d->smag_c) {
+        // Smagorinsky LES: a cell's tauMC ends with the constant of the cell
+        // that visits it last in the reference's face loop, the owner of the
+        // last face (in processing order) it touches - itself unless it owns
+        // no face (calc_VIS_Smagorinsky, src/cfd_v0.cpp:1596-1737)
+        std::vector<double> cf((size_t)s->nc);
+        for (int64_t c = 0; c < s->nc; ++c) {
+            int64_t last = -1;
+            for (int64_t e = d->cell_face_offsets[c]; e < d->cell_face_offsets[c + 1]; ++e)
+                last = std::max<int64_t>(last, d->cell_faces[e]);
+            cf[(size_t)c] = d->smag_c[last >= 0 ? d->face_p[last] : c];
+        }
+        if ((rc = uploadAs<T>(s, &p, cf.data(), cf.size()))) return rc;
+        a.smagC = p;
+    }
     {
         std::vector<double> lapc(nf);
         for (size_t f = 0; f < nf; ++f) lapc[f] = d->delta_mag[f] * d->dmag_inv[f];
@@ -426,7 +442,7 @@ int createSolver(const lfm_solver_desc* d, const lfm_solver_opts* opts, cudaStre
     // fused tile stages: FP32-bulk without halos, when a block's tile fits
     lfm::TileSet tiles;
     bool tiled = false;
-    if (s->precision == LFM_FP32_BULK && s->nh == 0) {
+    if (s->precision == LFM_FP32_BULK && s->nh == 0 && !d->smag_c) {
         const int tc = tileCellsOption();
         if (tc > 0) {
             try {
@@ -712,7 +728,7 @@ int residualNoalloc(const lfm_solver* s, const Args<T>& base, const double* q, i
     auto round = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t bq = round(nq * nt * sizeof(double));
     const size_t bPrim = round((size_t)lfm::dev::primRows<T>(s->D) * nt * sizeof(T));
-    const size_t bV = round((D * D + 2 * D) * nt * sizeof(T));
+    const size_t bV = round((D * D + 2 * D + (base.smagC ? D * D : 0)) * nt * sizeof(T));
     const size_t bGrad = ausm ? round((2 * D + D * D) * nt * sizeof(T)) : 0;
     const size_t bFlux = round(nq * nf * sizeof(T));
     const size_t need = bq + bPrim + bV + bGrad + bFlux;
@@ -1101,7 +1117,7 @@ void partitionedStages(lfm_partitioned* P, double dt) {
         if (s0->needVis)
             for (size_t p = 0; p < np; ++p) {
                 const lfm_solver* s = P->parts[p];
-                const int rows = s->D * s->D + 2 * s->D;
+                const int rows = s->D * s->D + 2 * s->D + (args(p).smagC ? s->D * s->D : 0);
                 lfm::dev::launch_halo_gather<T>(args(p).V, s->nt, s->nc + s->ng, rows, s->nh, P->haloPart[p],
                                                 P->haloCell[p], reinterpret_cast<T* const*>(P->dV), P->dNt,
                                                 P->stream);

@@ -38,6 +38,37 @@ __device__ __forceinline__ void stress(const T g[D][D], T mu, T tau[D][D]) {
     }
 }
 
+// Smagorinsky subgrid stress added to a cell's tauMC (calc_VIS_Smagorinsky,
+// src/cfd_v0.cpp:1675-1695): -C |S| S_ab + (C |S| div u / 3) delta_ab with
+// S the symmetric part of the velocity gradient g, |S| = sqrt(2 S_ab S_ab)
+// and C = -2 (0.16 Delta)^2 the cell's model constant.
+template <typename T, int D>
+__device__ __forceinline__ void sgs_stress(const T g[D][D], T C, T out[D][D]) {
+    T sm = T(0), divu = T(0);
+#pragma unroll
+    for (int x = 0; x < D; ++x) {
+#pragma unroll
+        for (int y = 0; y < D; ++y) {
+            const T s = T(0.5) * (g[x][y] + g[y][x]);
+            sm += s * s;
+        }
+        divu += g[x][x];
+    }
+    sm = sqrt(T(2) * sm);
+    const T cs = C * sm;
+#pragma unroll
+    for (int x = 0; x < D; ++x) {
+#pragma unroll
+        for (int y = 0; y < D; ++y) out[x][y] = -(cs * (T(0.5) * (g[x][y] + g[y][x])));
+        out[x][x] += cs * divu / T(3);
+    }
+}
+
+// Rows of the per-cell viscous array: dudx (D x D), dTdx, sigmaU, then with
+// Smagorinsky LES the SGS stress (D x D).
+template <int D>
+constexpr int kVisRows = D * D + 2 * D;
+
 // Minmod-limited face reconstruction from the upwind side (calc_r and
 // interp_minmod, api/cfdv0_solver.h:310-370): flux = +1 reconstructs from P,
 // -1 from N.

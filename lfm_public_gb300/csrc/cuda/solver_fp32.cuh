@@ -335,6 +335,14 @@ __device__ __forceinline__ void vis32(const Args<float>& a, int c) {
         a.V[(size_t)(D * D + x) * nt + c] = gT[x];
         a.V[(size_t)(D * D + D + x) * nt + c] = dotv<float, D>(U, tau[x]);
     }
+    if (a.smagC) {   // Smagorinsky LES: the cell's SGS stress
+        float sg[D][D];
+        sgs_stress<float, D>(g, a.smagC[c], sg);
+#pragma unroll
+        for (int x = 0; x < D; ++x)
+#pragma unroll
+            for (int y = 0; y < D; ++y) a.V[(size_t)(kVisRows<D> + x * D + y) * nt + c] = sg[x][y];
+    }
 }
 
 // d(M) = p5pos(M) - p5neg(M) is, for |M| < 1, the odd polynomial
@@ -537,6 +545,18 @@ __device__ __forceinline__ void flux32(const Args<float>& a, int f) {
             rhs[x + 1] += mu * gtS + dsum * S[x] + mu * (lapc * (uj[x] - ui[x]) + dotv<float, D>(Kf, g[x]));
         }
         rhs[D + 1] += dotv<float, D>(sU, S) + kc * (lapc * (Tj - Ti) + dotv<float, D>(Kf, gT));
+        if (a.smagC && !a.fGhost[f]) {   // Smagorinsky LES, as in the FP64 kernel
+#pragma unroll
+            for (int x = 0; x < D; ++x) {
+                float s = 0.0f;
+#pragma unroll
+                for (int y = 0; y < D; ++y)
+                    s += interp(w, a.V[(size_t)(kVisRows<D> + x * D + y) * nt + i],
+                                a.V[(size_t)(kVisRows<D> + x * D + y) * nt + j]) *
+                         S[y];
+                rhs[x + 1] += s;
+            }
+        }
     }
 #pragma unroll
     for (int v = 0; v < NQ; ++v) a.flux[(size_t)v * nf + f] = rhs[v];

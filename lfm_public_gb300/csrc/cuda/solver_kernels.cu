@@ -127,6 +127,14 @@ __global__ void __launch_bounds__(256) k_vis(Args<T> a) {
         a.V[(size_t)(D * D + x) * nt + c] = gT[x];
         a.V[(size_t)(D * D + D + x) * nt + c] = dotv<T, D>(U, tau[x]);
     }
+    if (a.smagC) {   // Smagorinsky LES: the cell's SGS stress
+        T sg[D][D];
+        sgs_stress<T, D>(g, a.smagC[c], sg);
+#pragma unroll
+        for (int x = 0; x < D; ++x)
+#pragma unroll
+            for (int y = 0; y < D; ++y) a.V[(size_t)(kVisRows<D> + x * D + y) * nt + c] = sg[x][y];
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -337,6 +345,20 @@ __global__ void __launch_bounds__(128) k_flux(Args<T> a) {
         }
         const T lapT = kc * (lapc * (aT - cT) + dotv<T, D>(Kf, gT));
         rhs[D + 1] += dotv<T, D>(sU, S) + lapT;
+        // Smagorinsky LES: the face tauMC also interpolates the cells' SGS
+        // stress (boundary faces keep the laminar two-point one, as in the
+        // reference)
+        if (a.smagC && !ghost) {
+#pragma unroll
+            for (int x = 0; x < D; ++x) {
+                T s = T(0);
+#pragma unroll
+                for (int y = 0; y < D; ++y)
+                    s += interp(w, a.V[(kVisRows<D> + x * D + y) * nt + i], a.V[(kVisRows<D> + x * D + y) * nt + j]) *
+                         S[y];
+                rhs[x + 1] += s;
+            }
+        }
     }
 #pragma unroll
     for (int v = 0; v < NQ; ++v) a.flux[v * nf + f] = rhs[v];

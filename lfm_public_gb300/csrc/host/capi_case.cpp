@@ -68,10 +68,6 @@ static int validateParams(const lfm::CaseParams& p) {
     if (p.solver < 0 || p.solver > 2) return lfm::setError(LFM_ERR_INVALID, "unknown solver type " + std::to_string(p.solver));
     if (p.dimension != 2 && p.dimension != 3)
         return lfm::setError(LFM_ERR_INVALID, "invalid dimension " + std::to_string(p.dimension));
-    if (!p.laminar)
-        return lfm::setError(LFM_ERR_UNSUPPORTED,
-                             "turbulenceProperties simulationType must be laminar (the Smagorinsky viscous pass is "
-                             "not part of this build)");
     if (p.rkOrder < 0 || p.rkOrder > 5) return lfm::setError(LFM_ERR_INVALID, "rkOrder must be 0..5");
     if (p.renumber < LFM_RENUMBER_NONE || p.renumber > LFM_RENUMBER_HILBERT)
         return lfm::setError(LFM_ERR_INVALID, "unknown renumbering (none, rcm or hilbert)");

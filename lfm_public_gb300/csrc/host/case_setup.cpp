@@ -342,6 +342,14 @@ SolverCase buildSolverCase(IMeshReader& r, const CaseParams& prm, const HaloLook
     sc.volInv.resize((size_t)nc);
     sc.sponge.assign((size_t)nc, 0.0);
     for (int64_t c = 0; c < nc; ++c) sc.volInv[(size_t)c] = 1.0 / r.getCellVolume((int)sc.cellId[(size_t)c]);
+    if (!prm.laminar) {
+        // Smagorinsky model constant of each cell, -2 (Cs Delta)^2 with
+        // Cs = 0.16 and Delta = V^(1/3), evaluated as calc_VIS_Smagorinsky
+        // does (src/cfd_v0.cpp:1601)
+        sc.smagC.resize((size_t)nc);
+        for (int64_t c = 0; c < nc; ++c)
+            sc.smagC[(size_t)c] = -(double)2.0 * std::pow((double)0.16 * std::pow(1.0 / sc.volInv[(size_t)c], 1. / 3.), 2);
+    }
     if (prm.Ls > 0) {
         const double sigma0 = 3.0 * (1.0 - prm.mach * prm.mach) / (prm.kSponge * prm.Ls);
         const int ia = r.readScalarField("alpha");
@@ -449,6 +457,7 @@ void describeSolverCase(const SolverCase& s, lfm_solver_desc* d) {
     d->halo_src_part = s.haloSrcPart.empty() ? nullptr : s.haloSrcPart.data();
     d->halo_src_cell = s.haloSrcCell.empty() ? nullptr : s.haloSrcCell.data();
     d->ghost_patch = s.ghostPatch.data();
+    d->smag_c = s.smagC.empty() ? nullptr : s.smagC.data();
 }
 
 namespace {

@@ -63,6 +63,7 @@ struct SolverCase {
     // cells (solver order) -----------------------------------------------------
     std::vector<int64_t> cellId;         // polyMesh cell label
     std::vector<double> volInv, sponge;  // per cell
+    std::vector<double> smagC;           // per cell, Smagorinsky LES only (see lfm_solver_desc)
     std::vector<double> q0;              // initial state, nq x nCells (SoA)
 
     // boundary ghosts ------------------------------------------------------------

@@ -96,10 +96,6 @@ int GpuMesh::initializeSolver() {
     p.molWeight = m_pInput->m_dMolWeight;
     p.mu = m_pInput->m_dMu0;
     p.Pr = m_pInput->m_dPrandtl;
-    if (!p.laminar) {
-        std::cerr << "Only laminar simulations run on the device path" << std::endl;
-        return 2;
-    }
     try {
         if (m_nPartitions <= 0) {
             m_parts[0].sc = new lfm::SolverCase(lfm::buildSolverCase(*m_parts[0].reader, p));
@@ -269,7 +265,8 @@ void GpuMesh::solve() {
               << "\n    - flux faces   : " << faces
               << "\n~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~~\n";
     static const char* schemes[] = {"M1", "M2", "M2 AUSM"};
-    std::cout << "Running with " << schemes[c0.solver] << " discretization\nLaminar simulation\n" << std::endl;
+    std::cout << "Running with " << schemes[c0.solver] << " discretization\n"
+              << (c0.smagC.empty() ? "Laminar simulation" : "LES simulation (Smagorinsky)") << "\n" << std::endl;
 
     static const char* resNames[] = {"uRES", "vRES", "wRES"};
     const bool saveRes = m_pInput->m_bHaveResidual && m_pInput->m_bSaveResiduals;

@@ -10,6 +10,7 @@
  *   set_boundary_conditions   src/cfd_v0.cpp:1009-1221
  *   calc_gradients_M2AUSM     src/cfd_v0.cpp:1383-1495 (the gradients M2AUSM reads)
  *   calc_VIS                  src/cfd_v0.cpp:1743-1860
+ *   calc_VIS_Smagorinsky      src/cfd_v0.cpp:1573-1737 (desc->smag_c set)
  *   one_rk_step_M2            src/cfd_v0.cpp:1896-2179
  *   one_rk_step_M2AUSM        src/cfd_v0.cpp:2185-2523, p5Pos/p5Neg :1862-1894,
  *                             calc_r / interp_minmod api/cfdv0_solver.h:306-370
@@ -87,8 +88,10 @@ static void stress(const double* g, double mu, int D, double tau[MAXD][MAXD]) {
     }
 }
 
-/* tauMC and sigmaU of a cell from its current dudx (src/cfd_v0.cpp:1813-1857). */
-static void viscous_derived(Port* P, int64_t i, const double* U, double mu) {
+/* tauMC and sigmaU of a cell from its current dudx (src/cfd_v0.cpp:1813-1857);
+ * with a Smagorinsky constant C (smag, or NULL for laminar) the SGS terms of
+ * calc_VIS_Smagorinsky (src/cfd_v0.cpp:1675-1695) are added to tauMC. */
+static void viscous_derived(Port* P, int64_t i, const double* U, double mu, const double* smag) {
     const int D = P->D;
     const double* g = &P->dudx[i * D * D];
     double tau[MAXD][MAXD];
@@ -100,6 +103,25 @@ static void viscous_derived(Port* P, int64_t i, const double* U, double mu) {
         P->sigmaU[i * D + a] = dot(U, tau[a], D);
         for (int b = 0; b < D; ++b) P->tauMC[i * D * D + a * D + b] = mu * g[b * D + a];
         P->tauMC[i * D * D + a * D + a] += diagSum;
+    }
+    if (smag) {
+        const double C = *smag;
+        double strainMag = 0.0, divu = 0.0;
+        for (int a = 0; a < D; ++a) {
+            for (int b = 0; b < D; ++b) {
+                const double sij = 0.5 * (g[a * D + b] + g[b * D + a]);
+                strainMag += pow(sij, 2);
+            }
+            divu += g[a * D + a];
+        }
+        strainMag = sqrt(2.0 * strainMag);
+        for (int a = 0; a < D; ++a) {
+            for (int b = 0; b < D; ++b) {
+                const double sij = 0.5 * (g[a * D + b] + g[b * D + a]);
+                P->tauMC[i * D * D + a * D + b] -= C * strainMag * sij;
+            }
+            P->tauMC[i * D * D + a * D + a] += C * strainMag * divu / 3.0;
+        }
     }
 }
 
@@ -227,8 +249,11 @@ static void calc_VIS(Port* P) {
             cU[k] = Q(P, k + 1, i) / Q(P, 0, i);
             aU[k] = Q(P, k + 1, j) / Q(P, 0, j);
         }
-        viscous_derived(P, i, cU, mu);
-        viscous_derived(P, j, aU, mu);
+        /* the owner's constant for both sides, as calc_VIS_Smagorinsky
+         * computes it once per visiting cell (src/cfd_v0.cpp:1601) */
+        const double* smag = c->smag_c ? &c->smag_c[i] : NULL;
+        viscous_derived(P, i, cU, mu, smag);
+        viscous_derived(P, j, aU, mu, smag);
     }
 }
 

@@ -50,6 +50,11 @@ FIXTURES = {
                                                     noise=0.01), 10),
     "tri8_m1": (cases.tri_case, dict(n=8, seed=3), 20),
     "tri8_m2": (cases.tri_case, dict(n=8, seed=4, solver=1), 20),
+    # Smagorinsky LES (turbulenceProperties simulationType LES)
+    "les_cyl24x12_m2": (cases.cylinder_case, dict(n_theta=24, n_r=12, r1=10, first=0.05, Ls=3, solver=1,
+                                                  minmod=False, noise=0.05, reynolds=50.0), 20),
+    "les_cyl16x8x4_m1_3d": (cases.cylinder_case, dict(n_theta=16, n_r=8, r1=10, first=0.05, Ls=3, solver=0,
+                                                      n_span=4, noise=0.05, reynolds=50.0), 10),
 }
 
 
@@ -64,8 +69,8 @@ def case_to_arrays(case: cases.Case) -> dict:
                patch_neighbour=np.array([p.neighbour or "" for p in case.patches]))
     for k, v in case.fields.items():
         out["field_" + k] = v
-    for k in ("solver", "rk_order", "minmod", "residuals", "p_inf", "T_inf", "Ls", "mach", "k_sponge", "Cp",
-              "mol_weight", "mu", "Pr", "delta_t"):
+    for k in ("solver", "rk_order", "minmod", "residuals", "laminar", "p_inf", "T_inf", "Ls", "mach", "k_sponge",
+              "Cp", "mol_weight", "mu", "Pr", "delta_t"):
         out["param_" + k] = np.float64(getattr(case, k))
     out["param_U_inf"] = np.array(case.U_inf, dtype=np.float64)
     return out
@@ -83,6 +88,7 @@ def arrays_to_case(z) -> cases.Case:
         setattr(c, k, int(z["param_" + k]))
     for k in ("minmod", "residuals"):
         setattr(c, k, bool(z["param_" + k]))
+    c.laminar = bool(z["param_laminar"]) if "param_laminar" in z.files else True
     for k in ("p_inf", "T_inf", "Ls", "mach", "k_sponge", "Cp", "mol_weight", "mu", "Pr", "delta_t"):
         setattr(c, k, float(z["param_" + k]))
     c.U_inf = tuple(float(x) for x in z["param_U_inf"])
@@ -167,6 +173,8 @@ def main():
         case = gen(n_steps=n, **kw)
         if name.endswith("_res"):
             case.residuals = True
+        if name.startswith("les_"):
+            case.laminar = False
         tmp = tempfile.mkdtemp(prefix="lfm_golden_")
         try:
             res, cfl, _ = run_reference(case, n, tmp)

@@ -168,3 +168,22 @@ def test_fused_tile_stages_are_bitwise_the_separate_kernels(make, tiled, monkeyp
     s.sync()
     s.close()
     assert np.array_equal(q0, q1)
+
+
+def test_smagorinsky_les_fp32_bulk_and_batch():
+    """Smagorinsky LES: the FP32-bulk form stays within the acoustic bar of
+    the FP64 path (which the les_* fixtures pin to the reference); the batch
+    engine refuses LES cases."""
+    from tests.helpers import load_golden
+    case, _ = load_golden("les_cyl24x12_m2")
+    assert not case.laminar
+    ch = N.CaseHandle.from_case(case)
+    assert ch.desc.smag_c
+    q64 = _run(ch, 40, case.delta_t, N.LFM_FP64)
+    q32 = _run(ch, 40, case.delta_t, N.LFM_FP32_BULK)
+    err = acoustics.acoustic_rel_l2(q32, q64, ch.desc.gamma, case.dim, case.p_inf)
+    assert err <= ACOUSTIC_TOL, err
+    b = N.Batch(arena_bytes=64 << 20, max_cases=2)
+    with pytest.raises(N.LfmError):
+        b.add(ch, case.delta_t)
+    b.close()

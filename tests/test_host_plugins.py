@@ -125,12 +125,20 @@ def test_missing_mandatory_key(tmpdir_case):
     assert "Ls" in str(e.value)
 
 
-def test_turbulent_case_is_unsupported(tmpdir_case):
+def test_turbulent_case_selects_smagorinsky(tmpdir_case):
+    """simulationType other than laminar: the Smagorinsky LES viscous pass
+    (calc_VIS_Smagorinsky): every cell gets its model constant
+    -2 (0.16 V^(1/3))^2."""
     case = cases.vortex_case(n=6)
     _write_dicts(tmpdir_case, case, edits=[("constant/turbulenceProperties", "laminar", "LES")])
-    with pytest.raises(N.LfmError) as e:
-        N.CaseHandle.open(tmpdir_case)
-    assert e.value.code == -6
+    ch = N.CaseHandle.open(tmpdir_case)
+    d = ch.desc
+    c = np.ctypeslib.as_array(d.smag_c, shape=(d.n_cells,))
+    vol = 1.0 / np.ctypeslib.as_array(d.vol_inv, shape=(d.n_cells,))
+    np.testing.assert_allclose(c, -2.0 * (0.16 * vol ** (1.0 / 3.0)) ** 2, rtol=1e-15)
+    lam = cases.vortex_case(n=6)
+    _write_dicts(tmpdir_case, lam)
+    assert not N.CaseHandle.open(tmpdir_case).desc.smag_c
 
 
 def test_bad_solver_id(tmpdir_case):

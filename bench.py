@@ -469,8 +469,8 @@ def run_batch(args):
     b = N.Batch(device=local, arena_bytes=need + (64 << 20), max_cases=n_cases)
     slots = [b.add(ch, c.delta_t) for c, ch in built]
     if args.tuning:
-        blk, ipt, bps = (int(x) for x in args.tuning.split(","))
-        b.set_tuning(blk, ipt, bps)
+        v = [int(x) for x in args.tuning.split(",")]
+        b.set_tuning(v[0], v[1], v[2], phased=v[3] if len(v) > 3 else 0)
         tuning = b.tuning()
     else:
         tuning = b.autotune(trial_steps=2)
@@ -730,7 +730,7 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=None,
                     help="steps of the FP32-bulk vs FP64 comparison (default 1000; 200 for batch64)")
     ap.add_argument("--batch-cases", type=int, default=64)
-    ap.add_argument("--tuning", default=None, help="batch launch shape block,items_per_thread,blocks_per_sm "
+    ap.add_argument("--tuning", default=None, help="batch launch shape block,items_per_thread,blocks_per_sm[,phased] "
                                                    "(default: autotuned)")
     ap.add_argument("--serve-rates", default="5,20,100", help="request arrival rates (1/s) of the serving stream")
     ap.add_argument("--serve-requests", type=int, default=24)

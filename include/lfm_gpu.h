@@ -389,6 +389,10 @@ typedef struct lfm_batch_tuning {
     int items_per_thread; /* cells or faces per thread and tile (tile = block x items) */
     int blocks_per_sm;    /* resident blocks per SM of the persistent grid; 0 = all that fit */
     int cooperative;      /* 1: cooperative launch (co-residency guaranteed by the driver) */
+    /* 1: one kernel per phase instead of the persistent stage kernel (no
+     * grid barriers; each phase at its own occupancy; blocks_per_sm then
+     * caps each phase kernel's grid, 0 = all that fit) */
+    int phased;
 } lfm_batch_tuning;
 
 int lfm_batch_create(const lfm_batch_opts* opts, lfm_batch** out);

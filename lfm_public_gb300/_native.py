@@ -85,7 +85,7 @@ class BatchOpts(C.Structure):
 
 class BatchTuning(C.Structure):
     _fields_ = [("block", C.c_int), ("items_per_thread", C.c_int), ("blocks_per_sm", C.c_int),
-                ("cooperative", C.c_int)]
+                ("cooperative", C.c_int), ("phased", C.c_int)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -621,9 +621,10 @@ class Batch:
         check(load_library().lfm_batch_get_tuning(self._h, C.byref(t)))
         return t.as_dict()
 
-    def set_tuning(self, block: int, items_per_thread: int = 1, blocks_per_sm: int = 0, cooperative: int = 1):
+    def set_tuning(self, block: int, items_per_thread: int = 1, blocks_per_sm: int = 0, cooperative: int = 1,
+                   phased: int = 0):
         t = BatchTuning(block=block, items_per_thread=items_per_thread, blocks_per_sm=blocks_per_sm,
-                        cooperative=cooperative)
+                        cooperative=cooperative, phased=phased)
         check(load_library().lfm_batch_set_tuning(self._h, C.byref(t)))
 
     def autotune(self, trial_steps: int = 2) -> dict:

@@ -65,6 +65,11 @@ cudaError_t launch_batch_stage(const BatchArgs& b, int stage, int block, int var
                                cudaStream_t st);
 // Resident blocks per SM of the stage kernel at `block` threads.
 int batch_blocks_per_sm(int block, int variant);
+// Stage `stage` as one kernel per phase (grid-stride over each phase's
+// tiles, kernel boundaries in place of the grid barriers); each kernel's grid
+// is bps (0 = all that fit) resident blocks per SM x sms.
+cudaError_t launch_batch_phased(const BatchArgs& b, int stage, int block, int variant, int bps, int sms,
+                                cudaStream_t st);
 
 }  // namespace dev
 }  // namespace lfm

@@ -170,7 +170,7 @@ struct lfm_batch {
     int* dNTiles = nullptr;
     std::vector<lfm::batch::Slot> slots;
     int sms = 0;
-    lfm_batch_tuning tune{256, 1, 0, 1};
+    lfm_batch_tuning tune{256, 1, 0, 1, 0};
     int variant = lfm::dev::kBatchVariantGeneral;   // stage-kernel variant of the current cases
     int grid = 0;
     bool tilesDirty = true;

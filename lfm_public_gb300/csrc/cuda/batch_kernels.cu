@@ -1,4 +1,6 @@
 // Persistent multi-case stage kernel of the batch engine (batch.cuh).
+#include <algorithm>
+
 #include "batch.cuh"
 #include "solver_fp32.cuh"
 
@@ -136,6 +138,47 @@ __global__ void __launch_bounds__(BLOCK) k_batch_stage(const __grid_constant__ B
     phase_tiles<3, BLOCK, DIMS, FULL>(b, stage, sc, sSlot);
 }
 
+// One phase of a stage over every case, for the phased launch mode.
+template <int PH, int BLOCK, int DIMS, bool FULL>
+__global__ void __launch_bounds__(BLOCK) k_batch_phase(const __grid_constant__ BatchArgs b, int stage) {
+    __shared__ BatchCase sc;
+    __shared__ int sSlot;
+    if (threadIdx.x == 0) sSlot = -1;
+    __syncthreads();
+    phase_tiles<PH, BLOCK, DIMS, FULL>(b, stage, sc, sSlot);
+}
+
+template <int PH, int BLOCK, int DIMS, bool FULL>
+cudaError_t launch_phase(const BatchArgs& b, int stage, int bps, int sms, cudaStream_t st) {
+    static thread_local int fit = -1;   // resident blocks per SM of this kernel
+    auto k = k_batch_phase<PH, BLOCK, DIMS, FULL>;
+    if (fit < 0) {
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k, BLOCK, 0);
+        if (e != cudaSuccess || fit < 1) return e != cudaSuccess ? e : cudaErrorInvalidConfiguration;
+    }
+    const int per = bps > 0 ? std::min(bps, fit) : fit;
+    k<<<per * sms, BLOCK, 0, st>>>(b, stage);
+    return cudaGetLastError();
+}
+
+template <int BLOCK, int DIMS, bool FULL>
+cudaError_t launch_phases(const BatchArgs& b, int stage, int bps, int sms, cudaStream_t st) {
+    cudaError_t e = launch_phase<0, BLOCK, DIMS, FULL>(b, stage, bps, sms, st);
+    if (e == cudaSuccess && FULL) e = launch_phase<1, BLOCK, DIMS, FULL>(b, stage, bps, sms, st);
+    if (e == cudaSuccess) e = launch_phase<2, BLOCK, DIMS, FULL>(b, stage, bps, sms, st);
+    if (e == cudaSuccess) e = launch_phase<3, BLOCK, DIMS, FULL>(b, stage, bps, sms, st);
+    return e;
+}
+
+template <int BLOCK>
+cudaError_t launch_phases_variant(const BatchArgs& b, int stage, int variant, int bps, int sms, cudaStream_t st) {
+    switch (variant) {
+        case kBatchVariant2DInviscid: return launch_phases<BLOCK, 2, false>(b, stage, bps, sms, st);
+        case kBatchVariant2D: return launch_phases<BLOCK, 2, true>(b, stage, bps, sms, st);
+        default: return launch_phases<BLOCK, 0, true>(b, stage, bps, sms, st);
+    }
+}
+
 // Kernel of a launch shape and variant (kBatchVariant*).
 template <int BLOCK>
 auto kernel_of(int variant) -> void (*)(BatchArgs, int) {
@@ -169,6 +212,15 @@ cudaError_t launch_batch_stage(const BatchArgs& b, int stage, int block, int var
         case 128: return launch_block<128>(b, stage, variant, grid, cooperative, st);
         case 512: return launch_block<512>(b, stage, variant, grid, cooperative, st);
         default: return launch_block<256>(b, stage, variant, grid, cooperative, st);
+    }
+}
+
+cudaError_t launch_batch_phased(const BatchArgs& b, int stage, int block, int variant, int bps, int sms,
+                                cudaStream_t st) {
+    switch (block) {
+        case 128: return launch_phases_variant<128>(b, stage, variant, bps, sms, st);
+        case 512: return launch_phases_variant<512>(b, stage, variant, bps, sms, st);
+        default: return launch_phases_variant<256>(b, stage, variant, bps, sms, st);
     }
 }
 

@@ -170,7 +170,10 @@ int captureStep(lfm_batch* b, bool cooperative, cudaGraphExec_t* out) {
     LFM_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t le = cudaMemsetAsync(b->dCtl, 0, sizeof(BatchCtl), b->stream);
     for (int k = 0; k < b->rkOrder && le == cudaSuccess; ++k)
-        le = lfm::dev::launch_batch_stage(args, k, b->tune.block, b->variant, b->grid, cooperative, b->stream);
+        le = b->tune.phased ? lfm::dev::launch_batch_phased(args, k, b->tune.block, b->variant, b->tune.blocks_per_sm,
+                                                            b->sms, b->stream)
+                            : lfm::dev::launch_batch_stage(args, k, b->tune.block, b->variant, b->grid, cooperative,
+                                                           b->stream);
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (le != cudaSuccess || e != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
@@ -195,6 +198,7 @@ int ensureGraph(lfm_batch* b) {
         if (rc) return rc;
     }
     if (b->graph) return LFM_OK;
+    if (b->tune.phased) return captureStep(b, false, &b->graph);   // no co-residency needed
     const int fit = lfm::dev::batch_blocks_per_sm(b->tune.block, b->variant);
     if (fit <= 0) return lfm::setError(LFM_ERR_UNSUPPORTED, "batch kernel does not fit on an SM");
     const int bps = b->tune.blocks_per_sm > 0 ? std::min(b->tune.blocks_per_sm, fit) : fit;
@@ -674,8 +678,11 @@ extern "C" int lfm_batch_autotune(lfm_batch* b, int trial_steps, lfm_batch_tunin
     for (int bi = 0; bi < 3 && e == cudaSuccess && rc == LFM_OK; ++bi) {
         const int fit = lfm::dev::batch_blocks_per_sm(blocks[bi], currentVariant(b));
         for (int ii = 0; ii < 3 && rc == LFM_OK; ++ii) {
-            for (int bps = 1; bps <= fit && rc == LFM_OK; ++bps) {
-                lfm_batch_tuning t{blocks[bi], ipts[ii], bps, start.cooperative};
+            // persistent kernel at 1..fit blocks per SM, then the phased mode
+            // at full occupancy (bps 0)
+            for (int bps = 1; bps <= fit + 1 && rc == LFM_OK; ++bps) {
+                const bool phased = bps == fit + 1;
+                lfm_batch_tuning t{blocks[bi], ipts[ii], phased ? 0 : bps, start.cooperative, phased ? 1 : 0};
                 if ((rc = lfm_batch_set_tuning(b, &t))) break;
                 if ((rc = lfm_batch_step(b, 1))) break;   // warm-up, builds tiles and graph
                 cudaEventRecord(b->ev0, b->stream);

@@ -109,8 +109,10 @@ def test_batch_autotune_restores_state_and_keeps_results():
     b.close()
 
 
-@pytest.mark.parametrize("shape", [(128, 1, 0), (256, 4, 1), (512, 2, 0)])
+@pytest.mark.parametrize("shape", [(128, 1, 0), (256, 4, 1), (512, 2, 0), (128, 2, 0, 1, 1), (256, 1, 2, 1, 1)])
 def test_batch_launch_shapes_agree(shape):
+    """Persistent and phased (one kernel per phase) launch modes, any shape:
+    the same bits."""
     cs = _mixed_cases()[:3]
     chs = [N.CaseHandle.from_case(c) for c in cs]
     b = N.Batch(arena_bytes=128 << 20)

@@ -180,14 +180,36 @@ __device__ __forceinline__ void gather32(const Args<float>& a, int c, float* sum
     }
 }
 
-// apply32: the update of cell c from its rhs sum (see update32).
+// The cell's own values the update reads, loaded before its rhs gather so
+// that they are in flight together with it.
+template <int D>
+struct CellIn32 {
+    double qp[D + 2];   // q'
+    float dq[D + 2];
+    float vi, sg;       // 1/V, sponge sigma
+};
+
+template <int D>
+__device__ __forceinline__ void load_cell32(const Args<float>& a, int c, int first, CellIn32<D>& in) {
+    const size_t nt = (size_t)a.nt, nc = (size_t)a.nc;
+#pragma unroll
+    for (int v = 0; v < D + 2; ++v) {
+        in.qp[v] = a.q[v * nt + c];
+        in.dq[v] = first ? 0.0f : a.dq[v * nc + c];
+    }
+    in.vi = a.volInv32[c];
+    in.sg = a.sponge[c];
+}
+
+// apply32: the update of cell c from its rhs sum and its loaded values
+// (see update32).
 template <int D, bool RES, bool GH>
-__device__ __forceinline__ void apply32(const Args<float>& a, int c, const float* sum, double Ak, double Bk,
-                                        double dt, float dt32, int first) {
+__device__ __forceinline__ void apply32(const Args<float>& a, int c, const float* sum, const CellIn32<D>& in,
+                                        double Ak, double Bk, double dt, float dt32, int first) {
     constexpr int NQ = D + 2;
     const size_t nt = (size_t)a.nt, nc = (size_t)a.nc;
-    const float dtvi = __fmul_rn(dt32, a.volInv32[c]);
-    const float sg = a.sponge[c];
+    const float dtvi = __fmul_rn(dt32, in.vi);
+    const float sg = in.sg;
     const float dts = -__fmul_rn(dt32, sg);
     const float A32 = __double2float_rn(Ak);
     double qn[NQ];
@@ -195,8 +217,8 @@ __device__ __forceinline__ void apply32(const Args<float>& a, int c, const float
 #pragma unroll
     for (int v = 0; v < NQ; ++v) {
         const float inc = __fmul_rn(dtvi, sum[v]);
-        float acc = first ? inc : __fmaf_rn(A32, a.dq[v * nc + c], inc);
-        const double qp = a.q[v * nt + c];
+        float acc = first ? inc : __fmaf_rn(A32, in.dq[v], inc);
+        const double qp = in.qp[v];
         if (sg != 0.0f) acc = __fmaf_rn(dts, f64_to_f32(qp), acc);
         a.dq[v * nc + c] = acc;
         qn[v] = fma(Bk, f32_to_f64(acc), qp);
@@ -222,9 +244,11 @@ __device__ __forceinline__ void apply32(const Args<float>& a, int c, const float
 template <int D, bool RES, bool GH = false>
 __device__ __forceinline__ void update32(const Args<float>& a, int c, double Ak, double Bk, double dt,
                                          float dt32, int first) {
+    CellIn32<D> in;
+    load_cell32<D>(a, c, first, in);
     float sum[D + 2];
     gather32<D>(a, c, sum);
-    apply32<D, RES, GH>(a, c, sum, Ak, Bk, dt, dt32, first);
+    apply32<D, RES, GH>(a, c, sum, in, Ak, Bk, dt, dt32, first);
 }
 
 // Perturbation state q' = q - q_ref of cells [0, n) from a caller's absolute

@@ -87,9 +87,11 @@ __global__ void __launch_bounds__(256) k_tile_stage(const __grid_constant__ Args
     for (int lf = threadIdx.x; lf < td.nFA; lf += blockDim.x) flux32<D, SCH>(a, lf);
     __syncthreads();
     for (int lc = threadIdx.x; lc < td.nA; lc += blockDim.x) {
+        CellIn32<D> in;
+        load_cell32<D>(g, td.c0 + lc, first, in);
         float sum[R::Q];
         gather32<D>(a, lc, sum);
-        apply32<D, RES, true>(g, td.c0 + lc, sum, Ak, Bk, dt, dt32, first);
+        apply32<D, RES, true>(g, td.c0 + lc, sum, in, Ak, Bk, dt, dt32, first);
     }
 }
 

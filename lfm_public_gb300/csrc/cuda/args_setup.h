@@ -58,7 +58,7 @@ inline bool needVis(const lfm_solver_desc* d) { return d->mu != 0.0 || d->solver
 
 // 32-bit device index arrays of a description.
 struct DescIndex {
-    std::vector<int> fP, fN, cfOff, cfList, gCell, gKind, gFace;
+    std::vector<int> fP, fN, cfOff, cfList, cfNbr, gCell, gKind, gFace;
     std::vector<double> lapc;   // |delta| / |d| per face
 
     explicit DescIndex(const lfm_solver_desc* d) {
@@ -75,9 +75,14 @@ struct DescIndex {
         for (size_t c = 0; c <= nc; ++c) cfOff[c] = (int)d->cell_face_offsets[c];
         const size_t ne = (size_t)d->cell_face_offsets[nc];
         cfList.resize(ne);
-        // face index, one's complement when the cell is the face's N side
-        for (size_t k = 0; k < ne; ++k)
-            cfList[k] = d->cell_face_sign[k] > 0 ? (int)d->cell_faces[k] : ~(int)d->cell_faces[k];
+        // face index, one's complement when the cell is the face's N side,
+        // and the cell (ghost, halo) across the face
+        cfNbr.resize(ne);
+        for (size_t k = 0; k < ne; ++k) {
+            const int64_t f = d->cell_faces[k];
+            cfList[k] = d->cell_face_sign[k] > 0 ? (int)f : ~(int)f;
+            cfNbr[k] = (int)(d->cell_face_sign[k] > 0 ? d->face_n[f] : d->face_p[f]);
+        }
         gCell.resize(ng);
         gKind.resize(ng);
         gFace.assign(ng, 0);

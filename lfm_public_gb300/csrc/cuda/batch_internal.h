@@ -80,7 +80,7 @@ private:
 struct CaseLayout {
     size_t total = 0;
     size_t q, dq, res, prim, V, grad, flux, S, d, w, dinv, dnorm, K, lapc, fP, fN, fGhost, volInv, volInv32,
-        sponge, cfOff, cfList, cellGhosts, gCell, gKind, gFace;
+        sponge, cfOff, cfList, cfNbr, cellGhosts, gCell, gKind, gFace;
 
     explicit CaseLayout(const lfm_solver_desc* d) {
         const size_t D = (size_t)d->dim, nq = (size_t)d->nq, nc = (size_t)d->n_cells, ng = (size_t)d->n_ghosts;
@@ -108,6 +108,7 @@ struct CaseLayout {
         sponge = add(nc * 4);
         cfOff = add((nc + 1) * 4);
         cfList = add(ne * 4);
+        cfNbr = add(ne * 4);
         cellGhosts = add(nc);
         gCell = add(ng * 4);
         gKind = add(ng * 4);

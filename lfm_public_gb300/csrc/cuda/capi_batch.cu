@@ -82,6 +82,7 @@ std::vector<unsigned char> packCase(const lfm_solver_desc* d, const CaseLayout& 
     conv(L.sponge, d->sponge, nc);
     std::memcpy(i32(L.cfOff), ix.cfOff.data(), (nc + 1) * 4);
     std::memcpy(i32(L.cfList), ix.cfList.data(), ix.cfList.size() * 4);
+    std::memcpy(i32(L.cfNbr), ix.cfNbr.data(), ix.cfNbr.size() * 4);
     unsigned char* cg = img.data() + L.cellGhosts;   // cells whose update writes ghosts
     for (size_t f = 0; f < nf; ++f)
         if (ix.fN[f] >= (int)nc && ix.fN[f] < (int)(nc + ng)) cg[(size_t)ix.fP[f]] = 1;
@@ -391,6 +392,7 @@ int commitCase(lfm_batch* b, const PreparedCase& pc, int* slot) {
     a.sponge = reinterpret_cast<const float*>(P(L.sponge));
     a.cfOff = reinterpret_cast<const int*>(P(L.cfOff));
     a.cfList = reinterpret_cast<const int*>(P(L.cfList));
+    a.cfNbr = reinterpret_cast<const int*>(P(L.cfNbr));
     a.cellGhosts = reinterpret_cast<const uint8_t*>(P(L.cellGhosts));
     a.smagC = nullptr;
     a.gCell = reinterpret_cast<const int*>(P(L.gCell));

@@ -139,7 +139,8 @@ std::vector<int> toInt(const int64_t* p, size_t n) {
 
 template <typename T>
 int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP, const int* fN,
-              const uint8_t* fGhost, const int* cfOff, const int* cfList, const int* gCell, const int* gKind,
+              const uint8_t* fGhost, const int* cfOff, const int* cfList, const int* cfNbr, const int* gCell,
+              const int* gKind,
               const int* gFace) {
     lfm::setup::setConstants(a, d);
     a.q = s->q;
@@ -150,6 +151,7 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
     a.volInv = s->volInv;
     a.cfOff = cfOff;
     a.cfList = cfList;
+    a.cfNbr = cfNbr;
     a.gCell = gCell;
     a.gKind = gKind;
     a.gFace = gFace;
@@ -414,30 +416,34 @@ int createSolver(const lfm_solver_desc* d, const lfm_solver_opts* opts, cudaStre
     std::vector<int> fP = toInt(d->face_p, nf), fN = toInt(d->face_n, nf);
     std::vector<int> cfOff = toInt(d->cell_face_offsets, nc + 1);
     const size_t ne = (size_t)d->cell_face_offsets[nc];
-    std::vector<int> cfList(ne);
-    for (size_t k = 0; k < ne; ++k)
-        cfList[k] = d->cell_face_sign[k] > 0 ? (int)d->cell_faces[k] : ~(int)d->cell_faces[k];
+    std::vector<int> cfList(ne), cfNbr(ne);
+    for (size_t k = 0; k < ne; ++k) {
+        const int64_t f = d->cell_faces[k];
+        cfList[k] = d->cell_face_sign[k] > 0 ? (int)f : ~(int)f;
+        cfNbr[k] = (int)(d->cell_face_sign[k] > 0 ? d->face_n[f] : d->face_p[f]);
+    }
     std::vector<int> gCell = toInt(d->ghost_cell, (size_t)s->ng), gKind((size_t)s->ng), gFace((size_t)s->ng, 0);
     for (int g = 0; g < s->ng; ++g) gKind[(size_t)g] = d->ghost_kind[g];
     for (int f = 0; f < s->nf; ++f)   // ghosts only (halos follow them)
         if (fN[(size_t)f] >= s->nc && fN[(size_t)f] < s->nc + s->ng) gFace[(size_t)(fN[(size_t)f] - s->nc)] = f;
     std::vector<int> sOff = toInt(d->cell_s_offsets, nc + 1);
-    int *dP, *dN, *dOff, *dList, *dGC, *dGK, *dGF;
+    int *dP, *dN, *dOff, *dList, *dNbr, *dGC, *dGK, *dGF;
     uint8_t* dG;
     if ((rc = upload(s, &dP, fP.data(), nf))) return fail(rc);
     if ((rc = upload(s, &dN, fN.data(), nf))) return fail(rc);
     if ((rc = upload(s, &dG, d->face_ghost, nf))) return fail(rc);
     if ((rc = upload(s, &dOff, cfOff.data(), nc + 1))) return fail(rc);
     if ((rc = upload(s, &dList, cfList.data(), ne))) return fail(rc);
+    if ((rc = upload(s, &dNbr, cfNbr.data(), ne))) return fail(rc);
     if ((rc = upload(s, &dGC, gCell.data(), (size_t)s->ng))) return fail(rc);
     if ((rc = upload(s, &dGK, gKind.data(), (size_t)s->ng))) return fail(rc);
     if ((rc = upload(s, &dGF, gFace.data(), (size_t)s->ng))) return fail(rc);
     if ((rc = upload(s, &s->sOff, sOff.data(), nc + 1))) return fail(rc);
     if ((rc = upload(s, &s->cellS, d->cell_s, (size_t)d->cell_s_offsets[nc] * (size_t)s->D))) return fail(rc);
     if (s->precision == LFM_FP32_BULK)
-        rc = buildArgs<float>(s, d, s->a32, dP, dN, dG, dOff, dList, dGC, dGK, dGF);
+        rc = buildArgs<float>(s, d, s->a32, dP, dN, dG, dOff, dList, dNbr, dGC, dGK, dGF);
     else
-        rc = buildArgs<double>(s, d, s->a64, dP, dN, dG, dOff, dList, dGC, dGK, dGF);
+        rc = buildArgs<double>(s, d, s->a64, dP, dN, dG, dOff, dList, dNbr, dGC, dGK, dGF);
     if (rc) return fail(rc);
     // fused tile stages: FP32-bulk without halos, when a block's tile fits
     lfm::TileSet tiles;

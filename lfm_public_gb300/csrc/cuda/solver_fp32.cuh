@@ -276,21 +276,34 @@ __device__ __forceinline__ void grad32(const Args<float>& a, int c) {
         for (int l = 0; l < D; ++l) gu[k][l] = 0.0f;
     }
     const float vi = a.volInv32[c];
+    // the cell's own primitives once; the cell across each face from the
+    // face list's neighbour column (P and N sides kept for the interpolation)
+    float cu[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) cu[k] = ld(a.prim, P::u + k, nt, c);
+    const float cr = ld(a.prim, P::r, nt, c);
+    const float cpr = pressure_dev(R, cr, ld(a.prim, P::Rpsi, nt, c));
     for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
         const int code = a.cfList[e];
-        const int f = code >= 0 ? code : ~code;
-        const int i = a.fP[f], j = a.fN[f];
+        const int o = a.cfNbr[e];
+        const bool own = code >= 0;   // c is the face's P side
+        const int f = own ? code : ~code;
         const float w = a.w[f];
+        float ou[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) ou[k] = ld(a.prim, P::u + k, nt, o);
+        const float orr = ld(a.prim, P::r, nt, o);
+        const float opr = pressure_dev(R, orr, ld(a.prim, P::Rpsi, nt, o));
         float so[D], uu[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) {
             const float Sk = a.S[(size_t)k * nf + f];
-            so[k] = (code >= 0) ? Sk * vi : -Sk * vi;
-            uu[k] = interp(w, ld(a.prim, P::u + k, nt, i), ld(a.prim, P::u + k, nt, j));
+            so[k] = own ? Sk * vi : -Sk * vi;
+            uu[k] = own ? interp(w, cu[k], ou[k]) : interp(w, ou[k], cu[k]);
         }
-        const float ri = ld(a.prim, P::r, nt, i), rj = ld(a.prim, P::r, nt, j);
-        const float pi = pressure_dev(R, ri, ld(a.prim, P::Rpsi, nt, i));
-        const float pj = pressure_dev(R, rj, ld(a.prim, P::Rpsi, nt, j));
+        const float ri = own ? cr : orr, rj = own ? orr : cr;
+        const float pi = own ? cpr : opr;
+        const float pj = own ? opr : cpr;
         const float rho = interp(w, ri, rj);
         const float p = interp(w, pi, pj);
 #pragma unroll
@@ -326,19 +339,28 @@ __device__ __forceinline__ void vis32(const Args<float>& a, int c) {
     }
     const float vi = a.volInv32[c];
     const float Rinv = a.ref.Rinv;
+    // the cell's own primitives once; the cell across each face from the
+    // face list's neighbour column (P and N sides kept for the interpolation)
+    float cu[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) cu[k] = ld(a.prim, P::u + k, nt, c);
+    const float cR = ld(a.prim, P::Rpsi, nt, c);
     for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
         const int code = a.cfList[e];
-        const int f = code >= 0 ? code : ~code;
-        const int i = a.fP[f], j = a.fN[f];
+        const int o = a.cfNbr[e];
+        const bool own = code >= 0;   // c is the face's P side
+        const int f = own ? code : ~code;
         const float w = a.w[f];
         float so[D], fU[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) {
             const float Sk = a.S[(size_t)k * nf + f];
-            so[k] = (code >= 0) ? Sk * vi : -Sk * vi;
-            fU[k] = interp(w, ld(a.prim, P::u + k, nt, i), ld(a.prim, P::u + k, nt, j));
+            const float ouk = ld(a.prim, P::u + k, nt, o);
+            so[k] = own ? Sk * vi : -Sk * vi;
+            fU[k] = own ? interp(w, cu[k], ouk) : interp(w, ouk, cu[k]);
         }
-        const float fT = interp(w, ld(a.prim, P::Rpsi, nt, i), ld(a.prim, P::Rpsi, nt, j)) * Rinv;
+        const float oR = ld(a.prim, P::Rpsi, nt, o);
+        const float fT = (own ? interp(w, cR, oR) : interp(w, oR, cR)) * Rinv;
 #pragma unroll
         for (int x = 0; x < D; ++x) {
 #pragma unroll
@@ -351,7 +373,7 @@ __device__ __forceinline__ void vis32(const Args<float>& a, int c) {
     stress<float, D>(g, mu, tau);
     float U[D];
 #pragma unroll
-    for (int k = 0; k < D; ++k) U[k] = a.ref.U[k] + ld(a.prim, P::u + k, nt, c);
+    for (int k = 0; k < D; ++k) U[k] = a.ref.U[k] + cu[k];
 #pragma unroll
     for (int x = 0; x < D; ++x) {
 #pragma unroll

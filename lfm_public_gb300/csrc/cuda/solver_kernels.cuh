@@ -84,6 +84,7 @@ struct Args {
     const T* sponge;          // sponge coefficient sigma per cell
     const int* cfOff;         // nc + 1
     const int* cfList;        // face index, negative (~f) when the cell is N
+    const int* cfNbr;         // per cfList entry: the cell (or ghost, halo) across the face
     const T* smagC;           // Smagorinsky LES: the constant each cell's tauMC is built with
                               // (V then holds D x D more rows: its SGS stress), or null
     const uint8_t* cellGhosts;  // FP32-bulk single case: boundary faces of each cell

@@ -27,7 +27,7 @@ struct TileDesc {
     int nV;          // nA + nB1
     int nFA, nLF;    // faces of A cells, all local faces
     int nE;          // entries of the local cell -> face lists of the V cells
-    int64_t iOff;    // ints:  L[nL] fP[nLF] fN[nLF] cfOff[nV + 1] cfList[nE]
+    int64_t iOff;    // ints:  L[nL] fP[nLF] fN[nLF] cfOff[nV + 1] cfList[nE] cfNbr[nE]
     int64_t fOff;    // floats: S[D][nLF] d[D][nLF] w[nLF] K[D][nLF] lapc[nLF] dinv[nLF]
                      //         dnorm[D][nLF] volInv32[nV]
     int64_t bOff;    // bytes: fGhost[nLF]

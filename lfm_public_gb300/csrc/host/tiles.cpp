@@ -112,20 +112,25 @@ TileSet buildTiles(const lfm_solver_desc* d, int tileCells, int maxLocal) {
             if (ln < 0 || ln >= td.nL) throw std::runtime_error("tiles: face neighbour outside its tile");
             ts.ints.push_back(ln);
         }
-        std::vector<int> cfList;
+        std::vector<int> cfList, cfNbr;
         ts.ints.push_back(0);
         for (int v = 0; v < td.nV; ++v) {
             codesOf(L[(size_t)v], codes);
             for (int64_t code : codes) {
-                const int lf = faceLocal[(size_t)faceOf(code)];
+                const int f = faceOf(code);
+                const int lf = faceLocal[(size_t)f];
                 if (lf < 0 || lf >= td.nLF || (v < td.nA && lf >= td.nFA))
                     throw std::runtime_error("tiles: cell face outside its tile");
                 cfList.push_back(code >= 0 ? lf : ~lf);
+                const int other = localOf[(size_t)(code >= 0 ? d->face_n[f] : d->face_p[f])];
+                if (other < 0 || other >= td.nL) throw std::runtime_error("tiles: neighbour outside its tile");
+                cfNbr.push_back(other);
             }
             ts.ints.push_back((int)cfList.size());
         }
         td.nE = (int)cfList.size();
         ts.ints.insert(ts.ints.end(), cfList.begin(), cfList.end());
+        ts.ints.insert(ts.ints.end(), cfNbr.begin(), cfNbr.end());
 
         // floats (converted as the solver's device copies are: (float) of the FP64 value)
         td.fOff = (int64_t)ts.floats.size();

@@ -326,7 +326,8 @@ __device__ __forceinline__ void grad32(const Args<float>& a, int c) {
 // ---------------------------------------------------------------------------
 // vis32: dudx and dTdx from u' and T', sigmaU = (U_inf + u') . tau.
 // ---------------------------------------------------------------------------
-template <int D>
+// LES compiles in the Smagorinsky SGS stress (cases with a.smagC).
+template <int D, bool LES = false>
 __device__ __forceinline__ void vis32(const Args<float>& a, int c) {
     using P = PRow<D>;
     const size_t nt = (size_t)a.nt, nf = (size_t)a.nf;
@@ -381,7 +382,7 @@ __device__ __forceinline__ void vis32(const Args<float>& a, int c) {
         a.V[(size_t)(D * D + x) * nt + c] = gT[x];
         a.V[(size_t)(D * D + D + x) * nt + c] = dotv<float, D>(U, tau[x]);
     }
-    if (a.smagC) {   // Smagorinsky LES: the cell's SGS stress
+    if (LES && a.smagC) {   // Smagorinsky LES: the cell's SGS stress
         float sg[D][D];
         sgs_stress<float, D>(g, a.smagC[c], sg);
 #pragma unroll
@@ -406,7 +407,7 @@ __device__ __forceinline__ float p5diff_dd(float a, float b, float alpha) {
 // viscous terms (linear in the gradients, so unchanged in form).
 // ---------------------------------------------------------------------------
 // VIS = false compiles the viscous terms out (for callers that know mu = 0).
-template <int D, int SCH, bool VIS = true>
+template <int D, int SCH, bool VIS = true, bool LES = false>
 __device__ __forceinline__ void flux32(const Args<float>& a, int f) {
     constexpr int NQ = D + 2;
     using P = PRow<D>;
@@ -591,7 +592,7 @@ __device__ __forceinline__ void flux32(const Args<float>& a, int f) {
             rhs[x + 1] += mu * gtS + dsum * S[x] + mu * (lapc * (uj[x] - ui[x]) + dotv<float, D>(Kf, g[x]));
         }
         rhs[D + 1] += dotv<float, D>(sU, S) + kc * (lapc * (Tj - Ti) + dotv<float, D>(Kf, gT));
-        if (a.smagC && !a.fGhost[f]) {   // Smagorinsky LES, as in the FP64 kernel
+        if (LES && a.smagC && !a.fGhost[f]) {   // Smagorinsky LES, as in the FP64 kernel
 #pragma unroll
             for (int x = 0; x < D; ++x) {
                 float s = 0.0f;

@@ -80,7 +80,8 @@ __global__ void __launch_bounds__(256) k_grad(Args<T> a) {
 // ---------------------------------------------------------------------------
 // k_vis: dudx, dTdx and sigmaU per cell (tauMC is rebuilt per face from dudx).
 // ---------------------------------------------------------------------------
-template <typename T, int D>
+// LES compiles in the Smagorinsky SGS stress (cases with a.smagC).
+template <typename T, int D, bool LES>
 __global__ void __launch_bounds__(256) k_vis(Args<T> a) {
     const int c = LFM_GLOBAL_ID();
     if (c >= a.nc) return;
@@ -127,7 +128,7 @@ __global__ void __launch_bounds__(256) k_vis(Args<T> a) {
         a.V[(size_t)(D * D + x) * nt + c] = gT[x];
         a.V[(size_t)(D * D + D + x) * nt + c] = dotv<T, D>(U, tau[x]);
     }
-    if (a.smagC) {   // Smagorinsky LES: the cell's SGS stress
+    if (LES && a.smagC) {   // Smagorinsky LES: the cell's SGS stress
         T sg[D][D];
         sgs_stress<T, D>(g, a.smagC[c], sg);
 #pragma unroll
@@ -140,7 +141,7 @@ __global__ void __launch_bounds__(256) k_vis(Args<T> a) {
 // ---------------------------------------------------------------------------
 // k_flux: rhs of one face.
 // ---------------------------------------------------------------------------
-template <typename T, int D, int SCH>
+template <typename T, int D, int SCH, bool LES>
 __global__ void __launch_bounds__(128) k_flux(Args<T> a) {
     const int f = LFM_GLOBAL_ID();
     if (f >= a.nf) return;
@@ -348,7 +349,7 @@ __global__ void __launch_bounds__(128) k_flux(Args<T> a) {
         // Smagorinsky LES: the face tauMC also interpolates the cells' SGS
         // stress (boundary faces keep the laminar two-point one, as in the
         // reference)
-        if (a.smagC && !ghost) {
+        if (LES && a.smagC && !ghost) {
 #pragma unroll
             for (int x = 0; x < D; ++x) {
                 T s = T(0);
@@ -461,79 +462,53 @@ __global__ void k_set_flag(int* flag, int v) { *flag = v; }
 // ---------------------------------------------------------------------------
 static inline unsigned blocks(int n, int b) { return (unsigned)((n + b - 1) / b); }
 
-template <typename T, int D>
-void launch_stage_t(const Args<T>& a, const StageConfig& s, cudaStream_t st) {
-    k_prep<T, D><<<blocks(a.nt, 256), 256, 0, st>>>(a);
-    if (s.needGrad) k_grad<T, D><<<blocks(a.nc, 256), 256, 0, st>>>(a);
-    if (s.needVis) k_vis<T, D><<<blocks(a.nc, 256), 256, 0, st>>>(a);
-    switch (s.scheme) {
-        case kSchemeM1: k_flux<T, D, kSchemeM1><<<blocks(a.nf, 128), 128, 0, st>>>(a); break;
-        case kSchemeM2: k_flux<T, D, kSchemeM2><<<blocks(a.nf, 128), 128, 0, st>>>(a); break;
-        default: k_flux<T, D, kSchemeAUSM><<<blocks(a.nf, 128), 128, 0, st>>>(a); break;
+template <typename T, int D, int SCH, bool LES>
+void launch_flux(const Args<T>& a, cudaStream_t st) {
+    k_flux<T, D, SCH, LES><<<blocks(a.nf, 128), 128, 0, st>>>(a);
+}
+
+template <typename T, int D, bool LES>
+void launch_fp64(const Args<T>& a, const StageConfig& s, int which, cudaStream_t st) {
+    switch (which) {
+        case 0: k_prep<T, D><<<blocks(a.nt, 256), 256, 0, st>>>(a); break;
+        case 1:
+            if (s.needGrad) k_grad<T, D><<<blocks(a.nc, 256), 256, 0, st>>>(a);
+            break;
+        case 2:
+            if (s.needVis) k_vis<T, D, LES><<<blocks(a.nc, 256), 256, 0, st>>>(a);
+            break;
+        case 3:
+            if (s.scheme == kSchemeM1) launch_flux<T, D, kSchemeM1, LES>(a, st);
+            else if (s.scheme == kSchemeM2) launch_flux<T, D, kSchemeM2, LES>(a, st);
+            else launch_flux<T, D, kSchemeAUSM, LES>(a, st);
+            break;
+        case 4:
+            if (s.withRes) k_update<T, D, true><<<blocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
+            else k_update<T, D, false><<<blocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
+            break;
+        default: break;
     }
-    if (s.withRes)
-        k_update<T, D, true><<<blocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
+}
+
+// Individual kernels (a stage is kernels 0..kKernelsPerStage-1 in order).
+template <typename T>
+void launch_kernel(const Args<T>& a, const StageConfig& s, int which, cudaStream_t st) {
+    const bool les = a.smagC != nullptr;
+    if (a.D == 2)
+        les ? launch_fp64<T, 2, true>(a, s, which, st) : launch_fp64<T, 2, false>(a, s, which, st);
     else
-        k_update<T, D, false><<<blocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
+        les ? launch_fp64<T, 3, true>(a, s, which, st) : launch_fp64<T, 3, false>(a, s, which, st);
 }
 
 template <typename T>
 void launch_stage(const Args<T>& a, const StageConfig& s, cudaStream_t st) {
-    if (a.D == 2)
-        launch_stage_t<T, 2>(a, s, st);
-    else
-        launch_stage_t<T, 3>(a, s, st);
+    for (int k = 0; k < kKernelsPerStage; ++k) launch_kernel<T>(a, s, k, st);
 }
 template void launch_stage<double>(const Args<double>&, const StageConfig&, cudaStream_t);
 // The FP32-bulk form runs its own kernels (solver_kernels_fp32.cu).
 template <>
 void launch_stage<float>(const Args<float>& a, const StageConfig& s, cudaStream_t st) {
     for (int k = 0; k < kKernelsPerStage; ++k) launch_kernel_fp32(a, s, k, st);
-}
-
-// Individual kernels, for per-kernel timing.
-template <typename T>
-void launch_kernel(const Args<T>& a, const StageConfig& s, int which, cudaStream_t st) {
-    const bool d2 = a.D == 2;
-    switch (which) {
-        case 0:
-            if (d2) k_prep<T, 2><<<blocks(a.nt, 256), 256, 0, st>>>(a);
-            else k_prep<T, 3><<<blocks(a.nt, 256), 256, 0, st>>>(a);
-            break;
-        case 1:
-            if (!s.needGrad) break;
-            if (d2) k_grad<T, 2><<<blocks(a.nc, 256), 256, 0, st>>>(a);
-            else k_grad<T, 3><<<blocks(a.nc, 256), 256, 0, st>>>(a);
-            break;
-        case 2:
-            if (!s.needVis) break;
-            if (d2) k_vis<T, 2><<<blocks(a.nc, 256), 256, 0, st>>>(a);
-            else k_vis<T, 3><<<blocks(a.nc, 256), 256, 0, st>>>(a);
-            break;
-        case 3: {
-            if (d2) {
-                if (s.scheme == kSchemeM1) k_flux<T, 2, kSchemeM1><<<blocks(a.nf, 128), 128, 0, st>>>(a);
-                else if (s.scheme == kSchemeM2) k_flux<T, 2, kSchemeM2><<<blocks(a.nf, 128), 128, 0, st>>>(a);
-                else k_flux<T, 2, kSchemeAUSM><<<blocks(a.nf, 128), 128, 0, st>>>(a);
-            } else {
-                if (s.scheme == kSchemeM1) k_flux<T, 3, kSchemeM1><<<blocks(a.nf, 128), 128, 0, st>>>(a);
-                else if (s.scheme == kSchemeM2) k_flux<T, 3, kSchemeM2><<<blocks(a.nf, 128), 128, 0, st>>>(a);
-                else k_flux<T, 3, kSchemeAUSM><<<blocks(a.nf, 128), 128, 0, st>>>(a);
-            }
-            break;
-        }
-        case 4:
-            if (d2) {
-                if (s.withRes) k_update<T, 2, true><<<blocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
-                else k_update<T, 2, false><<<blocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
-            } else {
-                if (s.withRes) k_update<T, 3, true><<<blocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
-                else k_update<T, 3, false><<<blocks(a.nc, 256), 256, 0, st>>>(a, s.A, s.B, s.dt, s.first);
-            }
-            break;
-        default:
-            break;
-    }
 }
 template void launch_kernel<double>(const Args<double>&, const StageConfig&, int, cudaStream_t);
 template <>

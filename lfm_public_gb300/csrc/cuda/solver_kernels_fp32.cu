@@ -22,16 +22,17 @@ __global__ void __launch_bounds__(256) k_grad32(const __grid_constant__ Args<flo
     if (c < a.nc) grad32<D>(a, c);
 }
 
-template <int D>
-__global__ void __launch_bounds__(256) k_vis32(const __grid_constant__ Args<float> a) {
+// Six blocks per SM (40 registers, no spills): full-occupancy gathers.
+template <int D, bool LES>
+__global__ void __launch_bounds__(256, 6) k_vis32(const __grid_constant__ Args<float> a) {
     const int c = LFM_GLOBAL_ID();
-    if (c < a.nc) vis32<D>(a, c);
+    if (c < a.nc) vis32<D, LES>(a, c);
 }
 
-template <int D, int SCH>
+template <int D, int SCH, bool LES>
 __global__ void __launch_bounds__(256) k_flux32(const __grid_constant__ Args<float> a) {
     const int f = LFM_GLOBAL_ID();
-    if (f < a.nf) flux32<D, SCH>(a, f);
+    if (f < a.nf) flux32<D, SCH, true, LES>(a, f);
 }
 
 template <int D, bool RES, bool GH>
@@ -65,12 +66,19 @@ void launch_fp32(const Args<float>& a, const StageConfig& s, int which, cudaStre
             if (s.needGrad) k_grad32<D><<<nblocks(a.nc, 256), 256, 0, st>>>(a);
             break;
         case 2:
-            if (s.needVis) k_vis32<D><<<nblocks(a.nc, 256), 256, 0, st>>>(a);
+            if (s.needVis && a.smagC) k_vis32<D, true><<<nblocks(a.nc, 256), 256, 0, st>>>(a);
+            else if (s.needVis) k_vis32<D, false><<<nblocks(a.nc, 256), 256, 0, st>>>(a);
             break;
         case 3:
-            if (s.scheme == kSchemeM1) k_flux32<D, kSchemeM1><<<nblocks(a.nf, 256), 256, 0, st>>>(a);
-            else if (s.scheme == kSchemeM2) k_flux32<D, kSchemeM2><<<nblocks(a.nf, 256), 256, 0, st>>>(a);
-            else k_flux32<D, kSchemeAUSM><<<nblocks(a.nf, 256), 256, 0, st>>>(a);
+            if (a.smagC) {   // Smagorinsky LES variants
+                if (s.scheme == kSchemeM1) k_flux32<D, kSchemeM1, true><<<nblocks(a.nf, 256), 256, 0, st>>>(a);
+                else if (s.scheme == kSchemeM2) k_flux32<D, kSchemeM2, true><<<nblocks(a.nf, 256), 256, 0, st>>>(a);
+                else k_flux32<D, kSchemeAUSM, true><<<nblocks(a.nf, 256), 256, 0, st>>>(a);
+            } else {
+                if (s.scheme == kSchemeM1) k_flux32<D, kSchemeM1, false><<<nblocks(a.nf, 256), 256, 0, st>>>(a);
+                else if (s.scheme == kSchemeM2) k_flux32<D, kSchemeM2, false><<<nblocks(a.nf, 256), 256, 0, st>>>(a);
+                else k_flux32<D, kSchemeAUSM, false><<<nblocks(a.nf, 256), 256, 0, st>>>(a);
+            }
             break;
         case 4: {
             const unsigned nb = nblocks(a.nc, 256);

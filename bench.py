@@ -349,15 +349,11 @@ def run_gpu(args):
     host = torch.empty((nq, nc), dtype=torch.float64, pin_memory=True).numpy()
     s.get_state(out=host)
     for _ in range(2):
-        s.set_state(host)
-        s.step(1, dt)
-        s.get_state(out=host)
+        s.advance(host, 1, dt, host)
     e2e_steps = max(1, args.steps)
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        s.set_state(host)
-        s.step(1, dt)
-        s.get_state(out=host)
+    for _ in range(e2e_steps):   # lfm_solver_advance: state in, one step, state out
+        s.advance(host, 1, dt, host)
     s.sync()
     e2e_s = _allmax(pg, time.perf_counter() - t0)
     e2e_value = ws * nc * stages * e2e_steps / e2e_s

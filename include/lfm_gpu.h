@@ -204,6 +204,12 @@ int lfm_solver_stage(lfm_solver* s, int rk_stage, double dt);
 /* nsteps full time steps at constant dt (rk_order stages each), replayed from
  * a CUDA graph. Asynchronous on the solver stream. */
 int lfm_solver_step(lfm_solver* s, int nsteps, double dt);
+/* Host state in, nsteps time steps, host state out, in one call with one
+ * synchronisation at the end: q_in (may be NULL: continue from the device
+ * state) is uploaded as by lfm_solver_set_state, q_out (may be NULL) receives
+ * the state as from lfm_solver_get_state ([nq][n_cells], solver order, host
+ * memory; pinned memory copies fastest). Returns lfm_solver_sync's status. */
+int lfm_solver_advance(lfm_solver* s, const double* q_in, int nsteps, double dt, double* q_out);
 
 /* Same as lfm_solver_step, timed with CUDA events on the solver stream;
  * waits for completion and returns the elapsed milliseconds. */

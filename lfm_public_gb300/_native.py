@@ -138,6 +138,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "lfm_solver_probes_record": ([vp], C.c_int),
         "lfm_solver_probes_read": ([vp, _dp, C.POINTER(C.c_int)], C.c_int),
         "lfm_partitioned_solver": ([vp, C.c_int, C.POINTER(vp)], C.c_int),
+        "lfm_solver_advance": ([vp, _dp, C.c_int, C.c_double, _dp], C.c_int),
         "lfm_tiles_stats": ([C.POINTER(SolverDesc), C.c_int, C.c_int, C.POINTER(C.c_int64)], C.c_int),
         "lfm_case_open": ([C.c_char_p, C.c_int, C.POINTER(vp)], C.c_int),
         "lfm_case_from_polymesh": ([C.POINTER(PolyMesh), C.POINTER(Params), C.POINTER(Fields), C.POINTER(vp)],
@@ -358,6 +359,18 @@ class Solver:
 
     def step(self, nsteps: int, dt: float):
         check(load_library().lfm_solver_step(self._h, nsteps, dt))
+
+    def advance(self, q_in: Optional[np.ndarray], nsteps: int, dt: float, q_out: Optional[np.ndarray] = None):
+        """Host state in (or None), nsteps steps, host state out (into q_out,
+        a C-contiguous float64 (nq, n_cells) array, or None), one sync."""
+        shape = (self.nq, self.n_cells)
+        for a in (q_in, q_out):
+            if a is not None and (a.dtype != np.float64 or a.shape != shape or not a.flags.c_contiguous):
+                raise ValueError("states must be C-contiguous float64 arrays of shape (nq, n_cells)")
+        pin = _ptr(q_in, C.c_double) if q_in is not None else None
+        pout = _ptr(q_out, C.c_double) if q_out is not None else None
+        check(load_library().lfm_solver_advance(self._h, pin, nsteps, dt, pout))
+        return q_out
 
     def stage(self, rk: int, dt: float):
         check(load_library().lfm_solver_stage(self._h, rk, dt))

@@ -548,9 +548,10 @@ extern "C" void lfm_solver_destroy(lfm_solver* s) {
     delete s;
 }
 
-extern "C" int lfm_solver_set_state(lfm_solver* s, const double* q) {
-    if (!s || !q) return lfm::setError(LFM_ERR_INVALID, "null argument");
-    LFM_CUDA(cudaSetDevice(s->device));
+namespace {
+
+// The state upload of lfm_solver_set_state, enqueued on the solver stream.
+int enqueueSetState(lfm_solver* s, const double* q) {
     // a new state starts with a clear non-finite flag
     LFM_CUDA(cudaMemsetAsync(s->flag, 0, sizeof(int), s->stream));
     const size_t nc = (size_t)s->nc;
@@ -561,21 +562,18 @@ extern "C" int lfm_solver_set_state(lfm_solver* s, const double* q) {
         for (int v = 0; v < 5; ++v) qo.v[v] = s->qRef[v];
         lfm::dev::launch_offset_rows(s->q, s->nt, s->stage, s->nc, s->nc, s->nq, qo, -1.0, s->stream);
         LFM_CUDA(cudaGetLastError());
-    } else {
-        for (int v = 0; v < s->nq; ++v)
-            LFM_CUDA(cudaMemcpyAsync(s->q + (size_t)v * s->nt, q + (size_t)v * nc, nc * sizeof(double),
-                                     cudaMemcpyHostToDevice, s->stream));
+    } else {   // rows of nc values into rows of nt
+        LFM_CUDA(cudaMemcpy2DAsync(s->q, (size_t)s->nt * sizeof(double), q, nc * sizeof(double),
+                                   nc * sizeof(double), (size_t)s->nq, cudaMemcpyHostToDevice, s->stream));
     }
-    LFM_CUDA(cudaStreamSynchronize(s->stream));
     s->primsValid = false;
     s->primParity = 0;
     s->ghostRowsValid = false;
     return LFM_OK;
 }
 
-extern "C" int lfm_solver_get_state(lfm_solver* s, double* q) {
-    if (!s || !q) return lfm::setError(LFM_ERR_INVALID, "null argument");
-    LFM_CUDA(cudaSetDevice(s->device));
+// The state download of lfm_solver_get_state, enqueued on the solver stream.
+int enqueueGetState(lfm_solver* s, double* q) {
     if (s->precision == LFM_FP32_BULK) {   // stored as q - q_ref
         lfm::dev::QOffset qo;
         for (int v = 0; v < 5; ++v) qo.v[v] = s->qRef[v];
@@ -584,12 +582,41 @@ extern "C" int lfm_solver_get_state(lfm_solver* s, double* q) {
         LFM_CUDA(cudaMemcpyAsync(q, s->stage, (size_t)s->nq * s->nc * sizeof(double), cudaMemcpyDeviceToHost,
                                  s->stream));
     } else {
-        for (int v = 0; v < s->nq; ++v)
-            LFM_CUDA(cudaMemcpyAsync(q + (size_t)v * s->nc, s->q + (size_t)v * s->nt, (size_t)s->nc * sizeof(double),
-                                     cudaMemcpyDeviceToHost, s->stream));
+        LFM_CUDA(cudaMemcpy2DAsync(q, (size_t)s->nc * sizeof(double), s->q, (size_t)s->nt * sizeof(double),
+                                   (size_t)s->nc * sizeof(double), (size_t)s->nq, cudaMemcpyDeviceToHost,
+                                   s->stream));
     }
+    return LFM_OK;
+}
+
+}  // namespace
+
+extern "C" int lfm_solver_set_state(lfm_solver* s, const double* q) {
+    if (!s || !q) return lfm::setError(LFM_ERR_INVALID, "null argument");
+    LFM_CUDA(cudaSetDevice(s->device));
+    int rc = enqueueSetState(s, q);
+    if (rc) return rc;
     LFM_CUDA(cudaStreamSynchronize(s->stream));
     return LFM_OK;
+}
+
+extern "C" int lfm_solver_get_state(lfm_solver* s, double* q) {
+    if (!s || !q) return lfm::setError(LFM_ERR_INVALID, "null argument");
+    LFM_CUDA(cudaSetDevice(s->device));
+    int rc = enqueueGetState(s, q);
+    if (rc) return rc;
+    LFM_CUDA(cudaStreamSynchronize(s->stream));
+    return LFM_OK;
+}
+
+extern "C" int lfm_solver_advance(lfm_solver* s, const double* q_in, int nsteps, double dt, double* q_out) {
+    if (!s || nsteps < 0) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    LFM_CUDA(cudaSetDevice(s->device));
+    int rc = LFM_OK;
+    if (q_in && (rc = enqueueSetState(s, q_in))) return rc;
+    if (nsteps > 0 && (rc = lfm_solver_step(s, nsteps, dt))) return rc;
+    if (q_out && (rc = enqueueGetState(s, q_out))) return rc;
+    return lfm_solver_sync(s);
 }
 
 extern "C" int lfm_solver_stage(lfm_solver* s, int rk, double dt) {

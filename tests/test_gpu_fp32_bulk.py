@@ -77,6 +77,37 @@ def test_fp32_bulk_bitwise_reproducible_and_stage_api():
     s.close()
 
 
+@pytest.mark.parametrize("precision", [N.LFM_FP64, N.LFM_FP32_BULK])
+def test_advance_is_set_state_step_get_state(precision):
+    """lfm_solver_advance (state in, steps, state out, one synchronisation)
+    gives the bits of set_state + step + get_state, step by step, and a
+    None input or output skips that copy."""
+    case = cases.cylinder_case(n_theta=48, n_r=24, r1=15, first=0.02, Ls=4, solver=1, minmod=True, noise=0.02)
+    ch = N.CaseHandle.from_case(case)
+    dt = case.delta_t
+    a = N.Solver(ch, precision=precision)
+    b = N.Solver(ch, precision=precision)
+    host = np.ascontiguousarray(a.get_state())
+    out = np.empty_like(host)
+    for _ in range(3):
+        b.set_state(host)
+        b.step(1, dt)
+        b.sync()
+        ref = b.get_state()
+        a.advance(host, 1, dt, out)
+        assert np.array_equal(out, ref)
+        host = out.copy()
+    a.advance(None, 2, dt, None)
+    b.step(2, dt)
+    b.sync()
+    a.advance(None, 0, dt, out)
+    assert np.array_equal(out, b.get_state())
+    with pytest.raises(ValueError):
+        a.advance(host[:, :-1].copy(), 1, dt, None)
+    a.close()
+    b.close()
+
+
 def test_fp32_bulk_free_stream_is_preserved():
     # A uniform free stream (inlet, outlet and walls) has zero perturbation in
     # the interior and FP64-derived ghost primitives: the state may move only

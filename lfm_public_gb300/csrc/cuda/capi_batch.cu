@@ -394,6 +394,7 @@ int commitCase(lfm_batch* b, const PreparedCase& pc, int* slot) {
     a.cfList = reinterpret_cast<const int*>(P(L.cfList));
     a.cfNbr = reinterpret_cast<const int*>(P(L.cfNbr));
     a.cellGhosts = reinterpret_cast<const uint8_t*>(P(L.cellGhosts));
+    a.cfEll = nullptr;
     a.smagC = nullptr;
     a.gCell = reinterpret_cast<const int*>(P(L.gCell));
     a.gKind = reinterpret_cast<const int*>(P(L.gKind));

@@ -157,6 +157,7 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
     a.gFace = gFace;
     a.flag = s->flag;
     a.cellGhosts = nullptr;
+    a.cfEll = nullptr;
     a.smagC = nullptr;
     const size_t nt = (size_t)s->nt, nf = (size_t)s->nf, D = (size_t)s->D;
     int rc;
@@ -471,6 +472,22 @@ int createSolver(const lfm_solver_desc* d, const lfm_solver_opts* opts, cudaStre
         uint8_t* dCG = nullptr;
         if ((rc = upload(s, &dCG, cg.data(), nc))) return fail(rc);
         s->a32.cellGhosts = dCG;
+    }
+    if (s->precision == LFM_FP32_BULK && !tiled && s->D == 3) {
+        // the update's fixed-width cell -> face table, when every cell fits it
+        // (3D: six faces a cell, a shorter gather; in 2D the extra table costs
+        // the other kernels more L2 hits than it saves)
+        const size_t W = (size_t)(s->D == 2 ? lfm::dev::kEllWidth<2> : lfm::dev::kEllWidth<3>);
+        bool fits = true;
+        for (size_t c = 0; c < nc && fits; ++c) fits = (size_t)(cfOff[c + 1] - cfOff[c]) <= W;
+        if (fits) {
+            std::vector<int> ell(W * nc, lfm::dev::kEllPad);
+            for (size_t c = 0; c < nc; ++c)
+                for (int e = cfOff[c]; e < cfOff[c + 1]; ++e) ell[(size_t)(e - cfOff[c]) * nc + c] = cfList[(size_t)e];
+            int* dEll = nullptr;
+            if ((rc = upload(s, &dEll, ell.data(), W * nc))) return fail(rc);
+            s->a32.cfEll = dEll;
+        }
     }
     {   // ghost face geometry in FP64 and patch ids (post-processing)
         const size_t ng = (size_t)s->ng, D = (size_t)s->D;

@@ -14,7 +14,8 @@
 namespace lfm {
 namespace dev {
 
-__device__ __forceinline__ double f32_to_f64(float x) {
+// The general conversions (every class of input).
+__device__ __forceinline__ double f32_to_f64_any(float x) {
     const unsigned u = __float_as_uint(x);
     const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
     const unsigned ex = (u >> 23) & 0xffu;
@@ -34,7 +35,7 @@ __device__ __forceinline__ double f32_to_f64(float x) {
     return __longlong_as_double((long long)bits);
 }
 
-__device__ __forceinline__ float f64_to_f32(double x) {
+__device__ __forceinline__ float f64_to_f32_any(double x) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
     const int ex = (int)((b >> 52) & 0x7ffu);
@@ -71,6 +72,41 @@ __device__ __forceinline__ float f64_to_f32(double x) {
         r = (unsigned)q;                        // may round up into the smallest normal
     }
     return __uint_as_float(sign | r);
+}
+
+// Fast paths on 32-bit words for the common classes, the general code for
+// the rest.
+//
+// float -> double, normal x: the 11-bit exponent is the 8-bit one + 896 and
+// the 52-bit fraction the 23-bit one followed by 29 zeros, so the high word
+// is sign | ((x & 0x7fffffff) >> 3) + (896 << 20) and the low word x << 29;
+// zeros keep only the sign.
+__device__ __forceinline__ double f32_to_f64(float x) {
+    const unsigned u = __float_as_uint(x);
+    const unsigned mag = u & 0x7fffffffu;
+    if (mag - 0x00800000u < 0x7f000000u)        // normal: exponent field 1 .. 254
+        return __hiloint2double((int)((u & 0x80000000u) | ((mag >> 3) + 0x38000000u)), (int)(u << 29));
+    if (mag == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+    return f32_to_f64_any(x);
+}
+
+// double -> float with a normal result before rounding (double exponent
+// field 897 .. 1150, binary32 exponent 1 .. 254): the top 31 bits below the
+// sign of (exponent - 896, 23 fraction bits) are one funnel shift of the high
+// and low words minus 896 << 23 (mod 2^32); the 29 dropped fraction bits
+// round to nearest even by adding 0x0fffffff plus the kept lowest bit and
+// carrying bit 29 in. A carry out of the fraction raises the exponent, and out
+// of exponent 254 gives the infinity that rounding to nearest produces.
+__device__ __forceinline__ float f64_to_f32(double x) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned ex = (hi >> 20) & 0x7ffu;
+    if (ex - 897u < 254u) {
+        const unsigned r = __funnelshift_l(lo, hi, 3) - 0xc0000000u;
+        const unsigned up = ((lo & 0x1fffffffu) + (r & 1u) + 0x0fffffffu) >> 29;
+        return __uint_as_float((hi & 0x80000000u) | (r + up));
+    }
+    if (((hi & 0x7fffffffu) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
+    return f64_to_f32_any(x);
 }
 
 }  // namespace dev

@@ -180,6 +180,34 @@ __device__ __forceinline__ void gather32(const Args<float>& a, int c, float* sum
     }
 }
 
+// gather32_ell: gather32 through the fixed-width table. Every face index of
+// the cell is loaded at once (coalesced rows), then every flux value, so the
+// gather costs two memory round trips instead of one per face; the sum runs
+// in the same (ascending face) order, so it has gather32's bits.
+template <int D>
+__device__ __forceinline__ void gather32_ell(const Args<float>& a, int c, float* sum) {
+    constexpr int NQ = D + 2, W = kEllWidth<D>;
+    const size_t nf = (size_t)a.nf, nc = (size_t)a.nc;
+    int code[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) code[k] = a.cfEll[k * nc + c];
+    float fl[W][NQ];
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+        const int f = code[k] >= 0 ? code[k] : ~code[k];
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) fl[k][v] = code[k] != kEllPad ? a.flux[v * nf + f] : 0.0f;
+    }
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) sum[v] = 0.0f;
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+        if (code[k] == kEllPad) continue;
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) sum[v] = code[k] >= 0 ? sum[v] + fl[k][v] : sum[v] - fl[k][v];
+    }
+}
+
 // The cell's own values the update reads, loaded before its rhs gather so
 // that they are in flight together with it.
 template <int D>
@@ -241,13 +269,14 @@ __device__ __forceinline__ void apply32(const Args<float>& a, int c, const float
     }
 }
 
-template <int D, bool RES, bool GH = false>
+template <int D, bool RES, bool GH = false, bool ELL = false>
 __device__ __forceinline__ void update32(const Args<float>& a, int c, double Ak, double Bk, double dt,
                                          float dt32, int first) {
     CellIn32<D> in;
     load_cell32<D>(a, c, first, in);
     float sum[D + 2];
-    gather32<D>(a, c, sum);
+    if (ELL) gather32_ell<D>(a, c, sum);
+    else gather32<D>(a, c, sum);
     apply32<D, RES, GH>(a, c, sum, in, Ak, Bk, dt, dt32, first);
 }
 

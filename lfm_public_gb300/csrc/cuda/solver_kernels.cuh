@@ -49,6 +49,12 @@ struct RefState32 {
 };
 
 // Arguments shared by the kernels (all device pointers).
+// Fixed-width cell -> face table (Args::cfEll): four entries per 2D cell
+// (quads, triangles), six per 3D cell (hexahedra, prisms, tetrahedra).
+template <int D>
+constexpr int kEllWidth = D == 2 ? 4 : 6;
+constexpr int kEllPad = -2147483647 - 1;
+
 template <typename T>
 struct Args {
     int D, nq;
@@ -89,6 +95,10 @@ struct Args {
                               // (V then holds D x D more rows: its SGS stress), or null
     const uint8_t* cellGhosts;  // FP32-bulk single case: boundary faces of each cell
                                 // (its update writes their ghosts' primitives), or null
+    const int* cfEll;         // FP32-bulk single case: the cfList entries of each cell at a
+                              // fixed width (kEllWidth<D>), entry k of cell c at k * nc + c,
+                              // kEllPad after the cell's faces; null when a cell has more
+                              // faces (the update then gathers through cfOff / cfList)
     // ghosts
     const int* gCell;
     const int* gKind;

@@ -35,11 +35,32 @@ __global__ void __launch_bounds__(256) k_flux32(const __grid_constant__ Args<flo
     if (f < a.nf) flux32<D, SCH, true, LES>(a, f);
 }
 
-template <int D, bool RES, bool GH>
+// Warp-interleaved cells: warp j of block b updates the 32 cells of chunk
+// j * gridDim.x + b (coalesced within the warp), so a block's eight warps lie
+// in chunks spread over the mesh. The cells with boundary faces come first in
+// the solver order and write their ghosts' next state in FP64 (boundary
+// conditions with divisions, on an FP64 pipe that issues about two
+// instructions per clock per SM); interleaved, their warps land on different
+// SMs instead of filling the first few blocks, whose SMs would otherwise
+// finish last.
+template <int D, bool RES, bool GH, bool ELL>
 __global__ void __launch_bounds__(256) k_update32(const __grid_constant__ Args<float> a, double Ak, double Bk,
                                                   double dt, float dt32, int first) {
-    const int c = LFM_GLOBAL_ID();
-    if (c < a.nc) update32<D, RES, GH>(a, c, Ak, Bk, dt, dt32, first);
+    const int c = (int)(((threadIdx.x >> 5) * gridDim.x + blockIdx.x) << 5) + (int)(threadIdx.x & 31u);
+    if (c < a.nc) update32<D, RES, GH, ELL>(a, c, Ak, Bk, dt, dt32, first);
+}
+
+template <int D, bool ELL>
+void launch_update32(const Args<float>& a, const StageConfig& s, cudaStream_t st) {
+    const unsigned nb = (unsigned)((a.nc + 255) / 256);   // eight 32-cell chunks per block
+    const float dt32 = (float)s.dt;
+    if (a.cellGhosts) {
+        if (s.withRes) k_update32<D, true, true, ELL><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, dt32, s.first);
+        else k_update32<D, false, true, ELL><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, dt32, s.first);
+    } else {
+        if (s.withRes) k_update32<D, true, false, ELL><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, dt32, s.first);
+        else k_update32<D, false, false, ELL><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, dt32, s.first);
+    }
 }
 
 template <int D>
@@ -80,18 +101,10 @@ void launch_fp32(const Args<float>& a, const StageConfig& s, int which, cudaStre
                 else k_flux32<D, kSchemeAUSM, false><<<nblocks(a.nf, 256), 256, 0, st>>>(a);
             }
             break;
-        case 4: {
-            const unsigned nb = nblocks(a.nc, 256);
-            const float dt32 = (float)s.dt;
-            if (a.cellGhosts) {
-                if (s.withRes) k_update32<D, true, true><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, dt32, s.first);
-                else k_update32<D, false, true><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, dt32, s.first);
-            } else {
-                if (s.withRes) k_update32<D, true, false><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, dt32, s.first);
-                else k_update32<D, false, false><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, dt32, s.first);
-            }
+        case 4:
+            if (a.cfEll) launch_update32<D, true>(a, s, st);
+            else launch_update32<D, false>(a, s, st);
             break;
-        }
         default: break;
     }
 }

@@ -60,6 +60,7 @@ __global__ void __launch_bounds__(256) k_tile_stage(const __grid_constant__ Args
         la.cfOff = cfOff;
         la.cfList = cfOff + td.nV + 1;
         la.cfNbr = la.cfList + td.nE;
+        la.cfEll = nullptr;
         la.S = F;
         la.d = F + (size_t)D * nLF;
         la.w = F + (size_t)2 * D * nLF;

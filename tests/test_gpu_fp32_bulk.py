@@ -149,7 +149,15 @@ def _conversion_inputs():
     fl = rng.standard_normal(20000).astype(np.float32)
     ties = (fl.astype(np.float64) + np.spacing(fl).astype(np.float64) / 2).view(np.uint64)   # halfway cases
     sub = rng.uniform(0, 2e-38, 11).view(np.uint64)                                           # binary32 subnormals
-    f64 = np.concatenate([bits, vals, ties, sub])[:f32.size]
+    edge64 = np.array([
+        0x47EFFFFFE0000000, 0x47EFFFFFF0000000, 0x47EFFFFFEFFFFFFF, 0xC7EFFFFFF0000000,   # FLT_MAX, tie -> inf
+        0x47F0000000000000, 0x47E0000000000000,                                         # 2^128, 2^127
+        0x3FF0000010000000, 0x3FF0000030000000, 0x3FF0000010000001, 0x3FF000000FFFFFFF,   # ties even / odd
+        0x3FFFFFFFF0000000, 0xBFFFFFFFF0000001,                                         # carry into the exponent
+        0x3810000000000000, 0x380FFFFFFFFFFFFF, 0x380FFFFFF0000000, 0x3800000000000000,   # smallest normal float
+        0x0000000000000001, 0x8000000000000000, 0x0000000000000000, 0x7FF0000000000000,
+        0x7FF8000000000001, 0xFFF0000000000000], dtype=np.uint64)
+    f64 = np.concatenate([edge64, bits, vals, ties, sub])[:f32.size]
     return f32, f64
 
 

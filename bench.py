@@ -90,7 +90,7 @@ WORKLOAD_DESC = {
 # each captured launch). Keyed by (workload, precision, kernel).
 # profiles/fp32_kernels_cylinder768x512.md
 DRAM_TRAFFIC = {
-    ("cylinder2d", "fp32", "k_update"): 42934272 + 166912,
+    ("cylinder2d", "fp32", "k_update"): 42939648 + 210688,
     ("cylinder2d", "fp64", "k_flux"): 95860992 + 7875328,
 }
 

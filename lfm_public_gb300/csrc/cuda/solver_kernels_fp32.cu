@@ -42,11 +42,13 @@ __global__ void __launch_bounds__(256) k_flux32(const __grid_constant__ Args<flo
 // conditions with divisions, on an FP64 pipe that issues about two
 // instructions per clock per SM); interleaved, their warps land on different
 // SMs instead of filling the first few blocks, whose SMs would otherwise
-// finish last.
+// finish last. Without the ghost work (GH false) a block keeps 256
+// consecutive cells, which the large cases' gathers from HBM prefer.
 template <int D, bool RES, bool GH, bool ELL>
 __global__ void __launch_bounds__(256) k_update32(const __grid_constant__ Args<float> a, double Ak, double Bk,
                                                   double dt, float dt32, int first) {
-    const int c = (int)(((threadIdx.x >> 5) * gridDim.x + blockIdx.x) << 5) + (int)(threadIdx.x & 31u);
+    const int c = GH ? (int)(((threadIdx.x >> 5) * gridDim.x + blockIdx.x) << 5) + (int)(threadIdx.x & 31u)
+                     : (int)LFM_GLOBAL_ID();
     if (c < a.nc) update32<D, RES, GH, ELL>(a, c, Ak, Bk, dt, dt32, first);
 }
 

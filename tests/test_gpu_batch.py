@@ -63,7 +63,9 @@ def test_batch_mix_matches_alone_and_single_solver_bitwise():
 def test_single_solver_ghost_pass_variants_bitwise():
     """Above a size threshold the single-case solver prepares its ghosts in a
     separate kernel instead of inside the update; both give the batch's bits
-    (the batch always writes ghosts from the update)."""
+    (the batch always writes ghosts from the update). 3D single-case updates
+    gather through the fixed-width cell -> face table, the batch through the
+    face list: the same sums in the same order."""
     case = cases.cylinder_case(n_theta=96, n_r=48, r1=12, first=0.03, Ls=3, solver=1, minmod=False, n_span=64,
                                noise=0.01)   # 294,912 cells: above the 3D threshold
     ch = N.CaseHandle.from_case(case)

@@ -62,7 +62,7 @@ typedef struct lfm_solver_desc {
     int dim;                 /* 2 or 3 */
     int nq;                  /* dim + 2 */
     int solver;              /* LFM_SOLVER_* */
-    int rk_order;            /* stages per time step */
+    int rk_order;            /* stages per time step, 0..8 (0: a time step runs no stage) */
     int minmod;              /* fvSchemes lfm/minmodExists */
     int residuals;           /* controlDict lfm/post/haveResiduals */
     int64_t n_cells, n_cells0, n_ghosts, n_faces;

@@ -174,6 +174,9 @@ def structured_block(X: np.ndarray, periodic_j: bool, boundary: Dict[str, Tuple[
         int_faces.append(face_k(I, J, K))
         int_own.append(cid(I, J, K - 1))
         int_nei.append(cid(I, J, K))
+    if not int_faces:   # a single cell: no internal face
+        int_faces, int_own, int_nei = [np.zeros((0, 4), dtype=np.int64)], [np.zeros(0, np.int64)], \
+            [np.zeros(0, np.int64)]
     F = np.concatenate(int_faces)
     own = np.concatenate(int_own)
     nei = np.concatenate(int_nei)

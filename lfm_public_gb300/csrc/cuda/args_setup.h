@@ -25,12 +25,14 @@ inline int validateDesc(const lfm_solver_desc* d) {
         return lfm::setError(LFM_ERR_UNSUPPORTED, "mesh too large for 32-bit device indexing");
     if (!d->face_p || !d->face_n || !d->face_ghost || !d->S || !d->d || !d->w || !d->smag || !d->dmag_inv ||
         !d->dnorm || !d->delta_mag || !d->K || !d->vol_inv || !d->sponge || !d->cell_face_offsets ||
-        !d->cell_faces || !d->cell_face_sign || !d->cell_s_offsets || !d->cell_s || !d->rkA || !d->rkB ||
+        !d->cell_faces || !d->cell_face_sign || !d->cell_s_offsets || !d->cell_s ||
+        (d->rk_order > 0 && (!d->rkA || !d->rkB)) ||
         (d->n_ghosts > 0 && (!d->ghost_cell || !d->ghost_kind)) ||
         (d->n_halos > 0 && (!d->halo_src_part || !d->halo_src_cell)))
         return lfm::setError(LFM_ERR_INVALID, "incomplete solver description");
     if (d->n_halos < 0) return lfm::setError(LFM_ERR_INVALID, "negative halo count");
-    if (d->rk_order < 1 || d->rk_order > 8) return lfm::setError(LFM_ERR_INVALID, "rk_order out of range");
+    // rkOrder 0 runs no stage (the reference's stage loop runs rkOrder times)
+    if (d->rk_order < 0 || d->rk_order > 8) return lfm::setError(LFM_ERR_INVALID, "rk_order out of range");
     const int64_t nt = d->n_cells + d->n_ghosts + d->n_halos;
     for (int64_t f = 0; f < d->n_faces; ++f) {
         if (d->face_p[f] < 0 || d->face_p[f] >= d->n_cells || d->face_n[f] < 0 || d->face_n[f] >= nt)

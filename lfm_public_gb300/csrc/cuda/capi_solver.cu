@@ -655,8 +655,12 @@ extern "C" int lfm_solver_stage(lfm_solver* s, int rk, double dt) {
 
 extern "C" int lfm_solver_step(lfm_solver* s, int nsteps, double dt) {
     if (!s || nsteps < 0) return lfm::setError(LFM_ERR_INVALID, "bad argument");
-    if (s->rkOrder == 0 || nsteps == 0) return LFM_OK;
+    if (nsteps == 0) return LFM_OK;
     LFM_CUDA(cudaSetDevice(s->device));
+    if (s->rkOrder == 0) {   // no stage: a time step only clears the residual (prepare_for_timestep)
+        if (s->residuals) LFM_CUDA(cudaMemsetAsync(s->res, 0, sizeof(double) * (size_t)s->nq * s->nc, s->stream));
+        return LFM_OK;
+    }
     int rc = ensureGraph(s, dt);
     if (rc) return rc;
     if ((rc = ensurePrims(s))) return rc;
@@ -667,7 +671,7 @@ extern "C" int lfm_solver_step(lfm_solver* s, int nsteps, double dt) {
 extern "C" int lfm_solver_step_timed(lfm_solver* s, int nsteps, double dt, float* ms) {
     if (!s || !ms) return lfm::setError(LFM_ERR_INVALID, "bad argument");
     LFM_CUDA(cudaSetDevice(s->device));
-    int rc = ensureGraph(s, dt);
+    int rc = s->rkOrder > 0 ? ensureGraph(s, dt) : LFM_OK;
     if (rc) return rc;
     LFM_CUDA(cudaEventRecord(s->ev0, s->stream));
     rc = lfm_solver_step(s, nsteps, dt);
@@ -1058,6 +1062,7 @@ extern "C" int lfm_solver_profile_step(lfm_solver* s, double dt, int n, float* m
     if (!s || !ms || n < lfm::dev::kKernelSlots) return lfm::setError(LFM_ERR_INVALID, "bad argument");
     LFM_CUDA(cudaSetDevice(s->device));
     for (int k = 0; k < n; ++k) ms[k] = 0.f;
+    if (s->rkOrder == 0) return LFM_OK;   // no stage, no kernel
     int rc = ensurePrims(s);
     if (rc) return rc;
     const int K = lfm::dev::kKernelsPerStage;

@@ -42,5 +42,9 @@ def primitives(q, gamma, dim):
 
 
 def rel_l2(a, b):
-    """Relative L2 error of each conserved field (rows)."""
-    return np.linalg.norm(a - b, axis=1) / np.linalg.norm(b, axis=1)
+    """Relative L2 error of each conserved field (rows); a field that is zero
+    in b counts 0 when a matches it exactly and infinity otherwise."""
+    num = np.linalg.norm(a - b, axis=1)
+    den = np.linalg.norm(b, axis=1)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return np.where(den > 0, num / np.where(den > 0, den, 1.0), np.where(num > 0, np.inf, 0.0))

@@ -6,7 +6,7 @@ run."""
 import numpy as np
 import pytest
 
-from lfm_public_gb300 import _native as N, cases
+from lfm_public_gb300 import _native as N, acoustics, cases
 from tests.helpers import golden_names, load_golden, reference_conserved, rel_l2
 
 pytestmark = pytest.mark.gpu
@@ -51,6 +51,66 @@ def test_fp64_matches_oracle_3d_and_triangles():
         q_gpu = _gpu_run(ch, n, case.delta_t)
         q_ref, _ = N.port_run(ch, ch.q0(), n, case.delta_t)
         assert np.all(rel_l2(q_gpu, q_ref) <= TOL), (case.name, rel_l2(q_gpu, q_ref))
+
+
+@pytest.mark.parametrize("rk", [0, 1, 2, 3, 4])
+def test_rk_orders_match_oracle(rk):
+    """rkOrder 0-4 (5 is every other test's): FP64 within 1e-12 of the
+    oracle, FP32-bulk p' within 1e-3 of FP64, and a batch of rkOrder-rk
+    cases bitwise the single-case FP32-bulk solver (rkOrder 0: no stage, the
+    state stays; batches take 1 and above)."""
+    case = cases.cylinder_case(n_theta=48, n_r=24, r1=15, first=0.02, Ls=4, solver=rk % 3, minmod=True, noise=0.02)
+    case.rk_order = rk
+    ch = N.CaseHandle.from_case(case)
+    assert ch.desc.rk_order == rk
+    n = 10
+    q64 = _gpu_run(ch, n, case.delta_t)
+    q_ref, _ = N.port_run(ch, ch.q0(), n, case.delta_t)
+    assert np.all(rel_l2(q64, q_ref) <= TOL), rel_l2(q64, q_ref)
+    q32 = _gpu_run(ch, n, case.delta_t, N.LFM_FP32_BULK)
+    assert acoustics.acoustic_rel_l2(q32, q64, ch.desc.gamma, case.dim, case.p_inf) <= 1e-3
+    if rk == 0:
+        assert np.array_equal(q64, ch.q0())
+        return
+    b = N.Batch(rk_order=rk, arena_bytes=256 << 20)
+    slot = b.add(ch, case.delta_t)
+    b.step(n)
+    b.sync()
+    assert np.array_equal(b.get_state(slot), q32)
+    b.close()
+
+
+@pytest.mark.parametrize("make", [lambda: cases.vortex_case(n=1), lambda: cases.vortex_case(n=2),
+                                  lambda: cases.vortex_case(n=3, ny=1), lambda: cases.tri_case(n=1, seed=3),
+                                  lambda: cases.tri_case(n=2, seed=3, solver=1)],
+                         ids=["1cell", "2x2", "3x1", "2tri", "8tri"])
+def test_tiny_meshes(make):
+    """One cell (no internal face), meshes without interior submesh, two
+    triangles: FP64 within 1e-12 of the oracle, FP32-bulk near FP64 and the
+    batch bitwise the single-case FP32-bulk solver."""
+    case = make()
+    ch = N.CaseHandle.from_case(case)
+    n = 5
+    q64 = _gpu_run(ch, n, case.delta_t)
+    q_ref, _ = N.port_run(ch, ch.q0(), n, case.delta_t)
+
+    def err(a, b):
+        # momentum as one vector field: on these symmetric meshes a momentum
+        # component can be pure rounding noise (1e-8 against 1e2)
+        e = rel_l2(a, b)
+        m = slice(1, 1 + case.dim)
+        e[m] = np.linalg.norm(a[m] - b[m], axis=1) / np.linalg.norm(b[m])
+        return e
+
+    assert np.all(err(q64, q_ref) <= TOL), err(q64, q_ref)
+    q32 = _gpu_run(ch, n, case.delta_t, N.LFM_FP32_BULK)
+    assert np.all(err(q32, q64) <= 1e-5), err(q32, q64)
+    b = N.Batch(arena_bytes=64 << 20)
+    slot = b.add(ch, case.delta_t)
+    b.step(n)
+    b.sync()
+    assert np.array_equal(b.get_state(slot), q32)
+    b.close()
 
 
 def test_bitwise_reproducible_and_stage_api_equivalent():

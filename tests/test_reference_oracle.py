@@ -50,3 +50,38 @@ def test_viscous_cylinder_ausm_bitwise():
     r, U, E, p = primitives(q, ch.desc.gamma, 2)
     assert np.array_equal(r, ref["rho"][ids]) and np.array_equal(E, ref["E"][ids])
     assert np.array_equal(U, ref["U"][ids][:, :2].T)
+
+
+@pytest.mark.parametrize("rk", [0, 1, 2, 3, 4])
+def test_rk_orders_bitwise(rk):
+    """Every rkOrder the reference accepts: 0 and 1 forward Euler (0 runs no
+    stage: the state stays), 2 the two-stage set, 3 the first three stages of
+    the four-stage low-storage set, 4 all four (src/cfd_v0.cpp:86-128; the
+    stage loop runs rkOrder stages, src/mesh_solver.cpp:500)."""
+    case = cases.cylinder_case(n_theta=16, n_r=8, r1=6, first=0.05, Ls=2, solver=rk % 2, minmod=True, noise=0.05,
+                               seed=9, reynolds=60.0)
+    case.rk_order = rk
+    ch, q, ref = _run_both(case, 4)
+    assert ch.desc.rk_order == rk
+    ids = ch.cell_ids()
+    r, U, E, p = primitives(q, ch.desc.gamma, 2)
+    assert np.array_equal(r, ref["rho"][ids]) and np.array_equal(E, ref["E"][ids])
+    assert np.array_equal(p, ref["p"][ids])
+    if rk == 0:
+        assert np.array_equal(q, ch.q0())
+
+
+@pytest.mark.parametrize("make", [lambda: cases.vortex_case(n=1), lambda: cases.vortex_case(n=2),
+                                  lambda: cases.vortex_case(n=3, ny=1), lambda: cases.tri_case(n=1, seed=3),
+                                  lambda: cases.tri_case(n=2, seed=3, solver=1)],
+                         ids=["1cell", "2x2", "3x1", "2tri", "8tri"])
+def test_tiny_meshes_bitwise(make):
+    """The smallest meshes: one cell (no internal face), every cell in the
+    boundary submesh, two triangles."""
+    case = make()
+    ch, q, ref = _run_both(case, 3)
+    assert ch.desc.n_cells0 == ch.desc.n_cells   # no interior submesh
+    ids = ch.cell_ids()
+    r, U, E, p = primitives(q, ch.desc.gamma, 2)
+    assert np.array_equal(r, ref["rho"][ids]) and np.array_equal(E, ref["E"][ids])
+    assert np.array_equal(p, ref["p"][ids])

@@ -456,6 +456,104 @@ def tri_case(n: int = 64, half: float = 10.0, jitter: float = 0.2, seed: int = 0
     return case
 
 
+def hybrid_case(n: int = 16, tri_fraction: float = 0.5, half: float = 10.0, jitter: float = 0.2, seed: int = 0,
+                mach: float = 0.5, beta: float = 5.0, solver: int = 0, n_steps: int = 100, cfl: float = 0.5) -> Case:
+    """Mixed quadrilaterals and triangles on [-half, half]^2: the jittered
+    n x n grid of ``tri_case`` with a random tri_fraction of its quads split
+    along a random diagonal, extruded one cell thick (cells of 4 and 3 faces
+    in one mesh; the reference sizes its solver for 4 and leaves a triangle's
+    fourth slot empty). Patches and flow as ``vortex_case``."""
+    rng = np.random.default_rng(seed)
+    h = 2 * half / n
+    xs = np.linspace(-half, half, n + 1)
+    XX, YY = np.meshgrid(xs, xs, indexing="ij")
+    inner = np.zeros_like(XX, dtype=bool)
+    inner[1:-1, 1:-1] = True
+    XX = XX + np.where(inner, rng.uniform(-jitter, jitter, XX.shape) * h, 0.0)
+    YY = YY + np.where(inner, rng.uniform(-jitter, jitter, YY.shape) * h, 0.0)
+    nodes = np.stack([XX.ravel(), YY.ravel()], axis=1)
+    polys = []
+    for i in range(n):
+        for j in range(n):
+            a, b, c, d = i * (n + 1) + j, (i + 1) * (n + 1) + j, (i + 1) * (n + 1) + j + 1, i * (n + 1) + j + 1
+            if rng.uniform() < tri_fraction:
+                if rng.integers(0, 2):
+                    polys += [(a, b, c), (a, c, d)]
+                else:
+                    polys += [(a, b, d), (b, c, d)]
+            else:
+                polys.append((a, b, c, d))
+    case = _polygon_mesh(nodes, polys, half, f"hybrid{n}", solver=solver, n_steps=n_steps)
+    c0 = sound_speed(case)
+    case.U_inf = (mach * c0, 0.0, 0.0)
+    case.mach = mach
+    x, y = case.cell_centres[:, 0], case.cell_centres[:, 1]
+    p, T, u, v = isentropic_vortex(case, x, y, beta)
+    case.fields = {"p": p, "T": T, "U": np.stack([u, v, np.zeros_like(u)], axis=1), "alpha": half - x}
+    case.delta_t = acoustic_dt(case, cfl, np.hypot(u, v), T, np.full(case.n_cells, 0.5 * h * (1 - 2 * jitter)))
+    return case
+
+
+def _polygon_mesh(nodes, polys, half, name, **kw) -> Case:
+    """polyMesh of counter-clockwise polygons (any vertex counts) extruded one
+    cell thick in z, patches as ``_prism_mesh``. A loop over the cells: for
+    test-sized meshes."""
+    N = nodes.shape[0]
+    T = len(polys)
+    pts = np.zeros((2 * N, 3))
+    pts[:N, :2] = nodes
+    pts[N:, :2] = nodes
+    pts[N:, 2] = 1.0
+    edges = {}
+    for t, pv in enumerate(polys):
+        for k in range(len(pv)):
+            a, b = pv[k], pv[(k + 1) % len(pv)]
+            edges.setdefault((min(a, b), max(a, b)), []).append((t, a, b))
+    internal, boundary = [], []
+    for es in edges.values():
+        if len(es) == 2:
+            (t0, a0, b0), (t1, a1, b1) = es
+            if t0 > t1:
+                (t0, a0, b0), (t1, a1, b1) = (t1, a1, b1), (t0, a0, b0)
+            internal.append((t0, t1, (a0, b0, b0 + N, a0 + N)))   # as seen by the owner
+        else:
+            t, a, b = es[0]
+            boundary.append((t, (a, b, b + N, a + N)))
+    internal.sort(key=lambda e: (e[0], e[1]))
+    tol = 1e-9 * half
+    groups = {"inlet": [], "outlet": [], "walls": []}
+    for t, f in boundary:
+        mx = 0.5 * (nodes[f[0], 0] + nodes[f[1], 0])
+        groups["inlet" if mx < -half + tol else "outlet" if mx > half - tol else "walls"].append((t, f))
+    faces = [f for _, _, f in internal]
+    owner = [t for t, _, _ in internal]
+    neighbour = [t1 for _, t1, _ in internal]
+    patches = []
+    start = len(faces)
+    for pname, ptype in (("inlet", "patch"), ("outlet", "patch"), ("walls", "wall")):
+        for t, f in groups[pname]:
+            faces.append(f)
+            owner.append(t)
+        patches.append(Patch(pname, ptype, start, len(groups[pname])))
+        start += len(groups[pname])
+    for t, pv in enumerate(polys):        # back (z = 0), normal -z
+        faces.append(tuple(pv[::-1]))
+        owner.append(t)
+    for t, pv in enumerate(polys):        # front (z = 1), normal +z
+        faces.append(tuple(v + N for v in pv))
+        owner.append(t)
+    patches.append(Patch("frontAndBack", "empty", start, 2 * T))
+    face_points = np.array([v for f in faces for v in f], dtype=np.int64)
+    face_offsets = np.concatenate([[0], np.cumsum([len(f) for f in faces])]).astype(np.int64)
+    cc = np.zeros((T, 3))
+    cc[:, :2] = np.array([nodes[list(pv)].mean(axis=0) for pv in polys])
+    cc[:, 2] = 0.5
+    R = RUNIVERSAL / 28.9647 * 1000
+    return Case(name=name, dim=2, points=pts, face_offsets=face_offsets, face_points=face_points,
+                owner=np.array(owner, dtype=np.int64), neighbour=np.array(neighbour, dtype=np.int64),
+                patches=patches, n_cells=T, cell_centres=cc, Cp=3.5 * R, mol_weight=28.9647, Pr=0.71, Ls=2.0, **kw)
+
+
 def _prism_mesh(nodes, tris, half, name, **kw) -> Case:
     N = nodes.shape[0]
     T = tris.shape[0]

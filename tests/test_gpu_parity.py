@@ -113,6 +113,30 @@ def test_tiny_meshes(make):
     b.close()
 
 
+@pytest.mark.parametrize("solver", [0, 1, 2])
+def test_mixed_quad_triangle_mesh(solver):
+    """Quadrilaterals and triangles in one mesh (cells of 4 and 3 faces; the
+    reference itself stops on such a submesh, so the oracle is the bar): FP64
+    within 1e-12 of the oracle, FP32-bulk p' within 1e-3 and the batch
+    bitwise the single-case FP32-bulk solver."""
+    case = cases.hybrid_case(n=24, tri_fraction=0.4, seed=5 + solver, solver=solver, beta=3.0)
+    ch = N.CaseHandle.from_case(case)
+    offs = np.ctypeslib.as_array(ch.desc.cell_face_offsets, shape=(ch.desc.n_cells + 1,))
+    assert set(np.diff(offs).tolist()) == {3, 4}
+    n = 20
+    q64 = _gpu_run(ch, n, case.delta_t)
+    q_ref, _ = N.port_run(ch, ch.q0(), n, case.delta_t)
+    assert np.all(rel_l2(q64, q_ref) <= TOL), rel_l2(q64, q_ref)
+    q32 = _gpu_run(ch, n, case.delta_t, N.LFM_FP32_BULK)
+    assert acoustics.acoustic_rel_l2(q32, q64, ch.desc.gamma, case.dim, case.p_inf) <= 1e-3
+    b = N.Batch(arena_bytes=64 << 20)
+    slot = b.add(ch, case.delta_t)
+    b.step(n)
+    b.sync()
+    assert np.array_equal(b.get_state(slot), q32)
+    b.close()
+
+
 def test_bitwise_reproducible_and_stage_api_equivalent():
     case = cases.cylinder_case(n_theta=64, n_r=32, r1=20, first=0.02, Ls=5, solver=2, minmod=True, noise=0.02)
     ch = N.CaseHandle.from_case(case)

@@ -85,3 +85,21 @@ def test_tiny_meshes_bitwise(make):
     r, U, E, p = primitives(q, ch.desc.gamma, 2)
     assert np.array_equal(r, ref["rho"][ids]) and np.array_equal(E, ref["E"][ids])
     assert np.array_equal(p, ref["p"][ids])
+
+
+@pytest.mark.parametrize("frac", [0.0, 1.0])
+def test_polygon_mesh_generator_bitwise(frac):
+    """The loop-based polygon generator behind the mixed-cell meshes gives the
+    reference's results on all-quad and all-triangle grids. (A mesh that
+    mixes quadrilaterals and triangles in one submesh stops the reference:
+    its reorder_faces reads every one of the solver's FACE_CNT neighbour
+    slots, src/cfd_v0.cpp:298-304, and a triangle's fourth is unset. The
+    device path runs such meshes; tests/test_gpu_parity.py checks them
+    against the oracle.)"""
+    case = cases.hybrid_case(n=5, tri_fraction=frac, seed=3 + int(frac))
+    ch, q, ref = _run_both(case, 4)
+    assert ch.desc.n_cells == (50 if frac else 25)
+    ids = ch.cell_ids()
+    r, U, E, p = primitives(q, ch.desc.gamma, 2)
+    assert np.array_equal(r, ref["rho"][ids]) and np.array_equal(E, ref["E"][ids])
+    assert np.array_equal(p, ref["p"][ids])

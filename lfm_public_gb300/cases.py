@@ -494,6 +494,139 @@ def hybrid_case(n: int = 16, tri_fraction: float = 0.5, half: float = 10.0, jitt
     return case
 
 
+def _polyhedral_mesh(pts: np.ndarray, cells, half: float, name: str, **kw) -> Case:
+    """3D polyMesh from convex cells given as lists of faces (vertex tuples in
+    cyclic order, either orientation): each face is oriented outward from its
+    cell by the cell-centroid test, a face shared by two cells is internal
+    (owner the lower cell, oriented outward from it), the others form the
+    patches inlet (x = -half), outlet (x = +half) and walls. A loop over the
+    cells: for test-sized meshes."""
+    T = len(cells)
+    cc = np.zeros((T, 3))
+    shared = {}
+    for t, faces in enumerate(cells):
+        verts = sorted({v for f in faces for v in f})
+        c = pts[verts].mean(axis=0)
+        cc[t] = c
+        for f in faces:
+            f = tuple(f)
+            P = pts[list(f)]
+            nrm = np.cross(P[1] - P[0], P[2] - P[0])
+            if np.dot(nrm, P.mean(axis=0) - c) < 0:
+                f = f[::-1]
+            shared.setdefault(tuple(sorted(f)), []).append((t, f))
+    internal, boundary = [], []
+    for es in shared.values():
+        if len(es) == 2:
+            (t0, f0), (t1, f1) = sorted(es, key=lambda e: e[0])
+            internal.append((t0, t1, f0))
+        else:
+            boundary.append(es[0])
+    internal.sort(key=lambda e: (e[0], e[1]))
+    tol = 1e-9 * half
+    groups = {"inlet": [], "outlet": [], "walls": []}
+    for t, f in boundary:
+        mx = pts[list(f), 0].mean()
+        groups["inlet" if mx < -half + tol else "outlet" if mx > half - tol else "walls"].append((t, f))
+    faces = [f for _, _, f in internal]
+    owner = [t for t, _, _ in internal]
+    neighbour = [t1 for _, t1, _ in internal]
+    patches = []
+    start = len(faces)
+    for pname, ptype in (("inlet", "patch"), ("outlet", "patch"), ("walls", "wall")):
+        for t, f in groups[pname]:
+            faces.append(f)
+            owner.append(t)
+        patches.append(Patch(pname, ptype, start, len(groups[pname])))
+        start += len(groups[pname])
+    face_points = np.array([v for f in faces for v in f], dtype=np.int64)
+    face_offsets = np.concatenate([[0], np.cumsum([len(f) for f in faces])]).astype(np.int64)
+    R = RUNIVERSAL / 28.9647 * 1000
+    return Case(name=name, dim=3, points=pts, face_offsets=face_offsets, face_points=face_points,
+                owner=np.array(owner, dtype=np.int64), neighbour=np.array(neighbour, dtype=np.int64),
+                patches=patches, n_cells=T, cell_centres=cc, Cp=3.5 * R, mol_weight=28.9647, Pr=0.71, Ls=2.0, **kw)
+
+
+def _vortex_tube(case: Case, half: float, beta: float, mach: float, h: float, cfl: float) -> Case:
+    c0 = sound_speed(case)
+    case.U_inf = (mach * c0, 0.0, 0.0)
+    case.mach = mach
+    x, y = case.cell_centres[:, 0], case.cell_centres[:, 1]
+    p, T, u, v = isentropic_vortex(case, x, y, beta)
+    case.fields = {"p": p, "T": T, "U": np.stack([u, v, np.zeros_like(u)], axis=1), "alpha": half - x}
+    case.delta_t = acoustic_dt(case, cfl, np.hypot(u, v), T, np.full(case.n_cells, h))
+    return case
+
+
+def prism_case(n: int = 8, nz: int = 3, half: float = 10.0, depth: float = 4.0, jitter: float = 0.2, seed: int = 0,
+               mach: float = 0.5, beta: float = 3.0, solver: int = 0, n_steps: int = 100, cfl: float = 0.5) -> Case:
+    """3D triangular prisms (five faces a cell): the jittered triangulation of
+    ``tri_case`` extruded into nz layers over z in [0, depth]; walls at the
+    ends in z, an isentropic vortex tube along z."""
+    rng = np.random.default_rng(seed)
+    h = 2 * half / n
+    xs = np.linspace(-half, half, n + 1)
+    XX, YY = np.meshgrid(xs, xs, indexing="ij")
+    inner = np.zeros_like(XX, dtype=bool)
+    inner[1:-1, 1:-1] = True
+    XX = XX + np.where(inner, rng.uniform(-jitter, jitter, XX.shape) * h, 0.0)
+    YY = YY + np.where(inner, rng.uniform(-jitter, jitter, YY.shape) * h, 0.0)
+    nn = (n + 1) * (n + 1)
+    zs = np.linspace(0.0, depth, nz + 1)
+    pts = np.zeros((nn * (nz + 1), 3))
+    for k in range(nz + 1):
+        pts[k * nn:(k + 1) * nn, 0] = XX.ravel()
+        pts[k * nn:(k + 1) * nn, 1] = YY.ravel()
+        pts[k * nn:(k + 1) * nn, 2] = zs[k]
+    tris = []
+    for i in range(n):
+        for j in range(n):
+            a, b, c, d = i * (n + 1) + j, (i + 1) * (n + 1) + j, (i + 1) * (n + 1) + j + 1, i * (n + 1) + j + 1
+            tris += [(a, b, c), (a, c, d)] if rng.integers(0, 2) else [(a, b, d), (b, c, d)]
+    cells = []
+    for k in range(nz):
+        lo, hi = k * nn, (k + 1) * nn
+        for (a, b, c) in tris:
+            tri_lo, tri_hi = (a + lo, b + lo, c + lo), (a + hi, b + hi, c + hi)
+            sides = [(u + lo, w + lo, w + hi, u + hi) for u, w in ((a, b), (b, c), (c, a))]
+            cells.append([tri_lo, tri_hi] + sides)
+    case = _polyhedral_mesh(pts, cells, half, f"prism{n}x{nz}", solver=solver, n_steps=n_steps)
+    return _vortex_tube(case, half, beta, mach, min(0.5 * h * (1 - 2 * jitter), 0.5 * depth / nz), cfl)
+
+
+def tet_case(n: int = 5, nz: int = 2, half: float = 10.0, depth: float = 4.0, seed: int = 0, mach: float = 0.5,
+             beta: float = 3.0, solver: int = 0, n_steps: int = 100, cfl: float = 0.5) -> Case:
+    """3D tetrahedra (four faces a cell): an n x n x nz box of hexahedra over
+    [-half, half]^2 x [0, depth], each split into the six tetrahedra of its
+    main diagonal (Kuhn's subdivision, conforming between neighbours); walls
+    at the ends in z, an isentropic vortex tube along z. seed jitters the
+    interior vertices in x and y by up to 15 % of the spacing."""
+    import itertools
+    rng = np.random.default_rng(seed)
+    h = 2 * half / n
+    xs, zs = np.linspace(-half, half, n + 1), np.linspace(0.0, depth, nz + 1)
+    X, Y, Z = np.meshgrid(xs, xs, zs, indexing="ij")
+    inner = np.zeros_like(X, dtype=bool)
+    inner[1:-1, 1:-1, :] = True
+    X = X + np.where(inner, rng.uniform(-0.15, 0.15, X.shape) * h, 0.0)
+    Y = Y + np.where(inner, rng.uniform(-0.15, 0.15, Y.shape) * h, 0.0)
+    pts = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    vid = lambda i, j, k: (i * (n + 1) + j) * (nz + 1) + k  # noqa: E731
+    cells = []
+    for i in range(n):
+        for j in range(n):
+            for k in range(nz):
+                for perm in itertools.permutations(range(3)):
+                    p = [0, 0, 0]
+                    path = [vid(i, j, k)]
+                    for ax in perm:
+                        p[ax] += 1
+                        path.append(vid(i + p[0], j + p[1], k + p[2]))
+                    cells.append([tuple(path[m] for m in range(4) if m != skip) for skip in range(4)])
+    case = _polyhedral_mesh(pts, cells, half, f"tet{n}x{nz}", solver=solver, n_steps=n_steps)
+    return _vortex_tube(case, half, beta, mach, 0.2 * min(h, depth / nz), cfl)
+
+
 def _polygon_mesh(nodes, polys, half, name, **kw) -> Case:
     """polyMesh of counter-clockwise polygons (any vertex counts) extruded one
     cell thick in z, patches as ``_prism_mesh``. A loop over the cells: for

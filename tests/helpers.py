@@ -41,6 +41,17 @@ def primitives(q, gamma, dim):
     return r, U, E, p
 
 
+def rel_l2_vec(a, b, dim):
+    """rel_l2 with the momentum rows measured as one vector field: each
+    component's error against the norm of the whole momentum (a component
+    that stays zero up to rounding, such as w in a flow uniform along z,
+    would otherwise compare rounding noise with rounding noise)."""
+    e = rel_l2(a, b)
+    m = slice(1, 1 + dim)
+    e[m] = np.linalg.norm(a[m] - b[m], axis=1) / np.linalg.norm(b[m])
+    return e
+
+
 def rel_l2(a, b):
     """Relative L2 error of each conserved field (rows); a field that is zero
     in b counts 0 when a matches it exactly and infinity otherwise."""

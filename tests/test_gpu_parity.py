@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from lfm_public_gb300 import _native as N, acoustics, cases
-from tests.helpers import golden_names, load_golden, reference_conserved, rel_l2
+from tests.helpers import golden_names, load_golden, reference_conserved, rel_l2, rel_l2_vec
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-12
@@ -93,15 +93,9 @@ def test_tiny_meshes(make):
     n = 5
     q64 = _gpu_run(ch, n, case.delta_t)
     q_ref, _ = N.port_run(ch, ch.q0(), n, case.delta_t)
-
-    def err(a, b):
-        # momentum as one vector field: on these symmetric meshes a momentum
-        # component can be pure rounding noise (1e-8 against 1e2)
-        e = rel_l2(a, b)
-        m = slice(1, 1 + case.dim)
-        e[m] = np.linalg.norm(a[m] - b[m], axis=1) / np.linalg.norm(b[m])
-        return e
-
+    # momentum as one vector field: on these symmetric meshes a momentum
+    # component can be pure rounding noise (1e-8 against 1e2)
+    err = lambda a, b: rel_l2_vec(a, b, case.dim)  # noqa: E731
     assert np.all(err(q64, q_ref) <= TOL), err(q64, q_ref)
     q32 = _gpu_run(ch, n, case.delta_t, N.LFM_FP32_BULK)
     assert np.all(err(q32, q64) <= 1e-5), err(q32, q64)
@@ -127,6 +121,31 @@ def test_mixed_quad_triangle_mesh(solver):
     q64 = _gpu_run(ch, n, case.delta_t)
     q_ref, _ = N.port_run(ch, ch.q0(), n, case.delta_t)
     assert np.all(rel_l2(q64, q_ref) <= TOL), rel_l2(q64, q_ref)
+    q32 = _gpu_run(ch, n, case.delta_t, N.LFM_FP32_BULK)
+    assert acoustics.acoustic_rel_l2(q32, q64, ch.desc.gamma, case.dim, case.p_inf) <= 1e-3
+    b = N.Batch(arena_bytes=64 << 20)
+    slot = b.add(ch, case.delta_t)
+    b.step(n)
+    b.sync()
+    assert np.array_equal(b.get_state(slot), q32)
+    b.close()
+
+
+@pytest.mark.parametrize("make", [lambda: cases.prism_case(n=10, nz=4, seed=3, solver=1),
+                                  lambda: cases.tet_case(n=6, nz=3, seed=4, solver=2)], ids=["prisms", "tets"])
+def test_3d_prisms_and_tetrahedra(make):
+    """Cells of five and four faces in 3D: FP64 within 1e-12 of the oracle,
+    FP32-bulk p' within 1e-3, and the batch bitwise the single-case FP32-bulk
+    solver (whose 3D update pads these cells' rows of the fixed-width face
+    table)."""
+    case = make()
+    ch = N.CaseHandle.from_case(case)
+    n = 10
+    q64 = _gpu_run(ch, n, case.delta_t)
+    q_ref, _ = N.port_run(ch, ch.q0(), n, case.delta_t)
+    # momentum as one vector: the prisms' w stays zero up to rounding (1e-12 against 6e3)
+    err = rel_l2_vec(q64, q_ref, case.dim)
+    assert np.all(err <= TOL), err
     q32 = _gpu_run(ch, n, case.delta_t, N.LFM_FP32_BULK)
     assert acoustics.acoustic_rel_l2(q32, q64, ch.desc.gamma, case.dim, case.p_inf) <= 1e-3
     b = N.Batch(arena_bytes=64 << 20)

@@ -103,3 +103,23 @@ def test_polygon_mesh_generator_bitwise(frac):
     r, U, E, p = primitives(q, ch.desc.gamma, 2)
     assert np.array_equal(r, ref["rho"][ids]) and np.array_equal(E, ref["E"][ids])
     assert np.array_equal(p, ref["p"][ids])
+
+
+@pytest.mark.parametrize("make,faces", [
+    (lambda: cases.prism_case(n=4, nz=2, seed=1), 5),
+    (lambda: cases.prism_case(n=5, nz=3, seed=2, solver=1), 5),
+    (lambda: cases.tet_case(n=3, nz=2, seed=1), 4),
+    (lambda: cases.tet_case(n=3, nz=2, seed=2, solver=2), 4),
+], ids=["prism_m1", "prism_m2", "tet_m1", "tet_ausm"])
+def test_3d_prisms_and_tetrahedra_bitwise(make, faces):
+    """The reference's 3D solvers for five and four faces a cell
+    (src/mesh_solver.cpp:56-70): extruded triangular prisms and Kuhn
+    tetrahedra."""
+    case = make()
+    ch, q, ref = _run_both(case, 3)
+    offs = np.ctypeslib.as_array(ch.desc.cell_face_offsets, shape=(ch.desc.n_cells + 1,))
+    assert set(np.diff(offs).tolist()) == {faces}
+    ids = ch.cell_ids()
+    r, U, E, p = primitives(q, ch.desc.gamma, 3)
+    assert np.array_equal(r, ref["rho"][ids]) and np.array_equal(E, ref["E"][ids])
+    assert np.array_equal(p, ref["p"][ids])

@@ -55,6 +55,13 @@ FIXTURES = {
                                                   minmod=False, noise=0.05, reynolds=50.0), 20),
     "les_cyl16x8x4_m1_3d": (cases.cylinder_case, dict(n_theta=16, n_r=8, r1=10, first=0.05, Ls=3, solver=0,
                                                       n_span=4, noise=0.05, reynolds=50.0), 10),
+    # the reference's 3D solvers for five and four faces a cell
+    "prism5x3_m2_3d": (cases.prism_case, dict(n=5, nz=3, seed=2, solver=1), 10),
+    "tet3x2_ausm_3d": (cases.tet_case, dict(n=3, nz=2, seed=2, solver=2), 10),
+    # edge cases: one cell (no internal face), rkOrder 3 (three stages of the four-stage set)
+    "vortex1_m1": (cases.vortex_case, dict(n=1), 5),
+    "cyl16x8_m1_rk3": (cases.cylinder_case, dict(n_theta=16, n_r=8, r1=6, first=0.05, Ls=2, solver=0, minmod=True,
+                                                 noise=0.05, seed=9, reynolds=60.0), 10),
 }
 
 
@@ -165,16 +172,23 @@ def main_post():
         print(f"{name}: {case.n_cells} cells, {n} steps, {forces.shape[0]} force records")
 
 
-def main():
+def main(only=()):
+    """Writes every fixture, or only the named ones."""
     if not os.path.exists(ORACLE):
         raise SystemExit(f"{ORACLE} is missing: run `make -C oracle` where the reference sources exist")
-    main_post()
+    if not only:
+        main_post()
     for name, (gen, kw, n) in FIXTURES.items():
+        if only and name not in only:
+            continue
         case = gen(n_steps=n, **kw)
         if name.endswith("_res"):
             case.residuals = True
         if name.startswith("les_"):
             case.laminar = False
+        m = re.search(r"_rk(\d)$", name)
+        if m:
+            case.rk_order = int(m.group(1))
         tmp = tempfile.mkdtemp(prefix="lfm_golden_")
         try:
             res, cfl, _ = run_reference(case, n, tmp)
@@ -189,4 +203,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

@@ -28,7 +28,7 @@ def test_fp64_matches_reference_fixture(name):
     ch = N.CaseHandle.from_case(case)
     q = _gpu_run(ch, int(z["n_steps"]), case.delta_t)
     ref = reference_conserved(z, ch.cell_ids(), case.dim)
-    err = rel_l2(q, ref)
+    err = rel_l2_vec(q, ref, case.dim)   # the prisms' w is rounding noise
     assert np.all(err <= TOL), err
 
 

@@ -39,6 +39,9 @@ def test_fixtures_cover_the_schemes_and_shapes():
     names = golden_names()
     assert any("m1" in n for n in names) and any("m2" in n for n in names) and any("ausm" in n for n in names)
     assert any("3d" in n for n in names) and any("tri" in n for n in names)
+    # the 3D element types of the reference's 5- and 4-face solvers, one cell, rkOrder 3
+    assert {"prism5x3_m2_3d", "tet3x2_ausm_3d", "vortex1_m1", "cyl16x8_m1_rk3"} <= set(names)
+    assert load_golden("cyl16x8_m1_rk3")[0].rk_order == 3
 
 
 def test_port_cell_residual_matches_reference_bitwise():

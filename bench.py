@@ -66,6 +66,9 @@ def workload(name: str):
     if name == "cylinder3d":
         return cases.cylinder_case(n_theta=384, n_r=256, n_span=96, solver=1, reynolds=3900.0, noise=0.01, seed=3900,
                                    minmod=False)
+    if name == "cylinder3d_small":
+        return cases.cylinder_case(n_theta=192, n_r=128, n_span=48, solver=1, reynolds=3900.0, noise=0.01, seed=3900,
+                                   minmod=False)
     raise ValueError(f"unknown workload {name}")
 
 
@@ -82,6 +85,10 @@ WORKLOAD_DESC = {
                      scheme="M1", faces_per_cell=4, viscous=False),
     "cylinder3d": dict(workload="3D cylinder wake 384x256x96, M2, cyclic span, rkOrder 5", cells=9437184, dim=3,
                        scheme="M2", faces_per_cell=6, viscous=True),
+    # the same wake at an eighth of the cells (working set ~0.9 GB, still
+    # beyond L2): the size the 3D kernels are profiled at
+    "cylinder3d_small": dict(workload="3D cylinder wake 192x128x48, M2, cyclic span, rkOrder 5", cells=1179648,
+                             dim=3, scheme="M2", faces_per_cell=6, viscous=True),
 }
 
 

@@ -436,11 +436,12 @@ __device__ __forceinline__ float p5diff_dd(float a, float b, float alpha) {
 // viscous terms (linear in the gradients, so unchanged in form).
 // ---------------------------------------------------------------------------
 // VIS = false compiles the viscous terms out (for callers that know mu = 0).
-// EARLYV loads the viscous rows of both cells together with the primitives,
-// so the two gathers overlap instead of following one another: 2 x 15 more
-// live values in 3D, where the gathers come from HBM (the stand-alone 3D flux
-// kernel); the fused kernels, whose registers other phases already fill, and
-// 2D, whose gathers hit L2, keep the late loads.
+// EARLYV loads the viscous rows of both cells and the face's viscous geometry
+// together with the primitives, so the gathers overlap instead of following
+// one another (2 x 8 more live values in 2D, 2 x 15 in 3D): the stand-alone
+// flux kernel (3D flux 4.05 -> 3.43 ms per step on the 9.4M-cell wake, whose
+// gathers come from HBM; 2 % in 2D, whose gathers hit L2). The fused kernels,
+// whose registers other phases already fill, keep the late loads.
 template <int D, int SCH, bool VIS = true, bool LES = false, bool EARLYV = false>
 __device__ __forceinline__ void flux32(const Args<float>& a, int f) {
     constexpr int NQ = D + 2;

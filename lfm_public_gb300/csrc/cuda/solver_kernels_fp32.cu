@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(256, 6) k_vis32(const __grid_constant__ Args<f
 template <int D, int SCH, bool LES>
 __global__ void __launch_bounds__(256) k_flux32(const __grid_constant__ Args<float> a) {
     const int f = LFM_GLOBAL_ID();
-    if (f < a.nf) flux32<D, SCH, true, LES, D == 3>(a, f);
+    if (f < a.nf) flux32<D, SCH, true, LES, true>(a, f);
 }
 
 // Warp-interleaved cells: warp j of block b updates the 32 cells of chunk

@@ -80,7 +80,7 @@ private:
 struct CaseLayout {
     size_t total = 0;
     size_t q, dq, res, prim, V, grad, flux, S, d, w, dinv, dnorm, K, lapc, fP, fN, fGhost, volInv, volInv32,
-        sponge, cfOff, cfList, cfNbr, cellGhosts, gCell, gKind, gFace;
+        sponge, cfOff, cfList, cfNbr, cfEll, cellGhosts, gCell, gKind, gFace;
 
     explicit CaseLayout(const lfm_solver_desc* d) {
         const size_t D = (size_t)d->dim, nq = (size_t)d->nq, nc = (size_t)d->n_cells, ng = (size_t)d->n_ghosts;
@@ -109,6 +109,12 @@ struct CaseLayout {
         cfOff = add((nc + 1) * 4);
         cfList = add(ne * 4);
         cfNbr = add(ne * 4);
+        // the update's fixed-width cell -> face table, when every cell fits it
+        const size_t W = (size_t)(D == 2 ? lfm::dev::kEllWidth<2> : lfm::dev::kEllWidth<3>);
+        bool fits = true;
+        for (size_t c = 0; c < nc && fits; ++c)
+            fits = (size_t)(d->cell_face_offsets[c + 1] - d->cell_face_offsets[c]) <= W;
+        cfEll = fits ? add(W * nc * 4) : npos();
         cellGhosts = add(nc);
         gCell = add(ng * 4);
         gKind = add(ng * 4);

@@ -64,12 +64,15 @@ __device__ __forceinline__ void item(const BatchCase& bc, int stage, int i) {
             flux32<D, kSchemeM2, FULL>(a, i);
         else
             flux32<D, kSchemeAUSM, FULL>(a, i);
-    } else {
+    } else {   // through the fixed-width face table where the case has one
         const int first = stage == 0;
-        if (bc.residuals && first)
-            update32<D, true, true>(a, i, bc.rkA[stage], bc.rkB[stage], bc.dt, bc.dt32, first);
-        else
-            update32<D, false, true>(a, i, bc.rkA[stage], bc.rkB[stage], bc.dt, bc.dt32, first);
+        if (bc.residuals && first) {
+            if (a.cfEll) update32<D, true, true, true>(a, i, bc.rkA[stage], bc.rkB[stage], bc.dt, bc.dt32, first);
+            else update32<D, true, true, false>(a, i, bc.rkA[stage], bc.rkB[stage], bc.dt, bc.dt32, first);
+        } else {
+            if (a.cfEll) update32<D, false, true, true>(a, i, bc.rkA[stage], bc.rkB[stage], bc.dt, bc.dt32, first);
+            else update32<D, false, true, false>(a, i, bc.rkA[stage], bc.rkB[stage], bc.dt, bc.dt32, first);
+        }
     }
 }
 

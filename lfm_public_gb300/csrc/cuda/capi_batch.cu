@@ -83,6 +83,14 @@ std::vector<unsigned char> packCase(const lfm_solver_desc* d, const CaseLayout& 
     std::memcpy(i32(L.cfOff), ix.cfOff.data(), (nc + 1) * 4);
     std::memcpy(i32(L.cfList), ix.cfList.data(), ix.cfList.size() * 4);
     std::memcpy(i32(L.cfNbr), ix.cfNbr.data(), ix.cfNbr.size() * 4);
+    if (L.cfEll != CaseLayout::npos()) {   // entry k of cell c at k * nc + c, padded
+        const size_t W = (size_t)(D == 2 ? lfm::dev::kEllWidth<2> : lfm::dev::kEllWidth<3>);
+        int* ell = i32(L.cfEll);
+        for (size_t k = 0; k < W * nc; ++k) ell[k] = lfm::dev::kEllPad;
+        for (size_t c = 0; c < nc; ++c)
+            for (int e = ix.cfOff[c]; e < ix.cfOff[c + 1]; ++e)
+                ell[(size_t)(e - ix.cfOff[c]) * nc + c] = ix.cfList[(size_t)e];
+    }
     unsigned char* cg = img.data() + L.cellGhosts;   // cells whose update writes ghosts
     for (size_t f = 0; f < nf; ++f)
         if (ix.fN[f] >= (int)nc && ix.fN[f] < (int)(nc + ng)) cg[(size_t)ix.fP[f]] = 1;
@@ -394,7 +402,7 @@ int commitCase(lfm_batch* b, const PreparedCase& pc, int* slot) {
     a.cfList = reinterpret_cast<const int*>(P(L.cfList));
     a.cfNbr = reinterpret_cast<const int*>(P(L.cfNbr));
     a.cellGhosts = reinterpret_cast<const uint8_t*>(P(L.cellGhosts));
-    a.cfEll = nullptr;
+    a.cfEll = reinterpret_cast<const int*>(P(L.cfEll));
     a.smagC = nullptr;
     a.gCell = reinterpret_cast<const int*>(P(L.gCell));
     a.gKind = reinterpret_cast<const int*>(P(L.gKind));

@@ -473,10 +473,11 @@ int createSolver(const lfm_solver_desc* d, const lfm_solver_opts* opts, cudaStre
         if ((rc = upload(s, &dCG, cg.data(), nc))) return fail(rc);
         s->a32.cellGhosts = dCG;
     }
-    if (s->precision == LFM_FP32_BULK && !tiled && s->D == 3) {
-        // the update's fixed-width cell -> face table, when every cell fits it
-        // (3D: six faces a cell, a shorter gather; in 2D the extra table costs
-        // the other kernels more L2 hits than it saves)
+    if (s->precision == LFM_FP32_BULK && !tiled && (s->D == 3 || s->nc > kFuseGhostCells2D)) {
+        // the update's fixed-width cell -> face table, when every cell fits it:
+        // cases whose gathers come from HBM (3D; 2D beyond 1M cells, 0.263 ->
+        // 0.255 ms per step on a 1.57M-cell cylinder); a 2D case that L2 holds
+        // loses more L2 hits to the extra table than the shorter gather saves
         const size_t W = (size_t)(s->D == 2 ? lfm::dev::kEllWidth<2> : lfm::dev::kEllWidth<3>);
         bool fits = true;
         for (size_t c = 0; c < nc && fits; ++c) fits = (size_t)(cfOff[c + 1] - cfOff[c]) <= W;

@@ -57,6 +57,34 @@ def test_geometry_closed_cells_and_volumes():
     assert vol.sum() == pytest.approx(400.0, rel=1e-12)   # [-10,10]^2 x 1
 
 
+@pytest.mark.parametrize("make,volume,faces", [
+    (lambda: cases.hybrid_case(n=6, tri_fraction=0.5, seed=1), 400.0, {3, 4}),
+    (lambda: cases.prism_case(n=5, nz=3, seed=2), 1600.0, {5}),
+    (lambda: cases.tet_case(n=3, nz=2, seed=1), 1600.0, {4}),
+], ids=["quad+tri", "prisms", "tets"])
+def test_generated_element_meshes_are_closed(make, volume, faces):
+    """The mixed-polygon, prism and tetrahedron generators: every cell closed
+    (its outward face vectors sum to zero), positive volumes filling the box,
+    the expected faces per cell."""
+    case = make()
+    ch = N.CaseHandle.from_case(case)
+    d = ch.desc
+    nf, nc, D = d.n_faces, d.n_cells, d.dim
+    S = ch.array("S", (D * nf,)).reshape(D, nf)
+    offs = ch.array("cell_face_offsets", (nc + 1,), np.int64)
+    fl = ch.array("cell_faces", (offs[-1],), np.int64)
+    sign = ch.array("cell_face_sign", (offs[-1],), np.int8)
+    assert set(np.diff(offs).tolist()) == faces
+    for c in range(nc):
+        tot = np.zeros(D)
+        for e in range(offs[c], offs[c + 1]):
+            tot += sign[e] * S[:, fl[e]]
+        assert np.abs(tot).max() < 1e-11 * max(1.0, np.abs(S).max()), c
+    vol = 1.0 / ch.array("vol_inv", (nc,))
+    assert np.all(vol > 0)
+    assert vol.sum() == pytest.approx(volume, rel=1e-12)
+
+
 def test_ownership_and_processing_order():
     case = cases.vortex_case(n=8)
     ch = N.CaseHandle.from_case(case)

@@ -95,9 +95,10 @@ struct Args {
                               // (V then holds D x D more rows: its SGS stress), or null
     const uint8_t* cellGhosts;  // FP32-bulk single case: boundary faces of each cell
                                 // (its update writes their ghosts' primitives), or null
-    const int* cfEll;         // FP32-bulk single case: the cfList entries of each cell at a
-                              // fixed width (kEllWidth<D>), entry k of cell c at k * nc + c,
-                              // kEllPad after the cell's faces; null when a cell has more
+    const int* cfEll;         // FP32-bulk update gather (single cases beyond L2, batch cases):
+                              // the cfList entries of each cell at a fixed width
+                              // (kEllWidth<D>), entry k of cell c at k * nc + c, kEllPad
+                              // after the cell's faces; null where unused or a cell has more
                               // faces (the update then gathers through cfOff / cfList)
     // ghosts
     const int* gCell;

@@ -97,7 +97,7 @@ WORKLOAD_DESC = {
 # each captured launch). Keyed by (workload, precision, kernel).
 # profiles/fp32_kernels_cylinder768x512.md
 DRAM_TRAFFIC = {
-    ("cylinder2d", "fp32", "k_update"): 42938624 + 216576,
+    ("cylinder2d", "fp32", "k_update"): 42937856 + 190976,
     # profiles/fp32_kernels_cylinder3d_192x128x48.md; the 384x256x96 wake is
     # too large for a full capture: its figure is the 192x128x48 capture
     # scaled by the cells (x8), the traffic being at the algorithmic bytes,

@@ -84,6 +84,16 @@ struct lfm_solver {
     float* prim1 = nullptr;
     int primParity = 0;
     cudaGraphExec_t graphOdd = nullptr;   // the step graph starting from prim1
+    // the non-finite flag's host copy (page-locked: read after one stream sync)
+    int* flagHost = nullptr;
+    // lfm_solver_advance between page-locked host states as one graph (copy
+    // in, conversion, primitives, steps, conversion, copy out, flag), kept
+    // for the pointers, step count and dt it was captured with
+    cudaGraphExec_t advGraph = nullptr;
+    const double* advIn = nullptr;
+    double* advOut = nullptr;
+    int advSteps = 0;
+    double advDt = 0;
 };
 
 namespace {
@@ -533,6 +543,9 @@ int createSolver(const lfm_solver_desc* d, const lfm_solver_opts* opts, cudaStre
         for (int v = 0; v < s->nq; ++v) s->qRef[v] = s->a32.qRef[v];
         if ((rc = devAlloc(s, &s->stage, nq * nc))) return fail(rc);
     }
+    if ((e = cudaHostAlloc(reinterpret_cast<void**>(&s->flagHost), sizeof(int), cudaHostAllocDefault)) != cudaSuccess)
+        return fail(cudaFail(e, "cudaHostAlloc"));
+    *s->flagHost = 0;
     if (d->q0) {
         if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return fail(cudaFail(e, "create"));
         if ((rc = lfm_solver_set_state(s, d->q0))) return fail(rc);
@@ -554,6 +567,8 @@ extern "C" void lfm_solver_destroy(lfm_solver* s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     if (s->graph) cudaGraphExecDestroy(s->graph);
     if (s->graphOdd) cudaGraphExecDestroy(s->graphOdd);
+    if (s->advGraph) cudaGraphExecDestroy(s->advGraph);
+    if (s->flagHost) cudaFreeHost(s->flagHost);
     for (void* p : s->allocations) cudaFree(p);
     if (s->scrub) cudaFree(s->scrub);
     if (s->dPatches) cudaFree(s->dPatches);
@@ -627,10 +642,65 @@ extern "C" int lfm_solver_get_state(lfm_solver* s, double* q) {
     return LFM_OK;
 }
 
+namespace {
+
+bool pageLocked(const void* p) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost;
+}
+
+// The whole advance between page-locked host states as one graph launch
+// (device work only; the host-side state flags are set as the enqueued path
+// leaves them). Captured once per (q_in, q_out, nsteps, dt).
+int advanceGraph(lfm_solver* s, const double* qIn, int nsteps, double dt, double* qOut) {
+    if (!(s->advGraph && s->advIn == qIn && s->advOut == qOut && s->advSteps == nsteps && s->advDt == dt)) {
+        if (s->advGraph) cudaGraphExecDestroy(s->advGraph);
+        s->advGraph = nullptr;
+        cudaGraph_t g = nullptr;
+        LFM_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueueSetState(s, qIn);
+        if (!rc) rc = ensurePrims(s);
+        for (int k = 0; k < nsteps && !rc; ++k) launchStep(s, dt, 0);
+        if (!rc) rc = enqueueGetState(s, qOut);
+        cudaError_t ce = cudaMemcpyAsync(s->flagHost, s->flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream);
+        cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+        if (rc || ce != cudaSuccess || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            return rc ? rc : cudaFail(ce != cudaSuccess ? ce : e, "advance capture");
+        }
+        e = cudaGraphInstantiate(&s->advGraph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cudaFail(e, "cudaGraphInstantiate");
+        s->advIn = qIn;
+        s->advOut = qOut;
+        s->advSteps = nsteps;
+        s->advDt = dt;
+    }
+    LFM_CUDA(cudaGraphLaunch(s->advGraph, s->stream));
+    // the flags the enqueued path leaves: a new state, its primitives, stages run
+    s->primParity = 0;
+    s->primsValid = s->precision == LFM_FP32_BULK;
+    s->ghostRowsValid = true;
+    s->lastStageB = s->rkB.empty() ? 0.0 : s->rkB.back();
+    LFM_CUDA(cudaStreamSynchronize(s->stream));
+    LFM_CUDA(cudaGetLastError());
+    if (*s->flagHost) return lfm::setError(LFM_ERR_NUMERIC, "non-finite conserved state");
+    return LFM_OK;
+}
+
+}  // namespace
+
 extern "C" int lfm_solver_advance(lfm_solver* s, const double* q_in, int nsteps, double dt, double* q_out) {
     if (!s || nsteps < 0) return lfm::setError(LFM_ERR_INVALID, "bad argument");
     LFM_CUDA(cudaSetDevice(s->device));
     int rc = LFM_OK;
+    if (q_in && q_out && nsteps > 0 && s->rkOrder > 0 && !s->tiled && pageLocked(q_in) && pageLocked(q_out))
+        return advanceGraph(s, q_in, nsteps, dt, q_out);
     if (q_in && (rc = enqueueSetState(s, q_in))) return rc;
     if (nsteps > 0 && (rc = lfm_solver_step(s, nsteps, dt))) return rc;
     if (q_out && (rc = enqueueGetState(s, q_out))) return rc;
@@ -990,11 +1060,10 @@ extern "C" int lfm_solver_probes_read(lfm_solver* s, double* out, int* n_records
 extern "C" int lfm_solver_sync(lfm_solver* s) {
     if (!s) return lfm::setError(LFM_ERR_INVALID, "null solver");
     LFM_CUDA(cudaSetDevice(s->device));
+    LFM_CUDA(cudaMemcpyAsync(s->flagHost, s->flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     LFM_CUDA(cudaStreamSynchronize(s->stream));
     LFM_CUDA(cudaGetLastError());
-    int flag = 0;
-    LFM_CUDA(cudaMemcpy(&flag, s->flag, sizeof(int), cudaMemcpyDeviceToHost));
-    if (flag) return lfm::setError(LFM_ERR_NUMERIC, "non-finite conserved state");
+    if (*s->flagHost) return lfm::setError(LFM_ERR_NUMERIC, "non-finite conserved state");
     return LFM_OK;
 }
 

@@ -108,6 +108,44 @@ def test_advance_is_set_state_step_get_state(precision):
     b.close()
 
 
+@pytest.mark.parametrize("precision", [N.LFM_FP64, N.LFM_FP32_BULK])
+def test_advance_between_page_locked_states_is_one_graph(precision):
+    """With page-locked host states lfm_solver_advance replays one captured
+    graph (copy in, conversion, primitives, steps, conversion, copy out, the
+    non-finite flag): the bits of set_state + step + get_state, for repeated
+    calls on the same buffers, a new dt and several steps, and a non-finite
+    state is reported."""
+    torch = pytest.importorskip("torch")
+    case = cases.cylinder_case(n_theta=48, n_r=24, r1=15, first=0.02, Ls=4, solver=2, minmod=True, noise=0.02)
+    ch = N.CaseHandle.from_case(case)
+    a = N.Solver(ch, precision=precision)
+    b = N.Solver(ch, precision=precision)
+    shape = (ch.desc.nq, ch.desc.n_cells)
+    hin = torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    hout = torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    hin[:] = a.get_state()
+    for dt, nsteps in ((case.delta_t, 1), (case.delta_t, 1), (0.5 * case.delta_t, 1), (case.delta_t, 3)):
+        b.set_state(hin)
+        b.step(nsteps, dt)
+        b.sync()
+        ref = b.get_state()
+        a.advance(hin, nsteps, dt, hout)
+        assert np.array_equal(hout, ref)
+        hin[:] = hout
+    # the solver keeps working through its other calls afterwards
+    a.step(1, case.delta_t)
+    b.step(1, case.delta_t)
+    a.sync()
+    b.sync()
+    assert np.array_equal(a.get_state(), b.get_state())
+    hin[0, 5] = np.nan
+    with pytest.raises(N.LfmError) as e:
+        a.advance(hin, 1, case.delta_t, hout)
+    assert e.value.code == N.LFM_ERR_NUMERIC
+    a.close()
+    b.close()
+
+
 def test_fp32_bulk_free_stream_is_preserved():
     # A uniform free stream (inlet, outlet and walls) has zero perturbation in
     # the interior and FP64-derived ghost primitives: the state may move only

@@ -510,12 +510,8 @@ def run_batch(args):
         h[:] = ch.q0()
     e2e_steps = max(1, min(args.steps, 20))
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        for s, h in zip(slots, hosts):
-            b.set_state(s, h)
-        b.step(1)
-        for s, h in zip(slots, hosts):
-            b.get_state(s, out=h)    # synchronous: the step is complete
+    for _ in range(e2e_steps):   # lfm_batch_advance: every state in, one step, every state out
+        b.advance(slots, hosts, 1, hosts)
     e2e_s = _allmax(pg, time.perf_counter() - t0)
     e2e_value = ws * cells * stages * e2e_steps / e2e_s
     io_bytes = sum(h.nbytes for h in hosts)

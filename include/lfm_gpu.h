@@ -414,6 +414,13 @@ int lfm_batch_remove(lfm_batch* b, int slot);
  * set_state also clears the case's non-finite flag. */
 int lfm_batch_set_state(lfm_batch* b, int slot, const double* q);
 int lfm_batch_get_state(lfm_batch* b, int slot, double* q);
+/* The cases slots[0..n) from host states q_in[i] ([nq][n_cells] as
+ * lfm_batch_set_state; a NULL array or entry keeps that case's state), nsteps
+ * steps of the batch, the states out into q_out[i] (NULL skips), all on the
+ * batch stream with one synchronisation at the end; returns lfm_batch_sync's
+ * status. Gives the bits of the separate calls. */
+int lfm_batch_advance(lfm_batch* b, int n, const int* slots, const double* const* q_in, int nsteps,
+                      double* const* q_out);
 /* nsteps time steps of every case in the batch; asynchronous. */
 int lfm_batch_step(lfm_batch* b, int nsteps);
 /* Waits for the batch stream; LFM_ERR_NUMERIC names the slots whose state

@@ -139,6 +139,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "lfm_solver_probes_read": ([vp, _dp, C.POINTER(C.c_int)], C.c_int),
         "lfm_partitioned_solver": ([vp, C.c_int, C.POINTER(vp)], C.c_int),
         "lfm_solver_advance": ([vp, _dp, C.c_int, C.c_double, _dp], C.c_int),
+        "lfm_batch_advance": ([vp, C.c_int, C.POINTER(C.c_int), C.POINTER(_dp), C.c_int, C.POINTER(_dp)], C.c_int),
         "lfm_tiles_stats": ([C.POINTER(SolverDesc), C.c_int, C.c_int, C.POINTER(C.c_int64)], C.c_int),
         "lfm_case_open": ([C.c_char_p, C.c_int, C.POINTER(vp)], C.c_int),
         "lfm_case_from_polymesh": ([C.POINTER(PolyMesh), C.POINTER(Params), C.POINTER(Fields), C.POINTER(vp)],
@@ -610,6 +611,29 @@ class Batch:
 
     def step(self, nsteps: int = 1):
         check(load_library().lfm_batch_step(self._h, nsteps))
+
+    def advance(self, slots, q_in, nsteps: int, q_out):
+        """lfm_batch_advance: the states q_in[i] (or None) of slots[i] in,
+        nsteps steps, the states out into q_out[i] (or None), one sync. The
+        arrays are C-contiguous float64 (nq, n_cells) of their case."""
+        n = len(slots)
+
+        def ptrs(arrs):
+            if arrs is None:
+                return None
+            out = (_dp * n)()
+            for i, (s, a) in enumerate(zip(slots, arrs)):
+                if a is None:
+                    continue
+                d = self._cases[s].desc
+                if a.dtype != np.float64 or a.shape != (d.nq, d.n_cells) or not a.flags.c_contiguous:
+                    raise ValueError("states must be C-contiguous float64 arrays of shape (nq, n_cells)")
+                out[i] = _ptr(a, C.c_double)
+            return out
+
+        pin, pout = ptrs(q_in), ptrs(q_out)
+        sl = (C.c_int * n)(*slots)
+        check(load_library().lfm_batch_advance(self._h, n, sl, pin, nsteps, pout))
 
     def sync(self):
         check(load_library().lfm_batch_sync(self._h))

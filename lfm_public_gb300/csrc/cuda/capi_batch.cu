@@ -463,24 +463,49 @@ extern "C" int lfm_batch_remove(lfm_batch* b, int slot) {
     return LFM_OK;
 }
 
-extern "C" int lfm_batch_set_state(lfm_batch* b, int slot, const double* q) {
-    int rc = checkSlot(b, slot);
-    if (rc) return rc;
-    if (!q) return lfm::setError(LFM_ERR_INVALID, "null state");
+namespace {
+
+// The state copies of one case, enqueued on the batch stream through the
+// shared staging buffer (stream order keeps successive cases apart).
+int enqueueBatchSet(lfm_batch* b, int slot, const double* q) {
     Slot& sl = b->slots[(size_t)slot];
-    LFM_CUDA(cudaSetDevice(b->device));
     // a new state starts with a clear non-finite flag
     LFM_CUDA(cudaMemsetAsync(b->dFlags + slot, 0, sizeof(int), b->stream));
     const size_t bytes = (size_t)sl.nq * sl.nc * sizeof(double);
-    if ((rc = ensureStage(b, bytes))) return rc;
+    int rc = ensureStage(b, bytes);
+    if (rc) return rc;
     LFM_CUDA(cudaMemcpyAsync(b->dStage, q, bytes, cudaMemcpyHostToDevice, b->stream));
     lfm::dev::QOffset qo;   // stored as q - qRef
     for (int v = 0; v < 5; ++v) qo.v[v] = sl.qRef[v];
     lfm::dev::launch_offset_rows(sl.q, sl.nt, b->dStage, sl.nc, sl.nc, sl.nq, qo, -1.0, b->stream);
     LFM_CUDA(cudaGetLastError());
-    LFM_CUDA(cudaStreamSynchronize(b->stream));
     sl.primsValid = false;
     b->tilesDirty = true;
+    return LFM_OK;
+}
+
+int enqueueBatchGet(lfm_batch* b, int slot, double* q) {
+    const Slot& sl = b->slots[(size_t)slot];
+    const size_t bytes = (size_t)sl.nq * sl.nc * sizeof(double);
+    int rc = ensureStage(b, bytes);
+    if (rc) return rc;
+    lfm::dev::QOffset qo;   // stored as q - qRef
+    for (int v = 0; v < 5; ++v) qo.v[v] = sl.qRef[v];
+    lfm::dev::launch_offset_rows(b->dStage, sl.nc, sl.q, sl.nt, sl.nc, sl.nq, qo, 1.0, b->stream);
+    LFM_CUDA(cudaGetLastError());
+    LFM_CUDA(cudaMemcpyAsync(q, b->dStage, bytes, cudaMemcpyDeviceToHost, b->stream));
+    return LFM_OK;
+}
+
+}  // namespace
+
+extern "C" int lfm_batch_set_state(lfm_batch* b, int slot, const double* q) {
+    int rc = checkSlot(b, slot);
+    if (rc) return rc;
+    if (!q) return lfm::setError(LFM_ERR_INVALID, "null state");
+    LFM_CUDA(cudaSetDevice(b->device));
+    if ((rc = enqueueBatchSet(b, slot, q))) return rc;
+    LFM_CUDA(cudaStreamSynchronize(b->stream));
     return LFM_OK;
 }
 
@@ -488,17 +513,31 @@ extern "C" int lfm_batch_get_state(lfm_batch* b, int slot, double* q) {
     int rc = checkSlot(b, slot);
     if (rc) return rc;
     if (!q) return lfm::setError(LFM_ERR_INVALID, "null state");
-    const Slot& sl = b->slots[(size_t)slot];
     LFM_CUDA(cudaSetDevice(b->device));
-    const size_t bytes = (size_t)sl.nq * sl.nc * sizeof(double);
-    if ((rc = ensureStage(b, bytes))) return rc;
-    lfm::dev::QOffset qo;   // stored as q - qRef
-    for (int v = 0; v < 5; ++v) qo.v[v] = sl.qRef[v];
-    lfm::dev::launch_offset_rows(b->dStage, sl.nc, sl.q, sl.nt, sl.nc, sl.nq, qo, 1.0, b->stream);
-    LFM_CUDA(cudaGetLastError());
-    LFM_CUDA(cudaMemcpyAsync(q, b->dStage, bytes, cudaMemcpyDeviceToHost, b->stream));
+    if ((rc = enqueueBatchGet(b, slot, q))) return rc;
     LFM_CUDA(cudaStreamSynchronize(b->stream));
     return LFM_OK;
+}
+
+extern "C" int lfm_batch_advance(lfm_batch* b, int n, const int* slots, const double* const* q_in, int nsteps,
+                                 double* const* q_out) {
+    if (!b || n < 0 || (n > 0 && !slots) || nsteps < 0) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    size_t most = 0;
+    for (int i = 0; i < n; ++i) {
+        int rc = checkSlot(b, slots[i]);
+        if (rc) return rc;
+        const Slot& sl = b->slots[(size_t)slots[i]];
+        most = std::max(most, (size_t)sl.nq * sl.nc * sizeof(double));
+    }
+    LFM_CUDA(cudaSetDevice(b->device));
+    int rc = ensureStage(b, most);   // sized once, before anything is enqueued
+    for (int i = 0; i < n && !rc && q_in; ++i)
+        if (q_in[i]) rc = enqueueBatchSet(b, slots[i], q_in[i]);
+    if (!rc && nsteps > 0) rc = lfm_batch_step(b, nsteps);
+    for (int i = 0; i < n && !rc && q_out; ++i)
+        if (q_out[i]) rc = enqueueBatchGet(b, slots[i], q_out[i]);
+    if (rc) return rc;
+    return lfm_batch_sync(b);
 }
 
 extern "C" int lfm_batch_step(lfm_batch* b, int nsteps) {

@@ -74,6 +74,44 @@ def test_single_solver_ghost_pass_variants_bitwise():
     assert np.array_equal(_single(ch, n, case.delta_t), _alone(ch, n, case.delta_t))
 
 
+def test_batch_advance_is_the_separate_calls():
+    """lfm_batch_advance (every state in, steps, every state out, one sync)
+    gives the bits of set_state per case, step and get_state per case; None
+    keeps a case's state or skips its copy out."""
+    cs = _mixed_cases()[:4]
+    chs = [N.CaseHandle.from_case(c) for c in cs]
+    a = N.Batch(arena_bytes=256 << 20)
+    b = N.Batch(arena_bytes=256 << 20)
+    sa = [a.add(ch, c.delta_t) for ch, c in zip(chs, cs)]
+    sb = [b.add(ch, c.delta_t) for ch, c in zip(chs, cs)]
+    hosts = [np.ascontiguousarray(ch.q0()) for ch in chs]
+    outs = [np.empty_like(h) for h in hosts]
+    for _ in range(2):
+        for s, h in zip(sb, hosts):
+            b.set_state(s, h)
+        b.step(2)
+        refs = [b.get_state(s) for s in sb]
+        a.advance(sa, hosts, 2, outs)
+        for o, r in zip(outs, refs):
+            assert np.array_equal(o, r)
+        hosts = [o.copy() for o in outs]
+    # keep case 0's state (None in), skip case 1's copy out (None out); a
+    # state read out and set again is q_ref + q' rounded, so the reference
+    # batch sets the same ones
+    keep0, keep1 = outs[0].copy(), outs[1].copy()
+    for s, h in zip(sb[1:], hosts[1:]):
+        b.set_state(s, h)
+    b.step(1)
+    a.advance(sa, [None] + hosts[1:], 1, [outs[0], None] + outs[2:])
+    assert np.array_equal(outs[0], b.get_state(sb[0])) and not np.array_equal(outs[0], keep0)
+    assert np.array_equal(outs[1], keep1)   # not written
+    assert np.array_equal(a.get_state(sa[1]), b.get_state(sb[1]))
+    for s, o in zip(sb[2:], outs[2:]):
+        assert np.array_equal(o, b.get_state(s))
+    a.close()
+    b.close()
+
+
 def test_batch_join_leave_between_steps():
     cs = _mixed_cases()[:4]
     chs = [N.CaseHandle.from_case(c) for c in cs]

@@ -591,15 +591,15 @@ int enqueueSetState(lfm_solver* s, const double* q) {
     if (s->precision == LFM_FP32_BULK) {   // stored as q - q_ref
         LFM_CUDA(cudaMemcpyAsync(s->stage, q, (size_t)s->nq * nc * sizeof(double), cudaMemcpyHostToDevice,
                                  s->stream));
-        lfm::dev::QOffset qo;
-        for (int v = 0; v < 5; ++v) qo.v[v] = s->qRef[v];
-        lfm::dev::launch_offset_rows(s->q, s->nt, s->stage, s->nc, s->nc, s->nq, qo, -1.0, s->stream);
+        // q' with the cells' primitives (and the ghosts' the update keeps) in
+        // one pass: the per-stage preparation covers the other ghosts and halos
+        lfm::dev::launch_set_state32(s->a32, s->stage, s->nc, s->stream);
         LFM_CUDA(cudaGetLastError());
     } else {   // rows of nc values into rows of nt
         LFM_CUDA(cudaMemcpy2DAsync(s->q, (size_t)s->nt * sizeof(double), q, nc * sizeof(double),
                                    nc * sizeof(double), (size_t)s->nq, cudaMemcpyHostToDevice, s->stream));
     }
-    s->primsValid = false;
+    s->primsValid = s->precision == LFM_FP32_BULK;
     s->primParity = 0;
     s->ghostRowsValid = false;
     return LFM_OK;

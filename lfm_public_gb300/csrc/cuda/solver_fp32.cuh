@@ -160,6 +160,22 @@ __device__ __forceinline__ void prep32(const Args<float>& a, int t) {
 // (a ghost depends on its interior cell only), so no preparation pass over
 // the ghosts is needed; the values are those prep32 computes.
 // ---------------------------------------------------------------------------
+// ghosts_of32: the FP64 states and FP32 primitives of the boundary ghosts of
+// cell c from its perturbation state qp (those prep32 computes).
+template <int D>
+__device__ __forceinline__ void ghosts_of32(const Args<float>& a, int c, const double* qp) {
+    constexpr int NQ = D + 2;
+    double qa[NQ];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) qa[v] = qp[v] + a.qRef[v];
+    for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
+        const int code = a.cfList[e];
+        if (code < 0) continue;
+        const int j = a.fN[code];
+        if (j >= a.nc && j < a.nc + a.ng) ghost32<D>(a, j - a.nc, qa);
+    }
+}
+
 // gather32: the face rhs sum of cell c (ascending face order).
 template <int D>
 __device__ __forceinline__ void gather32(const Args<float>& a, int c, float* sum) {
@@ -256,17 +272,7 @@ __device__ __forceinline__ void apply32(const Args<float>& a, int c, const float
     }
     if (!finite) atomicOr(a.flag, 1);
     prims32<D>(a, c, qn);
-    if (GH && a.cellGhosts[c]) {
-        double qa[NQ];
-#pragma unroll
-        for (int v = 0; v < NQ; ++v) qa[v] = qn[v] + a.qRef[v];
-        for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
-            const int code = a.cfList[e];
-            if (code < 0) continue;
-            const int j = a.fN[code];
-            if (j >= a.nc && j < a.nc + a.ng) ghost32<D>(a, j - a.nc, qa);
-        }
-    }
+    if (GH && a.cellGhosts[c]) ghosts_of32<D>(a, c, qn);
 }
 
 template <int D, bool RES, bool GH = false, bool ELL = false>
@@ -278,6 +284,22 @@ __device__ __forceinline__ void update32(const Args<float>& a, int c, double Ak,
     if (ELL) gather32_ell<D>(a, c, sum);
     else gather32<D>(a, c, sum);
     apply32<D, RES, GH>(a, c, sum, in, Ak, Bk, dt, dt32, first);
+}
+
+// A new state: q' = q - q_ref of cell c from a caller's absolute state q
+// ([nq][stride] doubles), its primitives and, where the update keeps them
+// (a.cellGhosts), its boundary ghosts' -- the values the preparation pass
+// derives from the stored q', from registers.
+template <int D>
+__device__ __forceinline__ void set_state32(const Args<float>& a, const double* q, int64_t stride, int c) {
+    double qp[D + 2];
+#pragma unroll
+    for (int v = 0; v < D + 2; ++v) {
+        qp[v] = q[(size_t)v * stride + c] - a.qRef[v];
+        a.q[(size_t)v * a.nt + c] = qp[v];
+    }
+    prims32<D>(a, c, qp);
+    if (a.cellGhosts && a.cellGhosts[c]) ghosts_of32<D>(a, c, qp);
 }
 
 // Perturbation state q' = q - q_ref of cells [0, n) from a caller's absolute

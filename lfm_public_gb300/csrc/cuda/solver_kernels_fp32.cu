@@ -92,6 +92,13 @@ void launch_update32(const Args<float>& a, const StageConfig& s, cudaStream_t st
 }
 
 template <int D>
+__global__ void __launch_bounds__(256) k_set_state32(const __grid_constant__ Args<float> a, const double* q,
+                                                     int64_t stride) {
+    const int c = LFM_GLOBAL_ID();
+    if (c < a.nc) set_state32<D>(a, q, stride, c);
+}
+
+template <int D>
 __global__ void __launch_bounds__(256) k_to_perturbation(const __grid_constant__ Args<float> a, const double* q,
                                                          int64_t stride) {
     const int c = LFM_GLOBAL_ID();
@@ -142,6 +149,13 @@ void launch_kernel_fp32(const Args<float>& a, const StageConfig& s, int which, c
         launch_fp32<2>(a, s, which, st);
     else
         launch_fp32<3>(a, s, which, st);
+}
+
+void launch_set_state32(const Args<float>& a, const double* q, int64_t stride, cudaStream_t st) {
+    if (a.D == 2)
+        k_set_state32<2><<<nblocks(a.nc, 256), 256, 0, st>>>(a, q, stride);
+    else
+        k_set_state32<3><<<nblocks(a.nc, 256), 256, 0, st>>>(a, q, stride);
 }
 
 void launch_to_perturbation(const Args<float>& a, const double* q, int64_t stride, cudaStream_t st) {

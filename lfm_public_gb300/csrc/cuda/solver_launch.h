@@ -37,6 +37,9 @@ void launch_kernel_fp32(const Args<float>& a, const StageConfig& s, int which, c
 // q' = q - q_ref for the cells of an FP32-bulk solver from an absolute state
 // [nq][stride] on the device.
 void launch_to_perturbation(const Args<float>& a, const double* q, int64_t stride, cudaStream_t st);
+// A new FP32-bulk state from an absolute one: q', the cells' primitives and
+// (with a.cellGhosts) their boundary ghosts' states and primitives.
+void launch_set_state32(const Args<float>& a, const double* q, int64_t stride, cudaStream_t st);
 
 // Rows of the per-cell primitive array: FP64 keeps 1/rho, u[D], R psi, c;
 // the FP32 perturbation form keeps rho', m'[D], u'[D], R psi', c.

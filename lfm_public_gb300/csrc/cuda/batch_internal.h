@@ -138,6 +138,7 @@ struct Slot {
     bool primsValid = false;   // cells' primitives current (kept so by the update phase)
     double qRef[5] = {0, 0, 0, 0, 0};   // the device state is q - qRef
     double* q = nullptr;   // device
+    lfm::dev::Args<float> a{};   // the case's kernel arguments (host copy)
 };
 
 // A case ready for admission: its arena block image (constant arrays and

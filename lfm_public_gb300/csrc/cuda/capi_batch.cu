@@ -431,6 +431,7 @@ int commitCase(lfm_batch* b, const PreparedCase& pc, int* slot) {
     sl.primsValid = false;
     for (int v = 0; v < 5; ++v) sl.qRef[v] = pc.bc.a.qRef[v];
     sl.q = a.q;
+    sl.a = a;
     b->tilesDirty = true;
     *slot = s;
     return LFM_OK;
@@ -475,12 +476,10 @@ int enqueueBatchSet(lfm_batch* b, int slot, const double* q) {
     int rc = ensureStage(b, bytes);
     if (rc) return rc;
     LFM_CUDA(cudaMemcpyAsync(b->dStage, q, bytes, cudaMemcpyHostToDevice, b->stream));
-    lfm::dev::QOffset qo;   // stored as q - qRef
-    for (int v = 0; v < 5; ++v) qo.v[v] = sl.qRef[v];
-    lfm::dev::launch_offset_rows(sl.q, sl.nt, b->dStage, sl.nc, sl.nc, sl.nq, qo, -1.0, b->stream);
+    // stored as q - qRef, with the primitives of the cells and their ghosts
+    // derived in the same pass: the tile lists need no preparation phase
+    lfm::dev::launch_set_state32(sl.a, b->dStage, sl.nc, b->stream);
     LFM_CUDA(cudaGetLastError());
-    sl.primsValid = false;
-    b->tilesDirty = true;
     return LFM_OK;
 }
 

@@ -192,6 +192,15 @@ def test_solver_create_rejects_bad_description():
     assert b"dim" in lib.lfm_last_error()
 
 
+def test_advance_calls_reject_bad_arguments():
+    """lfm_solver_advance / lfm_batch_advance: a null handle or a negative
+    count is LFM_ERR_INVALID before any device work."""
+    lib = N.load_library()
+    assert lib.lfm_solver_advance(None, None, 1, 1e-3, None) == N.LFM_ERR_INVALID
+    assert lib.lfm_batch_advance(None, 0, None, None, 1, None) == N.LFM_ERR_INVALID
+    assert b"bad argument" in lib.lfm_last_error()
+
+
 def test_library_exports_every_declared_symbol():
     hdr = open(os.path.join(ROOT, "include", "lfm_gpu.h")).read()
     names = set(re.findall(r"\b(lfm_[a-z0-9_]+)\s*\(", hdr))

@@ -156,6 +156,24 @@ def test_3d_prisms_and_tetrahedra(make):
     b.close()
 
 
+def test_smagorinsky_les_on_tetrahedra():
+    """Smagorinsky LES on 3D cells of four faces: FP64 within 1e-12 of the
+    oracle (itself bitwise the reference build on such meshes), FP32-bulk p'
+    within 1e-3."""
+    case = cases.tet_case(n=6, nz=3, seed=7, solver=1)
+    case.laminar = False
+    case.mu = 1.8e-3
+    ch = N.CaseHandle.from_case(case)
+    assert ch.desc.smag_c
+    n = 10
+    q64 = _gpu_run(ch, n, case.delta_t)
+    q_ref, _ = N.port_run(ch, ch.q0(), n, case.delta_t)
+    err = rel_l2_vec(q64, q_ref, case.dim)
+    assert np.all(err <= TOL), err
+    q32 = _gpu_run(ch, n, case.delta_t, N.LFM_FP32_BULK)
+    assert acoustics.acoustic_rel_l2(q32, q64, ch.desc.gamma, case.dim, case.p_inf) <= 1e-3
+
+
 def test_bitwise_reproducible_and_stage_api_equivalent():
     case = cases.cylinder_case(n_theta=64, n_r=32, r1=20, first=0.02, Ls=5, solver=2, minmod=True, noise=0.02)
     ch = N.CaseHandle.from_case(case)

@@ -123,3 +123,19 @@ def test_3d_prisms_and_tetrahedra_bitwise(make, faces):
     r, U, E, p = primitives(q, ch.desc.gamma, 3)
     assert np.array_equal(r, ref["rho"][ids]) and np.array_equal(E, ref["E"][ids])
     assert np.array_equal(p, ref["p"][ids])
+
+
+@pytest.mark.parametrize("make", [lambda: cases.prism_case(n=4, nz=3, seed=5, solver=1),
+                                  lambda: cases.tet_case(n=3, nz=2, seed=6, solver=0)], ids=["prism_m2", "tet_m1"])
+def test_smagorinsky_les_on_prisms_and_tetrahedra_bitwise(make):
+    """Smagorinsky LES (simulationType LES; the model constant built from
+    each cell's volume) on 3D cells of five and four faces."""
+    case = make()
+    case.laminar = False
+    case.mu = 1.8e-3
+    ch, q, ref = _run_both(case, 3)
+    assert ch.desc.smag_c
+    ids = ch.cell_ids()
+    r, U, E, p = primitives(q, ch.desc.gamma, 3)
+    assert np.array_equal(r, ref["rho"][ids]) and np.array_equal(E, ref["E"][ids])
+    assert np.array_equal(U, ref["U"][ids].T)

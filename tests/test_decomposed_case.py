@@ -69,6 +69,36 @@ def test_partitions_reproduce_whole_case_geometry(tmp_path, method, span):
     pc.close()
 
 
+@pytest.mark.parametrize("make", [lambda: cases.tet_case(n=4, nz=3, seed=2, solver=1),
+                                  lambda: cases.hybrid_case(n=8, tri_fraction=0.4, seed=3)], ids=["tets", "quad+tri"])
+def test_partitions_of_element_meshes_reproduce_geometry(tmp_path, make):
+    """Random partitions of a tetrahedral and of a mixed quadrilateral /
+    triangle mesh: every face of every partition is the undecomposed face."""
+    case = make()
+    root = str(tmp_path / "case")
+    cases.decompose_case(case, root, 3, method="random", seed=7)
+    whole = N.CaseHandle.open(root)
+    wt = _face_table(whole.desc, (whole.cell_ids(), None))
+    pc = N.PartitionedCase(root, 3)
+    gids = [pc.cell_global(p) for p in range(3)]
+    assert sorted(np.concatenate(gids).tolist()) == list(range(case.n_cells))
+    n_halo = 0
+    for p in range(3):
+        d = pc.descs[p]
+        n_halo += d.n_halos
+        for key, (S, dv, w) in _face_table(d, (gids[p], gids)).items():
+            if key in wt:
+                S0, d0, w0 = wt[key]
+            else:
+                S0, d0, w0 = wt[(key[1], key[0])]
+                S0, d0, w0 = -S0, -d0, 1.0 - w0
+            assert np.allclose(S, S0, rtol=1e-12, atol=1e-14), key
+            assert np.allclose(dv, d0, rtol=1e-11, atol=1e-12), key
+            assert abs(w - w0) < 1e-11, key
+    assert n_halo > 0
+    pc.close()
+
+
 def test_whole_case_open_rejects_a_single_partition(tmp_path):
     case = cases.vortex_case(n=12)
     root = str(tmp_path / "case")

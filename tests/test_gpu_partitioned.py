@@ -54,6 +54,9 @@ _CASES = {
                                                  minmod=False, noise=0.02, seed=11),
     "cylinder3d_m2": lambda: cases.cylinder_case(n_theta=24, n_r=12, r1=6, first=0.05, Ls=2, solver=1,
                                                  minmod=False, n_span=4, noise=0.01, seed=5),
+    # cells of four faces in 3D; quadrilaterals and triangles in one mesh
+    "tets_m2": lambda: cases.tet_case(n=6, nz=3, seed=4, solver=1),
+    "hybrid_m1": lambda: cases.hybrid_case(n=24, tri_fraction=0.4, seed=6, solver=0, beta=3.0),
 }
 
 

@@ -6,24 +6,30 @@ with minmod on, rkOrder 5, constant dt at acoustic CFL 0.5 -- synthetic mesh and
 free-stream initial field generated in memory. A "step" is one time step (5 RK
 stages over all cells). The metric is cell-RK-stage updates per second.
 
+The headline is the plain FP64 method, the arithmetic of the reference:
+
   value  -- device throughput with the state resident in HBM; every timed step
             is preceded (outside its timing) by a 512 MB write that evicts L2.
   e2e    -- the same metric through the C ABI with host buffers: each step
-            copies the state from pinned host memory to the device, advances one
-            time step and copies the state back, timed on the host clock.
+            lfm_solver_advance copies the state from pinned host memory to the
+            device, advances one time step and copies the state back, timed on
+            the host clock.
+
+Beside it, in the same line: ``fp32_bulk`` -- the FP32-bulk form (FP32 fluxes,
+limiter, residual sums and RK increment register on perturbations from the
+free stream; FP64 accumulation of the conserved state, ghost states and
+geometry) with its own value, e2e, roofline and speed-up over FP64;
+``accuracy`` -- the acoustic-pressure error of the FP32-bulk state against the
+FP64 state after --accuracy-steps time steps (all cells and 72 probes at
+r = 50 D); ``wake3d`` -- the 3D cylinder wake (384x256x96, 9.4M hex cells)
+device-timed in both precisions, the HBM-bound case; ``fp64_pipe`` -- the
+FP64 instruction roofline that bounds the plain method on GB300.
 
 --impl reference times the reference's CPU implementation of the same
-workload on the host cores (the oracle port: one process per core, each on
-the full mesh, aggregate throughput).
+workload on the host cores (the oracle port, set up by its own code: one
+process per core, each on the full mesh, aggregate throughput, FP64).
 
-The default precision is the FP32-bulk form (FP32 fluxes, limiter and
-residual sums and the RK increment register on perturbations from the free
-stream; FP64 accumulation of the conserved state, ghost states and geometry). The same run also times the plain FP64 path
-(``plain_fp64``: value and speed-up) and states the acoustic-pressure error of
-the FP32-bulk state against the FP64 state after --accuracy-steps time steps
-(``accuracy``: over all cells and on 72 probes at r = 50 D).
-
-Launch: python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp32|fp64]
+Launch: python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|fp32]
 Under torchrun each rank runs its own replica (weak scaling); rank 0 prints.
 """
 from __future__ import annotations
@@ -44,7 +50,7 @@ sys.path.insert(0, ROOT)
 METRIC = "cell-RK-stage updates/s"
 UNIT = "cell-stage/s"
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
-FP64_PEAK_TFLOPS = 1.195  # measured DFMA rate on this machine's GB300 (profiles/fp64_throughput_probe.md)
+FP64_PEAK_TFLOPS = 1.195  # DFMA rate measured on GB300 with a dependent-chain-free FMA loop
 
 
 def workload(name: str):
@@ -95,11 +101,10 @@ WORKLOAD_DESC = {
 # DRAM bytes (read + write) of one launch of the dominant kernel, from one ncu
 # capture of this bench's own command (cold L2: ncu flushes the caches before
 # each captured launch). Keyed by (workload, precision, kernel).
-# profiles/fp32_kernels_cylinder768x512.md
 DRAM_TRAFFIC = {
     ("cylinder2d", "fp32", "k_update"): 42937856 + 190976,
-    # profiles/fp32_kernels_cylinder3d_192x128x48.md; the 384x256x96 wake is
-    # too large for a full capture: its figure is the 192x128x48 capture
+    # the 384x256x96 wake is too large for a full capture: its figure is the
+    # 192x128x48 capture
     # scaled by the cells (x8), the traffic being at the algorithmic bytes,
     # which grow in proportion
     ("cylinder3d_small", "fp32", "k_flux"): 280696832 + 52857856,
@@ -110,7 +115,7 @@ DRAM_TRAFFIC = {
 # FP64 pipe thread-instructions per cell of one launch of each kernel of the
 # plain FP64 path (DFMA, DMUL, DADD and the FP64 parts of divisions and square
 # roots), counted by ncu (sm__thread_inst_executed_pipe_fp64_pred_on.sum /
-# cells) on the 768x512 cylinder, M1, viscous. profiles/fp64_pipe_cylinder768x512.md
+# cells) on the 768x512 cylinder, M1, viscous.
 FP64_INST_PER_CELL = {
     "cylinder2d": {"k_prep": 22.19, "k_grad": 0.0, "k_vis": 85.00, "k_flux": 202.26, "k_update": 34.31},
 }
@@ -175,8 +180,39 @@ def kernel_bytes(dim: int, faces_per_cell: int, fp32: bool, scheme: str, viscous
     return b
 
 
+class _Nvml:
+    """Read-only NVML queries through ctypes (the driver's libnvidia-ml):
+    SM clock, its maximum and the clock event (throttle) reasons."""
+
+    SM = 1   # NVML_CLOCK_SM
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, index: int):
+        import ctypes as C
+        self.C = C
+        self.lib = C.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        self.h = C.c_void_p()
+        if self.lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(index), C.byref(self.h)) != 0:
+            raise RuntimeError("no NVML device")
+        self.reasons_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+
+    def sample(self):
+        C = self.C
+        sm, mx, r = C.c_uint(), C.c_uint(), C.c_ulonglong()
+        self.lib.nvmlDeviceGetClockInfo(self.h, self.SM, C.byref(sm))
+        self.lib.nvmlDeviceGetMaxClockInfo(self.h, self.SM, C.byref(mx))
+        self.reasons_fn(self.h, C.byref(r))
+        return float(sm.value), float(mx.value), int(r.value)
+
+
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+    """SM clocks and throttle reasons sampled every few milliseconds through
+    NVML while the timed regions run (mark() opens and closes a timed region);
+    nvidia-smi every 0.2 s where NVML cannot be loaded."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -184,22 +220,47 @@ class ClockSampler:
 
     def __init__(self, device: int):
         self.device = device
-        self.samples = []
+        self.samples = []     # (timed, sm_mhz, max_mhz, set of reasons)
+        self.timed = False
         self._stop = threading.Event()
         self._t = None
+        self.source = "nvml"
+
+    def mark(self):
+        self.timed = not self.timed
+
+    def _smi(self):
+        out = subprocess.run(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                              "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                             timeout=5).stdout.strip()
+        if not out:
+            return None
+        f = [x.strip() for x in out.split(",")]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        num = lambda x: float(x) if x.replace(".", "").isdigit() else None   # noqa: E731
+        return num(f[1]), num(f[2]), {n for k, n in enumerate(names) if len(f) > 5 + k and
+                                      f[5 + k].lower().startswith("active")}
 
     def __enter__(self):
         def run():
+            nv = None
+            try:
+                nv = _Nvml(self.device)
+            except Exception:
+                self.source = "nvidia-smi"
             while not self._stop.is_set():
+                timed = self.timed
                 try:
-                    out = subprocess.run(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits"], capture_output=True, text=True,
-                                         timeout=5).stdout.strip()
-                    if out:
-                        self.samples.append([x.strip() for x in out.split(",")])
+                    if nv is not None:
+                        sm, mx, r = nv.sample()
+                        rec = (sm, mx, {n for b, n in _Nvml.REASONS.items() if r & b})
+                    else:
+                        rec = self._smi()
+                    if rec:
+                        self.samples.append((timed,) + rec)
                 except Exception:
                     pass
-                self._stop.wait(0.2)
+                self._stop.wait(0.002 if nv is not None else 0.2)
         self._t = threading.Thread(target=run, daemon=True)
         self._t.start()
         return self
@@ -210,35 +271,36 @@ class ClockSampler:
             self._t.join(timeout=10)
 
     def summary(self):
-        if not self.samples:
+        sel = [x for x in self.samples if x[0]] or self.samples
+        if not sel:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
-        sm = sorted(float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit())
-        mx = max((float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()), default=None)
+        sm = sorted(x[1] for x in sel if x[1] is not None)
+        mx = max((x[2] for x in sel if x[2] is not None), default=None)
         reasons = set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for s in self.samples:
-            for k, n in enumerate(names):
-                if len(s) > 5 + k and s[5 + k].lower().startswith("active"):
-                    reasons.add(n)
+        for x in sel:
+            reasons |= x[3]
         return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(self.samples)}
+                "samples": len(sel), "samples_in_timed_regions": sum(1 for x in self.samples if x[0]),
+                "source": self.source}
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline: the oracle port, one process per core
+# CPU baseline: the oracle port, one process per core. Each process sets its
+# case up with the oracle's own code (oracle/port), so the reference arm maps
+# nothing of the device library.
 # ---------------------------------------------------------------------------
 def _port_worker(name, steps, repeats, barrier, out):
     sys.path.insert(0, ROOT)
-    from lfm_public_gb300 import _native as N
+    import oracle.port as P
     case = workload(name)
-    ch = N.CaseHandle.from_case(case)
-    q0 = ch.q0()
+    pc = P.PortCase.from_case(case)
+    q0 = pc.q0()
     for _ in range(repeats):
         barrier.wait()
         t0 = time.time()
-        N.port_run(ch, q0, steps, case.delta_t)
+        P.run(pc, q0, steps, case.delta_t)
         t1 = time.time()
-        out.put((ch.desc.n_cells * ch.desc.rk_order * steps, t0, t1))
+        out.put((pc.desc.n_cells * pc.desc.rk_order * steps, t0, t1))
 
 
 def cpu_baseline(name: str, steps_per_proc: int, procs: int, repeats: int = 1):
@@ -286,6 +348,8 @@ def _allmax(pg, v: float) -> float:
 
 
 def run_reference(args):
+    """The reference's CPU time step on the host cores: the oracle port (set
+    up by its own code), one process per core, each on the full mesh, FP64."""
     ws, rank, _, pg = _dist()
     if rank != 0:
         return 0
@@ -300,44 +364,145 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * desc["cells"] * 5 / value,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": desc["workload"], "cells": desc["cells"], "rk_stages": 5},
+            "config": {"workload": desc["workload"], "cells": desc["cells"], "rk_stages": 5, "precision": "fp64"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
-def _time_solver(N, ch, precision, dt, steps, warmup, local, pg, clk_device=None):
+def _peaks():
+    peaks = json.load(open(PEAKS_FILE)) if os.path.exists(PEAKS_FILE) else {}
+    return peaks.get("hbm_gbs", 6800.0), ("measured" if "hbm_gbs" in peaks else "fallback")
+
+
+def _time_leg(N, ch, precision, dt, steps, warmup, local, pg, clk=None):
     """Device throughput of one solver: W warm-up steps, then K steps timed
-    with CUDA events, each preceded by a 512 MB write that evicts L2."""
+    with CUDA events, each preceded by a 512 MB write that evicts L2; then the
+    per-kernel times (prefix differences, lfm_solver_profile_step). Returns
+    (solver, total ms of the K steps (max over ranks), kernel ms per step,
+    launches per step)."""
     s = N.Solver(ch, precision=precision, device=local)
     for _ in range(warmup):
         s.step(1, dt)
     s.sync()
     if pg:
         pg.barrier()
-    clk = None
-    if clk_device is not None:
-        clk = ClockSampler(clk_device).__enter__()
-        time.sleep(0.3)
+    if clk is not None:
+        clk.mark()
     times = s.bench(steps, dt, 512 << 20)
     s.sync()
     if clk is not None:
-        clk.__exit__()
+        clk.mark()
     if pg:
         pg.barrier()
     total_ms = _allmax(pg, float(times.sum()))
     prof = s.profile_step(dt)
     s.sync()
-    return s, total_ms, prof, s.launches_per_step(), clk
+    return s, total_ms, prof, s.launches_per_step()
+
+
+def _e2e(s, nq, nc, dt, steps, pg):
+    """The metric end to end through lfm_solver_advance: every step the state
+    in from pinned host memory, one time step, the state out (host clock)."""
+    import torch
+    host = torch.empty((nq, nc), dtype=torch.float64, pin_memory=True).numpy()
+    s.get_state(out=host)
+    for _ in range(2):
+        s.advance(host, 1, dt, host)
+    t0 = time.perf_counter()
+    for _ in range(steps):   # lfm_solver_advance: state in, one step, state out
+        s.advance(host, 1, dt, host)
+    s.sync()
+    return _allmax(pg, time.perf_counter() - t0)
+
+
+def _hbm_roofline(desc, fp32, prof, nc, stages, workload, precision, hbm, peak_src, extra=None):
+    """HBM roofline of the dominant kernel: algorithmic bytes per launch over
+    its time per launch (from the prefix-difference profile)."""
+    kb = kernel_bytes(desc["dim"], desc["faces_per_cell"], fp32, desc["scheme"], desc["viscous"])
+    dominant = max(prof, key=prof.get)
+    per_launch_ms = prof[dominant] / stages
+    achieved = kb[dominant] * nc / (per_launch_ms * 1e-3) / 1e9
+    step_bytes = sum(v for k, v in kb.items() if k != "k_tile_stage")
+    r = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+         "frac": achieved / hbm, "peak_source": peak_src, "traffic": DRAM_TRAFFIC.get((workload, precision, dominant)),
+         "algorithmic_bytes_per_cell": kb[dominant], "cells_per_launch": nc,
+         "kernel_ms_per_launch": per_launch_ms, "step_algorithmic_bytes_per_cell_stage": step_bytes}
+    if extra:
+        r.update(extra)
+    return r, step_bytes
+
+
+def _leg_record(N, ch, precision, dt, args, ws, local, pg, desc, workload, hbm, peak_src, clk=None, e2e=True):
+    """Device-timed value, per-kernel times, HBM roofline and (optionally)
+    e2e of one precision on one case."""
+    nc, nq, stages = ch.desc.n_cells, ch.desc.nq, ch.desc.rk_order
+    fp32 = precision == N.LFM_FP32_BULK
+    s, total_ms, prof, launches = _time_leg(N, ch, precision, dt, args.steps, args.warmup, local, pg, clk)
+    value = ws * nc * stages * args.steps / (total_ms / 1000.0)
+    ms_step = total_ms / args.steps
+    roof, step_bytes = _hbm_roofline(desc, fp32, prof, nc, stages, workload, "fp32" if fp32 else "fp64", hbm,
+                                     peak_src)
+    roof["step_achieved"] = step_bytes * nc * stages / (ms_step * 1e-3) / 1e9
+    roof["step_frac"] = roof["step_achieved"] / hbm
+    rec = {"value": value, "unit": UNIT, "ms_per_step": ms_step, "kernels_ms_per_step": prof,
+           "kernels_sum_ms": sum(prof.values()), "roofline": roof, "launches_per_step": launches}
+    if e2e:
+        e2e_steps = max(1, args.steps)
+        e2e_s = _e2e(s, nq, nc, dt, e2e_steps, pg)
+        rec["e2e"] = {"value": ws * nc * stages * e2e_steps / e2e_s, "unit": UNIT,
+                      "h2d_bytes_per_step": nq * nc * 8, "d2h_bytes_per_step": nq * nc * 8}
+    s.close()
+    return rec
+
+
+def _accuracy(N, acoustics, case, ch, dt, n_acc, local, ring_r):
+    """Acoustic-pressure error of the FP32-bulk state against the FP64 state
+    after n_acc steps: all cells and the probe ring."""
+    import numpy as np
+    qs = []
+    for p in (N.LFM_FP64, N.LFM_FP32_BULK):
+        sa = N.Solver(ch, precision=p, device=local)
+        sa.step(n_acc, dt)
+        sa.sync()
+        qs.append(sa.get_state())
+        sa.close()
+    g, d = ch.desc.gamma, case.dim
+    acc = {"acoustic_p_rel_l2": acoustics.acoustic_rel_l2(qs[1], qs[0], g, d, case.p_inf), "steps": n_acc,
+           "against": "FP64 device path (itself within 1e-12 of the oracle), same case and steps"}
+    if ring_r is not None:
+        cells = acoustics.probe_ring(case.cell_centres, ch.cell_ids(), ring_r)
+        p64 = acoustics.pressure(qs[0], g, d)[cells] - case.p_inf
+        rms = float(np.sqrt(np.mean(p64 ** 2)))
+        acc["probe_ring"] = {
+            "radius": ring_r, "probes": len(cells), "p_rms_ref": rms,
+            "rel_l2": acoustics.acoustic_rel_l2(qs[1], qs[0], g, d, case.p_inf, cells) if rms > 0 else None}
+    return acc
+
+
+def _wake_record(N, built, args, local, hbm, peak_src):
+    """Device-timed sub-record of the 3D cylinder wake (384x256x96, 9.4M hex
+    cells, working set far beyond L2): FP32-bulk and FP64, no CPU leg."""
+    case, ch = built
+    dt = case.delta_t
+    desc = WORKLOAD_DESC["cylinder3d"]
+    sub = argparse.Namespace(steps=args.wake_steps, warmup=3)
+    r32 = _leg_record(N, ch, N.LFM_FP32_BULK, dt, sub, 1, local, None, desc, "cylinder3d", hbm, peak_src, e2e=False)
+    r32["roofline"]["traffic_note"] = ("DRAM bytes of one k_flux launch of the 192x128x48 wake scaled by the cells "
+                                       "(x8); the traffic sits at the algorithmic bytes, which grow in proportion")
+    r64 = _leg_record(N, ch, N.LFM_FP64, dt, argparse.Namespace(steps=max(2, args.wake_steps // 2), warmup=2), 1,
+                      local, None, desc, "cylinder3d", hbm, peak_src, e2e=False)
+    return {"workload": desc["workload"], "cells": ch.desc.n_cells, "steps": args.wake_steps,
+            "l2": "512 MB write between timed steps (working set ~7 GB FP32-bulk, beyond L2)",
+            "fp32_bulk": r32, "fp64": r64, "speedup_fp32_bulk_vs_fp64": r32["value"] / r64["value"]}
 
 
 def run_gpu(args):
     ws, rank, local, pg = _dist()
-    import numpy as np
     from lfm_public_gb300 import _native as N, acoustics
     desc = WORKLOAD_DESC[args.workload]
-    fp32 = args.precision == "fp32"
+    fp32_head = args.precision == "fp32"
 
     base = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -349,97 +514,74 @@ def run_gpu(args):
 
     case = workload(args.workload)
     ch = N.CaseHandle.from_case(case, renumber={"none": 0, "rcm": 1, "hilbert": 2}[args.renumber])
-    nc, nq, stages = ch.desc.n_cells, ch.desc.nq, ch.desc.rk_order
+    nc, stages = ch.desc.n_cells, ch.desc.rk_order
     dt = case.delta_t
-    prec = N.LFM_FP32_BULK if fp32 else N.LFM_FP64
+    hbm, peak_src = _peaks()
 
-    s, total_ms, prof, launches, clk = _time_solver(N, ch, prec, dt, args.steps, args.warmup, local, pg, local)
-    value = ws * nc * stages * args.steps / (total_ms / 1000.0)
+    # the plain FP64 method and the FP32-bulk form, each device-timed, with
+    # its per-kernel times, roofline and end-to-end rate
+    with ClockSampler(local) as clk:
+        time.sleep(0.3)
+        legs = {}
+        for name, prec in (("fp64", N.LFM_FP64), ("fp32", N.LFM_FP32_BULK)):
+            legs[name] = _leg_record(N, ch, prec, dt, args, ws, local, pg, desc, args.workload, hbm, peak_src,
+                                     clk=clk)
+    head, other = (legs["fp32"], legs["fp64"]) if fp32_head else (legs["fp64"], legs["fp32"])
+    pipe64 = fp64_pipe_roofline(args.workload, nc, stages, legs["fp64"]["ms_per_step"],
+                                legs["fp64"]["kernels_ms_per_step"])
 
-    # end to end through the C ABI with pinned host buffers: copy the state in,
-    # advance one time step, copy it out, every step
-    import torch
-    host = torch.empty((nq, nc), dtype=torch.float64, pin_memory=True).numpy()
-    s.get_state(out=host)
-    for _ in range(2):
-        s.advance(host, 1, dt, host)
-    e2e_steps = max(1, args.steps)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):   # lfm_solver_advance: state in, one step, state out
-        s.advance(host, 1, dt, host)
-    s.sync()
-    e2e_s = _allmax(pg, time.perf_counter() - t0)
-    e2e_value = ws * nc * stages * e2e_steps / e2e_s
-    s.close()
+    # the 3D wake case is set up on a host thread while the long accuracy run
+    # keeps the GPU busy
+    wake_built, wake_err = [None], [None]
 
-    # the plain FP64 path on the same workload, for the speed-up, and the
-    # acoustic-pressure error of the FP32-bulk form against it
-    plain = None
+    def build_wake():
+        try:
+            c3 = workload("cylinder3d")
+            wake_built[0] = (c3, N.CaseHandle.from_case(c3))
+        except Exception as e:   # reported in the line
+            wake_err[0] = repr(e)
+
+    wake_thread = None
+    if args.wake and args.workload.startswith("cylinder2d"):
+        wake_thread = threading.Thread(target=build_wake, daemon=True)
+        wake_thread.start()
     accuracy = None
-    if fp32:
-        s64, ms64, prof64, _, _ = _time_solver(N, ch, N.LFM_FP64, dt, args.steps, args.warmup, local, pg)
-        s64.close()
-        v64 = ws * nc * stages * args.steps / (ms64 / 1000.0)
-        plain = {"value": v64, "unit": UNIT, "ms_per_step": ms64 / args.steps, "kernels_ms_per_step": prof64,
-                 "speedup": value / v64,
-                 "roofline": fp64_pipe_roofline(args.workload, nc, stages, ms64 / args.steps, prof64)}
-        n_acc = args.accuracy_steps
-        if n_acc > 0:
-            qs = []
-            for p in (N.LFM_FP64, N.LFM_FP32_BULK):
-                sa = N.Solver(ch, precision=p, device=local)
-                sa.step(n_acc, dt)
-                sa.sync()
-                qs.append(sa.get_state())
-                sa.close()
-            g, d = ch.desc.gamma, case.dim
-            err = acoustics.acoustic_rel_l2(qs[1], qs[0], g, d, case.p_inf)
-            ring_r = 50.0 if args.workload.startswith("cylinder") else None
-            accuracy = {"acoustic_p_rel_l2": err, "steps": n_acc,
-                        "against": "FP64 device path (itself within 1e-12 of the oracle), same case and steps"}
-            if ring_r is not None:
-                cells = acoustics.probe_ring(case.cell_centres, ch.cell_ids(), ring_r)
-                p64 = acoustics.pressure(qs[0], g, d)[cells] - case.p_inf
-                rms = float(np.sqrt(np.mean(p64 ** 2)))
-                # before the first wave reaches the ring p' is zero there in both
-                accuracy["probe_ring"] = {
-                    "radius": ring_r, "probes": len(cells), "p_rms_ref": rms,
-                    "rel_l2": acoustics.acoustic_rel_l2(qs[1], qs[0], g, d, case.p_inf, cells) if rms > 0 else None}
+    if args.accuracy_steps > 0:
+        accuracy = _accuracy(N, acoustics, case, ch, dt, args.accuracy_steps, local,
+                             50.0 if args.workload.startswith("cylinder") else None)
+    wake = None
+    if wake_thread is not None:
+        wake_thread.join()
+        wake = _wake_record(N, wake_built[0], args, local, hbm, peak_src) if wake_built[0] else {"error": wake_err[0]}
 
     if rank != 0:
         return 0
-    peaks = {}
-    if os.path.exists(PEAKS_FILE):
-        peaks = json.load(open(PEAKS_FILE))
-    hbm = peaks.get("hbm_gbs", 6800.0)
-    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    kb = kernel_bytes(desc["dim"], desc["faces_per_cell"], fp32, desc["scheme"], desc["viscous"])
-    dominant = max(prof, key=prof.get)
-    dom_ms_per_launch = prof[dominant] / stages
-    achieved = kb[dominant] * nc / (dom_ms_per_launch * 1e-3) / 1e9
-    step_bytes = sum(v for k, v in kb.items() if k != "k_tile_stage")
-    step_achieved = step_bytes * nc * stages * args.steps / (total_ms / ws * 1e-3) / 1e9
+    fp32_rec = dict(legs["fp32"])
+    fp32_rec["speedup_vs_fp64"] = legs["fp32"]["value"] / legs["fp64"]["value"]
+    fp32_rec["e2e_speedup_vs_fp64"] = legs["fp32"]["e2e"]["value"] / legs["fp64"]["e2e"]["value"]
+    fp32_rec["accuracy"] = accuracy
+    fp32_rec["dtype"] = "f32-flux/f64-rk"
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32-flux/f64-rk" if fp32 else "f64", "data": "synthetic (generated mesh and initial field)",
+        "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32-flux/f64-rk" if fp32_head else "f64",
+        "data": "synthetic (generated mesh and initial field)",
         "config": {"workload": desc["workload"], "cells": nc, "rk_stages": stages,
-                   "precision": "fp32-bulk" if fp32 else "fp64", "l2": "512 MB write between timed steps",
-                   "renumber": args.renumber,
-                   "parallelism": f"replicas x{ws}"},
-        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "peak_source": peak_src,
-                     "traffic": DRAM_TRAFFIC.get((args.workload, args.precision, dominant)),
-                     "algorithmic_bytes_per_cell": kb[dominant], "cells_per_launch": nc,
-                     "step_achieved": step_achieved, "step_frac": step_achieved / hbm,
-                     "step_algorithmic_bytes_per_cell_stage": step_bytes},
-        "kernels_ms_per_step": prof, "dominant_kernel": dominant,
-        "fp64_pipe": None if fp32 else fp64_pipe_roofline(args.workload, nc, stages, total_ms / args.steps, prof),
-        "plain_fp64": plain, "accuracy": accuracy,
+                   "precision": "fp32-bulk" if fp32_head else "fp64", "l2": "512 MB write between timed steps",
+                   "renumber": args.renumber, "parallelism": f"replicas x{ws}"},
+        "roofline": dict(head["roofline"], **({} if fp32_head else {
+            "limiter": "fp64-pipe (see fp64_pipe: GB300 issues about two FP64 instructions per clock per SM)"})),
+        "fp64_pipe": pipe64,
+        "kernels_ms_per_step": head["kernels_ms_per_step"], "kernels_sum_ms": head["kernels_sum_ms"],
+        "dominant_kernel": head["roofline"]["kernel"],
+        "e2e": head["e2e"],
+        "fp32_bulk": fp32_rec if not fp32_head else None,
+        "plain_fp64": dict(other, speedup=head["value"] / other["value"]) if fp32_head else None,
+        "accuracy": accuracy,
+        "wake3d": wake,
         "cpu_baseline": base,
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nq * nc * 8, "d2h_bytes_per_step": nq * nc * 8},
-        "gpu_launches": launches * args.steps,
-        "clocks": clk.summary() if clk else None,
+        "gpu_launches": head["launches_per_step"] * args.steps,
+        "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -493,7 +635,9 @@ def run_batch(args):
         pg.barrier()
     with ClockSampler(local) as clk:
         time.sleep(0.3)
+        clk.mark()
         times = b.bench(args.steps, 512 << 20)
+        clk.mark()
     nonfinite = [k for k, s in enumerate(slots) if b.case_status(s) != N.LFM_OK]
     if pg:
         pg.barrier()
@@ -731,9 +875,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="cylinder2d", choices=sorted(WORKLOAD_DESC) + ["batch64", "serve"])
-    ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"],
+                    help="precision of the headline value (the other is reported beside it)")
     ap.add_argument("--accuracy-steps", type=int, default=None,
-                    help="steps of the FP32-bulk vs FP64 comparison (default 1000; 200 for batch64)")
+                    help="steps of the FP32-bulk vs FP64 comparison (default: 20000 for the 2D cylinder, the "
+                         "configured run length; 1000 otherwise; 2000 for batch64)")
+    ap.add_argument("--no-wake", dest="wake", action="store_false",
+                    help="skip the 3D wake sub-record of the 2D cylinder workloads")
+    ap.add_argument("--wake-steps", type=int, default=10)
     ap.add_argument("--batch-cases", type=int, default=64)
     ap.add_argument("--tuning", default=None, help="batch launch shape block,items_per_thread,blocks_per_sm[,phased] "
                                                    "(default: autotuned)")
@@ -747,7 +896,7 @@ def main():
                     help="solver order of the cells (single-case workloads)")
     args = ap.parse_args()
     if args.accuracy_steps is None:
-        args.accuracy_steps = 200 if args.workload == "batch64" else 1000
+        args.accuracy_steps = {"batch64": 2000, "cylinder2d": 20000, "cylinder2d_m2": 20000}.get(args.workload, 1000)
     if args.impl == "reference":
         if args.workload in ("batch64", "serve"):
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched form; its CPU path is "

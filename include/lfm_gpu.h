@@ -245,7 +245,10 @@ int lfm_solver_cell_residual(lfm_solver* s, double* res);
  * buffers and stream are not touched. Scratch (ghost states, primitives,
  * viscous terms, face rhs) lives in one static device array of
  * LFM_NOALLOC_SCRATCH_BYTES per GPU, held from the library's load until the
- * process exits; cases that need more return LFM_ERR_UNSUPPORTED. The first
+ * process exits; cases that need more return LFM_ERR_UNSUPPORTED, and so
+ * does a partition of a decomposed case (a solver from
+ * lfm_partitioned_solver): its processor-face halo states come from the
+ * other partitions, which a caller's state q does not cover. The first
  * call on a device looks up that array's device address (set-up), so make it
  * before any stream capture. All calls share the array: calls whose work
  * overlaps on the GPU race with each other. */
@@ -302,10 +305,12 @@ int lfm_solver_bench(lfm_solver* s, int nsteps, double dt, size_t flush_bytes, f
 int lfm_solver_launches_per_step(const lfm_solver* s, int* launches);
 
 /* Per-kernel times of one time step ([n] entries, ms summed over the RK
- * stages, names in lfm_solver_kernel_name), measured with event nodes around
- * every kernel in a captured step graph (no host gaps), averaged over a few
- * launches that each start from an evicted L2 when lfm_solver_bench has
- * allocated its scrub buffer. Synchronizes. */
+ * stages, names in lfm_solver_kernel_name), by prefix differences: the graph
+ * of the step's first m kernel launches is timed (median of a few launches,
+ * each after an L2 eviction when lfm_solver_bench has allocated its scrub
+ * buffer) for every m, and the m-th launch is charged the difference. Each
+ * kernel is so timed where it runs in the step, and the times add up to the
+ * step's. Advances the state by partial steps. Synchronizes. */
 int lfm_solver_profile_step(lfm_solver* s, double dt, int n, float* ms);
 const char* lfm_solver_kernel_name(int i);
 
@@ -445,6 +450,14 @@ int lfm_batch_autotune(lfm_batch* b, int trial_steps, lfm_batch_tuning* chosen);
 int lfm_batch_bench(lfm_batch* b, int nsteps, size_t flush_bytes, float* ms);
 /* Kernel launches per time step (one per RK stage). */
 int lfm_batch_launches_per_step(const lfm_batch* b, int* launches);
+/* Failure-detection test aid, no reference counterpart: every grid barrier of
+ * the persistent stage kernel then waits for extra_arrivals blocks more than
+ * its grid has (0: normal operation). With extra_arrivals > 0 no barrier is
+ * ever reached: each block gives up after its bounded wait (about a second),
+ * the kernel returns, and lfm_batch_sync reports LFM_ERR_CUDA; the batch's
+ * case states are then undefined. Affects the persistent launch mode only
+ * (lfm_batch_tuning.phased = 0). */
+int lfm_batch_debug_barrier(lfm_batch* b, int extra_arrivals);
 
 /* ---- request server: continuous batching of solve requests ---------------
  *

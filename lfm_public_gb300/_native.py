@@ -1,8 +1,8 @@
 """ctypes binding of the C ABI in include/lfm_gpu.h.
 
 The library is the in-tree ``liblfm_gpu.so``; importing a solver without it is
-an error (there is no CPU fallback). The oracle port library is loaded only by
-``load_port`` for tests and the CPU baseline.
+an error (there is no CPU fallback). The oracle's binding lives beside the
+oracle (``oracle/port``), outside this package.
 """
 from __future__ import annotations
 
@@ -15,7 +15,6 @@ import numpy as np
 PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 LIB_PATH = os.path.join(PKG, "liblfm_gpu.so")
-PORT_PATH = os.path.join(ROOT, "oracle", "port", "liblfm_port.so")
 
 LFM_FP64 = 0
 LFM_FP32_BULK = 1
@@ -117,7 +116,6 @@ class LfmError(RuntimeError):
 
 
 _lib: Optional[C.CDLL] = None
-_port: Optional[C.CDLL] = None
 
 
 def load_library(path: str = LIB_PATH) -> C.CDLL:
@@ -198,6 +196,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "lfm_batch_autotune": ([vp, C.c_int, C.POINTER(BatchTuning)], C.c_int),
         "lfm_batch_bench": ([vp, C.c_int, C.c_size_t, C.POINTER(C.c_float)], C.c_int),
         "lfm_batch_launches_per_step": ([vp, C.POINTER(C.c_int)], C.c_int),
+        "lfm_batch_debug_barrier": ([vp, C.c_int], C.c_int),
         "lfm_server_create": ([C.POINTER(ServerOpts), C.POINTER(vp)], C.c_int),
         "lfm_server_destroy": ([vp], None),
         "lfm_server_submit": ([vp, C.POINTER(SolverDesc), C.c_double, C.c_int, C.POINTER(C.c_int64)], C.c_int),
@@ -211,26 +210,6 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         fn.argtypes = args
         fn.restype = res
     _lib = lib
-    return lib
-
-
-def load_port(path: str = PORT_PATH) -> C.CDLL:
-    """Loads the oracle port (test infrastructure only)."""
-    global _port
-    if _port is not None:
-        return _port
-    if not os.path.exists(path):
-        raise ImportError(f"{path} is missing: build it with lfm_public_gb300.build.build_port()")
-    lib = C.CDLL(path)
-    lib.lfm_port_run.argtypes = [C.POINTER(SolverDesc), _dp, C.c_int, C.c_double, _dp]
-    lib.lfm_port_run.restype = C.c_int
-    lib.lfm_port_run_cell_residual.argtypes = [C.POINTER(SolverDesc), _dp, C.c_int, C.c_double, _dp]
-    lib.lfm_port_run_cell_residual.restype = C.c_int
-    lib.lfm_port_cfl.argtypes = [C.POINTER(SolverDesc), _dp, C.c_double, _dp]
-    lib.lfm_port_cfl.restype = C.c_int
-    lib.lfm_port_min_dt.argtypes = [C.POINTER(SolverDesc), _dp, C.c_double, _dp]
-    lib.lfm_port_min_dt.restype = C.c_int
-    _port = lib
     return lib
 
 
@@ -718,6 +697,11 @@ class Batch:
         check(load_library().lfm_batch_launches_per_step(self._h, C.byref(v)))
         return v.value
 
+    def debug_barrier(self, extra_arrivals: int):
+        """Failure-detection test aid (lfm_batch_debug_barrier): the stage
+        kernel's grid barriers wait for that many blocks beyond the grid."""
+        check(load_library().lfm_batch_debug_barrier(self._h, extra_arrivals))
+
     def close(self):
         if getattr(self, "_h", None):
             load_library().lfm_batch_destroy(self._h)
@@ -802,40 +786,3 @@ def selftest_fp_convert(f32_bits: np.ndarray, f64_bits: np.ndarray):
     if rc != 0:
         raise LfmError(rc, "conversion self-test failed to run")
     return o64, o32
-
-
-def port_run(case: CaseHandle, q: np.ndarray, nsteps: int, dt: float, residual: bool = False):
-    """Runs the oracle port on q (copied) and returns (q, residual or None)."""
-    lib = load_port()
-    qq = np.ascontiguousarray(q, dtype=np.float64).copy()
-    res = np.zeros(case.desc.nq)
-    rc = lib.lfm_port_run(C.byref(case.desc), _ptr(qq, C.c_double), nsteps, dt,
-                          _ptr(res, C.c_double) if residual else None)
-    if rc != 0:
-        raise RuntimeError(f"oracle port failed with {rc}")
-    return qq, (res if residual else None)
-
-
-def port_cell_residual(case: CaseHandle, q: np.ndarray, nsteps: int, dt: float):
-    """Oracle port: (q after nsteps, per-cell stage-0 residual of the last step)."""
-    qq = np.ascontiguousarray(q, dtype=np.float64).copy()
-    res = np.zeros((case.desc.nq, case.desc.n_cells))
-    rc = load_port().lfm_port_run_cell_residual(C.byref(case.desc), _ptr(qq, C.c_double), nsteps, dt,
-                                                 _ptr(res, C.c_double))
-    if rc != 0:
-        raise RuntimeError(f"oracle port failed with {rc}")
-    return qq, res
-
-
-def port_cfl(case: CaseHandle, q: np.ndarray, dt: float) -> float:
-    v = C.c_double()
-    qq = np.ascontiguousarray(q, dtype=np.float64)
-    load_port().lfm_port_cfl(C.byref(case.desc), _ptr(qq, C.c_double), dt, C.byref(v))
-    return v.value
-
-
-def port_min_dt(case: CaseHandle, q: np.ndarray, max_co: float) -> float:
-    v = C.c_double()
-    qq = np.ascontiguousarray(q, dtype=np.float64)
-    load_port().lfm_port_min_dt(C.byref(case.desc), _ptr(qq, C.c_double), max_co, C.byref(v))
-    return v.value

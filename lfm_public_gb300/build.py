@@ -43,7 +43,10 @@ CUDA_FLAGS = {"solver_kernels_fp32.cu": ["-fmad=false"], "batch_kernels.cu": ["-
 LIB = os.path.join(PKG, "liblfm_gpu.so")
 CLI = os.path.join(PKG, "lfm_solve_gpu")
 PORT = os.path.join(ROOT, "oracle", "port", "liblfm_port.so")
-REF_DIR = os.environ.get("LFM_REFERENCE_DIR", "/root/reference")
+# The reference sources, when a checkout is at hand: $LFM_REFERENCE_DIR, else a
+# checkout named "reference" beside this repository. Without one the reference
+# oracle is not built (the CPU restatement in oracle/port is always built).
+REF_DIR = os.environ.get("LFM_REFERENCE_DIR") or os.path.join(os.path.dirname(ROOT), "reference")
 
 
 def _nvcc() -> str:
@@ -120,11 +123,14 @@ def build_library(verbose: bool = False) -> str:
 
 
 def build_port() -> str:
-    src = os.path.join(ROOT, "oracle", "port", "lfm_port.c")
+    """The oracle's CPU restatement: the stage loop (lfm_port.c) and its own
+    case set-up (lfm_port_setup.c), one shared library that needs nothing
+    from liblfm_gpu.so."""
+    srcs = [os.path.join(ROOT, "oracle", "port", n) for n in ("lfm_port.c", "lfm_port_setup.c")]
     hdr = [os.path.join(ROOT, "oracle", "port", "lfm_port.h"), os.path.join(ROOT, "include", "lfm_gpu.h")]
-    if not _newer(PORT, [src] + hdr):
+    if not _newer(PORT, srcs + hdr):
         _run(["gcc", "-O2", "-std=c99", "-ffp-contract=off", "-fPIC", "-shared", f"-I{os.path.join(ROOT, 'include')}",
-              "-o", PORT, src, "-lm"])
+              "-o", PORT, *srcs, "-lm"])
     return PORT
 
 

@@ -51,6 +51,7 @@ struct BatchArgs {
     BatchCtl* ctl;
     int* error;                 // set when a grid barrier gives up waiting
     int itemsPerThread;
+    unsigned barrierExtra;      // arrivals every barrier waits for beyond the grid's (test aid; 0)
 };
 
 // Kernel variants, chosen from the cases in the batch: compiling out what no

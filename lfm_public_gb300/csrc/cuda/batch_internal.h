@@ -188,4 +188,5 @@ struct lfm_batch {
     size_t scrubBytes = 0;
     double* dStage = nullptr;   // a case's absolute state in transit to or from the host
     size_t stageBytes = 0;
+    unsigned barrierExtra = 0;  // lfm_batch_debug_barrier
 };

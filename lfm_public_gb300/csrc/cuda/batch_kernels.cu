@@ -9,14 +9,23 @@ namespace dev {
 
 namespace {
 
-// Polls before a grid barrier gives up (each poll sleeps ~40 ns: about 0.7 s).
-constexpr unsigned kBarrierSpinLimit = 1u << 24;
+// A grid barrier gives up after kBarrierTimeoutNs of waiting (read from the
+// GPU's global nanosecond timer), or after kBarrierSpinLimit polls should
+// that timer not advance.
+constexpr unsigned long long kBarrierTimeoutNs = 1000000000ull;   // 1 s
+constexpr unsigned kBarrierSpinLimit = 1u << 25;
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 // Grid-wide barrier of the blocks of one launch (all resident: the launch is
 // cooperative, or its grid is sized to the resident capacity). Arrival is an
-// atomic increment after a release fence; waiting is bounded: after
-// kBarrierSpinLimit polls, or once another block has given up, the block sets
-// the error flag and the caller returns without touching further data.
+// atomic increment after a release fence; waiting is bounded: after about a
+// second, or once another block has given up, the block sets the error flag
+// and the caller returns without touching further data.
 __device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target, int* error) {
     __shared__ int sOk;
     __syncthreads();
@@ -25,8 +34,9 @@ __device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target,
         atomicAdd(counter, 1u);
         int ok = 1;
         unsigned spins = 0;
+        const unsigned long long t0 = global_ns();
         while (*(volatile unsigned*)counter < target) {
-            if (*(volatile int*)error != 0 || ++spins > kBarrierSpinLimit) {
+            if (*(volatile int*)error != 0 || ++spins > kBarrierSpinLimit || global_ns() - t0 > kBarrierTimeoutNs) {
                 atomicOr(error, 1);
                 ok = 0;
                 break;
@@ -124,7 +134,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch_stage(const __grid_constant__ B
     if (threadIdx.x == 0) sSlot = -1;
     __syncthreads();
     unsigned* counter = &b.ctl->barrier[stage];
-    unsigned target = 0;
+    unsigned target = b.barrierExtra;   // 0 except under lfm_batch_debug_barrier
     if (b.nTiles[0] > 0) {
         phase_tiles<0, BLOCK, DIMS, FULL>(b, stage, sc, sSlot);
         target += gridDim.x;

@@ -170,6 +170,7 @@ BatchArgs makeArgs(lfm_batch* b) {
     a.ctl = b->dCtl;
     a.error = b->dError;
     a.itemsPerThread = b->tune.items_per_thread;
+    a.barrierExtra = b->barrierExtra;
     return a;
 }
 
@@ -634,6 +635,18 @@ extern "C" int lfm_batch_set_tuning(lfm_batch* b, const lfm_batch_tuning* t) {
         b->graph = nullptr;
     }
     b->tilesDirty = true;
+    return LFM_OK;
+}
+
+extern "C" int lfm_batch_debug_barrier(lfm_batch* b, int extra_arrivals) {
+    if (!b || extra_arrivals < 0) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    LFM_CUDA(cudaSetDevice(b->device));
+    LFM_CUDA(cudaStreamSynchronize(b->stream));
+    b->barrierExtra = (unsigned)extra_arrivals;
+    if (b->graph) {   // the step graph holds the kernels' arguments
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
     return LFM_OK;
 }
 

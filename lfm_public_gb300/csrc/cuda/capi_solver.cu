@@ -268,17 +268,20 @@ void untile(lfm_solver* s) {
     }
 }
 
-// Called before stages are launched. FP32-bulk: primitives of every cell from
-// the stored state, once after a new state (the update kernels keep them
-// current afterwards). FP64: the stages that follow store the ghosts' states.
+// Called before stages are launched: primitives of every cell (and the
+// ghosts' states and primitives) from the stored state, once after a new state
+// -- the update kernels keep them current afterwards.
 int ensurePrims(lfm_solver* s) {
     s->ghostRowsValid = true;
     s->lastStageB = s->rkB.empty() ? 0.0 : s->rkB.back();
-    if (s->precision != LFM_FP32_BULK || s->primsValid) return LFM_OK;
+    if (s->primsValid) return LFM_OK;
     s->primParity = 0;   // rebuilt into a32.prim
     StageConfig c;
     c.fullPrep = true;
-    lfm::dev::launch_kernel<float>(s->a32, c, 0, s->stream);
+    if (s->precision == LFM_FP32_BULK)
+        lfm::dev::launch_kernel<float>(s->a32, c, 0, s->stream);
+    else
+        lfm::dev::launch_kernel<double>(s->a64, c, 0, s->stream);
     LFM_CUDA(cudaGetLastError());
     s->primsValid = true;
     return LFM_OK;
@@ -472,16 +475,19 @@ int createSolver(const lfm_solver_desc* d, const lfm_solver_opts* opts, cudaStre
             }
         }
     }
-    // the tile stages need the update to write the ghosts
-    if (s->precision == LFM_FP32_BULK &&
-        (tiled || s->nc <= (s->D == 2 ? kFuseGhostCells2D : kFuseGhostCells3D))) {
+    // the tile stages need the update to write the ghosts; the FP64 update
+    // always writes them (its kernel is bound by the FP64 pipe, not by the
+    // registers the ghost branch adds)
+    if (s->precision == LFM_FP64 ||
+        tiled || s->nc <= (s->D == 2 ? kFuseGhostCells2D : kFuseGhostCells3D)) {
         // cells with boundary faces: their update writes the ghosts' next state
         std::vector<uint8_t> cg(nc, 0);
         for (size_t f = 0; f < nf; ++f)
             if (fN[f] >= s->nc && fN[f] < s->nc + s->ng) cg[(size_t)fP[f]] = 1;
         uint8_t* dCG = nullptr;
         if ((rc = upload(s, &dCG, cg.data(), nc))) return fail(rc);
-        s->a32.cellGhosts = dCG;
+        if (s->precision == LFM_FP32_BULK) s->a32.cellGhosts = dCG;
+        else s->a64.cellGhosts = dCG;
     }
     if (s->precision == LFM_FP32_BULK && !tiled && (s->D == 3 || s->nc > kFuseGhostCells2D)) {
         // the update's fixed-width cell -> face table, when every cell fits it:
@@ -599,7 +605,7 @@ int enqueueSetState(lfm_solver* s, const double* q) {
         LFM_CUDA(cudaMemcpy2DAsync(s->q, (size_t)s->nt * sizeof(double), q, nc * sizeof(double),
                                    nc * sizeof(double), (size_t)s->nq, cudaMemcpyHostToDevice, s->stream));
     }
-    s->primsValid = s->precision == LFM_FP32_BULK;
+    s->primsValid = s->precision == LFM_FP32_BULK;   // FP64: rebuilt by ensurePrims
     s->primParity = 0;
     s->ghostRowsValid = false;
     return LFM_OK;
@@ -684,7 +690,7 @@ int advanceGraph(lfm_solver* s, const double* qIn, int nsteps, double dt, double
     LFM_CUDA(cudaGraphLaunch(s->advGraph, s->stream));
     // the flags the enqueued path leaves: a new state, its primitives, stages run
     s->primParity = 0;
-    s->primsValid = s->precision == LFM_FP32_BULK;
+    s->primsValid = true;
     s->ghostRowsValid = true;
     s->lastStageB = s->rkB.empty() ? 0.0 : s->rkB.back();
     LFM_CUDA(cudaStreamSynchronize(s->stream));
@@ -880,9 +886,9 @@ int residualNoalloc(const lfm_solver* s, const Args<T>& base, const double* q, i
         // the FP32-bulk kernels read the state as q - q_ref
         lfm::dev::launch_to_perturbation(a, q, qStride, st);
     } else {
-        for (size_t v = 0; v < nq; ++v)
-            LFM_CUDA(cudaMemcpyAsync(a.q + v * nt, q + (size_t)v * (size_t)qStride, (size_t)s->nc * sizeof(double),
-                                     cudaMemcpyDeviceToDevice, st));
+        // rows of nc values (stride q_stride) into rows of nt, one strided copy
+        LFM_CUDA(cudaMemcpy2DAsync(a.q, nt * sizeof(double), q, (size_t)qStride * sizeof(double),
+                                   (size_t)s->nc * sizeof(double), nq, cudaMemcpyDeviceToDevice, st));
     }
     StageConfig c;
     c.scheme = s->scheme;
@@ -904,6 +910,13 @@ extern "C" int lfm_solver_residual_noalloc(const lfm_solver* s, const double* q,
                                            void* stream) {
     if (!s || !q || !res) return lfm::setError(LFM_ERR_INVALID, "lfm_solver_residual_noalloc: null argument");
     if (q_stride < s->nc) return lfm::setError(LFM_ERR_INVALID, "q_stride is smaller than the cell count");
+    // A partition of a decomposed case reads processor-face halo states that
+    // its partitioned solver copies in before each stage; a caller's state
+    // here covers the partition's own cells only, so those rows would be stale
+    // (or zero) in the scratch array.
+    if (s->nh > 0)
+        return lfm::setError(LFM_ERR_UNSUPPORTED,
+                             "lfm_solver_residual_noalloc: partitions with processor-face halos are not supported");
     LFM_CUDA(cudaSetDevice(s->device));
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (s->precision == LFM_FP32_BULK) return residualNoalloc<float>(s, s->a32, q, q_stride, res, st);
@@ -993,10 +1006,9 @@ extern "C" int lfm_solver_forces(lfm_solver* s, int n_patches, const int32_t* pa
     LFM_CUDA(cudaMemcpyAsync(s->dPatches, pl.data(), pl.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
     LFM_CUDA(cudaMemsetAsync(s->dForces, 0, 2 * nv * sizeof(double), s->stream));
     // ghost states of the last stage's start, as the reference's ghost cells
-    // hold after a step: stored on the FP64 path, recovered from the last
-    // update on the FP32-bulk path; the current state's before any stage
-    const int mode = !s->ghostRowsValid ? lfm::dev::kGhostFresh
-                     : s->precision == LFM_FP64 ? lfm::dev::kGhostStored : lfm::dev::kGhostUndo;
+    // hold after a step: recovered from the last update (the update writes the
+    // ghosts of the next stage's state); the current state's before any stage
+    const int mode = !s->ghostRowsValid ? lfm::dev::kGhostFresh : lfm::dev::kGhostUndo;
     if (s->precision == LFM_FP32_BULK)
         lfm::dev::launch_forces<float>(s->a32, stateOffset(s), s->gS, s->gD, s->gPatch, mode, s->lastStageB,
                                        s->dPatches, n_patches, s->forceTerms, s->dForces, s->dForces + nv, s->stream);
@@ -1110,24 +1122,76 @@ extern "C" int lfm_solver_bench(lfm_solver* s, int nsteps, double dt, size_t flu
 
 extern "C" int lfm_solver_launches_per_step(const lfm_solver* s, int* launches) {
     if (!s || !launches) return lfm::setError(LFM_ERR_INVALID, "bad argument");
-    // preparation: every stage on the FP64 path; on the FP32-bulk path the
-    // update writes the cells' and ghosts' primitives, so only halos remain
-    const bool prep = s->precision != LFM_FP32_BULK || !s->a32.cellGhosts || s->nh > 0;
+    // preparation: the update writes the cells' and (cellGhosts) the ghosts'
+    // primitives, so only halos remain
+    const bool fused = s->precision == LFM_FP32_BULK ? s->a32.cellGhosts != nullptr : s->a64.cellGhosts != nullptr;
+    const bool prep = !fused || s->nh > 0;
     *launches = s->tiled ? s->rkOrder : s->rkOrder * ((prep ? 1 : 0) + 2 + (s->needGrad ? 1 : 0) + (s->needVis ? 1 : 0));
     return LFM_OK;
 }
 
 extern "C" const char* lfm_solver_kernel_name(int i) { return lfm::dev::kernelName(i); }
 
-// Per-kernel times of a time step as it runs in the step's CUDA graph: one
-// step captured with an event record node on each side of every kernel (no
-// host launch gaps between them), launched a few times, each after the L2
-// scrub of the benchmark loop when one exists; times averaged over launches.
-// Each stage also records an empty pair of event nodes: its time, the cost
-// of a pair of event nodes alone, is taken off every kernel's. With tile
-// stages the graph holds two steps (so that it starts and ends on the same
-// primitive buffer) and the fused kernel's time goes to slot
-// kKernelsPerStage ("k_tile_stage").
+// Per-kernel times of a time step, by prefix differences: the step's kernel
+// launches in order are L1..LM; for every m the graph of L1..Lm runs a few
+// times, each after the L2 scrub of the benchmark loop (when one exists),
+// timed with events on the stream around the graph launch, and T(m) is the
+// median. Launch Lm is charged T(m) - T(m-1) (T(0): the empty event pair),
+// so each kernel is timed where it runs in the step - after the same
+// kernels, with the L2 contents they leave - and the charges add up to the
+// step's own time T(M). With tile stages the whole stage is one kernel and
+// the step's time goes to slot kKernelsPerStage ("k_tile_stage").
+namespace {
+
+struct Launch {
+    int stage, slot;
+};
+
+// Median over reps of the time of `body` enqueued after an L2 scrub.
+template <typename F>
+cudaError_t medianTime(lfm_solver* s, int reps, cudaEvent_t e0, cudaEvent_t e1, F body, float* out) {
+    std::vector<float> t;
+    cudaError_t e = cudaSuccess;
+    for (int r = 0; r < reps && e == cudaSuccess; ++r) {
+        if (s->scrub) e = cudaMemsetAsync(s->scrub, 0x5a + (r & 1), s->scrubBytes, s->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(e0, s->stream);
+        if (e == cudaSuccess) e = body();
+        if (e == cudaSuccess) e = cudaEventRecord(e1, s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        t.push_back(ms);
+    }
+    if (e != cudaSuccess) return e;
+    std::sort(t.begin(), t.end());
+    *out = t[t.size() / 2];
+    return cudaSuccess;
+}
+
+void launchOne(lfm_solver* s, const Launch& l, double dt) {
+    const StageConfig c = stageConfig(s, l.stage, dt);
+    if (s->precision == LFM_FP32_BULK)
+        lfm::dev::launch_kernel<float>(s->a32, c, l.slot, s->stream);
+    else
+        lfm::dev::launch_kernel<double>(s->a64, c, l.slot, s->stream);
+}
+
+// Graph of the launches [0, m) of `seq` (nullptr when m == 0).
+cudaError_t prefixGraph(lfm_solver* s, const std::vector<Launch>& seq, size_t m, double dt, cudaGraphExec_t* out) {
+    *out = nullptr;
+    if (m == 0) return cudaSuccess;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    for (size_t k = 0; k < m; ++k) launchOne(s, seq[k], dt);
+    e = cudaStreamEndCapture(s->stream, &g);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(out, g, 0);
+    if (g) cudaGraphDestroy(g);
+    return e;
+}
+
+}  // namespace
+
 extern "C" int lfm_solver_profile_step(lfm_solver* s, double dt, int n, float* ms) {
     if (!s || !ms || n < lfm::dev::kKernelSlots) return lfm::setError(LFM_ERR_INVALID, "bad argument");
     LFM_CUDA(cudaSetDevice(s->device));
@@ -1135,62 +1199,50 @@ extern "C" int lfm_solver_profile_step(lfm_solver* s, double dt, int n, float* m
     if (s->rkOrder == 0) return LFM_OK;   // no stage, no kernel
     int rc = ensurePrims(s);
     if (rc) return rc;
-    const int K = lfm::dev::kKernelsPerStage;
-    const int K1 = K + 1;   // slot K: the empty calibration pair
-    const int steps = s->tiled ? 2 : 1;
-    const int nStages = steps * s->rkOrder;
-    std::vector<cudaEvent_t> ev(2 * (size_t)nStages * (size_t)K1);
-    for (auto& x : ev) LFM_CUDA(cudaEventCreate(&x));
-    auto destroy = [&]() {
-        for (auto& x : ev) cudaEventDestroy(x);
-    };
-    cudaGraph_t g = nullptr;
-    cudaGraphExec_t ge = nullptr;
-    cudaError_t e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
-    for (int kk = 0; kk < nStages && e == cudaSuccess; ++kk) {
-        const int k = kk % s->rkOrder;
-        const StageConfig c = stageConfig(s, k, dt);
-        for (int w = 0; w < K1 && e == cudaSuccess; ++w) {
-            const size_t base = 2 * ((size_t)kk * (size_t)K1 + (size_t)w);
-            e = cudaEventRecordWithFlags(ev[base], s->stream, cudaEventRecordExternal);
-            if (s->tiled) {
-                if (w == 0) tileStage(s, kk, dt, s->primParity);
-            } else if (w < K && s->precision == LFM_FP32_BULK) {
-                lfm::dev::launch_kernel<float>(s->a32, c, w, s->stream);
-            } else if (w < K) {
-                lfm::dev::launch_kernel<double>(s->a64, c, w, s->stream);
+    constexpr int kReps = 7;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    LFM_CUDA(cudaEventCreate(&e0));
+    LFM_CUDA(cudaEventCreate(&e1));
+    cudaError_t e = cudaSuccess;
+    float t0 = 0.f;
+    e = medianTime(s, kReps, e0, e1, [] { return cudaSuccess; }, &t0);
+    if (s->tiled) {
+        // whole steps (the primitive buffers alternate between the stages)
+        if (e == cudaSuccess && !(rc = ensureGraph(s, dt))) {
+            float t = 0.f;
+            e = medianTime(s, kReps, e0, e1, [s] { return launchStepGraph(s); }, &t);
+            ms[lfm::dev::kKernelsPerStage] = std::max(0.f, t - t0);
+        }
+    } else if (e == cudaSuccess) {
+        // the launches of one step: a (stage, slot) pair counts when its
+        // capture holds a kernel
+        std::vector<Launch> seq;
+        for (int k = 0; k < s->rkOrder && e == cudaSuccess; ++k)
+            for (int w = 0; w < lfm::dev::kKernelsPerStage && e == cudaSuccess; ++w) {
+                cudaGraph_t g = nullptr;
+                e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
+                if (e != cudaSuccess) break;
+                launchOne(s, Launch{k, w}, dt);
+                e = cudaStreamEndCapture(s->stream, &g);
+                size_t nodes = 0;
+                if (e == cudaSuccess) e = cudaGraphGetNodes(g, nullptr, &nodes);
+                if (g) cudaGraphDestroy(g);
+                if (e == cudaSuccess && nodes > 0) seq.push_back(Launch{k, w});
             }
-            if (e == cudaSuccess) e = cudaEventRecordWithFlags(ev[base + 1], s->stream, cudaEventRecordExternal);
+        float prev = t0;
+        for (size_t m = 1; m <= seq.size() && e == cudaSuccess; ++m) {
+            cudaGraphExec_t ge = nullptr;
+            e = prefixGraph(s, seq, m, dt, &ge);
+            float t = 0.f;
+            if (e == cudaSuccess) e = medianTime(s, kReps, e0, e1, [s, ge] { return cudaGraphLaunch(ge, s->stream); }, &t);
+            if (ge) cudaGraphExecDestroy(ge);
+            ms[seq[m - 1].slot] += t - prev;
+            prev = t;
         }
     }
-    const cudaError_t ec = cudaStreamEndCapture(s->stream, &g);
-    if (e == cudaSuccess) e = ec;
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
-    if (g) cudaGraphDestroy(g);
-    if (e != cudaSuccess) {
-        destroy();
-        return cudaFail(e, "profile graph");
-    }
-    constexpr int kReps = 5;
-    for (int r = 0; r < kReps && e == cudaSuccess; ++r) {
-        if (s->scrub) e = cudaMemsetAsync(s->scrub, 0x5a + (r & 1), s->scrubBytes, s->stream);
-        if (e == cudaSuccess) e = cudaGraphLaunch(ge, s->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-        for (int kk = 0; kk < nStages && e == cudaSuccess; ++kk) {
-            float t[16] = {0};
-            for (int w = 0; w < K1 && e == cudaSuccess; ++w) {
-                const size_t base = 2 * ((size_t)kk * (size_t)K1 + (size_t)w);
-                e = cudaEventElapsedTime(&t[w], ev[base], ev[base + 1]);
-            }
-            const float scale = 1.0f / (kReps * steps);
-            if (s->tiled)
-                ms[K] += std::max(0.f, t[0] - t[K]) * scale;
-            else
-                for (int w = 0; w < K && e == cudaSuccess; ++w) ms[w] += std::max(0.f, t[w] - t[K]) * scale;
-        }
-    }
-    cudaGraphExecDestroy(ge);
-    destroy();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
     if (e != cudaSuccess) return cudaFail(e, "profile step");
     return LFM_OK;
 }

@@ -177,14 +177,57 @@ __device__ __forceinline__ void stage_state(const Args<T>& a, int t, double* qv)
     for (int v = 0; v < NQ; ++v) a.q[(size_t)v * a.nt + t] = qv[v];
 }
 
+// FP64 path: the primitives every face reads (1/rho, u, R psi = p/rho, c) of
+// cell, ghost or halo t from its conservative state qv (compute_Rpsi,
+// api/cfdv0_solver.h:252-261).
+template <int D>
+__device__ __forceinline__ void prims64(const Args<double>& a, int t, const double* qv) {
+    const size_t nt = (size_t)a.nt;
+    const double rinv = 1.0 / qv[0];
+    double s = qv[1] * qv[1];
+#pragma unroll
+    for (int k = 1; k < D; ++k) s += qv[k + 1] * qv[k + 1];
+    const double Rpsi = a.gm1 * (qv[D + 1] - 0.5 * s * rinv) * rinv;
+    a.prim[t] = rinv;
+#pragma unroll
+    for (int k = 0; k < D; ++k) a.prim[(size_t)(1 + k) * nt + t] = qv[k + 1] * rinv;
+    a.prim[(size_t)(D + 1) * nt + t] = Rpsi;
+    a.prim[(size_t)(D + 2) * nt + t] = sqrt(a.gamma * Rpsi);
+}
+
+// FP64 path: the states and primitives of the boundary ghosts of cell c from
+// its conservative state qc (those k_prep computes for the next stage).
+template <int D>
+__device__ __forceinline__ void ghosts_of64(const Args<double>& a, int c, const double* qc) {
+    constexpr int NQ = D + 2;
+    const size_t nt = (size_t)a.nt;
+    for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
+        const int code = a.cfList[e];
+        if (code < 0) continue;
+        const int j = a.fN[code];
+        if (j < a.nc || j >= a.nc + a.ng) continue;
+        double qv[NQ];
+        ghost_bc<double, D>(a, j - a.nc, qc, qv);
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) a.q[(size_t)v * nt + j] = qv[v];
+        prims64<D>(a, j, qv);
+    }
+}
+
 // FP64 path: gather of the face rhs of cell c, sponge source and low-storage
 // RK update (src/cfd_v0.cpp:2800-2822). The rhs are summed in ascending face
 // order (the order in which the reference's scatter reaches the cell); the
-// sum is the cell residual RES.
-template <typename T, int D, bool RES>
+// sum is the cell residual RES. PRIM: the cell also writes the next stage's
+// primitives from the registers it holds, and (a.cellGhosts) the next stage's
+// states and primitives of its boundary ghosts -- a ghost depends on its
+// interior cell only -- so that no preparation pass runs between the stages.
+template <typename T, int D, bool RES, bool PRIM = false>
 __device__ __forceinline__ void update_cell(const Args<T>& a, int c, double Ak, double Bk, double dt, int first) {
     constexpr int NQ = D + 2;
     const size_t nt = (size_t)a.nt, nf = (size_t)a.nf, nc = (size_t)a.nc;
+    double qv[NQ];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) qv[v] = a.q[v * nt + c];
     T sum[NQ];
 #pragma unroll
     for (int v = 0; v < NQ; ++v) sum[v] = T(0);
@@ -204,9 +247,6 @@ __device__ __forceinline__ void update_cell(const Args<T>& a, int c, double Ak, 
     const double dtvi = dt * a.volInv[c];
 #pragma unroll
     for (int v = 0; v < NQ; ++v) acc[v] = (first ? 0.0 : Ak * a.dq[v * nc + c]) + dtvi * (double)sum[v];
-    double qv[NQ];
-#pragma unroll
-    for (int v = 0; v < NQ; ++v) qv[v] = a.q[v * nt + c];
     const double sg = a.sponge[c];
     if (sg != 0.0) {
         acc[0] += dt * sg * (a.rhoInf - qv[0]);
@@ -214,15 +254,20 @@ __device__ __forceinline__ void update_cell(const Args<T>& a, int c, double Ak, 
         for (int k = 0; k < D; ++k) acc[k + 1] += dt * sg * (a.rhoInf * a.UInf[k] - qv[k + 1]);
         acc[D + 1] += dt * sg * (a.rhoInf * a.EInf - qv[D + 1]);
     }
+    double qn[NQ];
 #pragma unroll
     for (int v = 0; v < NQ; ++v) {
         a.dq[v * nc + c] = acc[v];
-        const double qn = qv[v] + Bk * acc[v];
-        finite = finite && isfinite(qn);
-        a.q[v * nt + c] = qn;
+        qn[v] = qv[v] + Bk * acc[v];
+        finite = finite && isfinite(qn[v]);
+        a.q[v * nt + c] = qn[v];
         if (RES) a.res[v * nc + c] = (double)sum[v];
     }
     if (!finite) atomicOr(a.flag, 1);
+    if constexpr (PRIM) {
+        prims64<D>(a, c, qn);
+        if (a.cellGhosts && a.cellGhosts[c]) ghosts_of64<D>(a, c, qn);
+    }
 }
 
 }  // namespace dev

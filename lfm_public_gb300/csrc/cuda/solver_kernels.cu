@@ -6,26 +6,18 @@ namespace lfm {
 namespace dev {
 
 // ---------------------------------------------------------------------------
-// k_prep: ghost states and per-cell primitives.
+// k_prep: ghost states and per-cell primitives of entries [first, nt). The
+// update writes the cells' and ghosts' primitives for the next stage, so
+// between stages only processor halos (copied in) need this pass.
 // ---------------------------------------------------------------------------
 template <typename T, int D>
-__global__ void __launch_bounds__(256) k_prep(Args<T> a) {
-    const int t = LFM_GLOBAL_ID();
+__global__ void __launch_bounds__(256) k_prep(Args<T> a, int first) {
+    const int t = first + LFM_GLOBAL_ID();
     if (t >= a.nt) return;
     constexpr int NQ = D + 2;
     double qv[NQ];
     stage_state<T, D>(a, t, qv);
-    // compute_Rpsi (api/cfdv0_solver.h:252-261)
-    const double rinv = 1.0 / qv[0];
-    double s = qv[1] * qv[1];
-#pragma unroll
-    for (int k = 1; k < D; ++k) s += qv[k + 1] * qv[k + 1];
-    const double Rpsi = a.gm1 * (qv[D + 1] - 0.5 * s * rinv) * rinv;
-    a.prim[t] = (T)rinv;
-#pragma unroll
-    for (int k = 0; k < D; ++k) a.prim[(size_t)(1 + k) * a.nt + t] = (T)(qv[k + 1] * rinv);
-    a.prim[(size_t)(D + 1) * a.nt + t] = (T)Rpsi;
-    a.prim[(size_t)(D + 2) * a.nt + t] = (T)sqrt(a.gamma * Rpsi);
+    prims64<D>(a, t, qv);
 }
 
 // ---------------------------------------------------------------------------
@@ -366,13 +358,15 @@ __global__ void __launch_bounds__(128) k_flux(Args<T> a) {
 }
 
 // ---------------------------------------------------------------------------
-// k_update: gather, sponge, RK update (update_cell, solver_device.cuh).
+// k_update: gather, sponge, RK update (update_cell, solver_device.cuh), then
+// the next stage's primitives of the cell and, with a.cellGhosts, the states
+// and primitives of its boundary ghosts.
 // ---------------------------------------------------------------------------
 template <typename T, int D, bool RES>
 __global__ void __launch_bounds__(256) k_update(const __grid_constant__ Args<T> a, double Ak, double Bk, double dt, int first) {
     const int c = LFM_GLOBAL_ID();
     if (c >= a.nc) return;
-    update_cell<T, D, RES>(a, c, Ak, Bk, dt, first);
+    update_cell<T, D, RES, true>(a, c, Ak, Bk, dt, first);
 }
 
 // ---------------------------------------------------------------------------
@@ -470,7 +464,13 @@ void launch_flux(const Args<T>& a, cudaStream_t st) {
 template <typename T, int D, bool LES>
 void launch_fp64(const Args<T>& a, const StageConfig& s, int which, cudaStream_t st) {
     switch (which) {
-        case 0: k_prep<T, D><<<blocks(a.nt, 256), 256, 0, st>>>(a); break;
+        case 0: {
+            // the update keeps the cells' and (a.cellGhosts) the ghosts'
+            // primitives current: only halos remain, unless the state is new
+            const int first = s.fullPrep ? 0 : (a.cellGhosts ? a.nc + a.ng : a.nc);
+            if (a.nt > first) k_prep<T, D><<<blocks(a.nt - first, 256), 256, 0, st>>>(a, first);
+            break;
+        }
         case 1:
             if (s.needGrad) k_grad<T, D><<<blocks(a.nc, 256), 256, 0, st>>>(a);
             break;

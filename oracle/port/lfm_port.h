@@ -21,6 +21,19 @@ int lfm_port_run_cell_residual(const lfm_solver_desc* desc, double* q, int nstep
 int lfm_port_cfl(const lfm_solver_desc* desc, const double* q, double dt, double* cfl);
 int lfm_port_min_dt(const lfm_solver_desc* desc, const double* q, double max_co, double* dt);
 
+/* Case set-up of the oracle itself (lfm_port_setup.c): the solver description
+ * of an in-memory polyMesh with its parameters and initial fields, built
+ * without the device library. Whole cases in the reference's cell order only
+ * (params->renumber must be LFM_RENUMBER_NONE). Returns 0 on success, -1 with
+ * lfm_port_last_error() set otherwise. */
+typedef struct lfm_port_case lfm_port_case;
+int lfm_port_case_build(const lfm_polymesh* mesh, const lfm_params* params, const lfm_fields* fields,
+                        lfm_port_case** out);
+/* Pointers into the case's arrays, valid until lfm_port_case_free. */
+int lfm_port_case_describe(const lfm_port_case* c, lfm_solver_desc* out);
+void lfm_port_case_free(lfm_port_case* c);
+const char* lfm_port_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

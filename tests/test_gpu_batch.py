@@ -198,3 +198,29 @@ def test_batch_acoustic_pressure_against_fp64():
         err = acoustics.acoustic_rel_l2(b.get_state(s), q64, ch.desc.gamma, c.dim, c.p_inf)
         assert err <= 1e-3, (c.name, err)
     b.close()
+
+
+def test_grid_barrier_wait_is_bounded():
+    """Failure detection without a GPU fault: a grid barrier made to wait for
+    one block more than the grid has (a count nothing reaches) gives up after
+    its bounded wait (about a second); the kernel returns, lfm_batch_sync
+    reports LFM_ERR_CUDA, and the context stays usable: a fresh batch then
+    steps and gives the single-case solver's bits."""
+    import time
+    case = cases.vortex_case(n=32, solver=1)
+    ch = N.CaseHandle.from_case(case)
+    b = N.Batch(arena_bytes=N.Batch.case_bytes(ch) + (1 << 20), max_cases=1)
+    b.add(ch, case.delta_t)
+    b.set_tuning(128, 1, 1, cooperative=1, phased=0)
+    b.debug_barrier(1)
+    t0 = time.perf_counter()
+    b.step(1)
+    with pytest.raises(N.LfmError) as e:
+        b.sync()
+    waited = time.perf_counter() - t0
+    b.close()
+    assert e.value.code == N.LFM_ERR_CUDA and "barrier" in str(e.value)
+    assert waited < 10.0, waited
+    # the same GPU context, a fresh batch
+    q = _alone(ch, 3, case.delta_t, shape=(128, 1, 1))
+    assert np.array_equal(q, _single(ch, 3, case.delta_t))

@@ -6,6 +6,7 @@ run."""
 import numpy as np
 import pytest
 
+import oracle.port as P
 from lfm_public_gb300 import _native as N, acoustics, cases
 from tests.helpers import golden_names, load_golden, reference_conserved, rel_l2, rel_l2_vec
 
@@ -39,7 +40,7 @@ def test_fp64_matches_oracle_cylinder(solver, minmod):
     ch = N.CaseHandle.from_case(case)
     n = 20
     q_gpu = _gpu_run(ch, n, case.delta_t)
-    q_ref, _ = N.port_run(ch, ch.q0(), n, case.delta_t)
+    q_ref, _ = P.run(ch, ch.q0(), n, case.delta_t)
     assert np.all(rel_l2(q_gpu, q_ref) <= TOL), rel_l2(q_gpu, q_ref)
 
 
@@ -49,7 +50,7 @@ def test_fp64_matches_oracle_3d_and_triangles():
                     (cases.tri_case(n=40, seed=9, solver=0, beta=4.0), 20)):
         ch = N.CaseHandle.from_case(case)
         q_gpu = _gpu_run(ch, n, case.delta_t)
-        q_ref, _ = N.port_run(ch, ch.q0(), n, case.delta_t)
+        q_ref, _ = P.run(ch, ch.q0(), n, case.delta_t)
         assert np.all(rel_l2(q_gpu, q_ref) <= TOL), (case.name, rel_l2(q_gpu, q_ref))
 
 
@@ -65,7 +66,7 @@ def test_rk_orders_match_oracle(rk):
     assert ch.desc.rk_order == rk
     n = 10
     q64 = _gpu_run(ch, n, case.delta_t)
-    q_ref, _ = N.port_run(ch, ch.q0(), n, case.delta_t)
+    q_ref, _ = P.run(ch, ch.q0(), n, case.delta_t)
     assert np.all(rel_l2(q64, q_ref) <= TOL), rel_l2(q64, q_ref)
     q32 = _gpu_run(ch, n, case.delta_t, N.LFM_FP32_BULK)
     assert acoustics.acoustic_rel_l2(q32, q64, ch.desc.gamma, case.dim, case.p_inf) <= 1e-3
@@ -92,7 +93,7 @@ def test_tiny_meshes(make):
     ch = N.CaseHandle.from_case(case)
     n = 5
     q64 = _gpu_run(ch, n, case.delta_t)
-    q_ref, _ = N.port_run(ch, ch.q0(), n, case.delta_t)
+    q_ref, _ = P.run(ch, ch.q0(), n, case.delta_t)
     # momentum as one vector field: on these symmetric meshes a momentum
     # component can be pure rounding noise (1e-8 against 1e2)
     err = lambda a, b: rel_l2_vec(a, b, case.dim)  # noqa: E731
@@ -119,7 +120,7 @@ def test_mixed_quad_triangle_mesh(solver):
     assert set(np.diff(offs).tolist()) == {3, 4}
     n = 20
     q64 = _gpu_run(ch, n, case.delta_t)
-    q_ref, _ = N.port_run(ch, ch.q0(), n, case.delta_t)
+    q_ref, _ = P.run(ch, ch.q0(), n, case.delta_t)
     assert np.all(rel_l2(q64, q_ref) <= TOL), rel_l2(q64, q_ref)
     q32 = _gpu_run(ch, n, case.delta_t, N.LFM_FP32_BULK)
     assert acoustics.acoustic_rel_l2(q32, q64, ch.desc.gamma, case.dim, case.p_inf) <= 1e-3
@@ -142,7 +143,7 @@ def test_3d_prisms_and_tetrahedra(make):
     ch = N.CaseHandle.from_case(case)
     n = 10
     q64 = _gpu_run(ch, n, case.delta_t)
-    q_ref, _ = N.port_run(ch, ch.q0(), n, case.delta_t)
+    q_ref, _ = P.run(ch, ch.q0(), n, case.delta_t)
     # momentum as one vector: the prisms' w stays zero up to rounding (1e-12 against 6e3)
     err = rel_l2_vec(q64, q_ref, case.dim)
     assert np.all(err <= TOL), err
@@ -167,7 +168,7 @@ def test_smagorinsky_les_on_tetrahedra():
     assert ch.desc.smag_c
     n = 10
     q64 = _gpu_run(ch, n, case.delta_t)
-    q_ref, _ = N.port_run(ch, ch.q0(), n, case.delta_t)
+    q_ref, _ = P.run(ch, ch.q0(), n, case.delta_t)
     err = rel_l2_vec(q64, q_ref, case.dim)
     assert np.all(err <= TOL), err
     q32 = _gpu_run(ch, n, case.delta_t, N.LFM_FP32_BULK)
@@ -194,8 +195,8 @@ def test_cfl_and_dt_reductions_match_oracle():
     s = N.Solver(ch)
     s.step(3, case.delta_t)
     q = s.get_state()
-    assert s.cfl(case.delta_t) == pytest.approx(N.port_cfl(ch, q, case.delta_t), rel=1e-14)
-    assert s.min_dt(0.5) == pytest.approx(N.port_min_dt(ch, q, 0.5), rel=1e-14)
+    assert s.cfl(case.delta_t) == pytest.approx(P.cfl(ch, q, case.delta_t), rel=1e-14)
+    assert s.min_dt(0.5) == pytest.approx(P.min_dt(ch, q, 0.5), rel=1e-14)
 
 
 def test_residual_matches_oracle():
@@ -205,7 +206,7 @@ def test_residual_matches_oracle():
     s = N.Solver(ch)
     s.step(4, case.delta_t)
     gpu_res = s.residual()
-    _, port_res = N.port_run(ch, ch.q0(), 4, case.delta_t, residual=True)
+    _, port_res = P.run(ch, ch.q0(), 4, case.delta_t, residual=True)
     assert np.allclose(gpu_res, port_res, rtol=1e-10, atol=0)
 
 
@@ -229,7 +230,7 @@ def test_full_size_cylinder_matches_oracle():
     case = cases.cylinder_case(solver=0, minmod=True)
     ch = N.CaseHandle.from_case(case)
     q_gpu = _gpu_run(ch, 2, case.delta_t)
-    q_ref, _ = N.port_run(ch, ch.q0(), 2, case.delta_t)
+    q_ref, _ = P.run(ch, ch.q0(), 2, case.delta_t)
     assert np.all(rel_l2(q_gpu, q_ref) <= TOL), rel_l2(q_gpu, q_ref)
 
 

@@ -57,3 +57,20 @@ def test_reference_arm_runs_on_rank_zero_only():
     assert len(lines) == 1, r.stdout
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["value"] > 0 and d["cpu_baseline"]["cores"] >= 1
+
+
+def test_reference_arm_maps_no_device_library():
+    """The CPU arm sets its cases up with the oracle's own code: a process that
+    builds a case and runs the oracle on it never loads liblfm_gpu.so."""
+    code = ("import sys; sys.path.insert(0, %r)\n"
+            "import bench\n"
+            "import oracle.port as P\n"
+            "c = bench.workload('vortex2d')\n"
+            "pc = P.PortCase.from_case(c)\n"
+            "P.run(pc, pc.q0(), 1, c.delta_t)\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "print('port' if 'liblfm_port.so' in maps else 'no-port', 'gpu' if 'liblfm_gpu.so' in maps else 'no-gpu')\n"
+            % ROOT)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-3000:]
+    assert r.stdout.split() == ["port", "no-gpu"]

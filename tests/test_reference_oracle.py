@@ -11,6 +11,7 @@ import tempfile
 import numpy as np
 import pytest
 
+import oracle.port as P
 from lfm_public_gb300 import _native as N, cases
 from tests.helpers import primitives
 
@@ -27,7 +28,7 @@ def _run_both(case, n):
         assert r.returncode == 0, r.stderr[-2000:]
         ref = cases.read_result_fields(tmp)
         ch = N.CaseHandle.open(tmp)   # the file route: plugins read the case directory
-        q, _ = N.port_run(ch, ch.q0(), n, ch.time()["delta_t"])
+        q, _ = P.run(ch, ch.q0(), n, ch.time()["delta_t"])
         return ch, q, ref
     finally:
         shutil.rmtree(tmp, ignore_errors=True)

@@ -7,6 +7,7 @@ the unrenumbered case)."""
 import numpy as np
 import pytest
 
+import oracle.port as P
 from lfm_public_gb300 import _native as N, cases
 
 
@@ -56,9 +57,9 @@ def test_renumbered_case_matches_oracle(shuffled, method):
     c, cs, _ = shuffled
     n = 10
     a = N.CaseHandle.from_case(cs)
-    qa, _ = N.port_run(a, a.q0(), n, c.delta_t)
+    qa, _ = P.run(a, a.q0(), n, c.delta_t)
     b = N.CaseHandle.from_case(cs, renumber=method)
-    qb, _ = N.port_run(b, b.q0(), n, c.delta_t)
+    qb, _ = P.run(b, b.q0(), n, c.delta_t)
     ga = np.empty_like(qa)
     ga[:, a.cell_ids()] = qa
     gb = np.empty_like(qb)
@@ -86,7 +87,7 @@ def test_renumbered_device_run_matches_oracle(shuffled, method):
     c, cs, _ = shuffled
     n = 10
     a = N.CaseHandle.from_case(cs)
-    qa, _ = N.port_run(a, a.q0(), n, c.delta_t)
+    qa, _ = P.run(a, a.q0(), n, c.delta_t)
     ga = np.empty_like(qa)
     ga[:, a.cell_ids()] = qa
     b = N.CaseHandle.from_case(cs, renumber=method)
@@ -115,8 +116,8 @@ def test_renumbered_3d_elements_match_oracle(make, method):
     a = N.CaseHandle.from_case(c)
     b = N.CaseHandle.from_case(c, renumber=method)
     assert sorted(b.cell_ids().tolist()) == list(range(c.n_cells))
-    qa, _ = N.port_run(a, a.q0(), n, c.delta_t)
-    qb, _ = N.port_run(b, b.q0(), n, c.delta_t)
+    qa, _ = P.run(a, a.q0(), n, c.delta_t)
+    qb, _ = P.run(b, b.q0(), n, c.delta_t)
     ga = np.empty_like(qa)
     ga[:, a.cell_ids()] = qa
     gb = np.empty_like(qb)

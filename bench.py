@@ -457,27 +457,44 @@ def _leg_record(N, ch, precision, dt, args, ws, local, pg, desc, workload, hbm, 
     return rec
 
 
-def _accuracy(N, acoustics, case, ch, dt, n_acc, local, ring_r):
+RING_RADII = (5.0, 10.0, 20.0, 50.0)
+
+
+def _accuracy(N, acoustics, case, ch, dt, checkpoints, local, rings):
     """Acoustic-pressure error of the FP32-bulk state against the FP64 state
-    after n_acc steps: all cells and the probe ring."""
+    at each checkpoint (time steps from the initial state): all cells and the
+    72-probe rings. A ring whose FP64 p' is exactly zero has not been reached
+    by any disturbance yet (rel_l2 null there)."""
     import numpy as np
-    qs = []
-    for p in (N.LFM_FP64, N.LFM_FP32_BULK):
-        sa = N.Solver(ch, precision=p, device=local)
-        sa.step(n_acc, dt)
-        sa.sync()
-        qs.append(sa.get_state())
-        sa.close()
+    sol = [N.Solver(ch, precision=p, device=local) for p in (N.LFM_FP64, N.LFM_FP32_BULK)]
     g, d = ch.desc.gamma, case.dim
-    acc = {"acoustic_p_rel_l2": acoustics.acoustic_rel_l2(qs[1], qs[0], g, d, case.p_inf), "steps": n_acc,
-           "against": "FP64 device path (itself within 1e-12 of the oracle), same case and steps"}
-    if ring_r is not None:
-        cells = acoustics.probe_ring(case.cell_centres, ch.cell_ids(), ring_r)
-        p64 = acoustics.pressure(qs[0], g, d)[cells] - case.p_inf
-        rms = float(np.sqrt(np.mean(p64 ** 2)))
-        acc["probe_ring"] = {
-            "radius": ring_r, "probes": len(cells), "p_rms_ref": rms,
-            "rel_l2": acoustics.acoustic_rel_l2(qs[1], qs[0], g, d, case.p_inf, cells) if rms > 0 else None}
+    ring_cells = {r: acoustics.probe_ring(case.cell_centres, ch.cell_ids(), r) for r in rings}
+    out, done = [], 0
+    for n in checkpoints:
+        for s in sol:
+            s.step(n - done, dt)
+        done = n
+        qs = []
+        for s in sol:
+            s.sync()
+            qs.append(s.get_state())
+        rec = {"steps": n, "acoustic_p_rel_l2": acoustics.acoustic_rel_l2(qs[1], qs[0], g, d, case.p_inf)}
+        ring_recs = []
+        for r, cells in ring_cells.items():
+            p64 = acoustics.pressure(qs[0], g, d)[cells] - case.p_inf
+            rms = float(np.sqrt(np.mean(p64 ** 2)))
+            ring_recs.append({"radius": r, "probes": len(cells), "p_rms_ref": rms,
+                              "rel_l2": acoustics.acoustic_rel_l2(qs[1], qs[0], g, d, case.p_inf, cells)
+                              if rms > 0 else None})
+        rec["probe_rings"] = ring_recs
+        out.append(rec)
+    for s in sol:
+        s.close()
+    acc = dict(out[0])
+    acc["against"] = "FP64 device path (itself within 1e-12 of the oracle), same case and steps"
+    acc["probe_ring"] = next((x for x in acc["probe_rings"] if x["radius"] == 50.0), None)
+    if len(out) > 1:
+        acc["longer"] = out[1:]
     return acc
 
 
@@ -546,9 +563,9 @@ def run_gpu(args):
         wake_thread = threading.Thread(target=build_wake, daemon=True)
         wake_thread.start()
     accuracy = None
-    if args.accuracy_steps > 0:
+    if args.accuracy_steps:
         accuracy = _accuracy(N, acoustics, case, ch, dt, args.accuracy_steps, local,
-                             50.0 if args.workload.startswith("cylinder") else None)
+                             RING_RADII if args.workload.startswith("cylinder") else ())
     wake = None
     if wake_thread is not None:
         wake_thread.join()
@@ -674,8 +691,8 @@ def run_batch(args):
 
     # each case against its own FP64 run
     accuracy = None
-    if args.accuracy_steps > 0:
-        n_acc = args.accuracy_steps
+    if args.accuracy_steps:
+        n_acc = args.accuracy_steps[-1]
         ba = N.Batch(device=local, arena_bytes=need + (64 << 20), max_cases=n_cases)
         sa = [ba.add(ch, c.delta_t) for c, ch in built]
         ba.step(n_acc)
@@ -877,9 +894,10 @@ def main():
     ap.add_argument("--workload", default="cylinder2d", choices=sorted(WORKLOAD_DESC) + ["batch64", "serve"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"],
                     help="precision of the headline value (the other is reported beside it)")
-    ap.add_argument("--accuracy-steps", type=int, default=None,
-                    help="steps of the FP32-bulk vs FP64 comparison (default: 20000 for the 2D cylinder, the "
-                         "configured run length; 1000 otherwise; 2000 for batch64)")
+    ap.add_argument("--accuracy-steps", default=None,
+                    help="steps of the FP32-bulk vs FP64 comparison, comma-separated checkpoints (default: "
+                         "20000,80000 for the 2D cylinder -- the configured run length, then long enough for the "
+                         "start-up pulse to reach the r = 50 D ring; 1000 otherwise; 2000 for batch64; 0: none)")
     ap.add_argument("--no-wake", dest="wake", action="store_false",
                     help="skip the 3D wake sub-record of the 2D cylinder workloads")
     ap.add_argument("--wake-steps", type=int, default=10)
@@ -896,7 +914,9 @@ def main():
                     help="solver order of the cells (single-case workloads)")
     args = ap.parse_args()
     if args.accuracy_steps is None:
-        args.accuracy_steps = {"batch64": 2000, "cylinder2d": 20000, "cylinder2d_m2": 20000}.get(args.workload, 1000)
+        args.accuracy_steps = {"batch64": "2000", "cylinder2d": "20000,80000",
+                               "cylinder2d_m2": "20000,80000"}.get(args.workload, "1000")
+    args.accuracy_steps = [int(x) for x in str(args.accuracy_steps).split(",") if int(x) > 0]
     if args.impl == "reference":
         if args.workload in ("batch64", "serve"):
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched form; its CPU path is "

@@ -859,10 +859,11 @@ def write_field(case: Case, d: str, name: str, values: np.ndarray, dims: str) ->
 
 
 def write_case(case: Case, root: str, n_steps: Optional[int] = None, write_interval: Optional[int] = None,
-               post: Optional[dict] = None) -> str:
+               post: Optional[dict] = None, adjust_time_step: bool = False, max_co: float = 0.5) -> str:
     """Writes ``case`` as an OpenFOAM case directory under ``root``. ``post``
     sets lfm/post entries of controlDict (haveAverage, tStartAverage,
-    haveForces, saveForcesStep, printInfoFreq, ...)."""
+    haveForces, saveForcesStep, printInfoFreq, ...); ``adjust_time_step`` and
+    ``max_co`` its adjustTimeStep and maxCo (endTime stays n_steps x deltaT)."""
     pe = {"haveProbes": "false", "haveSampling": "false", "haveAverage": "false", "haveForces": "false",
           "haveResiduals": "true" if case.residuals else "false", "printInfoFreq": str(case.print_freq),
           "saveResiduals": "false", "saveBlendFactor": "false"}
@@ -889,7 +890,7 @@ def write_case(case: Case, root: str, n_steps: Optional[int] = None, write_inter
                 f"endTime         {_fmt(end)};\ndeltaT          {_fmt(case.delta_t)};\n"
                 f"writeControl    timeStep;\nwriteInterval   {wi};\nwriteFormat     ascii;\n"
                 f"writePrecision  {case.write_precision};\ntimeFormat      general;\ntimePrecision   12;\n"
-                "adjustTimeStep  no;\nmaxCo           0.5;\n")
+                f"adjustTimeStep  {'yes' if adjust_time_step else 'no'};\nmaxCo           {_fmt(max_co)};\n")
     with open(os.path.join(root, "system", "fvSchemes"), "w") as f:
         f.write(_header("dictionary", "fvSchemes", "system"))
         f.write(f"lfm\n{{\n    solver          {case.solver};\n    dimension       {case.dim};\n"

@@ -338,9 +338,9 @@ void GpuMesh::solve() {
             check(lfm_solver_sync(m_parts[0].solver), "time step");
         }
         rkLoop += std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
-        const bool print = ((timeStep + 1) % std::max(1, m_pInput->m_nPrintInfoFrequency) == 0) ||
-                           (time + dt >= tEnd);
         if (m_pRunTime->isAdjustDeltaTime()) {   // compute_dt + MPI_Allreduce(MIN)
+            // the reduction writes the new dt into the variable the step's
+            // time is then advanced by (src/mesh_solver.cpp:705-716, 733)
             double ndt = 0.0;
             for (size_t k = 0; k < m_parts.size(); ++k) {
                 double d = dt;
@@ -348,7 +348,11 @@ void GpuMesh::solve() {
                 ndt = k == 0 ? d : std::min(ndt, d);
             }
             for (Part& p : m_parts) p.runTime->setDeltaTime(ndt);
-        } else if (print) {   // compute_cfl + MPI_Allreduce(MAX)
+            dt = ndt;
+        }
+        const bool print = ((timeStep + 1) % std::max(1, m_pInput->m_nPrintInfoFrequency) == 0) ||
+                           (time + dt >= tEnd);
+        if (!m_pRunTime->isAdjustDeltaTime() && print) {   // compute_cfl + MPI_Allreduce(MAX)
             for (size_t k = 0; k < m_parts.size(); ++k) {
                 double cfl = 0.0;
                 check(lfm_solver_cfl(m_parts[k].solver, dt, &cfl), "compute_cfl");

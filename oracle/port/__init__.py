@@ -45,6 +45,7 @@ def load(path: str = PORT_PATH) -> C.CDLL:
                                 C.c_int),
         "lfm_port_case_describe": ([vp, C.POINTER(SolverDesc)], C.c_int),
         "lfm_port_case_free": ([vp], None),
+        "lfm_port_case_cell_ids": ([vp, C.POINTER(C.c_int64)], C.c_int),
         "lfm_port_last_error": ([], C.c_char_p),
     }
     for name, (args, res) in sig.items():
@@ -116,6 +117,12 @@ class PortCase:
         if rc != 0:
             raise RuntimeError("oracle case set-up failed: " + lib.lfm_port_last_error().decode(errors="replace"))
         return cls(h)
+
+    def cell_ids(self) -> np.ndarray:
+        """polyMesh cell label of each solver-order cell."""
+        out = np.empty(self.desc.n_cells, dtype=np.int64)
+        load().lfm_port_case_cell_ids(self._h, _ptr(out, C.c_int64))
+        return out
 
     def q0(self) -> np.ndarray:
         d = self.desc

@@ -31,6 +31,8 @@ int lfm_port_case_build(const lfm_polymesh* mesh, const lfm_params* params, cons
                         lfm_port_case** out);
 /* Pointers into the case's arrays, valid until lfm_port_case_free. */
 int lfm_port_case_describe(const lfm_port_case* c, lfm_solver_desc* out);
+/* polyMesh cell label of each solver-order cell ([n_cells]). */
+int lfm_port_case_cell_ids(const lfm_port_case* c, int64_t* out);
 void lfm_port_case_free(lfm_port_case* c);
 const char* lfm_port_last_error(void);
 

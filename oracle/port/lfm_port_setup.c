@@ -59,6 +59,7 @@ struct lfm_port_case {
     int8_t* cf_sign;
     int64_t* cs_off;
     double* cs;
+    int64_t* cell_id;   /* polyMesh cell of each solver-order cell */
     double gamma, Rgas, rhoInf, EInf, pInf, TInf, UInf[3], mu, Cp, PrInv;
     double rkA[8], rkB[8];
 };
@@ -266,7 +267,7 @@ void lfm_port_case_free(lfm_port_case* c) {
     if (!c) return;
     void* arrays[] = {c->face_p, c->face_n, c->face_ghost, c->S, c->d, c->w, c->smag, c->dmag_inv, c->dnorm,
                       c->delta_mag, c->K, c->vol_inv, c->sponge, c->smag_c, c->q0, c->ghost_cell, c->ghost_kind,
-                      c->ghost_patch, c->cf_off, c->cf_list, c->cf_sign, c->cs_off, c->cs};
+                      c->ghost_patch, c->cf_off, c->cf_list, c->cf_sign, c->cs_off, c->cs, c->cell_id};
     for (size_t i = 0; i < sizeof arrays / sizeof arrays[0]; ++i) free(arrays[i]);
     free(c);
 }
@@ -619,10 +620,17 @@ int lfm_port_case_build(const lfm_polymesh* m, const lfm_params* prm, const lfm_
         pc->q0[(D + 1) * g.nc + c] = rho * E;
     }
 
-    free(slots), free(slot_off), free(cell_of), free(solver_of), free(local_of), free(sm);
+    pc->cell_id = cell_of;
+    free(slots), free(slot_off), free(solver_of), free(local_of), free(sm);
     free(r.patch_of), free(r.valid), free(r.cyclic), free(r.cyc_shift);
     free_geom(&g);
     *out = pc;
+    return 0;
+}
+
+int lfm_port_case_cell_ids(const lfm_port_case* c, int64_t* out) {
+    if (!c || !out) return fail("null argument");
+    memcpy(out, c->cell_id, (size_t)c->nc * sizeof(int64_t));
     return 0;
 }
 

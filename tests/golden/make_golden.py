@@ -122,6 +122,106 @@ def run_reference(case: cases.Case, n_steps: int, workdir: str):
     return fields, cfl, r.stdout
 
 
+# Adaptive time step (adjustTimeStep yes): the reference's compute_dt and its
+# MPI_Allreduce(MIN) (src/cfd_v0.cpp:2912-2942, src/mesh_solver.cpp:705-716)
+# set each next dt; printInfoFreq 1 prints every step's time and new dt, and
+# every step is written (the run ends at endTime, before step n_steps).
+# name -> (generator, kwargs, nominal n_steps, maxCo)
+ADJUST_FIXTURES = {
+    "vortex16_m2_adjustdt": (cases.vortex_case, dict(n=16, solver=1, mu=1e-3), 20, 0.2),
+    "cyl24x12_m1_adjustdt": (cases.cylinder_case, dict(n_theta=24, n_r=12, r1=10, first=0.05, Ls=3, solver=0,
+                                                       minmod=True, noise=0.02), 20, 0.25),
+}
+
+_STEP_LINE = re.compile(r"Time step:\s*(\d+)\s+Time:\s*([0-9eE+\-.]+)\s+dt:\s*([0-9eE+\-.]+)")
+
+
+def run_reference_adjust(case: cases.Case, n_steps: int, max_co: float, workdir: str):
+    cases.write_case(case, workdir, n_steps=n_steps, write_interval=1, post=dict(printInfoFreq=1),
+                     adjust_time_step=True, max_co=max_co)
+    r = subprocess.run([ORACLE], cwd=workdir, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference run failed:\n" + r.stdout[-3000:] + r.stderr[-3000:])
+    rows = np.array([(int(a), float(b), float(c)) for a, b, c in _STEP_LINE.findall(r.stdout)])
+    return cases.read_result_fields(workdir), rows
+
+
+def main_adjust():
+    for name, (gen, kw, n, max_co) in ADJUST_FIXTURES.items():
+        case = gen(n_steps=n, **kw)
+        tmp = tempfile.mkdtemp(prefix="lfm_golden_")
+        try:
+            res, rows = run_reference_adjust(case, n, max_co, tmp)
+        finally:
+            shutil.rmtree(tmp, ignore_errors=True)
+        arrs = case_to_arrays(case)
+        arrs.update({f"ref_{k}": v for k, v in res.items()})
+        arrs["n_steps"] = np.int64(n)
+        arrs["max_co"] = np.float64(max_co)
+        arrs["ref_step"] = rows[:, 0].astype(np.int64)
+        arrs["ref_time"] = rows[:, 1]
+        arrs["ref_dt"] = rows[:, 2]
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrs)
+        print(f"{name}: {case.n_cells} cells, {len(rows)} steps to endTime {case.delta_t * n:.6g}, "
+              f"dt {rows[0, 2]:.6g} .. {rows[-1, 2]:.6g}")
+
+
+# The configured workloads at full size and length, checked against the
+# reference: the mesh is regenerated from its generator (the fixture holds a
+# digest of the generated mesh and initial fields, which the test checks),
+# and the fixture keeps the reference's fields on a seeded sample of cells.
+# name -> (generator, kwargs, n_steps)
+CONFIG_FIXTURES = {
+    # 2D isentropic vortex, 256 x 256, M1, rkOrder 5, CFL 0.5, 1000 steps
+    "cfg_vortex256_m1_1000": (cases.vortex_case, dict(n=256, solver=0), 1000),
+    # 2D cylinder O-grid 768 x 512, M1, minmod on, 20 steps (100 RK stages)
+    "cfg_cyl768x512_m1_20": (cases.cylinder_case, dict(n_theta=768, n_r=512, solver=0, minmod=True), 20),
+}
+SAMPLE_CELLS = 4096
+
+
+def case_fingerprint(case: cases.Case) -> dict:
+    """Values that pin a regenerated case to the one the reference ran: the
+    norms of the points and of every initial field, dt, and the initial
+    fields on the sampled cells. They are compared with a relative tolerance:
+    numpy's transcendental functions may differ in the last bit between
+    hosts, which moves a 1000-step FP64 result by far less than 1e-12."""
+    cells = sample_cells(case.n_cells)
+    out = {"fp_points_norm": np.float64(np.linalg.norm(case.points)), "fp_delta_t": np.float64(case.delta_t),
+           "fp_n_faces": np.int64(len(case.owner)), "fp_n_internal": np.int64(len(case.neighbour))}
+    for k in sorted(case.fields):
+        v = np.asarray(case.fields[k], dtype=np.float64)
+        out["fp_norm_" + k] = np.float64(np.linalg.norm(v))
+        out["fp_sample_" + k] = v[cells]
+    return out
+
+
+def sample_cells(n_cells: int) -> np.ndarray:
+    return np.sort(np.random.default_rng(20261204).choice(n_cells, size=min(SAMPLE_CELLS, n_cells), replace=False))
+
+
+def main_config():
+    import json
+    for name, (gen, kw, n) in CONFIG_FIXTURES.items():
+        case = gen(**kw)
+        tmp = tempfile.mkdtemp(prefix="lfm_golden_")
+        try:
+            res, cfl, _ = run_reference(case, n, tmp)
+        finally:
+            shutil.rmtree(tmp, ignore_errors=True)
+        cells = sample_cells(case.n_cells)
+        arrs = {"generator": np.array(gen.__name__), "kwargs": np.array(json.dumps(kw)),
+                "n_steps": np.int64(n), "n_cells": np.int64(case.n_cells), "sample": cells,
+                "ref_cfl": np.float64(cfl)}
+        arrs.update(case_fingerprint(case))
+        for k in ("rho", "E", "p"):
+            arrs["ref_" + k] = res[k][cells]
+            arrs["ref_norm_" + k] = np.float64(np.linalg.norm(res[k]))
+        arrs["ref_U"] = res["U"][cells]
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrs)
+        print(f"{name}: {case.n_cells} cells, {n} steps, {len(cells)} sampled cells, CFL {cfl}")
+
+
 # Post-processing fixtures: the same runs with haveAverage (pAvg, pRMS fields)
 # and haveForces (output/postProcess_Forces_1) switched on.
 # name -> (generator, kwargs, n_steps, averaging start step, saveForcesStep)
@@ -178,6 +278,12 @@ def main(only=()):
         raise SystemExit(f"{ORACLE} is missing: run `make -C oracle` where the reference sources exist")
     if not only:
         main_post()
+        main_adjust()
+        main_config()
+    if any(n in ADJUST_FIXTURES for n in only):
+        main_adjust()
+    if any(n in CONFIG_FIXTURES for n in only):
+        main_config()
     for name, (gen, kw, n) in FIXTURES.items():
         if only and name not in only:
             continue

@@ -11,7 +11,30 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def golden_names():
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    """Fixtures of runs at constant dt (every fixture but the adaptive-dt ones)."""
+    return sorted(n for n in (os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+                  if not n.endswith("_adjustdt") and not n.startswith("cfg_"))
+
+
+def adjust_names():
+    """Fixtures of runs with adjustTimeStep yes (the reference's dt sequence)."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*_adjustdt.npz")))
+
+
+def adaptive_run(step, min_dt, case, z):
+    """The reference's adaptive time loop (src/mesh_solver.cpp:474-740 with the
+    run-time manager's running(): time < endTime - deltaT/2): step(dt) runs
+    one time step, min_dt() is compute_dt's minimum on the new state, and
+    the time advances by that new dt. Returns the new dts and times."""
+    end = case.delta_t * int(z["n_steps"])
+    dt, t, dts, times = case.delta_t, 0.0, [], []
+    while t < end - 0.5 * dt:
+        step(dt)
+        dt = min_dt()
+        t += dt
+        dts.append(dt)
+        times.append(t)
+    return np.array(dts), np.array(times)
 
 
 def load_golden(name):
@@ -59,3 +82,24 @@ def rel_l2(a, b):
     den = np.linalg.norm(b, axis=1)
     with np.errstate(divide="ignore", invalid="ignore"):
         return np.where(den > 0, num / np.where(den > 0, den, 1.0), np.where(num > 0, np.inf, 0.0))
+
+
+def config_case(name):
+    """A configured workload (cfg_* fixture) regenerated from its generator,
+    checked against the fingerprint the fixture recorded when the reference
+    ran it (relative 1e-13: the inputs may differ in the last bit between
+    hosts, which no 1e-12 parity check can see)."""
+    import json
+
+    from lfm_public_gb300 import cases
+    from tests.golden.make_golden import case_fingerprint
+    z = np.load(os.path.join(GOLDEN, name + ".npz"), allow_pickle=False)
+    case = getattr(cases, str(z["generator"]))(**json.loads(str(z["kwargs"])))
+    fp = case_fingerprint(case)
+    for k, v in fp.items():
+        ref = z[k]
+        if np.issubdtype(np.asarray(v).dtype, np.integer):
+            assert int(v) == int(ref), k
+        else:
+            assert np.allclose(v, ref, rtol=1e-13, atol=0), k
+    return case, z

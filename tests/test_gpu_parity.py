@@ -8,7 +8,8 @@ import pytest
 
 import oracle.port as P
 from lfm_public_gb300 import _native as N, acoustics, cases
-from tests.helpers import golden_names, load_golden, reference_conserved, rel_l2, rel_l2_vec
+from tests.helpers import (adaptive_run, adjust_names, config_case, golden_names, load_golden, primitives,
+                           reference_conserved, rel_l2, rel_l2_vec)
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-12
@@ -30,6 +31,28 @@ def test_fp64_matches_reference_fixture(name):
     q = _gpu_run(ch, int(z["n_steps"]), case.delta_t)
     ref = reference_conserved(z, ch.cell_ids(), case.dim)
     err = rel_l2_vec(q, ref, case.dim)   # the prisms' w is rounding noise
+    assert np.all(err <= TOL), err
+
+
+@pytest.mark.parametrize("name", adjust_names())
+def test_fp64_adaptive_dt_matches_reference(name):
+    """adjustTimeStep yes through the C ABI: one step at a time, the next dt
+    from lfm_solver_min_dt (compute_dt's deterministic minimum on the
+    device). Same step count as the reference, every dt and time within
+    1e-9 (the reference prints 10 significant digits), final fields within
+    1e-12."""
+    case, z = load_golden(name)
+    ch = N.CaseHandle.from_case(case)
+    s = N.Solver(ch, precision=N.LFM_FP64)
+    max_co = float(z["max_co"])
+    dts, times = adaptive_run(lambda dt: s.step(1, dt), lambda: s.min_dt(max_co), case, z)
+    s.sync()
+    q = s.get_state()
+    s.close()
+    assert len(dts) == len(z["ref_dt"])
+    np.testing.assert_allclose(dts, z["ref_dt"], rtol=1e-9, atol=0)
+    np.testing.assert_allclose(times, z["ref_time"], rtol=1e-9, atol=0)
+    err = rel_l2_vec(q, reference_conserved(z, ch.cell_ids(), case.dim), case.dim)
     assert np.all(err <= TOL), err
 
 
@@ -226,11 +249,13 @@ def test_non_finite_state_is_reported():
 
 
 def test_full_size_cylinder_matches_oracle():
-    """The 768 x 512 cylinder workload, two time steps (10 RK stages)."""
+    """The 768 x 512 cylinder workload, 20 time steps (100 RK stages), every
+    cell against the oracle set up by its own code."""
     case = cases.cylinder_case(solver=0, minmod=True)
     ch = N.CaseHandle.from_case(case)
-    q_gpu = _gpu_run(ch, 2, case.delta_t)
-    q_ref, _ = P.run(ch, ch.q0(), 2, case.delta_t)
+    q_gpu = _gpu_run(ch, 20, case.delta_t)
+    pc = P.PortCase.from_case(case)
+    q_ref, _ = P.run(pc, pc.q0(), 20, case.delta_t)
     assert np.all(rel_l2(q_gpu, q_ref) <= TOL), rel_l2(q_gpu, q_ref)
 
 
@@ -243,3 +268,40 @@ def test_cell_residual_matches_reference_fixture():
     ids = ch.cell_ids()
     ref = np.vstack([z["ref_" + n][ids] for n in ("rhoRES", "uRES", "vRES", "eRES")])
     assert np.all(rel_l2(res, ref) <= 1e-10), rel_l2(res, ref)
+
+
+def _sample_conserved(z, q, ids, dim, gamma):
+    """The device state at the fixture's sampled polyMesh cells, as the
+    reference's written rho, E, p; and the reference's."""
+    inv = np.empty_like(ids)
+    inv[ids] = np.arange(len(ids))
+    cells = inv[z["sample"]]
+    r, U, E, p = primitives(q[:, cells], gamma, dim)
+    return {"rho": r, "E": E, "p": p}, {k: z["ref_" + k] for k in ("rho", "E", "p")}
+
+
+@pytest.mark.parametrize("name", ["cfg_vortex256_m1_1000", "cfg_cyl768x512_m1_20"])
+def test_configured_workload_matches_reference(name):
+    """The configured workloads at full size and length against the reference
+    solver run with the same settings: the 256 x 256 isentropic vortex for
+    1000 steps (5000 RK stages) and the 768 x 512 cylinder for 20 steps
+    (100 RK stages). FP64: rho, E and p within 1e-12 relative L2 on 4096
+    seeded cells, and the whole-field norms within 1e-12; FP32-bulk: acoustic
+    pressure within 1e-3 there."""
+    case, z = config_case(name)
+    ch = N.CaseHandle.from_case(case)
+    n = int(z["n_steps"])
+    ids = ch.cell_ids()
+    for prec in (N.LFM_FP64, N.LFM_FP32_BULK):
+        q = _gpu_run(ch, n, case.delta_t, precision=prec)
+        got, ref = _sample_conserved(z, q, ids, case.dim, ch.desc.gamma)
+        if prec == N.LFM_FP64:
+            for k in got:
+                assert rel_l2(got[k][None], ref[k][None])[0] <= TOL, k
+            r, U, E, p = primitives(q, ch.desc.gamma, case.dim)
+            for k, v in (("rho", r), ("E", E), ("p", p)):
+                assert abs(np.linalg.norm(v) - float(z["ref_norm_" + k])) <= TOL * float(z["ref_norm_" + k]), k
+        else:
+            pp = got["p"] - case.p_inf
+            pr = ref["p"] - case.p_inf
+            assert np.linalg.norm(pp - pr) <= 1e-3 * np.linalg.norm(pr)

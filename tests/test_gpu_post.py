@@ -19,7 +19,9 @@ import pytest
 
 from lfm_public_gb300 import _native as N, cases
 from tests.golden.make_golden import read_forces
-from tests.helpers import load_golden, rel_l2
+import re
+
+from tests.helpers import adjust_names, load_golden, rel_l2
 
 pytestmark = pytest.mark.gpu
 POST = ["post_cyl24x12_m2", "post_cyl16x8x4_ausm_3d"]
@@ -170,3 +172,28 @@ def test_driver_runs_decomposed_case(tmp_path, name, nparts, method):
         assert rel_l2(glob[k][None], z["ref_" + k][None])[0] <= tol, k
     rows = read_forces(os.path.join(root, "output", "postProcess_Forces_1"))
     _check_forces(rows, z["ref_forces"], case.dim)
+
+
+@pytest.mark.parametrize("name", adjust_names())
+def test_driver_adaptive_dt_matches_reference(tmp_path, name):
+    """lfm_solve_gpu with adjustTimeStep yes: every step's printed time and
+    dt (printInfoFreq 1) are the reference's to its printed precision, the
+    run ends after the same step, and the final fields match within 1e-12."""
+    if not os.path.exists(CLI):
+        pytest.fail(f"{CLI} is missing: build() makes it")
+    case, z = load_golden(name)
+    root = str(tmp_path / "case")
+    cases.write_case(case, root, n_steps=int(z["n_steps"]), write_interval=1, post=dict(printInfoFreq=1),
+                     adjust_time_step=True, max_co=float(z["max_co"]))
+    r = subprocess.run([CLI], cwd=root, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    rows = np.array([(int(a), float(b), float(c)) for a, b, c in
+                     re.findall(r"Time step:\s*(\d+)\s+Time:\s*([0-9eE+\-.]+)\s+dt:\s*([0-9eE+\-.]+)", r.stdout)])
+    assert rows.shape[0] == len(z["ref_dt"]), r.stdout[-1500:]
+    np.testing.assert_array_equal(rows[:, 0], z["ref_step"])
+    np.testing.assert_allclose(rows[:, 1], z["ref_time"], rtol=1e-9, atol=0)
+    np.testing.assert_allclose(rows[:, 2], z["ref_dt"], rtol=1e-9, atol=0)
+    f = cases.read_result_fields(root, names=("rho", "E", "p"))
+    for k in ("rho", "E", "p"):
+        assert rel_l2(f[k][None], z["ref_" + k][None])[0] <= 1e-12, k
+    shutil.rmtree(root, ignore_errors=True)

@@ -10,7 +10,7 @@ import pytest
 
 import oracle.port as P
 from lfm_public_gb300 import _native as N
-from tests.helpers import golden_names, load_golden, primitives
+from tests.helpers import adaptive_run, adjust_names, config_case, golden_names, load_golden, primitives
 
 
 @pytest.mark.parametrize("name", golden_names())
@@ -52,3 +52,42 @@ def test_port_cell_residual_matches_reference_bitwise():
     ids = ch.cell_ids()
     for v, name in enumerate(["rhoRES", "uRES", "vRES", "eRES"]):
         assert np.array_equal(res[v], z["ref_" + name][ids]), name
+
+
+@pytest.mark.parametrize("name", adjust_names())
+def test_port_adaptive_dt_matches_reference(name):
+    """adjustTimeStep yes: the reference's compute_dt minimum sets every next
+    dt (src/cfd_v0.cpp:2912-2942, src/mesh_solver.cpp:705-716). The oracle,
+    set up by its own code and run through the same time loop, takes the same
+    number of steps, prints the same dt and time at every step (10 significant
+    digits, the reference's output precision) and ends on the reference's
+    fields bit for bit."""
+    case, z = load_golden(name)
+    pc = P.PortCase.from_case(case)
+    state = {"q": pc.q0()}
+    max_co = float(z["max_co"])
+
+    def step(dt):
+        state["q"], _ = P.run(pc, state["q"], 1, dt)
+
+    dts, times = adaptive_run(step, lambda: P.min_dt(pc, state["q"], max_co), case, z)
+    assert len(dts) == len(z["ref_dt"])
+    np.testing.assert_allclose(dts, z["ref_dt"], rtol=1e-9, atol=0)
+    np.testing.assert_allclose(times, z["ref_time"], rtol=1e-9, atol=0)
+    ids = pc.cell_ids()
+    r, U, E, p = primitives(state["q"], pc.desc.gamma, case.dim)
+    assert np.array_equal(r, z["ref_rho"][ids]) and np.array_equal(E, z["ref_E"][ids])
+    assert np.array_equal(p, z["ref_p"][ids])
+
+
+def test_port_matches_reference_at_configured_cylinder_size():
+    """The 768 x 512 cylinder for 20 steps (100 RK stages): the oracle, set up
+    by its own code, gives the reference's written fields bit for bit on the
+    fixture's 4096 sampled cells."""
+    case, z = config_case("cfg_cyl768x512_m1_20")
+    pc = P.PortCase.from_case(case)
+    q, _ = P.run(pc, pc.q0(), int(z["n_steps"]), case.delta_t)
+    inv = np.empty(pc.desc.n_cells, dtype=np.int64)
+    inv[pc.cell_ids()] = np.arange(pc.desc.n_cells)
+    r, U, E, p = primitives(q[:, inv[z["sample"]]], pc.desc.gamma, case.dim)
+    assert np.array_equal(r, z["ref_rho"]) and np.array_equal(E, z["ref_E"]) and np.array_equal(p, z["ref_p"])

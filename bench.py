@@ -177,6 +177,9 @@ def kernel_bytes(dim: int, faces_per_cell: int, fp32: bool, scheme: str, viscous
         # update kernels: the same algorithmic bytes (its intermediate arrays
         # stay in shared memory, so its traffic is below them)
         b["k_tile_stage"] = b["k_grad"] + b["k_vis"] + b["k_flux"] + b["k_update"]
+        # the fused flux + update: both kernels' bytes without the face rhs,
+        # which it never writes or reads back
+        b["k_flux_update"] = b["k_flux"] + b["k_update"] - 2 * fpc * nq * w
     return b
 
 
@@ -424,7 +427,7 @@ def _hbm_roofline(desc, fp32, prof, nc, stages, workload, precision, hbm, peak_s
     dominant = max(prof, key=prof.get)
     per_launch_ms = prof[dominant] / stages
     achieved = kb[dominant] * nc / (per_launch_ms * 1e-3) / 1e9
-    step_bytes = sum(v for k, v in kb.items() if k != "k_tile_stage")
+    step_bytes = sum(v for k, v in kb.items() if k in prof)
     r = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm, "unit": "GB/s",
          "frac": achieved / hbm, "peak_source": peak_src, "traffic": DRAM_TRAFFIC.get((workload, precision, dominant)),
          "algorithmic_bytes_per_cell": kb[dominant], "cells_per_launch": nc,
@@ -724,7 +727,7 @@ def run_batch(args):
     step_bytes = 0.0
     for sp, (c, ch) in zip(spec, built):
         kb = kernel_bytes(2, 4 if sp["kind"] == "quad" else 3, True, "M1" if sp["solver"] == 0 else "M2", False)
-        step_bytes += sum(v for k, v in kb.items() if k != "k_tile_stage") * ch.desc.n_cells
+        step_bytes += sum(v for k, v in kb.items() if k not in ("k_tile_stage", "k_flux_update")) * ch.desc.n_cells
     stage_ms = total_ms / ws / args.steps / stages
     achieved = step_bytes / (stage_ms * 1e-3) / 1e9
     line = {

@@ -438,12 +438,14 @@ class Solver:
     def profile_step(self, dt: float) -> dict:
         """ms per time step of each kernel; kernels that did not run are left out."""
         lib = load_library()
-        n = 6
+        n = 7
         ms = (C.c_float * n)()
         check(lib.lfm_solver_profile_step(self._h, dt, n, ms))
         names = [lib.lfm_solver_kernel_name(i).decode() for i in range(n)]
         if ms[5] > 0:   # fused tile stages
             return {names[5]: ms[5]}
+        if ms[6] != 0:  # fused flux + update stages
+            return {names[i]: ms[i] for i in (0, 1, 2, 6)}
         return {names[i]: ms[i] for i in range(5)}
 
     def close(self):

@@ -383,6 +383,7 @@ int commitCase(lfm_batch* b, const PreparedCase& pc, int* slot) {
     a.dq = reinterpret_cast<float*>(P(L.dq));
     a.res = reinterpret_cast<double*>(P(L.res));
     a.prim = reinterpret_cast<float*>(P(L.prim));
+    a.primW = a.prim;
     a.V = reinterpret_cast<float*>(P(L.V));
     a.grad = reinterpret_cast<float*>(P(L.grad));
     a.flux = reinterpret_cast<float*>(P(L.flux));

@@ -83,6 +83,9 @@ struct lfm_solver {
     lfm::dev::TileArgs tile{};
     float* prim1 = nullptr;
     int primParity = 0;
+    // fused flux + update stages (FP32-bulk single case): two primitive
+    // buffers alternate like the tile stages'
+    bool fluxUpdate = false;
     cudaGraphExec_t graphOdd = nullptr;   // the step graph starting from prim1
     // the non-finite flag's host copy (page-locked: read after one stream sync)
     int* flagHost = nullptr;
@@ -173,6 +176,7 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
     int rc;
     if ((rc = devAlloc(s, &a.dq, (size_t)s->nq * s->nc))) return rc;
     if ((rc = devAlloc(s, &a.prim, (size_t)lfm::dev::primRows<T>(s->D) * nt))) return rc;
+    a.primW = a.prim;
     if ((rc = devAlloc(s, &a.V, (D * D + 2 * D + (d->smag_c ? D * D : 0)) * nt))) return rc;
     // M2AUSM always reads the gradients (all zero when minmod is off, as in the
     // reference, whose prepare_for_RKstep zeroes them every stage).
@@ -253,16 +257,36 @@ void tileStage(lfm_solver* s, int k, double dt, int parity) {
     const int in = (parity + k) & 1;
     Args<float> g = s->a32;
     g.prim = buf[in ^ 1];
+    g.primW = g.prim;
     lfm::dev::TileArgs t = s->tile;
     t.primIn = buf[in];
     lfm::dev::launch_tile_stage(g, t, stageConfig(s, k, dt), s->stream);
 }
 
-// The tile stages keep the current primitives in either buffer; the other
-// kernels read a32.prim. Before those run, the primitives are rebuilt there
-// from the state when they sit in the other buffer.
+// Stage kernels that alternate two primitive buffers (tile stages, fused
+// flux + update stages).
+bool alternating(const lfm_solver* s) { return s->tiled || s->fluxUpdate; }
+
+// Fused flux + update stage k of a step that starts from primitive buffer
+// `parity`: the preparation (halos and ghosts it still has), gradient and
+// viscous kernels read buffer (parity + k) % 2, the fused kernel writes the
+// other.
+void fluxUpdateStage(lfm_solver* s, int k, double dt, int parity) {
+    float* buf[2] = {s->a32.prim, s->prim1};
+    const int in = (parity + k) & 1;
+    Args<float> g = s->a32;
+    g.prim = buf[in];
+    g.primW = buf[in ^ 1];
+    const StageConfig c = stageConfig(s, k, dt);
+    for (int w = 0; w < 3; ++w) lfm::dev::launch_kernel<float>(g, c, w, s->stream);   // prep, grad, vis
+    lfm::dev::launch_fluxupdate32(g, c, s->stream);
+}
+
+// The alternating stages keep the current primitives in either buffer; the
+// other kernels read a32.prim. Before those run, the primitives are rebuilt
+// there from the state when they sit in the other buffer.
 void untile(lfm_solver* s) {
-    if (s->tiled && s->primParity != 0) {
+    if (alternating(s) && s->primParity != 0) {
         s->primsValid = false;
         s->primParity = 0;
     }
@@ -290,6 +314,8 @@ int ensurePrims(lfm_solver* s) {
 void launchStep(lfm_solver* s, double dt, int parity) {
     if (s->tiled)
         for (int k = 0; k < s->rkOrder; ++k) tileStage(s, k, dt, parity);
+    else if (s->fluxUpdate)
+        for (int k = 0; k < s->rkOrder; ++k) fluxUpdateStage(s, k, dt, parity);
     else if (s->precision == LFM_FP32_BULK)
         stageAll<float>(s, s->a32, dt);
     else
@@ -316,7 +342,7 @@ int ensureGraph(lfm_solver* s, double dt) {
     if (s->graphOdd) cudaGraphExecDestroy(s->graphOdd);
     s->graph = s->graphOdd = nullptr;
     int rc = captureStep(s, dt, 0, &s->graph);
-    if (!rc && s->tiled) rc = captureStep(s, dt, 1, &s->graphOdd);
+    if (!rc && alternating(s)) rc = captureStep(s, dt, 1, &s->graphOdd);
     if (rc) return rc;
     s->graphDt = dt;
     return LFM_OK;
@@ -324,8 +350,8 @@ int ensureGraph(lfm_solver* s, double dt) {
 
 // Launches the step graph matching the current primitive buffer.
 cudaError_t launchStepGraph(lfm_solver* s) {
-    const cudaError_t e = cudaGraphLaunch(s->tiled && s->primParity ? s->graphOdd : s->graph, s->stream);
-    if (s->tiled) s->primParity ^= (s->rkOrder & 1);
+    const cudaError_t e = cudaGraphLaunch(alternating(s) && s->primParity ? s->graphOdd : s->graph, s->stream);
+    if (alternating(s)) s->primParity ^= (s->rkOrder & 1);
     return e;
 }
 
@@ -366,6 +392,17 @@ bool tileHaveGrad(const lfm_solver* s) { return s->scheme == LFM_SOLVER_M2AUSM; 
 int tileCellsOption() {
     const char* e = getenv("LFM_TILE_CELLS");
     return e ? atoi(e) : kTileCells;
+}
+
+// Fused flux + update stages, by dimension (LFM_FLUX_UPDATE=0/1 in the
+// environment overrides for a solver created afterwards).
+constexpr bool kFluxUpdate2D = false;
+constexpr bool kFluxUpdate3D = false;
+
+bool fluxUpdateOption(int D) {
+    const char* e = getenv("LFM_FLUX_UPDATE");
+    if (e) return atoi(e) != 0;
+    return D == 2 ? kFluxUpdate2D : kFluxUpdate3D;
 }
 
 // Creates a solver; `stream` (not owned) is shared by the partitions of a
@@ -545,6 +582,13 @@ int createSolver(const lfm_solver_desc* d, const lfm_solver_opts* opts, cudaStre
         s->tile.block = tiles.tileCells <= 128 ? 128 : 256;
         s->tiled = true;
     }
+    // fused flux + update stages: FP32-bulk single cases whose update writes
+    // the ghosts (no processor halos, laminar, no tile stages)
+    if (s->precision == LFM_FP32_BULK && !tiled && s->nh == 0 && !d->smag_c && s->a32.cellGhosts &&
+        fluxUpdateOption(s->D)) {
+        if ((rc = devAlloc(s, &s->prim1, (size_t)lfm::dev::primRows<float>(s->D) * nt))) return fail(rc);
+        s->fluxUpdate = true;
+    }
     if (s->precision == LFM_FP32_BULK) {
         for (int v = 0; v < s->nq; ++v) s->qRef[v] = s->a32.qRef[v];
         if ((rc = devAlloc(s, &s->stage, nq * nc))) return fail(rc);
@@ -670,7 +714,13 @@ int advanceGraph(lfm_solver* s, const double* qIn, int nsteps, double dt, double
         LFM_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
         int rc = enqueueSetState(s, qIn);
         if (!rc) rc = ensurePrims(s);
-        for (int k = 0; k < nsteps && !rc; ++k) launchStep(s, dt, 0);
+        // a new state starts in primitive buffer 0; alternating stages move
+        // the current primitives to the other buffer after an odd stage count
+        int parity = 0;
+        for (int k = 0; k < nsteps && !rc; ++k) {
+            launchStep(s, dt, parity);
+            if (alternating(s)) parity ^= (s->rkOrder & 1);
+        }
         if (!rc) rc = enqueueGetState(s, qOut);
         cudaError_t ce = cudaMemcpyAsync(s->flagHost, s->flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream);
         cudaError_t e = cudaStreamEndCapture(s->stream, &g);
@@ -689,7 +739,7 @@ int advanceGraph(lfm_solver* s, const double* qIn, int nsteps, double dt, double
     }
     LFM_CUDA(cudaGraphLaunch(s->advGraph, s->stream));
     // the flags the enqueued path leaves: a new state, its primitives, stages run
-    s->primParity = 0;
+    s->primParity = alternating(s) ? ((nsteps * s->rkOrder) & 1) : 0;
     s->primsValid = true;
     s->ghostRowsValid = true;
     s->lastStageB = s->rkB.empty() ? 0.0 : s->rkB.back();
@@ -705,7 +755,7 @@ extern "C" int lfm_solver_advance(lfm_solver* s, const double* q_in, int nsteps,
     if (!s || nsteps < 0) return lfm::setError(LFM_ERR_INVALID, "bad argument");
     LFM_CUDA(cudaSetDevice(s->device));
     int rc = LFM_OK;
-    if (q_in && q_out && nsteps > 0 && s->rkOrder > 0 && !s->tiled && pageLocked(q_in) && pageLocked(q_out))
+    if (q_in && q_out && nsteps > 0 && s->rkOrder > 0 && pageLocked(q_in) && pageLocked(q_out))
         return advanceGraph(s, q_in, nsteps, dt, q_out);
     if (q_in && (rc = enqueueSetState(s, q_in))) return rc;
     if (nsteps > 0 && (rc = lfm_solver_step(s, nsteps, dt))) return rc;
@@ -873,6 +923,7 @@ int residualNoalloc(const lfm_solver* s, const Args<T>& base, const double* q, i
     Args<T> a = base;
     a.q = reinterpret_cast<double*>(scratch);
     a.prim = reinterpret_cast<T*>(scratch + bq);
+    a.primW = a.prim;
     a.V = reinterpret_cast<T*>(scratch + bq + bPrim);
     a.grad = ausm ? reinterpret_cast<T*>(scratch + bq + bPrim + bV) : base.grad;
     a.flux = reinterpret_cast<T*>(scratch + bq + bPrim + bV + bGrad);
@@ -1126,7 +1177,9 @@ extern "C" int lfm_solver_launches_per_step(const lfm_solver* s, int* launches) 
     // primitives, so only halos remain
     const bool fused = s->precision == LFM_FP32_BULK ? s->a32.cellGhosts != nullptr : s->a64.cellGhosts != nullptr;
     const bool prep = !fused || s->nh > 0;
-    *launches = s->tiled ? s->rkOrder : s->rkOrder * ((prep ? 1 : 0) + 2 + (s->needGrad ? 1 : 0) + (s->needVis ? 1 : 0));
+    *launches = s->tiled ? s->rkOrder
+                         : s->rkOrder * ((prep ? 1 : 0) + (s->fluxUpdate ? 1 : 2) + (s->needGrad ? 1 : 0) +
+                                         (s->needVis ? 1 : 0));
     return LFM_OK;
 }
 
@@ -1170,6 +1223,15 @@ cudaError_t medianTime(lfm_solver* s, int reps, cudaEvent_t e0, cudaEvent_t e1, 
 
 void launchOne(lfm_solver* s, const Launch& l, double dt) {
     const StageConfig c = stageConfig(s, l.stage, dt);
+    if (s->fluxUpdate) {   // buffers of a step that starts from buffer 0
+        float* buf[2] = {s->a32.prim, s->prim1};
+        Args<float> g = s->a32;
+        g.prim = buf[l.stage & 1];
+        g.primW = buf[(l.stage & 1) ^ 1];
+        if (l.slot == lfm::dev::kSlotFluxUpdate) lfm::dev::launch_fluxupdate32(g, c, s->stream);
+        else if (l.slot < 3) lfm::dev::launch_kernel<float>(g, c, l.slot, s->stream);
+        return;
+    }
     if (s->precision == LFM_FP32_BULK)
         lfm::dev::launch_kernel<float>(s->a32, c, l.slot, s->stream);
     else
@@ -1211,14 +1273,19 @@ extern "C" int lfm_solver_profile_step(lfm_solver* s, double dt, int n, float* m
         if (e == cudaSuccess && !(rc = ensureGraph(s, dt))) {
             float t = 0.f;
             e = medianTime(s, kReps, e0, e1, [s] { return launchStepGraph(s); }, &t);
-            ms[lfm::dev::kKernelsPerStage] = std::max(0.f, t - t0);
+            ms[lfm::dev::kSlotTileStage] = std::max(0.f, t - t0);
         }
     } else if (e == cudaSuccess) {
         // the launches of one step: a (stage, slot) pair counts when its
         // capture holds a kernel
         std::vector<Launch> seq;
+        std::vector<int> slots;
+        for (int w = 0; w < lfm::dev::kKernelsPerStage; ++w)
+            if (!s->fluxUpdate || w < 3) slots.push_back(w);
+        if (s->fluxUpdate) slots.push_back(lfm::dev::kSlotFluxUpdate);
         for (int k = 0; k < s->rkOrder && e == cudaSuccess; ++k)
-            for (int w = 0; w < lfm::dev::kKernelsPerStage && e == cudaSuccess; ++w) {
+            for (int w : slots) {
+                if (e != cudaSuccess) break;
                 cudaGraph_t g = nullptr;
                 e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
                 if (e != cudaSuccess) break;
@@ -1242,6 +1309,10 @@ extern "C" int lfm_solver_profile_step(lfm_solver* s, double dt, int n, float* m
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (alternating(s)) {   // partial steps leave the primitives in either buffer
+        s->primsValid = false;
+        s->primParity = 0;
+    }
     if (rc) return rc;
     if (e != cudaSuccess) return cudaFail(e, "profile step");
     return LFM_OK;

@@ -57,7 +57,7 @@ __device__ __forceinline__ float pressure_dev(const RefState32& R, float r, floa
 // preparation and update kernels produce identical bits.
 // ---------------------------------------------------------------------------
 template <int D>
-__device__ __forceinline__ void prims32(const Args<float>& a, int t, const double* qp) {
+__device__ __forceinline__ void prims32(const Args<float>& a, int t, const double* qp, float* dst) {
     using P = PRow<D>;
     const RefState32& R = a.ref;
     const size_t nt = (size_t)a.nt;
@@ -80,14 +80,14 @@ __device__ __forceinline__ void prims32(const Args<float>& a, int t, const doubl
     const float K = __fmaf_rn(rho, __fmaf_rn(0.5f, uu, Uu), __fmul_rn(__fmul_rn(0.5f, r), U2));
     const float p = __fmul_rn(R.gm1, __fsub_rn(E, K));            // p - p_ref
     const float Rpsi = __fmul_rn(__fmaf_rn(-R.Rpsi, r, p), rinv);  // p/rho - p_ref/rho_inf
-    a.prim[(size_t)P::r * nt + t] = r;
+    dst[(size_t)P::r * nt + t] = r;
 #pragma unroll
     for (int k = 0; k < D; ++k) {
-        a.prim[(size_t)(P::m + k) * nt + t] = m[k];
-        a.prim[(size_t)(P::u + k) * nt + t] = u[k];
+        dst[(size_t)(P::m + k) * nt + t] = m[k];
+        dst[(size_t)(P::u + k) * nt + t] = u[k];
     }
-    a.prim[(size_t)P::Rpsi * nt + t] = Rpsi;
-    a.prim[(size_t)P::c * nt + t] = __fsqrt_rn(__fmul_rn(R.gamma, __fadd_rn(R.Rpsi, Rpsi)));
+    dst[(size_t)P::Rpsi * nt + t] = Rpsi;
+    dst[(size_t)P::c * nt + t] = __fsqrt_rn(__fmul_rn(R.gamma, __fadd_rn(R.Rpsi, Rpsi)));
 }
 
 // ---------------------------------------------------------------------------
@@ -98,7 +98,7 @@ __device__ __forceinline__ void prims32(const Args<float>& a, int t, const doubl
 // theirs is FP64.
 // ---------------------------------------------------------------------------
 template <int D>
-__device__ __forceinline__ void ghost32(const Args<float>& a, int g, const double* qi) {
+__device__ __forceinline__ void ghost32(const Args<float>& a, int g, const double* qi, float* dst) {
     constexpr int NQ = D + 2;
     using P = PRow<D>;
     const size_t nt = (size_t)a.nt;
@@ -107,17 +107,17 @@ __device__ __forceinline__ void ghost32(const Args<float>& a, int g, const doubl
     ghost_bc<float, D>(a, g, qi, qv);
     const double rinv = 1.0 / qv[0];
     double ke = 0.0;
-    a.prim[(size_t)P::r * nt + t] = (float)(qv[0] - a.qRef[0]);
+    dst[(size_t)P::r * nt + t] = (float)(qv[0] - a.qRef[0]);
 #pragma unroll
     for (int k = 0; k < D; ++k) {
-        a.prim[(size_t)(P::m + k) * nt + t] = (float)(qv[k + 1] - a.qRef[k + 1]);
-        a.prim[(size_t)(P::u + k) * nt + t] = (float)(qv[k + 1] * rinv - a.UInf[k]);
+        dst[(size_t)(P::m + k) * nt + t] = (float)(qv[k + 1] - a.qRef[k + 1]);
+        dst[(size_t)(P::u + k) * nt + t] = (float)(qv[k + 1] * rinv - a.UInf[k]);
         ke += qv[k + 1] * qv[k + 1];
     }
     const double p = a.gm1 * (qv[D + 1] - 0.5 * ke * rinv);
     const float Rpsi = (float)(p * rinv - a.pRef / a.qRef[0]);
-    a.prim[(size_t)P::Rpsi * nt + t] = Rpsi;
-    a.prim[(size_t)P::c * nt + t] = sqrtf(a.ref.gamma * (a.ref.Rpsi + Rpsi));
+    dst[(size_t)P::Rpsi * nt + t] = Rpsi;
+    dst[(size_t)P::c * nt + t] = sqrtf(a.ref.gamma * (a.ref.Rpsi + Rpsi));
 }
 
 // ---------------------------------------------------------------------------
@@ -133,7 +133,7 @@ __device__ __forceinline__ void prep32(const Args<float>& a, int t) {
         double qp[NQ];
 #pragma unroll
         for (int v = 0; v < NQ; ++v) qp[v] = a.q[(size_t)v * nt + t];
-        prims32<D>(a, t, qp);
+        prims32<D>(a, t, qp, a.prim);
         return;
     }
     const int g = t - a.nc;
@@ -141,7 +141,7 @@ __device__ __forceinline__ void prep32(const Args<float>& a, int t) {
     double qi[NQ];
 #pragma unroll
     for (int v = 0; v < NQ; ++v) qi[v] = a.q[(size_t)v * nt + in] + a.qRef[v];
-    ghost32<D>(a, g, qi);
+    ghost32<D>(a, g, qi, a.prim);
 }
 
 // ---------------------------------------------------------------------------
@@ -163,7 +163,7 @@ __device__ __forceinline__ void prep32(const Args<float>& a, int t) {
 // ghosts_of32: the FP64 states and FP32 primitives of the boundary ghosts of
 // cell c from its perturbation state qp (those prep32 computes).
 template <int D>
-__device__ __forceinline__ void ghosts_of32(const Args<float>& a, int c, const double* qp) {
+__device__ __forceinline__ void ghosts_of32(const Args<float>& a, int c, const double* qp, float* dst) {
     constexpr int NQ = D + 2;
     double qa[NQ];
 #pragma unroll
@@ -172,7 +172,7 @@ __device__ __forceinline__ void ghosts_of32(const Args<float>& a, int c, const d
         const int code = a.cfList[e];
         if (code < 0) continue;
         const int j = a.fN[code];
-        if (j >= a.nc && j < a.nc + a.ng) ghost32<D>(a, j - a.nc, qa);
+        if (j >= a.nc && j < a.nc + a.ng) ghost32<D>(a, j - a.nc, qa, dst);
     }
 }
 
@@ -271,8 +271,8 @@ __device__ __forceinline__ void apply32(const Args<float>& a, int c, const float
         if (RES) a.res[v * nc + c] = f32_to_f64(sum[v]);
     }
     if (!finite) atomicOr(a.flag, 1);
-    prims32<D>(a, c, qn);
-    if (GH && a.cellGhosts[c]) ghosts_of32<D>(a, c, qn);
+    prims32<D>(a, c, qn, a.primW);
+    if (GH && a.cellGhosts[c]) ghosts_of32<D>(a, c, qn, a.primW);
 }
 
 template <int D, bool RES, bool GH = false, bool ELL = false>
@@ -298,8 +298,8 @@ __device__ __forceinline__ void set_state32(const Args<float>& a, const double* 
         qp[v] = q[(size_t)v * stride + c] - a.qRef[v];
         a.q[(size_t)v * a.nt + c] = qp[v];
     }
-    prims32<D>(a, c, qp);
-    if (a.cellGhosts && a.cellGhosts[c]) ghosts_of32<D>(a, c, qp);
+    prims32<D>(a, c, qp, a.prim);
+    if (a.cellGhosts && a.cellGhosts[c]) ghosts_of32<D>(a, c, qp, a.prim);
 }
 
 // Perturbation state q' = q - q_ref of cells [0, n) from a caller's absolute
@@ -465,7 +465,7 @@ __device__ __forceinline__ float p5diff_dd(float a, float b, float alpha) {
 // gathers come from HBM; 2 % in 2D, whose gathers hit L2). The fused kernels,
 // whose registers other phases already fill, keep the late loads.
 template <int D, int SCH, bool VIS = true, bool LES = false, bool EARLYV = false>
-__device__ __forceinline__ void flux32(const Args<float>& a, int f) {
+__device__ __forceinline__ void face_rhs32(const Args<float>& a, int f, float* rhs) {
     constexpr int NQ = D + 2;
     using P = PRow<D>;
     const RefState32& R = a.ref;
@@ -500,8 +500,6 @@ __device__ __forceinline__ void flux32(const Args<float>& a, int f) {
             }
         }
     }
-    float rhs[NQ];
-
     // Face state: linear interpolation for M1, the mid-point for M2 / M2AUSM.
     const float wf = (SCH == kSchemeM1) ? w : 0.5f;
     const float rf = interp(wf, ri, rj);
@@ -687,8 +685,43 @@ __device__ __forceinline__ void flux32(const Args<float>& a, int f) {
             }
         }
     }
+}
+
+template <int D, int SCH, bool VIS = true, bool LES = false, bool EARLYV = false>
+__device__ __forceinline__ void flux32(const Args<float>& a, int f) {
+    float rhs[D + 2];
+    face_rhs32<D, SCH, VIS, LES, EARLYV>(a, f, rhs);
+    const size_t nf = (size_t)a.nf;
 #pragma unroll
-    for (int v = 0; v < NQ; ++v) a.flux[(size_t)v * nf + f] = rhs[v];
+    for (int v = 0; v < D + 2; ++v) a.flux[(size_t)v * nf + f] = rhs[v];
+}
+
+// ---------------------------------------------------------------------------
+// fluxupdate32: the rhs of every face of cell c, evaluated by the cell itself
+// (each face is evaluated by both of its cells, from the face's own data, so
+// both get the bits flux32 stores), summed in ascending face order as the
+// update's gather sums the stored values, then the update of apply32. The
+// face rhs never reaches memory and a stage needs one kernel less; the next
+// stage's primitives go to a.primW, the other of two buffers (the cells of
+// this launch still read a.prim).
+// ---------------------------------------------------------------------------
+template <int D, int SCH, bool LES, bool RES, bool GH>
+__device__ __forceinline__ void fluxupdate32(const Args<float>& a, int c, double Ak, double Bk, double dt,
+                                             float dt32, int first) {
+    constexpr int NQ = D + 2;
+    CellIn32<D> in;
+    load_cell32<D>(a, c, first, in);
+    float sum[NQ];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) sum[v] = 0.0f;
+    for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
+        const int code = a.cfList[e];
+        float r[NQ];
+        face_rhs32<D, SCH, true, LES, false>(a, code >= 0 ? code : ~code, r);
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) sum[v] = code >= 0 ? sum[v] + r[v] : sum[v] - r[v];
+    }
+    apply32<D, RES, GH>(a, c, sum, in, Ak, Bk, dt, dt32, first);
 }
 
 }  // namespace dev

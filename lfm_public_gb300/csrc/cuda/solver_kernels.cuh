@@ -67,6 +67,9 @@ struct Args {
     // per cell + ghost, computed every stage
     T* prim;                  // FP64: (D + 3) x nt: 1/rho, u[D], R psi, c
                               // FP32: (2D + 3) x nt: rho', m'[D], u'[D], R psi', c
+    T* primW;                 // where an update writes the next stage's primitives: prim, or
+                              // (fused flux-update stages) the other of two buffers, which no
+                              // thread of that launch reads
     T* V;                     // (D^2 + 2D) x nt: dudx, dTdx, sigmaU
     T* grad;                  // (2D + D^2) x nt: rho_grad, p_grad, U_grad (M2AUSM)
     T* flux;                  // nq x nf face rhs

@@ -68,6 +68,23 @@ __global__ void __launch_bounds__(256, 6) k_update32_2d(const __grid_constant__ 
     update_thread<2, RES, GH, false>(a, Ak, Bk, dt, dt32, first);
 }
 
+// Fused flux + update (fluxupdate32): one thread per cell, cells mapped as
+// in the update kernel that writes ghosts (warp-interleaved chunks).
+template <int D, int SCH, bool RES>
+__global__ void __launch_bounds__(256) k_fluxupdate32(const __grid_constant__ Args<float> a, double Ak, double Bk,
+                                                      double dt, float dt32, int first) {
+    const int c = (int)(((threadIdx.x >> 5) * gridDim.x + blockIdx.x) << 5) + (int)(threadIdx.x & 31u);
+    if (c < a.nc) fluxupdate32<D, SCH, false, RES, true>(a, c, Ak, Bk, dt, dt32, first);
+}
+
+template <int D, int SCH>
+void launch_fluxupdate32_scheme(const Args<float>& a, const StageConfig& s, cudaStream_t st) {
+    const unsigned nb = (unsigned)((a.nc + 255) / 256);
+    const float dt32 = (float)s.dt;
+    if (s.withRes) k_fluxupdate32<D, SCH, true><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, dt32, s.first);
+    else k_fluxupdate32<D, SCH, false><<<nb, 256, 0, st>>>(a, s.A, s.B, s.dt, dt32, s.first);
+}
+
 template <int D, bool ELL>
 void launch_update32(const Args<float>& a, const StageConfig& s, cudaStream_t st) {
     const unsigned nb = (unsigned)((a.nc + 255) / 256);   // eight 32-cell chunks per block
@@ -149,6 +166,18 @@ void launch_kernel_fp32(const Args<float>& a, const StageConfig& s, int which, c
         launch_fp32<2>(a, s, which, st);
     else
         launch_fp32<3>(a, s, which, st);
+}
+
+void launch_fluxupdate32(const Args<float>& a, const StageConfig& s, cudaStream_t st) {
+    if (a.D == 2) {
+        if (s.scheme == kSchemeM1) launch_fluxupdate32_scheme<2, kSchemeM1>(a, s, st);
+        else if (s.scheme == kSchemeM2) launch_fluxupdate32_scheme<2, kSchemeM2>(a, s, st);
+        else launch_fluxupdate32_scheme<2, kSchemeAUSM>(a, s, st);
+    } else {
+        if (s.scheme == kSchemeM1) launch_fluxupdate32_scheme<3, kSchemeM1>(a, s, st);
+        else if (s.scheme == kSchemeM2) launch_fluxupdate32_scheme<3, kSchemeM2>(a, s, st);
+        else launch_fluxupdate32_scheme<3, kSchemeAUSM>(a, s, st);
+    }
 }
 
 void launch_set_state32(const Args<float>& a, const double* q, int64_t stride, cudaStream_t st) {

@@ -34,6 +34,10 @@ template <>
 void launch_kernel<float>(const Args<float>& a, const StageConfig& s, int which, cudaStream_t st);
 // FP32-bulk kernels (perturbation form).
 void launch_kernel_fp32(const Args<float>& a, const StageConfig& s, int which, cudaStream_t st);
+// FP32-bulk fused flux + update of every cell (laminar, a.cellGhosts set): the
+// face rhs evaluated by the cells themselves; the next stage's primitives go
+// to a.primW, which must not be a.prim.
+void launch_fluxupdate32(const Args<float>& a, const StageConfig& s, cudaStream_t st);
 // q' = q - q_ref for the cells of an FP32-bulk solver from an absolute state
 // [nq][stride] on the device.
 void launch_to_perturbation(const Args<float>& a, const double* q, int64_t stride, cudaStream_t st);
@@ -96,10 +100,14 @@ cudaError_t launch_tile_stage(const Args<float>& g, const TileArgs& t, const Sta
 
 constexpr int kKernelsPerStage = 5;  // prep, grad, vis, flux, update
 // Timing slots of lfm_solver_profile_step: the five kernels, then the fused
-// tile stage (which does the work of the five).
-constexpr int kKernelSlots = 6;
+// tile stage (which does the work of the five), then the fused flux + update
+// (which does the work of the last two).
+constexpr int kKernelSlots = 7;
+constexpr int kSlotTileStage = 5;
+constexpr int kSlotFluxUpdate = 6;
 inline const char* kernelName(int i) {
-    static const char* names[] = {"k_prep", "k_grad", "k_vis", "k_flux", "k_update", "k_tile_stage"};
+    static const char* names[] = {"k_prep", "k_grad", "k_vis", "k_flux", "k_update", "k_tile_stage",
+                                  "k_flux_update"};
     return (i >= 0 && i < kKernelSlots) ? names[i] : "";
 }
 

@@ -264,3 +264,31 @@ def test_smagorinsky_les_fp32_bulk_and_batch():
     with pytest.raises(N.LfmError):
         b.add(ch, case.delta_t)
     b.close()
+
+
+@pytest.mark.parametrize("solver,minmod,mu", [(0, True, 1e-3), (1, False, 1e-3), (2, True, 1e-3), (0, False, 0.0)])
+def test_fused_flux_update_gives_the_separate_kernels_bits(monkeypatch, solver, minmod, mu):
+    """The fused flux + update stage (each cell evaluates the rhs of its own
+    faces, the next stage's primitives go to a second buffer) gives the bits
+    of the separate flux and update kernels, through stepping, single steps,
+    lfm_solver_advance and the residual."""
+    case = cases.cylinder_case(n_theta=64, n_r=32, r1=20, first=0.02, Ls=5, solver=solver, minmod=minmod,
+                               noise=0.02, seed=3)
+    case.mu = mu
+    case.residuals = True
+    ch = N.CaseHandle.from_case(case)
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("LFM_FLUX_UPDATE", mode)
+        s = N.Solver(ch, precision=N.LFM_FP32_BULK)
+        s.step(7, case.delta_t)   # an odd stage count per step: the buffers swap
+        s.sync()
+        q7 = s.get_state()
+        res = s.cell_residual()
+        host = np.ascontiguousarray(q7.copy())
+        outq = np.empty_like(host)
+        s.advance(host, 3, case.delta_t, outq)
+        out[mode] = (q7, res, outq)
+        s.close()
+    for a, b in zip(out["0"], out["1"]):
+        assert np.array_equal(a, b)

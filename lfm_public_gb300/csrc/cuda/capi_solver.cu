@@ -172,6 +172,9 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
     a.cellGhosts = nullptr;
     a.cfEll = nullptr;
     a.smagC = nullptr;
+    a.wN = nullptr;
+    a.cfSo = nullptr;
+    a.primC = s->scheme == LFM_SOLVER_M2AUSM ? 1 : 0;
     const size_t nt = (size_t)s->nt, nf = (size_t)s->nf, D = (size_t)s->D;
     int rc;
     if ((rc = devAlloc(s, &a.dq, (size_t)s->nq * s->nc))) return rc;
@@ -221,6 +224,26 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
         for (size_t f = 0; f < nf; ++f) lapc[f] = d->delta_mag[f] * d->dmag_inv[f];
         if ((rc = uploadAs<T>(s, &p, lapc.data(), nf))) return rc;
         a.lapc = p;
+    }
+    if (sizeof(T) == sizeof(double)) {
+        // FP64 face and face-entry constants, each the value the kernels would
+        // otherwise compute per face visit: 1 - w, and S/V of each cell's faces
+        std::vector<double> wN(nf);
+        for (size_t f = 0; f < nf; ++f) wN[f] = 1.0 - d->w[f];
+        if ((rc = uploadAs<T>(s, &p, wN.data(), nf))) return rc;
+        a.wN = p;
+        const size_t ne = (size_t)d->cell_face_offsets[s->nc];
+        std::vector<double> so(D * ne);
+        for (int64_t c = 0; c < s->nc; ++c)
+            for (int64_t e = d->cell_face_offsets[c]; e < d->cell_face_offsets[c + 1]; ++e) {
+                const int64_t f = d->cell_faces[e];
+                for (size_t k = 0; k < D; ++k) {
+                    const double Sk = d->S[k * nf + (size_t)f];
+                    so[k * ne + (size_t)e] = d->cell_face_sign[e] > 0 ? Sk * d->vol_inv[c] : -Sk * d->vol_inv[c];
+                }
+            }
+        if ((rc = uploadAs<T>(s, &p, so.data(), so.size()))) return rc;
+        a.cfSo = p;
     }
     a.volInv32 = nullptr;
     if (sizeof(T) == sizeof(float)) {

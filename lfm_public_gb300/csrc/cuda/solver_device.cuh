@@ -13,6 +13,12 @@ __device__ __forceinline__ T interp(T w, T a, T b) {
     return w * a + (T(1) - w) * b;
 }
 
+// interp with the weight of N given (1 - w, precomputed per face).
+template <typename T>
+__device__ __forceinline__ T interp2(T w, T wN, T a, T b) {
+    return w * a + wN * b;
+}
+
 template <typename T, int D>
 __device__ __forceinline__ T dotv(const T* a, const T* b) {
     T s = a[0] * b[0];
@@ -192,7 +198,7 @@ __device__ __forceinline__ void prims64(const Args<double>& a, int t, const doub
 #pragma unroll
     for (int k = 0; k < D; ++k) a.prim[(size_t)(1 + k) * nt + t] = qv[k + 1] * rinv;
     a.prim[(size_t)(D + 1) * nt + t] = Rpsi;
-    a.prim[(size_t)(D + 2) * nt + t] = sqrt(a.gamma * Rpsi);
+    if (a.primC) a.prim[(size_t)(D + 2) * nt + t] = sqrt(a.gamma * Rpsi);   // read by M2AUSM only
 }
 
 // FP64 path: the states and primitives of the boundary ghosts of cell c from

@@ -34,24 +34,23 @@ __global__ void __launch_bounds__(256) k_grad(Args<T> a) {
 #pragma unroll
         for (int l = 0; l < D; ++l) gu[k][l] = T(0);
     }
-    const T vi = (T)a.volInv[c];
+    const size_t ne = (size_t)a.cfOff[a.nc];
     for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
         const int code = a.cfList[e];
         const int f = code >= 0 ? code : ~code;
         const int i = a.fP[f], j = a.fN[f];
-        const T w = a.w[f];
+        const T w = a.w[f], wN = a.wN[f];
         T so[D], UU[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) {
-            const T Sk = a.S[(size_t)k * a.nf + f];
-            so[k] = (code >= 0) ? Sk * vi : -Sk * vi;
-            UU[k] = interp(w, a.prim[(size_t)(1 + k) * a.nt + i], a.prim[(size_t)(1 + k) * a.nt + j]);
+            so[k] = a.cfSo[(size_t)k * ne + e];   // S / V seen from c
+            UU[k] = interp2(w, wN, a.prim[(size_t)(1 + k) * a.nt + i], a.prim[(size_t)(1 + k) * a.nt + j]);
         }
         const T rhoi = (T)a.q[i], rhoj = (T)a.q[j];
         const T pi = rhoi * a.prim[(size_t)(D + 1) * a.nt + i];
         const T pj = rhoj * a.prim[(size_t)(D + 1) * a.nt + j];
-        const T rho = interp(w, rhoi, rhoj);
-        const T p = interp(w, pi, pj);
+        const T rho = interp2(w, wN, rhoi, rhoj);
+        const T p = interp2(w, wN, pi, pj);
 #pragma unroll
         for (int x = 0; x < D; ++x) {
             gp[x] += p * so[x];
@@ -84,28 +83,32 @@ __global__ void __launch_bounds__(256) k_vis(Args<T> a) {
 #pragma unroll
         for (int l = 0; l < D; ++l) g[k][l] = T(0);
     }
-    const T vi = (T)a.volInv[c];
-    const T Rinv = (T)a.Rinv;
+    // Gauss gradients of u and of R psi (T = R psi / R: the 1/R factor is
+    // applied once to the sum); S / V of each face seen from c is a
+    // precomputed entry constant, 1 - w a face constant
+    const size_t ne = (size_t)a.cfOff[a.nc];
     for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
         const int code = a.cfList[e];
         const int f = code >= 0 ? code : ~code;
         const int i = a.fP[f], j = a.fN[f];
-        const T w = a.w[f];
+        const T w = a.w[f], wN = a.wN[f];
         T so[D], fU[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) {
-            const T Sk = a.S[(size_t)k * a.nf + f];
-            so[k] = (code >= 0) ? Sk * vi : -Sk * vi;
-            fU[k] = interp(w, a.prim[(size_t)(1 + k) * a.nt + i], a.prim[(size_t)(1 + k) * a.nt + j]);
+            so[k] = a.cfSo[(size_t)k * ne + e];
+            fU[k] = interp2(w, wN, a.prim[(size_t)(1 + k) * a.nt + i], a.prim[(size_t)(1 + k) * a.nt + j]);
         }
-        const T fT = interp(w, a.prim[(size_t)(D + 1) * a.nt + i], a.prim[(size_t)(D + 1) * a.nt + j]) * Rinv;
+        const T fR = interp2(w, wN, a.prim[(size_t)(D + 1) * a.nt + i], a.prim[(size_t)(D + 1) * a.nt + j]);
 #pragma unroll
         for (int x = 0; x < D; ++x) {
 #pragma unroll
             for (int y = 0; y < D; ++y) g[x][y] += fU[x] * so[y];
-            gT[x] += fT * so[x];
+            gT[x] += fR * so[x];
         }
     }
+    const T Rinv = (T)a.Rinv;
+#pragma unroll
+    for (int x = 0; x < D; ++x) gT[x] *= Rinv;
     const T mu = (T)a.mu;
     T tau[D][D];
     stress<T, D>(g, mu, tau);
@@ -141,7 +144,7 @@ __global__ void __launch_bounds__(128) k_flux(Args<T> a) {
     const size_t nt = (size_t)a.nt, nf = (size_t)a.nf;
     const int i = a.fP[f], j = a.fN[f];
     const bool ghost = a.fGhost[f] != 0;
-    const T w = a.w[f];
+    const T w = a.w[f], wN = a.wN[f];
     T S[D], Kf[D];
 #pragma unroll
     for (int k = 0; k < D; ++k) {
@@ -174,19 +177,15 @@ __global__ void __launch_bounds__(128) k_flux(Args<T> a) {
         // wave-speed weights cancel: the flux is the central flux of the
         // interpolated state, F(q_f).S. It is evaluated in that form - one
         // division per face instead of three, no sound speeds - and equals
-        // the reference's value up to rounding.
-        const T rho = interp(w, qi[0], qj[0]);
+        // the reference's value up to rounding. The interpolated internal
+        // energy per unit mass is that of the interpolated R psi,
+        // e = R psi / (gamma - 1) (R psi = (gamma - 1) e in every cell), so
+        // e + R psi = gamma / (gamma - 1) R psi.
+        const T rho = interp2(w, wN, qi[0], qj[0]);
         T m[D];
 #pragma unroll
-        for (int k = 0; k < D; ++k) m[k] = interp(w, qi[k + 1], qj[k + 1]);
-        T ce = T(2) * qi[D + 1] * cri, ae = T(2) * qj[D + 1] * ari;
-#pragma unroll
-        for (int k = 0; k < D; ++k) {
-            ce -= cU[k] * cU[k];
-            ae -= aU[k] * aU[k];
-        }
-        const T e = T(0.5) * interp(w, ce, ae);          // internal energy per unit mass
-        const T Rpsi = interp(w, cRpsi, aRpsi);
+        for (int k = 0; k < D; ++k) m[k] = interp2(w, wN, qi[k + 1], qj[k + 1]);
+        const T Rpsi = interp2(w, wN, cRpsi, aRpsi);
         const T rinv = T(1) / rho;
         T mS = T(0), u2 = T(0);
 #pragma unroll
@@ -199,7 +198,7 @@ __global__ void __launch_bounds__(128) k_flux(Args<T> a) {
         rhs[0] = -mS;
 #pragma unroll
         for (int k = 0; k < D; ++k) rhs[k + 1] = -(m[k] * phi + p * S[k]);
-        rhs[D + 1] = -mS * (e + T(0.5) * u2 * (rinv * rinv) + Rpsi);
+        rhs[D + 1] = -mS * ((T)a.gh * Rpsi + T(0.5) * u2 * (rinv * rinv));
     } else {
         // Pirozzoli kinetic-energy-preserving mid-point flux (src/cfd_v0.cpp:1966-2023)
         const T rhoavg = T(0.5) * (qi[0] + qj[0]);
@@ -297,9 +296,10 @@ __global__ void __launch_bounds__(128) k_flux(Args<T> a) {
 #pragma unroll
             for (int x = 0; x < D; ++x) {
 #pragma unroll
-                for (int y = 0; y < D; ++y) g[x][y] = interp(w, a.V[(x * D + y) * nt + i], a.V[(x * D + y) * nt + j]);
-                gT[x] = interp(w, a.V[(D * D + x) * nt + i], a.V[(D * D + x) * nt + j]);
-                sU[x] = interp(w, a.V[(D * D + D + x) * nt + i], a.V[(D * D + D + x) * nt + j]);
+                for (int y = 0; y < D; ++y)
+                    g[x][y] = interp2(w, wN, a.V[(x * D + y) * nt + i], a.V[(x * D + y) * nt + j]);
+                gT[x] = interp2(w, wN, a.V[(D * D + x) * nt + i], a.V[(D * D + x) * nt + j]);
+                sU[x] = interp2(w, wN, a.V[(D * D + D + x) * nt + i], a.V[(D * D + D + x) * nt + j]);
             }
         } else {
             // explicit two-point gradients on physical boundaries

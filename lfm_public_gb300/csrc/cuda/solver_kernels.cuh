@@ -87,6 +87,7 @@ struct Args {
     const T* dmag;            // |delta|
     const T* K;               // D x nf
     const T* lapc;            // |delta| / |d| per face
+    const T* wN;              // FP64 path: 1 - w per face (the linear weight of N)
     // cells
     const double* volInv;
     const float* volInv32;    // FP32 copy (FP32-bulk gradient kernels)
@@ -94,6 +95,8 @@ struct Args {
     const int* cfOff;         // nc + 1
     const int* cfList;        // face index, negative (~f) when the cell is N
     const int* cfNbr;         // per cfList entry: the cell (or ghost, halo) across the face
+    const T* cfSo;            // FP64 path: D x (cfList entries), S / V of the entry's face seen
+                              // from its cell (the Gauss-gradient weight)
     const T* smagC;           // Smagorinsky LES: the constant each cell's tauMC is built with
                               // (V then holds D x D more rows: its SGS stress), or null
     const uint8_t* cellGhosts;  // FP32-bulk single case: boundary faces of each cell
@@ -109,11 +112,14 @@ struct Args {
     const int* gFace;
     // constants
     double gamma, gm1, Rinv, rhoInf, EInf, pInf, TInf, UInf[3], mu, kcond;
+    double gh;                // gamma / (gamma - 1): enthalpy per unit R psi
     // FP32-bulk: conservative reference state q_ref = (rho_inf, rho_inf U_inf,
     // rho_inf E_inf) in FP64 (index = variable) and its derived FP32 constants
     double qRef[5];
     double pRef;              // (gamma - 1)(rho_inf E_inf - rho_inf |U_inf|^2 / 2)
     RefState32 ref;
+    // FP64 path: the primitives include the sound speed (read by M2AUSM only)
+    int primC;
     // error flag (non-finite state)
     int* flag;
 };

@@ -151,15 +151,21 @@ typedef struct lfm_params {
     double Cp, mol_weight, mu, Pr;
     /* Solver order of the cells inside each submesh, for locality of the
      * device gathers: LFM_RENUMBER_NONE (polyMesh order, the reference's),
-     * _RCM (reverse Cuthill-McKee) or _HILBERT (Hilbert curve through the
-     * cell centres). lfm_case_open reads it from controlDict lfm/renumber
-     * (none | rcm | hilbert). Written fields keep the polyMesh numbering. */
+     * _RCM (reverse Cuthill-McKee), _HILBERT (Hilbert curve through the
+     * cell centres) or _HPATH (the reference's Hamiltonian path).
+     * lfm_case_open reads it from controlDict lfm/renumber
+     * (none | rcm | hilbert | hpath). Written fields keep the polyMesh
+     * numbering. */
     int renumber;
 } lfm_params;
 
 #define LFM_RENUMBER_NONE 0
 #define LFM_RENUMBER_RCM 1
 #define LFM_RENUMBER_HILBERT 2
+/* The reference's Hamiltonian-path order (its hpath renumberMesh method,
+ * hpathRenumber/hpathRenumber.C:127-180; designed for 2D meshes): boundary
+ * cells as one walk, then the interior cells as another. */
+#define LFM_RENUMBER_HPATH 3
 
 typedef struct lfm_fields {
     const double* p;      /* [n_cells] */

@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(PKG, "liblfm_gpu.so")
 
 LFM_FP64 = 0
 LFM_FP32_BULK = 1
-LFM_RENUMBER_NONE, LFM_RENUMBER_RCM, LFM_RENUMBER_HILBERT = 0, 1, 2
+LFM_RENUMBER_NONE, LFM_RENUMBER_RCM, LFM_RENUMBER_HILBERT, LFM_RENUMBER_HPATH = 0, 1, 2, 3
 # lfm_status codes (include/lfm_gpu.h)
 LFM_OK = 0
 LFM_ERR_INVALID = -1

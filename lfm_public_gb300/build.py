@@ -27,7 +27,7 @@ INCLUDES = [os.path.join(ROOT, "include"), os.path.join(ROOT, "include", "lfm"),
             os.path.join(CSRC, "cuda")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_SOURCES = ["foam_io.cpp", "foam_case.cpp", "dict_reader.cpp", "poly_mesh_reader.cpp", "run_time_manager.cpp",
-                "input_reader.cpp", "renumber.cpp", "case_setup.cpp", "tiles.cpp", "capi_case.cpp"]
+                "input_reader.cpp", "renumber.cpp", "hpath.cpp", "case_setup.cpp", "tiles.cpp", "capi_case.cpp"]
 CUDA_SOURCES = ["solver_kernels.cu", "solver_kernels_fp32.cu", "batch_kernels.cu", "tile_kernels.cu", "post_kernels.cu",
                 "capi_solver.cu", "capi_batch.cu", "capi_server.cu"]
 CLI_SOURCES = ["gpu_mesh.cpp", "lfm_solve_gpu.cpp"]

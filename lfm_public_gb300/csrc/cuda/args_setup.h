@@ -133,6 +133,7 @@ void setConstants(dev::Args<T>& a, const lfm_solver_desc* d) {
     const double gh = d->gamma / (d->gamma - 1.0);
     a.pRef = pRef;
     a.gh = gh;
+    a.mu23 = d->mu * 2.0 / 3.0;
     a.ref.rho = (float)d->rhoInf;
     for (int k = 0; k < 3; ++k) {
         a.ref.U[k] = k < D ? (float)d->UInf[k] : 0.0f;

@@ -417,15 +417,18 @@ int tileCellsOption() {
     return e ? atoi(e) : kTileCells;
 }
 
-// Fused flux + update stages, by dimension (LFM_FLUX_UPDATE=0/1 in the
-// environment overrides for a solver created afterwards).
-constexpr bool kFluxUpdate2D = false;
-constexpr bool kFluxUpdate3D = false;
-
-bool fluxUpdateOption(int D) {
+// Fused flux + update stages (LFM_FLUX_UPDATE=0/1 in the environment
+// overrides for a solver created afterwards). Measured on GB300, FP32-bulk,
+// per step: the 256 x 256 inviscid M1 vortex 0.075 -> 0.070 ms; the 768 x 512
+// viscous cylinder 0.192 -> 0.259 ms (M1), 0.198 -> 0.255 (M2), 0.45 -> 0.89
+// (M2AUSM); a 96 x 64 x 24 viscous 3D wake 0.201 -> 0.263. Each face is
+// evaluated twice, and with the viscous rows of both cells the fused kernel
+// needs 64 (2D) to 123 (3D M2AUSM) registers: it gains only where the flux is
+// short, the inviscid M1/M2 cases.
+bool fluxUpdateOption(const lfm_solver* s) {
     const char* e = getenv("LFM_FLUX_UPDATE");
     if (e) return atoi(e) != 0;
-    return D == 2 ? kFluxUpdate2D : kFluxUpdate3D;
+    return s->D == 2 && !s->needVis && s->scheme != LFM_SOLVER_M2AUSM;
 }
 
 // Creates a solver; `stream` (not owned) is shared by the partitions of a
@@ -608,7 +611,7 @@ int createSolver(const lfm_solver_desc* d, const lfm_solver_opts* opts, cudaStre
     // fused flux + update stages: FP32-bulk single cases whose update writes
     // the ghosts (no processor halos, laminar, no tile stages)
     if (s->precision == LFM_FP32_BULK && !tiled && s->nh == 0 && !d->smag_c && s->a32.cellGhosts &&
-        fluxUpdateOption(s->D)) {
+        fluxUpdateOption(s)) {
         if ((rc = devAlloc(s, &s->prim1, (size_t)lfm::dev::primRows<float>(s->D) * nt))) return fail(rc);
         s->fluxUpdate = true;
     }

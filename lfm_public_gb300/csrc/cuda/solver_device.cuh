@@ -13,6 +13,32 @@ __device__ __forceinline__ T interp(T w, T a, T b) {
     return w * a + (T(1) - w) * b;
 }
 
+// 1/x in FP64 by Newton-Raphson iteration for the reciprocal (y <- y + y(1 - xy),
+// each step squaring the relative error), seeded with the single-precision
+// reciprocal approximation of x truncated to binary32 (PTX rcp.approx.ftz.f32,
+// relative error near 2^-23 with the truncation): two steps leave the result
+// within an ulp or two of the correctly rounded 1/x, for four FP64 FMAs -- GB300
+// issues about two FP64 instructions per clock per SM, and a full-precision
+// division takes several more. Values outside binary32's normal range take
+// the division.
+__device__ __forceinline__ double rcp64(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int ex = (int)((b >> 52) & 0x7ffu) - 896;   // binary32 biased exponent
+    if (ex < 2 || ex > 252) return 1.0 / x;
+    const unsigned fb = ((unsigned)(b >> 32) & 0x80000000u) | ((unsigned)ex << 23) | (unsigned)((b >> 29) & 0x7fffffu);
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(__uint_as_float(fb)));
+    // widen r exactly: rebias its (normal) exponent, move its mantissa up
+    const unsigned rb = __float_as_uint(r);
+    double y = __longlong_as_double((long long)(((unsigned long long)(rb & 0x80000000u) << 32) |
+                                                ((unsigned long long)(((rb >> 23) & 0xffu) + 896u) << 52) |
+                                                ((unsigned long long)(rb & 0x7fffffu) << 29)));
+    double e = fma(-x, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-x, y, 1.0);
+    return fma(y, e, y);
+}
+
 // interp with the weight of N given (1 - w, precomputed per face).
 template <typename T>
 __device__ __forceinline__ T interp2(T w, T wN, T a, T b) {
@@ -189,7 +215,7 @@ __device__ __forceinline__ void stage_state(const Args<T>& a, int t, double* qv)
 template <int D>
 __device__ __forceinline__ void prims64(const Args<double>& a, int t, const double* qv) {
     const size_t nt = (size_t)a.nt;
-    const double rinv = 1.0 / qv[0];
+    const double rinv = rcp64(qv[0]);
     double s = qv[1] * qv[1];
 #pragma unroll
     for (int k = 1; k < D; ++k) s += qv[k + 1] * qv[k + 1];

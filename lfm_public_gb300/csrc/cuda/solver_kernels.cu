@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(128) k_flux(Args<T> a) {
     }
     const T cRpsi = a.prim[(D + 1) * nt + i], aRpsi = a.prim[(D + 1) * nt + j];
     const T Rinv = (T)a.Rinv;
-    const T cT = cRpsi * Rinv, aT = aRpsi * Rinv;
+    const T dT = (aRpsi - cRpsi) * Rinv;   // T_N - T_P
     T rhs[NQ];
 
     if (SCH == kSchemeM1) {
@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(128) k_flux(Args<T> a) {
 #pragma unroll
         for (int k = 0; k < D; ++k) m[k] = interp2(w, wN, qi[k + 1], qj[k + 1]);
         const T Rpsi = interp2(w, wN, cRpsi, aRpsi);
-        const T rinv = T(1) / rho;
+        const T rinv = rcp64(rho);
         T mS = T(0), u2 = T(0);
 #pragma unroll
         for (int k = 0; k < D; ++k) {
@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(128) k_flux(Args<T> a) {
     } else {
         // Pirozzoli kinetic-energy-preserving mid-point flux (src/cfd_v0.cpp:1966-2023)
         const T rhoavg = T(0.5) * (qi[0] + qj[0]);
-        const T rhoavg_inv = T(1) / rhoavg;
+        const T rhoavg_inv = rcp64(rhoavg);
         T rhoUavg[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) rhoUavg[k] = T(0.5) * (qi[k + 1] + qj[k + 1]);
@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(128) k_flux(Args<T> a) {
             for (int x = 0; x < D; ++x) {
 #pragma unroll
                 for (int y = 0; y < D; ++y) g[x][y] = (aU[x] - cU[x]) * dn[y] * dinv;
-                gT[x] = (aT - cT) * dn[x] * dinv;
+                gT[x] = dT * dn[x] * dinv;
                 Uf[x] = interp(w, cU[x], aU[x]);
             }
             stress<T, D>(g, mu, tau);
@@ -325,18 +325,17 @@ __global__ void __launch_bounds__(128) k_flux(Args<T> a) {
         T tr = g[0][0];
 #pragma unroll
         for (int x = 1; x < D; ++x) tr += g[x][x];
-        const T dsum = -(mu * T(2) / T(3)) * tr;
+        const T dsum = -(T)a.mu23 * tr;
         const T kc = (T)a.kcond;
 #pragma unroll
         for (int x = 0; x < D; ++x) {
             T gtS = g[0][x] * S[0];
 #pragma unroll
             for (int y = 1; y < D; ++y) gtS += g[y][x] * S[y];
-            const T divTau = mu * gtS + dsum * S[x];
-            const T lap = mu * (lapc * (aU[x] - cU[x]) + dotv<T, D>(Kf, g[x]));
-            rhs[x + 1] += divTau + lap;
+            // div tauMC + the Laplacian split: mu (g^T S + |delta|/|d| du + K.g) + dsum S
+            rhs[x + 1] += mu * (gtS + lapc * (aU[x] - cU[x]) + dotv<T, D>(Kf, g[x])) + dsum * S[x];
         }
-        const T lapT = kc * (lapc * (aT - cT) + dotv<T, D>(Kf, gT));
+        const T lapT = kc * (lapc * dT + dotv<T, D>(Kf, gT));
         rhs[D + 1] += dotv<T, D>(sU, S) + lapT;
         // Smagorinsky LES: the face tauMC also interpolates the cells' SGS
         // stress (boundary faces keep the laminar two-point one, as in the

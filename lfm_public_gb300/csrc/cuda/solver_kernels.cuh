@@ -113,6 +113,7 @@ struct Args {
     // constants
     double gamma, gm1, Rinv, rhoInf, EInf, pInf, TInf, UInf[3], mu, kcond;
     double gh;                // gamma / (gamma - 1): enthalpy per unit R psi
+    double mu23;              // 2/3 mu (the trace term of the deviatoric stress)
     // FP32-bulk: conservative reference state q_ref = (rho_inf, rho_inf U_inf,
     // rho_inf E_inf) in FP64 (index = variable) and its derived FP32 constants
     double qRef[5];

@@ -69,8 +69,8 @@ static int validateParams(const lfm::CaseParams& p) {
     if (p.dimension != 2 && p.dimension != 3)
         return lfm::setError(LFM_ERR_INVALID, "invalid dimension " + std::to_string(p.dimension));
     if (p.rkOrder < 0 || p.rkOrder > 5) return lfm::setError(LFM_ERR_INVALID, "rkOrder must be 0..5");
-    if (p.renumber < LFM_RENUMBER_NONE || p.renumber > LFM_RENUMBER_HILBERT)
-        return lfm::setError(LFM_ERR_INVALID, "unknown renumbering (none, rcm or hilbert)");
+    if (p.renumber < LFM_RENUMBER_NONE || p.renumber > LFM_RENUMBER_HPATH)
+        return lfm::setError(LFM_ERR_INVALID, "unknown renumbering (none, rcm, hilbert or hpath)");
     return LFM_OK;
 }
 

@@ -80,8 +80,19 @@ SolverCase buildSolverCase(IMeshReader& r, const CaseParams& prm, const HaloLook
     const int64_t nc = subOffset.back();
     if (nc != r.getCellCount()) throw std::runtime_error("submesh split does not cover every cell");
     // locality order of the cells inside each submesh (the polyMesh keeps its own)
-    if (prm.renumber != RENUMBER_NONE)
+    if (prm.renumber == RENUMBER_HPATH) {
+        // one walk over the whole mesh; each submesh in the order of the walk
+        const std::vector<int> order = hpathCellOrder(r);
+        if (!order.empty()) {
+            std::vector<int> rank((size_t)r.getCellCount());
+            for (size_t i = 0; i < order.size(); ++i) rank[(size_t)order[i]] = (int)i;
+            for (int s = 0; s < nSub; ++s)
+                std::sort(subCells[(size_t)s].begin(), subCells[(size_t)s].end(),
+                          [&](int a, int b) { return rank[(size_t)a] < rank[(size_t)b]; });
+        }
+    } else if (prm.renumber != RENUMBER_NONE) {
         for (int s = 0; s < nSub; ++s) renumberCells(r, subCells[(size_t)s], prm.renumber, D);
+    }
     sc.nCells = nc;
     sc.nCells0 = nSub > 0 ? (int64_t)subCells[0].size() : 0;
     std::vector<int64_t> solverOf((size_t)nc), smOf((size_t)nc), localOf((size_t)nc);

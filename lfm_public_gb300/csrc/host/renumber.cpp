@@ -12,7 +12,8 @@ namespace lfm {
 int renumberFromName(const std::string& name) {
     if (name == "none" || name.empty()) return RENUMBER_NONE;
     if (name == "rcm" || name == "RCM") return RENUMBER_RCM;
-    if (name == "hilbert" || name == "hpath") return RENUMBER_HILBERT;
+    if (name == "hilbert") return RENUMBER_HILBERT;
+    if (name == "hpath") return RENUMBER_HPATH;
     return -1;
 }
 

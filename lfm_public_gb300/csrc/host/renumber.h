@@ -17,9 +17,9 @@
 
 namespace lfm {
 
-enum Renumber { RENUMBER_NONE = 0, RENUMBER_RCM = 1, RENUMBER_HILBERT = 2 };
+enum Renumber { RENUMBER_NONE = 0, RENUMBER_RCM = 1, RENUMBER_HILBERT = 2, RENUMBER_HPATH = 3 };
 
-// "none" / "rcm" / "hilbert" -> Renumber; -1 for anything else.
+// "none" / "rcm" / "hilbert" / "hpath" -> Renumber; -1 for anything else.
 int renumberFromName(const std::string& name);
 
 // Reorders `cells` (polyMesh labels of one submesh) in place.
@@ -30,6 +30,13 @@ int renumberFromName(const std::string& name);
 //   Hilbert: cells sorted along a Hilbert curve through their centres (2D
 //        on a 2^31 grid of the bounding box, 3D on 2^21 per axis).
 void renumberCells(IMeshReader& r, std::vector<int>& cells, int method, int dim);
+
+// The reference's Hamiltonian-path cell order over the whole mesh (its hpath
+// renumbering method, hpathRenumber/hpathRenumber.C:127-180; hpath.cpp):
+// order[i] = the polyMesh label of the i-th cell, boundary cells first. The
+// solver order of a submesh is its cells sorted by their position here.
+// Empty when the walk does not give a permutation of the cells.
+std::vector<int> hpathCellOrder(IMeshReader& r);
 
 // Bandwidth of an order: max |pos(a) - pos(b)| over faces between cells of
 // the list (for tests and diagnostics).

@@ -1,4 +1,5 @@
-"""Cell renumbering (reverse Cuthill-McKee, Hilbert) of the solver order.
+"""Cell renumbering (reverse Cuthill-McKee, Hilbert, the reference's
+Hamiltonian path) of the solver order.
 
 The polyMesh keeps its numbering; only the solver's cell order inside each
 submesh changes, so results are those of the polyMesh order up to the
@@ -39,7 +40,10 @@ def test_renumber_cells_is_a_relabelling(shuffled):
     np.testing.assert_allclose(vb, va[perm], rtol=1e-12)
 
 
-@pytest.mark.parametrize("method", [N.LFM_RENUMBER_RCM, N.LFM_RENUMBER_HILBERT])
+METHODS = [N.LFM_RENUMBER_RCM, N.LFM_RENUMBER_HILBERT, N.LFM_RENUMBER_HPATH]
+
+
+@pytest.mark.parametrize("method", METHODS)
 def test_renumbering_restores_locality(shuffled, method):
     c, cs, _ = shuffled
     base = _order_stats(N.CaseHandle.from_case(cs))
@@ -52,7 +56,7 @@ def test_renumbering_restores_locality(shuffled, method):
         assert bw <= 2 * 48, bw   # about one ring of the O-grid
 
 
-@pytest.mark.parametrize("method", [N.LFM_RENUMBER_RCM, N.LFM_RENUMBER_HILBERT])
+@pytest.mark.parametrize("method", METHODS)
 def test_renumbered_case_matches_oracle(shuffled, method):
     c, cs, _ = shuffled
     n = 10
@@ -82,7 +86,7 @@ def test_controldict_renumber_option(tmp_path, shuffled):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("method", [N.LFM_RENUMBER_RCM, N.LFM_RENUMBER_HILBERT])
+@pytest.mark.parametrize("method", METHODS)
 def test_renumbered_device_run_matches_oracle(shuffled, method):
     c, cs, _ = shuffled
     n = 10
@@ -103,7 +107,7 @@ def test_renumbered_device_run_matches_oracle(shuffled, method):
         assert np.all(err <= tol), (prec, err)
 
 
-@pytest.mark.parametrize("method", [N.LFM_RENUMBER_RCM, N.LFM_RENUMBER_HILBERT])
+@pytest.mark.parametrize("method", METHODS)
 @pytest.mark.parametrize("make", [lambda: cases.prism_case(n=6, nz=3, seed=8, solver=1),
                                   lambda: cases.tet_case(n=4, nz=3, seed=9, solver=0)], ids=["prisms", "tets"])
 def test_renumbered_3d_elements_match_oracle(make, method):
@@ -124,3 +128,54 @@ def test_renumbered_3d_elements_match_oracle(make, method):
     gb[:, b.cell_ids()] = qb
     err = rel_l2_vec(gb, ga, 3)
     assert np.all(err <= 1e-12), err
+
+
+def _consecutive_adjacent(ch):
+    """Fractions of consecutive solver cells that share a face, in the
+    boundary and in the interior submesh."""
+    d = ch.desc
+    nf, nc, n0 = d.n_faces, d.n_cells, d.n_cells0
+    fp = np.ctypeslib.as_array(d.face_p, shape=(nf,))
+    fn = np.ctypeslib.as_array(d.face_n, shape=(nf,))
+    m = fn < nc
+    adj = set(zip(np.minimum(fp[m], fn[m]).tolist(), np.maximum(fp[m], fn[m]).tolist()))
+
+    def frac(lo, hi):
+        return sum((i, i + 1) in adj for i in range(lo, hi - 1)) / max(1, hi - lo - 1)
+    return frac(0, n0), frac(n0, nc)
+
+
+@pytest.mark.parametrize("make", [
+    lambda: cases.vortex_case(n=32),
+    lambda: cases.cylinder_case(n_theta=48, n_r=24, r1=10, first=0.03, Ls=3),
+    lambda: cases.tri_case(n=12, seed=3),
+    lambda: cases.hybrid_case(n=10, seed=2),
+], ids=["quads", "o-grid", "triangles", "quads+triangles"])
+def test_hpath_order_is_a_hamiltonian_walk(make):
+    """The reference's hpath method (hpathRenumber/hpathRenumber.C:127-180)
+    orders the boundary cells as one walk and the interior cells as another,
+    the cells a walk had to skip following it: consecutive cells share a
+    face almost everywhere (a random order: almost nowhere)."""
+    c = make()
+    ch = N.CaseHandle.from_case(c, renumber=N.LFM_RENUMBER_HPATH)
+    assert sorted(ch.cell_ids().tolist()) == list(range(c.n_cells))
+    b, i = _consecutive_adjacent(ch)
+    assert b >= 0.9 and i >= 0.9, (b, i)
+    # from a randomly numbered polyMesh the interior walk is found as well;
+    # the boundary walk moves to the nearest boundary cell within ten rings,
+    # so on an O-grid (wall ring and outer ring 24 cells apart) it covers one
+    # ring and the other follows in polyMesh order, as in the reference
+    cs = cases.renumber_cells(c, np.random.default_rng(5).permutation(c.n_cells))
+    b2, i2 = _consecutive_adjacent(N.CaseHandle.from_case(cs, renumber=N.LFM_RENUMBER_HPATH))
+    assert i2 >= 0.9 and b2 >= 0.45, (b2, i2)
+
+
+def test_controldict_accepts_hpath(tmp_path, shuffled):
+    _, cs, _ = shuffled
+    root = str(tmp_path / "c")
+    cases.write_case(cs, root, n_steps=2)
+    cd = tmp_path / "c" / "system" / "controlDict"
+    cd.write_text(cd.read_text().replace("    doublePrecision true;", "    doublePrecision true;\n    renumber        hpath;"))
+    ch = N.CaseHandle.open(root)
+    b, i = _consecutive_adjacent(ch)
+    assert i >= 0.9 and b >= 0.45, (b, i)

@@ -792,18 +792,48 @@ def sweep_case(spec: dict) -> Case:
 _BANNER = "/* generated by lfm_public_gb300.cases */\n"
 
 
-def _header(cls: str, obj: str, location: str = "") -> str:
+def _header(cls: str, obj: str, location: str = "", binary: bool = False) -> str:
     loc = f'    location    "{location}";\n' if location else ""
-    return (_BANNER + "FoamFile\n{\n    version     2.0;\n    format      ascii;\n"
+    fmt = ('binary;\n    arch        "LSB;label=32;scalar=64";\n' if binary else "ascii;\n")
+    return (_BANNER + "FoamFile\n{\n    version     2.0;\n    format      " + fmt +
             f"    class       {cls};\n{loc}    object      {obj};\n}}\n\n")
+
+
+def _binary_list(f, arr: np.ndarray, n: int) -> None:
+    """An OpenFOAM binary list body: the count, then '(' raw bytes ')'
+    (little-endian; labels int32, scalars float64)."""
+    f.write(f"{n}\n(".encode())
+    f.write(np.ascontiguousarray(arr).tobytes())
+    f.write(b")\n")
 
 
 def _fmt(x: float) -> str:
     return repr(float(x))
 
 
-def write_polymesh(case: Case, d: str) -> None:
+def write_polymesh_binary(case: Case, d: str) -> None:
+    """The polyMesh in OpenFOAM's binary format (points, faceCompactList
+    faces, owner and neighbour as raw little-endian arrays)."""
     os.makedirs(d, exist_ok=True)
+    with open(os.path.join(d, "points"), "wb") as f:
+        f.write(_header("vectorField", "points", "constant/polyMesh", True).encode())
+        _binary_list(f, np.asarray(case.points, dtype="<f8"), case.points.shape[0])
+    with open(os.path.join(d, "faces"), "wb") as f:
+        f.write(_header("faceCompactList", "faces", "constant/polyMesh", True).encode())
+        _binary_list(f, np.asarray(case.face_offsets, dtype="<i4"), len(case.face_offsets))
+        _binary_list(f, np.asarray(case.face_points, dtype="<i4"), len(case.face_points))
+    for name, arr in (("owner", case.owner), ("neighbour", case.neighbour)):
+        with open(os.path.join(d, name), "wb") as f:
+            f.write(_header("labelList", name, "constant/polyMesh", True).encode())
+            _binary_list(f, np.asarray(arr, dtype="<i4"), arr.shape[0])
+
+
+def write_polymesh(case: Case, d: str, binary: bool = False) -> None:
+    os.makedirs(d, exist_ok=True)
+    if binary:
+        write_polymesh_binary(case, d)
+        _write_boundary(case, d)
+        return
     with open(os.path.join(d, "points"), "w") as f:
         f.write(_header("vectorField", "points", "constant/polyMesh"))
         f.write(f"{case.points.shape[0]}\n(\n")
@@ -823,6 +853,10 @@ def write_polymesh(case: Case, d: str) -> None:
         with open(os.path.join(d, name), "w") as f:
             f.write(_header("labelList", name, "constant/polyMesh"))
             f.write(f"{arr.shape[0]}\n(\n" + "\n".join(str(int(v)) for v in arr) + "\n)\n")
+    _write_boundary(case, d)
+
+
+def _write_boundary(case: Case, d: str) -> None:
     with open(os.path.join(d, "boundary"), "w") as f:
         f.write(_header("polyBoundaryMesh", "boundary", "constant/polyMesh"))
         f.write(f"{len(case.patches)}\n(\n")
@@ -844,9 +878,17 @@ def _boundary_block(case: Case) -> str:
     return out
 
 
-def write_field(case: Case, d: str, name: str, values: np.ndarray, dims: str) -> None:
+def write_field(case: Case, d: str, name: str, values: np.ndarray, dims: str, binary: bool = False) -> None:
     vec = values.ndim == 2
     cls = "volVectorField" if vec else "volScalarField"
+    if binary:
+        with open(os.path.join(d, name), "wb") as f:
+            f.write(_header(cls, name, "0", True).encode())
+            f.write(f"dimensions      {dims};\n\ninternalField   nonuniform List<{'vector' if vec else 'scalar'}> \n"
+                    .encode())
+            _binary_list(f, np.asarray(values, dtype="<f8"), values.shape[0])
+            f.write(("\n;\n\nboundaryField\n{" + _boundary_block(case) + "}\n").encode())
+        return
     with open(os.path.join(d, name), "w") as f:
         f.write(_header(cls, name, "0"))
         f.write(f"dimensions      {dims};\n\n")
@@ -859,11 +901,14 @@ def write_field(case: Case, d: str, name: str, values: np.ndarray, dims: str) ->
 
 
 def write_case(case: Case, root: str, n_steps: Optional[int] = None, write_interval: Optional[int] = None,
-               post: Optional[dict] = None, adjust_time_step: bool = False, max_co: float = 0.5) -> str:
+               post: Optional[dict] = None, adjust_time_step: bool = False, max_co: float = 0.5,
+               binary: bool = False) -> str:
     """Writes ``case`` as an OpenFOAM case directory under ``root``. ``post``
     sets lfm/post entries of controlDict (haveAverage, tStartAverage,
     haveForces, saveForcesStep, printInfoFreq, ...); ``adjust_time_step`` and
-    ``max_co`` its adjustTimeStep and maxCo (endTime stays n_steps x deltaT)."""
+    ``max_co`` its adjustTimeStep and maxCo (endTime stays n_steps x deltaT);
+    ``binary`` writes the polyMesh and the initial fields in OpenFOAM's binary
+    format and sets writeFormat binary."""
     pe = {"haveProbes": "false", "haveSampling": "false", "haveAverage": "false", "haveForces": "false",
           "haveResiduals": "true" if case.residuals else "false", "printInfoFreq": str(case.print_freq),
           "saveResiduals": "false", "saveBlendFactor": "false"}
@@ -874,13 +919,13 @@ def write_case(case: Case, root: str, n_steps: Optional[int] = None, write_inter
     os.makedirs(root, exist_ok=True)
     for sub in ("system", "constant", "0"):
         os.makedirs(os.path.join(root, sub), exist_ok=True)
-    write_polymesh(case, os.path.join(root, "constant", "polyMesh"))
+    write_polymesh(case, os.path.join(root, "constant", "polyMesh"), binary=binary)
     z = os.path.join(root, "0")
-    write_field(case, z, "p", case.fields["p"], "[1 -1 -2 0 0 0 0]")
-    write_field(case, z, "T", case.fields["T"], "[0 0 0 1 0 0 0]")
-    write_field(case, z, "U", case.fields["U"], "[0 1 -1 0 0 0 0]")
+    write_field(case, z, "p", case.fields["p"], "[1 -1 -2 0 0 0 0]", binary)
+    write_field(case, z, "T", case.fields["T"], "[0 0 0 1 0 0 0]", binary)
+    write_field(case, z, "U", case.fields["U"], "[0 1 -1 0 0 0 0]", binary)
     if "alpha" in case.fields:
-        write_field(case, z, "alpha", case.fields["alpha"], "[0 1 0 0 0 0 0]")
+        write_field(case, z, "alpha", case.fields["alpha"], "[0 1 0 0 0 0 0]", binary)
     end = case.delta_t * n_steps
     with open(os.path.join(root, "system", "controlDict"), "w") as f:
         f.write(_header("dictionary", "controlDict", "system"))
@@ -888,7 +933,7 @@ def write_case(case: Case, root: str, n_steps: Optional[int] = None, write_inter
                 "    post\n    {\n" + "".join(f"        {k:<15} {v};\n" for k, v in pe.items()) + "    }\n}\n\n")
         f.write(f"startFrom       startTime;\nstartTime       0;\nstopAt          endTime;\n"
                 f"endTime         {_fmt(end)};\ndeltaT          {_fmt(case.delta_t)};\n"
-                f"writeControl    timeStep;\nwriteInterval   {wi};\nwriteFormat     ascii;\n"
+                f"writeControl    timeStep;\nwriteInterval   {wi};\nwriteFormat     {'binary' if binary else 'ascii'};\n"
                 f"writePrecision  {case.write_precision};\ntimeFormat      general;\ntimePrecision   12;\n"
                 f"adjustTimeStep  {'yes' if adjust_time_step else 'no'};\nmaxCo           {_fmt(max_co)};\n")
     with open(os.path.join(root, "system", "fvSchemes"), "w") as f:
@@ -934,7 +979,17 @@ def read_result_fields(root: str, names=("rho", "E", "p", "U")):
 
 
 def _read_internal_field(path: str) -> np.ndarray:
-    txt = open(path).read()
+    raw = open(path, "rb").read()
+    head = raw[:raw.index(b"internalField")].decode(errors="replace")
+    if "binary" in head.split("}", 1)[0]:
+        # nonuniform List<...> N ( raw little-endian float64 )
+        i = raw.index(b"internalField")
+        j = raw.index(b"(", i)
+        n = int(raw[i:j].split()[-1])
+        width = 3 if b"List<vector>" in raw[i:j] else 1
+        vals = np.frombuffer(raw[j + 1:j + 1 + 8 * n * width], dtype="<f8").copy()
+        return vals.reshape(n, 3) if width == 3 else vals
+    txt = raw.decode()
     i = txt.index("internalField")
     rest = txt[i:]
     if "nonuniform" not in rest.split("\n", 1)[0]:

@@ -314,13 +314,19 @@ static void readBinaryPayload(Tokenizer& tk, void* dst, size_t bytes) {
 static std::vector<int64_t> readLabelListBody(Tokenizer& tk, const Header& h) {
     const long long n = readListCount(tk);
     std::vector<int64_t> out((size_t)n);
-    Token t = tk.peek();
-    if (t.kind == Token::PUNCT && t.punct == '{') {
-        tk.next();
-        const long long v = tk.readInteger();
-        tk.expectPunct('}');
-        for (auto& x : out) x = v;
-        return out;
+    // the uniform form N{value}; looked for in the buffer itself, since a
+    // peeked token would consume the '(' that opens a binary payload
+    {
+        const std::string& b = tk.buffer();
+        size_t p = tk.position();
+        while (p < b.size() && std::isspace((unsigned char)b[p])) ++p;
+        if (p < b.size() && b[p] == '{') {
+            tk.expectPunct('{');
+            const long long v = tk.readInteger();
+            tk.expectPunct('}');
+            for (auto& x : out) x = v;
+            return out;
+        }
     }
     if (h.format == "binary") {
         if (h.labelBytes == 4) {

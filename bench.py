@@ -109,15 +109,16 @@ DRAM_TRAFFIC = {
     # which grow in proportion
     ("cylinder3d_small", "fp32", "k_flux"): 280696832 + 52857856,
     ("cylinder3d", "fp32", "k_flux"): 8 * (280696832 + 52857856),
-    ("cylinder2d", "fp64", "k_flux"): 95860992 + 7875328,
+    ("cylinder2d", "fp64", "k_flux"): 95838720 + 8762112,
 }
 
 # FP64 pipe thread-instructions per cell of one launch of each kernel of the
 # plain FP64 path (DFMA, DMUL, DADD and the FP64 parts of divisions and square
 # roots), counted by ncu (sm__thread_inst_executed_pipe_fp64_pred_on.sum /
-# cells) on the 768x512 cylinder, M1, viscous.
+# cells) on the 768x512 cylinder, M1, viscous; the update also derives the next
+# stage's primitives and boundary ghosts (no preparation kernel).
 FP64_INST_PER_CELL = {
-    "cylinder2d": {"k_prep": 22.19, "k_grad": 0.0, "k_vis": 85.00, "k_flux": 202.26, "k_update": 34.31},
+    "cylinder2d": {"k_prep": 0.0, "k_grad": 0.0, "k_vis": 63.00, "k_flux": 156.22, "k_update": 46.67},
 }
 # FP64 pipe instruction rate: the measured DFMA rate (FP64_PEAK_TFLOPS counts
 # an FMA as two operations) in instructions per second.

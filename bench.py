@@ -156,10 +156,10 @@ def kernel_bytes(dim: int, faces_per_cell: int, fp32: bool, scheme: str, viscous
     csr = 4 + 4 * faces_per_cell          # cell -> face offsets and list
     face_basic = 8 + (dim + 1) * w        # fP, fN, S, w
     b = {}
-    # FP32-bulk: the update writes the next stage's primitives of its cell and
-    # of its boundary ghosts, so the preparation pass only covers processor
-    # halos (none in a single-partition case)
-    b["k_prep"] = 0.0 if fp32 else nq * 8 + prim * w
+    # the update writes the next stage's primitives of its cell and of its
+    # boundary ghosts, so the preparation pass only covers processor halos
+    # (none in a single-partition case)
+    b["k_prep"] = 0.0
     b["k_grad"] = (prim * w + fpc * face_basic + csr + ng * w) if scheme == "M2AUSM" else 0.0
     b["k_vis"] = ((dim + 1) * w + fpc * face_basic + csr + nv * w) if (viscous or scheme == "M2AUSM") else 0.0
     flux_cell = (prim - 1) * w + (0 if fp32 else nq * 8)   # FP64 also reads q
@@ -171,8 +171,8 @@ def kernel_bytes(dim: int, faces_per_cell: int, fp32: bool, scheme: str, viscous
     b["k_flux"] = flux_cell + fpc * flux_face
     if fp32:   # q' read + written (FP64), dq read + written (FP32), 1/V, sigma, primitives out
         b["k_update"] = csr + fpc * nq * w + 2 * nq * 8 + 2 * nq * 4 + 8 + prim * 4
-    else:      # q and dq read + written, 1/V, sigma
-        b["k_update"] = csr + fpc * nq * w + 4 * nq * 8 + 16
+    else:      # q and dq read + written, 1/V, sigma, primitives out (the sound speed for M2AUSM only)
+        b["k_update"] = csr + fpc * nq * w + 4 * nq * 8 + 16 + (prim - (0 if scheme == "M2AUSM" else 1)) * 8
     if fp32:
         # the fused tile stage does the work of the gradient, viscous, flux and
         # update kernels: the same algorithmic bytes (its intermediate arrays
@@ -534,7 +534,7 @@ def run_gpu(args):
                 "sample": f"1 time step (5 RK stages) of the full {desc['cells']}-cell mesh, single thread, {t:.1f} s"}
 
     case = workload(args.workload)
-    ch = N.CaseHandle.from_case(case, renumber={"none": 0, "rcm": 1, "hilbert": 2}[args.renumber])
+    ch = N.CaseHandle.from_case(case, renumber={"none": 0, "rcm": 1, "hilbert": 2, "hpath": 3}[args.renumber])
     nc, stages = ch.desc.n_cells, ch.desc.rk_order
     dt = case.delta_t
     hbm, peak_src = _peaks()
@@ -966,7 +966,7 @@ def main():
     ap.add_argument("--serve-arena-gb", type=float, default=32.0)
     ap.add_argument("--serve-chunk", type=int, default=50)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--renumber", default="none", choices=["none", "rcm", "hilbert"],
+    ap.add_argument("--renumber", default="none", choices=["none", "rcm", "hilbert", "hpath"],
                     help="solver order of the cells (single-case workloads)")
     args = ap.parse_args()
     if args.accuracy_steps is None:

@@ -263,15 +263,38 @@ __device__ __forceinline__ void update_cell(const Args<T>& a, int c, double Ak, 
     T sum[NQ];
 #pragma unroll
     for (int v = 0; v < NQ; ++v) sum[v] = T(0);
-    for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
-        const int code = a.cfList[e];
-        if (code >= 0) {
+    const int e0 = a.cfOff[c], e1 = a.cfOff[c + 1];
+    constexpr int W = kEllWidth<D>;
+    if (e1 - e0 <= W) {
+        // every face index of the cell, then every rhs value, in flight at
+        // once; summed in the same (ascending face) order as the loop below
+        int code[W];
 #pragma unroll
-            for (int v = 0; v < NQ; ++v) sum[v] += a.flux[v * nf + code];
-        } else {
-            const int f = ~code;
+        for (int k = 0; k < W; ++k) code[k] = e0 + k < e1 ? a.cfList[e0 + k] : kEllPad;
+        T fl[W][NQ];
 #pragma unroll
-            for (int v = 0; v < NQ; ++v) sum[v] -= a.flux[v * nf + f];
+        for (int k = 0; k < W; ++k) {
+            const int f = code[k] >= 0 ? code[k] : ~code[k];
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) fl[k][v] = code[k] != kEllPad ? a.flux[v * nf + f] : T(0);
+        }
+#pragma unroll
+        for (int k = 0; k < W; ++k) {
+            if (code[k] == kEllPad) continue;
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) sum[v] = code[k] >= 0 ? sum[v] + fl[k][v] : sum[v] - fl[k][v];
+        }
+    } else {
+        for (int e = e0; e < e1; ++e) {
+            const int code = a.cfList[e];
+            if (code >= 0) {
+#pragma unroll
+                for (int v = 0; v < NQ; ++v) sum[v] += a.flux[v * nf + code];
+            } else {
+                const int f = ~code;
+#pragma unroll
+                for (int v = 0; v < NQ; ++v) sum[v] -= a.flux[v * nf + f];
+            }
         }
     }
     double acc[NQ];

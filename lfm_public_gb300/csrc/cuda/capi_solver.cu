@@ -211,10 +211,9 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
         // no face (calc_VIS_Smagorinsky, src/cfd_v0.cpp:1596-1737)
         std::vector<double> cf((size_t)s->nc);
         for (int64_t c = 0; c < s->nc; ++c) {
-            int64_t last = -1;
-            for (int64_t e = d->cell_face_offsets[c]; e < d->cell_face_offsets[c + 1]; ++e)
-                last = std::max<int64_t>(last, d->cell_faces[e]);
-            cf[(size_t)c] = d->smag_c[last >= 0 ? d->face_p[last] : c];
+            // a cell's entries are in processing order: the last is its last face
+            const int64_t e0 = d->cell_face_offsets[c], e1 = d->cell_face_offsets[c + 1];
+            cf[(size_t)c] = d->smag_c[e1 > e0 ? d->face_p[d->cell_faces[e1 - 1]] : c];
         }
         if ((rc = uploadAs<T>(s, &p, cf.data(), cf.size()))) return rc;
         a.smagC = p;
@@ -417,6 +416,9 @@ int tileCellsOption() {
     return e ? atoi(e) : kTileCells;
 }
 
+// Faces stored by owned-face slot (orderFacesBySlot), by dimension.
+constexpr bool kFaceOrderBySlot3D = false;
+
 // Fused flux + update stages (LFM_FLUX_UPDATE=0/1 in the environment
 // overrides for a solver created afterwards). Measured on GB300, FP32-bulk,
 // per step: the 256 x 256 inviscid M1 vortex 0.075 -> 0.070 ms; the 768 x 512
@@ -431,6 +433,79 @@ bool fluxUpdateOption(const lfm_solver* s) {
     return s->D == 2 && !s->needVis && s->scheme != LFM_SOLVER_M2AUSM;
 }
 
+// Device storage order of the flux faces. The description lists them in the
+// reference's processing order, cell by cell: face f is the k-th face that
+// its cell P owns (k = its slot). Stored by slot instead -- every cell's
+// first owned face, then every cell's second, ... -- the threads of a warp in
+// the flux kernel read 32 consecutive cells on the P side and, on a
+// structured mesh, 32 consecutive cells on the N side, and every face array
+// in whole lines. Each face's rhs is the same value in either order and each
+// cell still sums its faces in processing order (the entries of its face
+// list keep their order, only the indices are renamed), so results keep
+// their bits. LFM_FACE_ORDER=processing|slot in the environment overrides
+// the default for a solver created afterwards.
+struct FaceOrder {
+    lfm_solver_desc desc{};
+    std::vector<int64_t> faceP, faceN, cellFaces;
+    std::vector<uint8_t> ghost;
+    std::vector<double> S, dv, w, smag, dinv, dnorm, dmag, K;
+};
+
+bool faceOrderBySlot(const lfm_solver_desc* d) {
+    if (tileCellsOption() > 0) return false;   // the tiles are cut from the processing order
+    const char* e = getenv("LFM_FACE_ORDER");
+    if (e) return std::string(e) == "slot";
+    return kFaceOrderBySlot3D && d->dim == 3;
+}
+
+// fo.desc = *d with the faces in slot order.
+void orderFacesBySlot(const lfm_solver_desc* d, FaceOrder& fo) {
+    const size_t nf = (size_t)d->n_faces, D = (size_t)d->dim;
+    std::vector<int> slot(nf, 0);
+    for (size_t f = 1; f < nf; ++f) slot[f] = d->face_p[f] == d->face_p[f - 1] ? slot[f - 1] + 1 : 0;
+    std::vector<int64_t> order(nf);   // new position -> original face
+    for (size_t f = 0; f < nf; ++f) order[f] = (int64_t)f;
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return slot[(size_t)a] < slot[(size_t)b]; });
+    std::vector<int64_t> pos(nf);     // original face -> new position
+    for (size_t i = 0; i < nf; ++i) pos[(size_t)order[i]] = (int64_t)i;
+    auto perm1 = [&](const auto* src, auto& dst) {
+        dst.resize(nf);
+        for (size_t i = 0; i < nf; ++i) dst[i] = src[order[i]];
+    };
+    auto permD = [&](const double* src, std::vector<double>& dst) {
+        dst.resize(D * nf);
+        for (size_t k = 0; k < D; ++k)
+            for (size_t i = 0; i < nf; ++i) dst[k * nf + i] = src[k * nf + (size_t)order[i]];
+    };
+    perm1(d->face_p, fo.faceP);
+    perm1(d->face_n, fo.faceN);
+    perm1(d->face_ghost, fo.ghost);
+    permD(d->S, fo.S);
+    permD(d->d, fo.dv);
+    perm1(d->w, fo.w);
+    perm1(d->smag, fo.smag);
+    perm1(d->dmag_inv, fo.dinv);
+    permD(d->dnorm, fo.dnorm);
+    perm1(d->delta_mag, fo.dmag);
+    permD(d->K, fo.K);
+    const size_t ne = (size_t)d->cell_face_offsets[d->n_cells];
+    fo.cellFaces.resize(ne);
+    for (size_t e = 0; e < ne; ++e) fo.cellFaces[e] = pos[(size_t)d->cell_faces[e]];
+    fo.desc = *d;
+    fo.desc.face_p = fo.faceP.data();
+    fo.desc.face_n = fo.faceN.data();
+    fo.desc.face_ghost = fo.ghost.data();
+    fo.desc.S = fo.S.data();
+    fo.desc.d = fo.dv.data();
+    fo.desc.w = fo.w.data();
+    fo.desc.smag = fo.smag.data();
+    fo.desc.dmag_inv = fo.dinv.data();
+    fo.desc.dnorm = fo.dnorm.data();
+    fo.desc.delta_mag = fo.dmag.data();
+    fo.desc.K = fo.K.data();
+    fo.desc.cell_faces = fo.cellFaces.data();
+}
+
 // Creates a solver; `stream` (not owned) is shared by the partitions of a
 // decomposed case, which alone may carry processor-face halos.
 int createSolver(const lfm_solver_desc* d, const lfm_solver_opts* opts, cudaStream_t stream, lfm_solver** out) {
@@ -438,6 +513,11 @@ int createSolver(const lfm_solver_desc* d, const lfm_solver_opts* opts, cudaStre
     *out = nullptr;
     int rc = lfm::setup::validateDesc(d);
     if (rc) return rc;
+    FaceOrder faceOrder;
+    if (faceOrderBySlot(d)) {
+        orderFacesBySlot(d, faceOrder);
+        d = &faceOrder.desc;
+    }
     if (d->n_halos > 0 && !stream)
         return lfm::setError(LFM_ERR_INVALID, "a partition with processor-face halos runs in an lfm_partitioned");
     lfm_solver* s = new lfm_solver;

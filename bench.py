@@ -700,7 +700,7 @@ def run_batch(args):
         ba = N.Batch(device=local, arena_bytes=need + (64 << 20), max_cases=n_cases)
         sa = [ba.add(ch, c.delta_t) for c, ch in built]
         ba.step(n_acc)
-        errs, diverged64, diverged32 = [], [], []
+        errs, diverged64, diverged32, per_case = [], [], [], []
         for k, ((c, ch), s) in enumerate(zip(built, sa)):
             s64 = N.Solver(ch, precision=N.LFM_FP64, device=local)
             s64.step(n_acc, c.delta_t)
@@ -714,11 +714,20 @@ def run_batch(args):
                 diverged32.append(k)
             if f64 and f32:
                 errs.append(acoustics.acoustic_rel_l2(q32, q64, ch.desc.gamma, c.dim, c.p_inf))
+                # growth of the FP64 run's p' rms over the steps: a case on its
+                # way to the divergence above amplifies every difference
+                p0 = acoustics.pressure(ch.q0(), ch.desc.gamma, c.dim) - c.p_inf
+                p1 = acoustics.pressure(q64, ch.desc.gamma, c.dim) - c.p_inf
+                growth = float(np.sqrt(np.mean(p1 ** 2)) / max(np.sqrt(np.mean(p0 ** 2)), 1e-300))
+                per_case.append({"case": k, "kind": spec[k]["kind"], "cells": ch.desc.n_cells,
+                                 "scheme": "M1" if spec[k]["solver"] == 0 else "M2", "p_rel_l2": errs[-1],
+                                 "p_rms_growth": growth})
         ba.close()
         accuracy = {"acoustic_p_rel_l2_max": max(errs) if errs else None,
                     "acoustic_p_rel_l2_median": float(np.median(errs)) if errs else None,
+                    "cases_within_1e-3": int(sum(e <= 1e-3 for e in errs)),
                     "steps": n_acc, "cases_compared": len(errs),
-                    "diverged_fp64": diverged64, "diverged_fp32_bulk": diverged32,
+                    "diverged_fp64": diverged64, "diverged_fp32_bulk": diverged32, "per_case": per_case,
                     "against": "each case's own FP64 device run (within 1e-12 of the oracle), same steps"}
 
     if rank != 0:
@@ -858,7 +867,7 @@ def run_serve(args):
     arena = int(args.serve_arena_gb * (1 << 30))
     for ri, rate in enumerate(float(x) for x in args.serve_rates.split(",")):
         stream = serve_stream(rate, window, len(lib), args.serve_step_scale, 77 + ri)
-        srv = N.Server(device=local, arena_bytes=arena, chunk_steps=args.serve_chunk)
+        srv = N.Server(device=local, arena_bytes=arena, chunk_steps=args.serve_chunk, max_cases=args.serve_slots)
         ids, shed, depth = {}, [], []
         t_start = time.perf_counter() + 0.2
         # times of the server clock (seconds since its creation) are read
@@ -928,7 +937,8 @@ def run_serve(args):
         "dtype": "f32-flux/f64-rk", "data": "synthetic (generated meshes and initial fields)",
         "config": {"workload": SERVE_DESC, "library_cases": len(lib), "library_cells": int(sum(cells)),
                    "step_scale": args.serve_step_scale, "arena_gb": args.serve_arena_gb,
-                   "chunk_steps": args.serve_chunk, "rates": args.serve_rates, "window_s": window,
+                   "chunk_steps": args.serve_chunk, "slots": args.serve_slots, "rates": args.serve_rates,
+                   "window_s": window,
                    "client_queue_bound": args.serve_queue},
         "serving": per_rate,
         "fp64_serial_note": "FP64 server: the same streams first come first served, one request at a time, the "
@@ -965,6 +975,8 @@ def main():
     ap.add_argument("--serve-step-scale", type=float, default=1.0, help="scales the U(200,5000) step counts")
     ap.add_argument("--serve-arena-gb", type=float, default=32.0)
     ap.add_argument("--serve-chunk", type=int, default=50)
+    ap.add_argument("--serve-slots", type=int, default=8,
+                    help="requests on the GPU at once (the server admits by arena footprint up to this many)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--renumber", default="none", choices=["none", "rcm", "hilbert", "hpath"],
                     help="solver order of the cells (single-case workloads)")

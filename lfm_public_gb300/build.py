@@ -28,8 +28,8 @@ INCLUDES = [os.path.join(ROOT, "include"), os.path.join(ROOT, "include", "lfm"),
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_SOURCES = ["foam_io.cpp", "foam_case.cpp", "dict_reader.cpp", "poly_mesh_reader.cpp", "run_time_manager.cpp",
                 "input_reader.cpp", "renumber.cpp", "hpath.cpp", "case_setup.cpp", "tiles.cpp", "capi_case.cpp"]
-CUDA_SOURCES = ["solver_kernels.cu", "solver_kernels_fp32.cu", "batch_kernels.cu", "tile_kernels.cu", "post_kernels.cu",
-                "capi_solver.cu", "capi_batch.cu", "capi_server.cu"]
+CUDA_SOURCES = ["solver_kernels.cu", "solver_kernels_fp32.cu", "flux_staged_fp32.cu", "batch_kernels.cu",
+                "tile_kernels.cu", "post_kernels.cu", "capi_solver.cu", "capi_batch.cu", "capi_server.cu"]
 CLI_SOURCES = ["gpu_mesh.cpp", "lfm_solve_gpu.cpp"]
 # The FP32-bulk kernels are compiled without implicit FMA contraction (explicit
 # fmaf/fma calls stay fused): every kernel that inlines the same device
@@ -37,7 +37,8 @@ CLI_SOURCES = ["gpu_mesh.cpp", "lfm_solve_gpu.cpp"]
 # single-case solver, in any batch-kernel variant and in any mix of cases.
 # The post-processing kernels follow the reference's CPU arithmetic, which is
 # not contracted either.
-CUDA_FLAGS = {"solver_kernels_fp32.cu": ["-fmad=false"], "batch_kernels.cu": ["-fmad=false"],
+CUDA_FLAGS = {"solver_kernels_fp32.cu": ["-fmad=false"], "flux_staged_fp32.cu": ["-fmad=false"],
+              "batch_kernels.cu": ["-fmad=false"],
               "tile_kernels.cu": ["-fmad=false"], "post_kernels.cu": ["-fmad=false"]}
 
 LIB = os.path.join(PKG, "liblfm_gpu.so")

@@ -86,6 +86,8 @@ struct lfm_solver {
     // fused flux + update stages (FP32-bulk single case): two primitive
     // buffers alternate like the tile stages'
     bool fluxUpdate = false;
+    // FP32-bulk staged flux kernel (stages 0: the plain flux kernel)
+    lfm::dev::FluxStaging fluxStaging;
     cudaGraphExec_t graphOdd = nullptr;   // the step graph starting from prim1
     // the non-finite flag's host copy (page-locked: read after one stream sync)
     int* flagHost = nullptr;
@@ -171,6 +173,7 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
     a.flag = s->flag;
     a.cellGhosts = nullptr;
     a.cfEll = nullptr;
+    a.fOwn = nullptr;
     a.smagC = nullptr;
     a.wN = nullptr;
     a.cfSo = nullptr;
@@ -264,6 +267,7 @@ StageConfig stageConfig(const lfm_solver* s, int k, double dt) {
     c.first = (k == 0);
     c.withRes = (s->residuals && k == 0) ? 1 : 0;
     c.fullPrep = false;   // FP32-bulk: cells' primitives come from the previous update
+    if (s->precision == LFM_FP32_BULK) c.fluxStaging = s->fluxStaging;
     return c;
 }
 
@@ -431,6 +435,37 @@ bool fluxUpdateOption(const lfm_solver* s) {
     const char* e = getenv("LFM_FLUX_UPDATE");
     if (e) return atoi(e) != 0;
     return s->D == 2 && !s->needVis && s->scheme != LFM_SOLVER_M2AUSM;
+}
+
+// Cell-centred flux kernel (flux32_cell), on for 3D cases. Measured on
+// GB300, FP32-bulk M2, per step: the 9.4M-cell wake's flux 3.42 -> 3.27 ms
+// (the step 6.97 -> 6.82), the 1.18M-cell wake's 0.445 -> 0.416; the 768 x 512
+// M1 cylinder's 0.068 -> 0.085 (a 2D cell owns two faces, too few to repay
+// the registers it keeps). LFM_FLUX_CELL=0/1 in the environment overrides
+// for a solver created afterwards.
+bool fluxCellOption(const lfm_solver* s) {
+    const char* e = getenv("LFM_FLUX_CELL");
+    return e ? atoi(e) != 0 : s->D == 3;
+}
+
+// Staged flux kernel (flux_staged_fp32.cu): shared-memory buffers per
+// thread (the staging depth; 0 = the plain or cell-centred flux kernel, 1 =
+// the slot form) and faces per block. Off: measured slower in every
+// configuration (flux_staged_fp32.cu gives the numbers).
+// LFM_FLUX_STAGES=<0..4> and LFM_FLUX_FACES=<32..256> in the environment
+// override the defaults for a solver created afterwards.
+constexpr int kFluxStages = 0;
+constexpr int kFluxFaces = 128;
+
+lfm::dev::FluxStaging fluxStagingOption(const lfm_solver* s) {
+    (void)s;
+    lfm::dev::FluxStaging fs;
+    const char* e = getenv("LFM_FLUX_STAGES");
+    fs.stages = e ? atoi(e) : kFluxStages;
+    if (fs.stages < 1 || fs.stages > 4) fs.stages = 0;
+    const char* f = getenv("LFM_FLUX_FACES");
+    fs.faces = f ? atoi(f) : kFluxFaces;
+    return fs;
 }
 
 // Device storage order of the flux faces. The description lists them in the
@@ -694,6 +729,32 @@ int createSolver(const lfm_solver_desc* d, const lfm_solver_opts* opts, cudaStre
         fluxUpdateOption(s)) {
         if ((rc = devAlloc(s, &s->prim1, (size_t)lfm::dev::primRows<float>(s->D) * nt))) return fail(rc);
         s->fluxUpdate = true;
+    }
+    // cell-centred flux kernel: FP32-bulk M1 / M2 laminar cases with separate
+    // flux and update kernels, faces stored by owner (the description's order)
+    if (s->precision == LFM_FP32_BULK && !tiled && !s->fluxUpdate && !d->smag_c &&
+        s->scheme != LFM_SOLVER_M2AUSM && fluxCellOption(s)) {
+        bool byOwner = true;
+        for (size_t f = 1; f < nf && byOwner; ++f) byOwner = fP[f] >= fP[f - 1];
+        if (byOwner) {
+            std::vector<int> own(nc + 1, 0);
+            for (size_t f = 0; f < nf; ++f) ++own[(size_t)fP[f] + 1];
+            for (size_t c = 0; c < nc; ++c) own[c + 1] += own[c];
+            int* dOwn = nullptr;
+            if ((rc = upload(s, &dOwn, own.data(), nc + 1))) return fail(rc);
+            s->a32.fOwn = dOwn;
+        }
+    }
+    // staged flux kernel: FP32-bulk cases with separate flux and update
+    // kernels, M1 / M2, laminar
+    if (s->precision == LFM_FP32_BULK && !tiled && !s->fluxUpdate && !d->smag_c &&
+        lfm::dev::flux_staging_supported(s->scheme, false)) {
+        lfm::dev::FluxStaging fs = fluxStagingOption(s);
+        if (fs.stages > 0) {
+            if ((e = lfm::dev::configure_flux_staging(s->D, s->scheme, s->nf, fs)) != cudaSuccess)
+                return fail(cudaFail(e, "configure_flux_staging"));
+            s->fluxStaging = fs;
+        }
     }
     if (s->precision == LFM_FP32_BULK) {
         for (int v = 0; v < s->nq; ++v) s->qRef[v] = s->a32.qRef[v];

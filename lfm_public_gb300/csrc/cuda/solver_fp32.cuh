@@ -464,13 +464,16 @@ __device__ __forceinline__ float p5diff_dd(float a, float b, float alpha) {
 // flux kernel (3D flux 4.05 -> 3.43 ms per step on the 9.4M-cell wake, whose
 // gathers come from HBM; 2 % in 2D, whose gathers hit L2). The fused kernels,
 // whose registers other phases already fill, keep the late loads.
-template <int D, int SCH, bool VIS = true, bool LES = false, bool EARLYV = false>
-__device__ __forceinline__ void face_rhs32(const Args<float>& a, int f, float* rhs) {
-    constexpr int NQ = D + 2;
+//
+// face_rhs32_cells takes the face's cells i (P) and j (N) as arguments and
+// reads every array through `a`: the solver's Args, or a view of the same
+// rows staged in shared memory (the staged flux kernel, flux_staged_fp32.cu),
+// which gives the same bits because only the addresses differ.
+template <int D, int SCH, bool VIS, bool LES, bool EARLYV, class A>
+__device__ __forceinline__ void face_rhs32_cells(const A& a, int f, int i, int j, float* rhs) {
     using P = PRow<D>;
     const RefState32& R = a.ref;
     const size_t nt = (size_t)a.nt, nf = (size_t)a.nf;
-    const int i = a.fP[f], j = a.fN[f];
     const float w = a.w[f];
     float S[D];
 #pragma unroll
@@ -688,12 +691,80 @@ __device__ __forceinline__ void face_rhs32(const Args<float>& a, int f, float* r
 }
 
 template <int D, int SCH, bool VIS = true, bool LES = false, bool EARLYV = false>
+__device__ __forceinline__ void face_rhs32(const Args<float>& a, int f, float* rhs) {
+    face_rhs32_cells<D, SCH, VIS, LES, EARLYV>(a, f, a.fP[f], a.fN[f], rhs);
+}
+
+template <int D, int SCH, bool VIS = true, bool LES = false, bool EARLYV = false>
 __device__ __forceinline__ void flux32(const Args<float>& a, int f) {
     float rhs[D + 2];
     face_rhs32<D, SCH, VIS, LES, EARLYV>(a, f, rhs);
     const size_t nf = (size_t)a.nf;
 #pragma unroll
     for (int v = 0; v < D + 2; ++v) a.flux[(size_t)v * nf + f] = rhs[v];
+}
+
+// ---------------------------------------------------------------------------
+// flux32_cell: the rhs of the faces cell c owns (it is their P side), one
+// after another in face order. The cell's own primitive and viscous rows are
+// read once, into registers, for all its faces (a face-per-thread kernel
+// reads them once per face); the cell across each face is read per face, its
+// index one face ahead. face_rhs32_cells sees the rows through a view of the
+// registers (side 0 = P, 1 = N), so the rhs keeps flux32's bits. M1 / M2
+// without the LES terms (whose extra rows the view does not carry).
+// ---------------------------------------------------------------------------
+template <int D>
+struct CellFaceView32 {
+    const RefState32& ref;
+    float prim[2 * (2 * D + 2)];   // [row][side]: rho', m'[D], u'[D], R psi'
+    float V[2 * kVisRows<D>];      // [row][side]: dudx, dTdx, sigmaU
+    const float *S, *d, *w, *K, *lapc, *dinv, *dnorm;
+    const uint8_t* fGhost;
+    const float *grad, *smagC;
+    int nt, nf;
+};
+
+template <int D, int SCH>
+__device__ __forceinline__ void flux32_cell(const Args<float>& a, int c) {
+    static_assert(SCH != kSchemeAUSM, "the cell-centred flux carries no sound speed or gradients");
+    const int f0 = a.fOwn[c], f1 = a.fOwn[c + 1];
+    if (f0 >= f1) return;
+    const size_t nt = (size_t)a.nt, nf = (size_t)a.nf;
+    CellFaceView32<D> v{a.ref};
+    v.S = a.S;
+    v.d = a.d;
+    v.w = a.w;
+    v.K = a.K;
+    v.lapc = a.lapc;
+    v.dinv = a.dinv;
+    v.dnorm = a.dnorm;
+    v.fGhost = a.fGhost;
+    v.grad = nullptr;
+    v.smagC = nullptr;
+    v.nt = 2;
+    v.nf = a.nf;
+    const bool vis = a.ref.mu != 0.0f;
+#pragma unroll
+    for (int r = 0; r < 2 * D + 2; ++r) v.prim[2 * r] = a.prim[(size_t)r * nt + c];
+    if (vis) {
+#pragma unroll
+        for (int r = 0; r < kVisRows<D>; ++r) v.V[2 * r] = a.V[(size_t)r * nt + c];
+    }
+    int jn = a.fN[f0];
+    for (int f = f0; f < f1; ++f) {
+        const int j = jn;
+        if (f + 1 < f1) jn = a.fN[f + 1];
+#pragma unroll
+        for (int r = 0; r < 2 * D + 2; ++r) v.prim[2 * r + 1] = a.prim[(size_t)r * nt + j];
+        if (vis && !a.fGhost[f]) {
+#pragma unroll
+            for (int r = 0; r < kVisRows<D>; ++r) v.V[2 * r + 1] = a.V[(size_t)r * nt + j];
+        }
+        float rhs[D + 2];
+        face_rhs32_cells<D, SCH, true, false, false>(v, f, 0, 1, rhs);
+#pragma unroll
+        for (int q = 0; q < D + 2; ++q) a.flux[(size_t)q * nf + f] = rhs[q];
+    }
 }
 
 // ---------------------------------------------------------------------------

@@ -101,6 +101,9 @@ struct Args {
                               // (V then holds D x D more rows: its SGS stress), or null
     const uint8_t* cellGhosts;  // FP32-bulk single case: boundary faces of each cell
                                 // (its update writes their ghosts' primitives), or null
+    const int* fOwn;          // FP32-bulk cell-centred flux: nc + 1 offsets, the flux faces that
+                              // cell c owns (is P of) are fOwn[c] .. fOwn[c + 1] - 1 (the faces
+                              // are stored by owner); null where the face-per-thread kernel runs
     const int* cfEll;         // FP32-bulk update gather (single cases beyond L2, batch cases):
                               // the cfList entries of each cell at a fixed width
                               // (kEllWidth<D>), entry k of cell c at k * nc + c, kEllPad

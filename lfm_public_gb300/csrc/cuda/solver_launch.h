@@ -9,6 +9,17 @@
 namespace lfm {
 namespace dev {
 
+// Staged FP32-bulk flux kernel (flux_staged_fp32.cu): faces per block (one
+// chunk), shared-memory buffers per thread (the staging depth, 0 = the plain
+// flux kernel), and the persistent grid and dynamic shared memory set by
+// configure_flux_staging.
+struct FluxStaging {
+    int stages = 0;
+    int faces = 128;
+    int grid = 0;
+    size_t smem = 0;
+};
+
 // What one RK stage runs (src/mesh_solver.cpp:500-672).
 struct StageConfig {
     int scheme = 0;       // kSchemeM1 / M2 / AUSM
@@ -22,6 +33,8 @@ struct StageConfig {
     // preparation pass covers the ghosts only unless the cell primitives are
     // stale (a new state was set).
     bool fullPrep = true;
+    // FP32-bulk flux: the staged kernel when stages > 0
+    FluxStaging fluxStaging;
 };
 
 template <typename T>
@@ -38,6 +51,11 @@ void launch_kernel_fp32(const Args<float>& a, const StageConfig& s, int which, c
 // face rhs evaluated by the cells themselves; the next stage's primitives go
 // to a.primW, which must not be a.prim.
 void launch_fluxupdate32(const Args<float>& a, const StageConfig& s, cudaStream_t st);
+// Staged flux kernel: for M1 / M2 without the LES terms; configure sets the
+// kernel's shared-memory limit (outside graph capture) and fs.grid, fs.smem.
+bool flux_staging_supported(int scheme, bool les);
+cudaError_t configure_flux_staging(int D, int scheme, int nf, FluxStaging& fs);
+void launch_flux32_staged(const Args<float>& a, const StageConfig& s, cudaStream_t st);
 // q' = q - q_ref for the cells of an FP32-bulk solver from an absolute state
 // [nq][stride] on the device.
 void launch_to_perturbation(const Args<float>& a, const double* q, int64_t stride, cudaStream_t st);

@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from lfm_public_gb300 import _native as N, acoustics, cases
-from tests.helpers import rel_l2
+from tests.helpers import load_golden, rel_l2
 
 pytestmark = pytest.mark.gpu
 ACOUSTIC_TOL = 1e-3
@@ -251,7 +251,6 @@ def test_smagorinsky_les_fp32_bulk_and_batch():
     """Smagorinsky LES: the FP32-bulk form stays within the acoustic bar of
     the FP64 path (which the les_* fixtures pin to the reference); the batch
     engine refuses LES cases."""
-    from tests.helpers import load_golden
     case, _ = load_golden("les_cyl24x12_m2")
     assert not case.laminar
     ch = N.CaseHandle.from_case(case)
@@ -290,5 +289,81 @@ def test_fused_flux_update_gives_the_separate_kernels_bits(monkeypatch, solver, 
         s.advance(host, 3, case.delta_t, outq)
         out[mode] = (q7, res, outq)
         s.close()
+    for a, b in zip(out["0"], out["1"]):
+        assert np.array_equal(a, b)
+
+
+def _staged_cases():
+    return {
+        "cyl2d_m1": lambda: cases.cylinder_case(n_theta=64, n_r=32, r1=20, first=0.02, Ls=5, solver=0, minmod=True,
+                                                noise=0.02, seed=3),
+        "cyl2d_m2": lambda: cases.cylinder_case(n_theta=64, n_r=32, r1=20, first=0.02, Ls=5, solver=1, minmod=False,
+                                                noise=0.02, seed=4),
+        "vortex_inviscid": lambda: cases.vortex_case(n=40, solver=0),
+        "tri_m2": lambda: cases.tri_case(n=24, seed=4, solver=1),
+        "cyl3d_m2": lambda: cases.cylinder_case(n_theta=24, n_r=12, n_span=6, solver=1, reynolds=3900.0, noise=0.01,
+                                                seed=7),
+    }
+
+
+@pytest.mark.parametrize("name,stages,faces", [
+    ("cyl2d_m1", 2, 128), ("cyl2d_m1", 3, 96), ("cyl2d_m1", 4, 256), ("cyl2d_m2", 2, 96),
+    ("vortex_inviscid", 2, 128), ("tri_m2", 3, 32), ("cyl3d_m2", 2, 128), ("cyl3d_m2", 3, 160),
+    ("cyl2d_m1", 1, 256), ("cyl2d_m2", 1, 256), ("vortex_inviscid", 1, 256), ("tri_m2", 1, 256), ("cyl3d_m2", 1, 256),
+])
+def test_staged_flux_gives_the_plain_kernels_bits(monkeypatch, name, stages, faces):
+    """The staged flux kernel (the values of each face copied into shared
+    memory ahead of use, chunks of `faces` faces per block, `stages` buffers
+    per thread) gives the bits of the plain flux kernel: face counts that
+    are not a multiple of the chunk, boundary faces, inviscid and viscous
+    cases, 2D and 3D, through stepping, lfm_solver_advance and the residual."""
+    case = _staged_cases()[name]()
+    case.residuals = True
+    ch = N.CaseHandle.from_case(case)
+    assert ch.desc.n_faces % faces != 0 or faces == 32
+    monkeypatch.setenv("LFM_FLUX_UPDATE", "0")
+    out = {}
+    for mode in ("0", str(stages)):
+        monkeypatch.setenv("LFM_FLUX_STAGES", mode)
+        monkeypatch.setenv("LFM_FLUX_FACES", str(faces))
+        s = N.Solver(ch, precision=N.LFM_FP32_BULK)
+        s.step(4, case.delta_t)
+        s.sync()
+        q = s.get_state()
+        res = s.cell_residual()
+        host = np.ascontiguousarray(q.copy())
+        outq = np.empty_like(host)
+        s.advance(host, 2, case.delta_t, outq)
+        out[mode] = (q, res, outq)
+        s.close()
+    assert np.isfinite(out["0"][0]).all()
+    for a, b in zip(out["0"], out[str(stages)]):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", ["cyl2d_m1", "cyl2d_m2", "vortex_inviscid", "tri_m2", "cyl3d_m2"])
+def test_cell_centred_flux_gives_the_plain_kernels_bits(monkeypatch, name):
+    """The cell-centred flux kernel (one thread per cell over the faces it
+    owns, the cell's own rows read once) gives the plain flux kernel's bits,
+    through stepping, lfm_solver_advance and the residual."""
+    case = _staged_cases()[name]()
+    case.residuals = True
+    ch = N.CaseHandle.from_case(case)
+    monkeypatch.setenv("LFM_FLUX_UPDATE", "0")
+    monkeypatch.setenv("LFM_FLUX_STAGES", "0")
+    out = {}
+    for m in ("0", "1"):
+        monkeypatch.setenv("LFM_FLUX_CELL", m)
+        s = N.Solver(ch, precision=N.LFM_FP32_BULK)
+        s.step(4, case.delta_t)
+        s.sync()
+        q = s.get_state()
+        res = s.cell_residual()
+        host = np.ascontiguousarray(q.copy())
+        outq = np.empty_like(host)
+        s.advance(host, 2, case.delta_t, outq)
+        out[m] = (q, res, outq)
+        s.close()
+    assert np.isfinite(out["0"][0]).all()
     for a, b in zip(out["0"], out["1"]):
         assert np.array_equal(a, b)

@@ -107,8 +107,8 @@ DRAM_TRAFFIC = {
     # 192x128x48 capture
     # scaled by the cells (x8), the traffic being at the algorithmic bytes,
     # which grow in proportion
-    ("cylinder3d_small", "fp32", "k_flux"): 280696832 + 52857856,
-    ("cylinder3d", "fp32", "k_flux"): 8 * (280696832 + 52857856),
+    ("cylinder3d_small", "fp32", "k_flux"): 270532096 + 54157824,
+    ("cylinder3d", "fp32", "k_flux"): 8 * (270532096 + 54157824),
     ("cylinder2d", "fp64", "k_flux"): 95838720 + 8762112,
 }
 

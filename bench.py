@@ -387,6 +387,13 @@ def _time_leg(N, ch, precision, dt, steps, warmup, local, pg, clk=None):
     (solver, total ms of the K steps (max over ranks), kernel ms per step,
     launches per step)."""
     s = N.Solver(ch, precision=precision, device=local)
+    tune = None
+    if precision == N.LFM_FP32_BULK:
+        # flux kernel (face, cell-centred, staged at each staging depth): the
+        # fastest on this case, by lfm_solver_autotune (all give the same bits)
+        tried = []
+        t = s.autotune(dt, trial_steps=3, tried=tried)
+        tune = {"chosen": t.as_dict(), "tried": [x.as_dict() for x in tried]}
     for _ in range(warmup):
         s.step(1, dt)
     s.sync()
@@ -403,7 +410,7 @@ def _time_leg(N, ch, precision, dt, steps, warmup, local, pg, clk=None):
     total_ms = _allmax(pg, float(times.sum()))
     prof = s.profile_step(dt)
     s.sync()
-    return s, total_ms, prof, s.launches_per_step()
+    return s, total_ms, prof, s.launches_per_step(), tune
 
 
 def _e2e(s, nq, nc, dt, steps, pg):
@@ -443,7 +450,7 @@ def _leg_record(N, ch, precision, dt, args, ws, local, pg, desc, workload, hbm, 
     e2e of one precision on one case."""
     nc, nq, stages = ch.desc.n_cells, ch.desc.nq, ch.desc.rk_order
     fp32 = precision == N.LFM_FP32_BULK
-    s, total_ms, prof, launches = _time_leg(N, ch, precision, dt, args.steps, args.warmup, local, pg, clk)
+    s, total_ms, prof, launches, tune = _time_leg(N, ch, precision, dt, args.steps, args.warmup, local, pg, clk)
     value = ws * nc * stages * args.steps / (total_ms / 1000.0)
     ms_step = total_ms / args.steps
     roof, step_bytes = _hbm_roofline(desc, fp32, prof, nc, stages, workload, "fp32" if fp32 else "fp64", hbm,
@@ -452,6 +459,8 @@ def _leg_record(N, ch, precision, dt, args, ws, local, pg, desc, workload, hbm, 
     roof["step_frac"] = roof["step_achieved"] / hbm
     rec = {"value": value, "unit": UNIT, "ms_per_step": ms_step, "kernels_ms_per_step": prof,
            "kernels_sum_ms": sum(prof.values()), "roofline": roof, "launches_per_step": launches}
+    if tune is not None:
+        rec["flux_tuning"] = tune
     if e2e:
         e2e_steps = max(1, args.steps)
         e2e_s = _e2e(s, nq, nc, dt, e2e_steps, pg)

@@ -320,6 +320,42 @@ int lfm_solver_launches_per_step(const lfm_solver* s, int* launches);
 int lfm_solver_profile_step(lfm_solver* s, double dt, int n, float* ms);
 const char* lfm_solver_kernel_name(int i);
 
+/* Flux kernel of an FP32-bulk solver (no reference counterpart: the
+ * reference evaluates its faces in one loop). Every variant gives the same
+ * bits; they differ in how a face's values reach the SM:
+ *   LFM_FLUX_FACE    one thread per face;
+ *   LFM_FLUX_CELL    one thread per cell over the faces it owns, the cell's
+ *                    own rows read once (the default for 3D cases);
+ *   LFM_FLUX_STAGED  the values each face reads copied into shared memory
+ *                    ahead of use with cp.async: staging_depth buffers per
+ *                    thread (1: one slot beside the registers; 2..4: chunks
+ *                    of staging_faces faces per block, 32..256).
+ * The variants apply to M1 / M2 laminar solvers with separate flux and update
+ * kernels; other solvers report LFM_FLUX_FACE and refuse the others. */
+#define LFM_FLUX_FACE 0
+#define LFM_FLUX_CELL 1
+#define LFM_FLUX_STAGED 2
+typedef struct lfm_solver_tuning {
+    int flux_kernel;     /* LFM_FLUX_* */
+    int staging_depth;   /* LFM_FLUX_STAGED: shared-memory buffers per thread, 1..4 */
+    int staging_faces;   /* LFM_FLUX_STAGED: faces per block, 32..256 (depth 1: 256) */
+    float ms_per_step;   /* lfm_solver_autotune: median time step of the trial */
+} lfm_solver_tuning;
+int lfm_solver_get_tuning(const lfm_solver* s, lfm_solver_tuning* t);
+/* Waits for the solver stream; LFM_ERR_UNSUPPORTED where the variant does not
+ * apply, LFM_ERR_INVALID for a staged shape the device refuses (shared memory). */
+int lfm_solver_set_tuning(lfm_solver* s, const lfm_solver_tuning* t);
+/* Times trial_steps steps (after one untimed step, each after a write of
+ * flush_bytes of scratch memory) of every applicable flux kernel
+ * configuration -- the face and cell kernels and the staged kernel at depths
+ * 1..4 -- and keeps the fastest (*chosen, with its median time); the state is
+ * restored afterwards. tried[0..capacity) receives every configuration timed,
+ * *n_tried their count (either may be NULL; configurations the device refuses
+ * are skipped). Synchronous; copies the stored state on the device (device
+ * memory for one copy of it) and puts it back bit for bit. */
+int lfm_solver_autotune(lfm_solver* s, double dt, int trial_steps, size_t flush_bytes, lfm_solver_tuning* chosen,
+                        lfm_solver_tuning* tried, int capacity, int* n_tried);
+
 /* ---- decomposed cases on one GPU ------------------------------------------
  *
  * The reference runs a decomposed case (processor0..N-1, decomposePar) as one

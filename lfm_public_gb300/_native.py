@@ -90,6 +90,20 @@ class BatchTuning(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+LFM_FLUX_FACE, LFM_FLUX_CELL, LFM_FLUX_STAGED = 0, 1, 2
+FLUX_KERNEL_NAMES = {LFM_FLUX_FACE: "face", LFM_FLUX_CELL: "cell", LFM_FLUX_STAGED: "staged"}
+
+
+class SolverTuning(C.Structure):
+    _fields_ = [("flux_kernel", C.c_int), ("staging_depth", C.c_int), ("staging_faces", C.c_int),
+                ("ms_per_step", C.c_float)]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["flux_kernel"] = FLUX_KERNEL_NAMES.get(self.flux_kernel, self.flux_kernel)
+        return d
+
+
 class ServerOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("rk_order", C.c_int), ("arena_bytes", C.c_size_t), ("max_cases", C.c_int),
                 ("chunk_steps", C.c_int), ("max_bypass", C.c_int), ("tuning", BatchTuning)]
@@ -164,6 +178,10 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "lfm_solver_bench": ([vp, C.c_int, C.c_double, C.c_size_t, C.POINTER(C.c_float)], C.c_int),
         "lfm_solver_profile_step": ([vp, C.c_double, C.c_int, C.POINTER(C.c_float)], C.c_int),
         "lfm_solver_kernel_name": ([C.c_int], C.c_char_p),
+        "lfm_solver_get_tuning": ([vp, C.POINTER(SolverTuning)], C.c_int),
+        "lfm_solver_set_tuning": ([vp, C.POINTER(SolverTuning)], C.c_int),
+        "lfm_solver_autotune": ([vp, C.c_double, C.c_int, C.c_size_t, C.POINTER(SolverTuning),
+                                 C.POINTER(SolverTuning), C.c_int, C.POINTER(C.c_int)], C.c_int),
         "lfm_pcase_open": ([C.c_char_p, C.c_int, C.POINTER(vp)], C.c_int),
         "lfm_pcase_parts": ([vp, C.POINTER(C.c_int)], C.c_int),
         "lfm_pcase_describe": ([vp, C.c_int, C.POINTER(SolverDesc)], C.c_int),
@@ -434,6 +452,30 @@ class Solver:
         v = C.c_int()
         check(load_library().lfm_solver_launches_per_step(self._h, C.byref(v)))
         return v.value
+
+    def tuning(self) -> SolverTuning:
+        t = SolverTuning()
+        check(load_library().lfm_solver_get_tuning(self._h, C.byref(t)))
+        return t
+
+    def set_tuning(self, flux_kernel: int, staging_depth: int = 0, staging_faces: int = 0):
+        t = SolverTuning(flux_kernel, staging_depth, staging_faces, 0.0)
+        check(load_library().lfm_solver_set_tuning(self._h, C.byref(t)))
+
+    def autotune(self, dt: float, trial_steps: int = 5, flush_bytes: int = 512 << 20, tried: list = None
+                 ) -> SolverTuning:
+        """Times every applicable flux kernel configuration and keeps the
+        fastest (lfm_solver_autotune); the state is restored. `tried`, a list,
+        receives every configuration timed."""
+        t = SolverTuning()
+        cap = 32
+        arr = (SolverTuning * cap)()
+        n = C.c_int()
+        check(load_library().lfm_solver_autotune(self._h, dt, trial_steps, flush_bytes, C.byref(t), arr, cap,
+                                                 C.byref(n)))
+        if tried is not None:
+            tried.extend(arr[i] for i in range(min(n.value, cap)))
+        return t
 
     def profile_step(self, dt: float) -> dict:
         """ms per time step of each kernel; kernels that did not run are left out."""

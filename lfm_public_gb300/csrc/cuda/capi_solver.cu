@@ -86,7 +86,11 @@ struct lfm_solver {
     // fused flux + update stages (FP32-bulk single case): two primitive
     // buffers alternate like the tile stages'
     bool fluxUpdate = false;
-    // FP32-bulk staged flux kernel (stages 0: the plain flux kernel)
+    // FP32-bulk flux kernel variants (lfm_solver_tuning): whether they apply,
+    // the cell-centred kernel's owner offsets (kept while another variant
+    // runs), and the staged kernel's configuration (stages 0: not staged)
+    bool fluxVariants = false;
+    int* fOwnDev = nullptr;
     lfm::dev::FluxStaging fluxStaging;
     cudaGraphExec_t graphOdd = nullptr;   // the step graph starting from prim1
     // the non-finite flag's host copy (page-locked: read after one stream sync)
@@ -730,25 +734,23 @@ int createSolver(const lfm_solver_desc* d, const lfm_solver_opts* opts, cudaStre
         if ((rc = devAlloc(s, &s->prim1, (size_t)lfm::dev::primRows<float>(s->D) * nt))) return fail(rc);
         s->fluxUpdate = true;
     }
-    // cell-centred flux kernel: FP32-bulk M1 / M2 laminar cases with separate
-    // flux and update kernels, faces stored by owner (the description's order)
-    if (s->precision == LFM_FP32_BULK && !tiled && !s->fluxUpdate && !d->smag_c &&
-        s->scheme != LFM_SOLVER_M2AUSM && fluxCellOption(s)) {
+    // flux kernel variants: FP32-bulk M1 / M2 laminar cases with separate flux
+    // and update kernels; the cell-centred one where the faces are stored by
+    // owner (the description's order)
+    s->fluxVariants = s->precision == LFM_FP32_BULK && !tiled && !s->fluxUpdate && !d->smag_c &&
+                      lfm::dev::flux_staging_supported(s->scheme, false);
+    if (s->fluxVariants) {
         bool byOwner = true;
         for (size_t f = 1; f < nf && byOwner; ++f) byOwner = fP[f] >= fP[f - 1];
         if (byOwner) {
             std::vector<int> own(nc + 1, 0);
             for (size_t f = 0; f < nf; ++f) ++own[(size_t)fP[f] + 1];
             for (size_t c = 0; c < nc; ++c) own[c + 1] += own[c];
-            int* dOwn = nullptr;
-            if ((rc = upload(s, &dOwn, own.data(), nc + 1))) return fail(rc);
-            s->a32.fOwn = dOwn;
+            if ((rc = upload(s, &s->fOwnDev, own.data(), nc + 1))) return fail(rc);
+            if (fluxCellOption(s)) s->a32.fOwn = s->fOwnDev;
         }
     }
-    // staged flux kernel: FP32-bulk cases with separate flux and update
-    // kernels, M1 / M2, laminar
-    if (s->precision == LFM_FP32_BULK && !tiled && !s->fluxUpdate && !d->smag_c &&
-        lfm::dev::flux_staging_supported(s->scheme, false)) {
+    if (s->fluxVariants) {
         lfm::dev::FluxStaging fs = fluxStagingOption(s);
         if (fs.stages > 0) {
             if ((e = lfm::dev::configure_flux_staging(s->D, s->scheme, s->nf, fs)) != cudaSuccess)
@@ -1694,4 +1696,158 @@ extern "C" int lfm_partitioned_sync(lfm_partitioned* P) {
         if (rc) return rc;
     }
     return LFM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Flux kernel tuning (FP32-bulk): the face-per-thread kernel, the cell-centred
+// kernel and the staged kernels at each staging depth give the same bits;
+// lfm_solver_autotune times them on the solver's own case and keeps the
+// fastest.
+// ---------------------------------------------------------------------------
+namespace {
+
+void dropGraphs(lfm_solver* s) {
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    if (s->graphOdd) cudaGraphExecDestroy(s->graphOdd);
+    if (s->advGraph) cudaGraphExecDestroy(s->advGraph);
+    s->graph = s->graphOdd = s->advGraph = nullptr;
+    s->graphDt = 0;
+    s->advIn = nullptr;
+    s->advOut = nullptr;
+}
+
+lfm_solver_tuning currentTuning(const lfm_solver* s) {
+    lfm_solver_tuning t{};
+    if (s->fluxStaging.stages > 0) {
+        t.flux_kernel = LFM_FLUX_STAGED;
+        t.staging_depth = s->fluxStaging.stages;
+        t.staging_faces = s->fluxStaging.faces;
+    } else {
+        t.flux_kernel = s->a32.fOwn ? LFM_FLUX_CELL : LFM_FLUX_FACE;
+    }
+    t.ms_per_step = 0.0f;
+    return t;
+}
+
+int applyTuning(lfm_solver* s, const lfm_solver_tuning& t) {
+    if (t.flux_kernel == LFM_FLUX_FACE || t.flux_kernel == LFM_FLUX_CELL) {
+        if (t.flux_kernel == LFM_FLUX_CELL && !s->fOwnDev)
+            return lfm::setError(LFM_ERR_UNSUPPORTED, "cell-centred flux: faces not stored by owner");
+        s->a32.fOwn = t.flux_kernel == LFM_FLUX_CELL ? s->fOwnDev : nullptr;
+        s->fluxStaging = lfm::dev::FluxStaging{};
+    } else if (t.flux_kernel == LFM_FLUX_STAGED) {
+        lfm::dev::FluxStaging fs;
+        fs.stages = t.staging_depth;
+        fs.faces = t.staging_faces;
+        if (fs.stages < 1 || fs.stages > 4) return lfm::setError(LFM_ERR_INVALID, "staging depth must be 1..4");
+        const cudaError_t e = lfm::dev::configure_flux_staging(s->D, s->scheme, s->nf, fs);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return lfm::setError(LFM_ERR_INVALID, std::string("staged flux configuration refused: ") +
+                                                      cudaGetErrorString(e));
+        }
+        s->fluxStaging = fs;
+        s->a32.fOwn = nullptr;
+    } else {
+        return lfm::setError(LFM_ERR_INVALID, "unknown flux kernel");
+    }
+    dropGraphs(s);
+    return LFM_OK;
+}
+
+}  // namespace
+
+extern "C" int lfm_solver_get_tuning(const lfm_solver* s, lfm_solver_tuning* t) {
+    if (!s || !t) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    *t = currentTuning(s);
+    return LFM_OK;
+}
+
+extern "C" int lfm_solver_set_tuning(lfm_solver* s, const lfm_solver_tuning* t) {
+    if (!s || !t) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    if (!s->fluxVariants) {
+        if (t->flux_kernel == LFM_FLUX_FACE) return LFM_OK;
+        return lfm::setError(LFM_ERR_UNSUPPORTED, "flux kernel variants: FP32-bulk M1 / M2 laminar solvers with "
+                                                  "separate flux and update kernels only");
+    }
+    LFM_CUDA(cudaSetDevice(s->device));
+    LFM_CUDA(cudaStreamSynchronize(s->stream));
+    return applyTuning(s, *t);
+}
+
+extern "C" int lfm_solver_autotune(lfm_solver* s, double dt, int trial_steps, size_t flush_bytes,
+                                   lfm_solver_tuning* chosen, lfm_solver_tuning* tried, int capacity,
+                                   int* n_tried) {
+    if (!s || trial_steps <= 0 || !(dt > 0) || capacity < 0) return lfm::setError(LFM_ERR_INVALID, "bad argument");
+    if (n_tried) *n_tried = 0;
+    LFM_CUDA(cudaSetDevice(s->device));
+    std::vector<lfm_solver_tuning> cand;
+    cand.push_back(currentTuning(s));
+    if (s->fluxVariants) {
+        cand.clear();
+        cand.push_back(lfm_solver_tuning{LFM_FLUX_FACE, 0, 0, 0.0f});
+        if (s->fOwnDev) cand.push_back(lfm_solver_tuning{LFM_FLUX_CELL, 0, 0, 0.0f});
+        cand.push_back(lfm_solver_tuning{LFM_FLUX_STAGED, 1, 256, 0.0f});
+        const int shapes[][2] = {{2, 64}, {2, 128}, {2, 256}, {3, 64}, {3, 128}, {4, 64}};
+        for (const auto& sh : shapes) cand.push_back(lfm_solver_tuning{LFM_FLUX_STAGED, sh[0], sh[1], 0.0f});
+    }
+    const lfm_solver_tuning before = currentTuning(s);
+    // the stored state and primitives, copied on the device (the FP32-bulk
+    // state is q - q_ref: a round trip through the absolute state would not
+    // keep its bits)
+    LFM_CUDA(cudaStreamSynchronize(s->stream));
+    int rc = ensurePrims(s);
+    if (rc) return rc;
+    const size_t qBytes = (size_t)s->nq * (size_t)s->nt * sizeof(double);
+    const size_t pBytes = s->precision == LFM_FP32_BULK
+                              ? (size_t)lfm::dev::primRows<float>(s->D) * (size_t)s->nt * sizeof(float) : 0;
+    void* saved = nullptr;
+    LFM_CUDA(cudaMalloc(&saved, qBytes + pBytes));
+    char* sq = static_cast<char*>(saved);
+    auto restore = [&]() -> int {
+        LFM_CUDA(cudaMemsetAsync(s->flag, 0, sizeof(int), s->stream));
+        LFM_CUDA(cudaMemcpyAsync(s->q, sq, qBytes, cudaMemcpyDeviceToDevice, s->stream));
+        if (pBytes) LFM_CUDA(cudaMemcpyAsync(s->a32.prim, sq + qBytes, pBytes, cudaMemcpyDeviceToDevice, s->stream));
+        s->primsValid = pBytes != 0;   // FP64: rebuilt by ensurePrims
+        s->primParity = 0;
+        LFM_CUDA(cudaStreamSynchronize(s->stream));
+        return LFM_OK;
+    };
+    cudaError_t ce = cudaMemcpyAsync(sq, s->q, qBytes, cudaMemcpyDeviceToDevice, s->stream);
+    if (ce == cudaSuccess && pBytes)
+        ce = cudaMemcpyAsync(sq + qBytes, s->a32.prim, pBytes, cudaMemcpyDeviceToDevice, s->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(s->stream);
+    if (ce != cudaSuccess) {
+        cudaFree(saved);
+        return cudaFail(ce, "autotune state copy");
+    }
+    std::vector<float> ms((size_t)trial_steps);
+    int best = -1;
+    for (size_t k = 0; k < cand.size(); ++k) {
+        if (s->fluxVariants && applyTuning(s, cand[k]) != LFM_OK) continue;   // refused shapes are skipped
+        if ((rc = restore())) break;
+        float warm = 0.0f;
+        if ((rc = lfm_solver_bench(s, 1, dt, flush_bytes, &warm))) break;   // captures the step graph
+        if ((rc = restore())) break;
+        if ((rc = lfm_solver_bench(s, trial_steps, dt, flush_bytes, ms.data()))) break;
+        std::vector<float> sorted(ms);
+        std::sort(sorted.begin(), sorted.end());
+        cand[k].ms_per_step = sorted[sorted.size() / 2];
+        if (best < 0 || cand[k].ms_per_step < cand[(size_t)best].ms_per_step) best = (int)k;
+        if (n_tried) {
+            if (tried && *n_tried < capacity) tried[*n_tried] = cand[k];
+            ++*n_tried;
+        }
+    }
+    const lfm_solver_tuning pick = best >= 0 ? cand[(size_t)best] : before;
+    if (s->fluxVariants) {
+        const int rc2 = applyTuning(s, pick);
+        if (!rc) rc = rc2;
+    }
+    const int rc3 = restore();
+    if (!rc) rc = rc3;
+    cudaFree(saved);
+    if (!rc && best < 0) rc = lfm::setError(LFM_ERR_INVALID, "no flux kernel configuration could be timed");
+    if (chosen) *chosen = pick;
+    return rc;
 }

@@ -367,3 +367,59 @@ def test_cell_centred_flux_gives_the_plain_kernels_bits(monkeypatch, name):
     assert np.isfinite(out["0"][0]).all()
     for a, b in zip(out["0"], out["1"]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", ["cyl2d_m1", "cyl3d_m2"])
+def test_flux_autotune_restores_the_state_and_keeps_the_bits(monkeypatch, name):
+    """lfm_solver_autotune times the face, cell and staged flux kernels (the
+    staging depths 1..4) and keeps the fastest; the state is restored, and
+    stepping on with the chosen kernel gives the bits of an untuned solver."""
+    case = _staged_cases()[name]()
+    ch = N.CaseHandle.from_case(case)
+    monkeypatch.setenv("LFM_FLUX_UPDATE", "0")
+    ref = N.Solver(ch, precision=N.LFM_FP32_BULK)
+    ref.step(6, case.delta_t)
+    ref.sync()
+    q_ref = ref.get_state()
+    ref.close()
+    s = N.Solver(ch, precision=N.LFM_FP32_BULK)
+    s.step(3, case.delta_t)
+    s.sync()
+    q3 = s.get_state()
+    t = s.autotune(case.delta_t, trial_steps=3, flush_bytes=1 << 20)
+    assert t.flux_kernel in (N.LFM_FLUX_FACE, N.LFM_FLUX_CELL, N.LFM_FLUX_STAGED)
+    assert t.ms_per_step > 0
+    assert s.tuning().flux_kernel == t.flux_kernel
+    assert np.array_equal(s.get_state(), q3)
+    s.step(3, case.delta_t)
+    s.sync()
+    assert np.array_equal(s.get_state(), q_ref)
+    # every variant by hand
+    for kern, depth, faces in [(N.LFM_FLUX_FACE, 0, 0), (N.LFM_FLUX_CELL, 0, 0), (N.LFM_FLUX_STAGED, 1, 256),
+                               (N.LFM_FLUX_STAGED, 3, 96)]:
+        s.set_tuning(kern, depth, faces)
+        s.set_state(ch.q0())
+        s.step(6, case.delta_t)
+        s.sync()
+        assert np.array_equal(s.get_state(), q_ref), (kern, depth, faces)
+    with pytest.raises(N.LfmError):
+        s.set_tuning(N.LFM_FLUX_STAGED, 5, 128)
+    with pytest.raises(N.LfmError):
+        s.set_tuning(N.LFM_FLUX_STAGED, 2, 48)
+    s.close()
+
+
+def test_flux_tuning_where_the_variants_do_not_apply():
+    """FP64 solvers and M2AUSM report the face kernel and refuse the others;
+    lfm_solver_autotune times the one configuration they have."""
+    case = cases.cylinder_case(n_theta=32, n_r=16, r1=20, first=0.02, Ls=5, solver=2, minmod=True)
+    ch = N.CaseHandle.from_case(case)
+    for prec in (N.LFM_FP64, N.LFM_FP32_BULK):
+        s = N.Solver(ch, precision=prec)
+        assert s.tuning().flux_kernel == N.LFM_FLUX_FACE
+        s.set_tuning(N.LFM_FLUX_FACE)
+        with pytest.raises(N.LfmError):
+            s.set_tuning(N.LFM_FLUX_CELL)
+        t = s.autotune(case.delta_t, trial_steps=2, flush_bytes=1 << 20)
+        assert t.flux_kernel == N.LFM_FLUX_FACE and t.ms_per_step > 0
+        s.close()

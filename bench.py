@@ -118,7 +118,7 @@ DRAM_TRAFFIC = {
 # cells) on the 768x512 cylinder, M1, viscous; the update also derives the next
 # stage's primitives and boundary ghosts (no preparation kernel).
 FP64_INST_PER_CELL = {
-    "cylinder2d": {"k_prep": 0.0, "k_grad": 0.0, "k_vis": 63.00, "k_flux": 156.22, "k_update": 46.67},
+    "cylinder2d": {"k_prep": 0.0, "k_grad": 0.0, "k_vis": 45.00, "k_flux": 156.22, "k_update": 42.67},
 }
 # FP64 pipe instruction rate: the measured DFMA rate (FP64_PEAK_TFLOPS counts
 # an FMA as two operations) in instructions per second.

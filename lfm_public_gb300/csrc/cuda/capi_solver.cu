@@ -180,7 +180,8 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
     a.fOwn = nullptr;
     a.smagC = nullptr;
     a.wN = nullptr;
-    a.cfSo = nullptr;
+    a.cfSoN = nullptr;
+    a.cellSoW = nullptr;
     a.primC = s->scheme == LFM_SOLVER_M2AUSM ? 1 : 0;
     const size_t nt = (size_t)s->nt, nf = (size_t)s->nf, D = (size_t)s->D;
     int rc;
@@ -232,24 +233,35 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
         a.lapc = p;
     }
     if (sizeof(T) == sizeof(double)) {
-        // FP64 face and face-entry constants, each the value the kernels would
-        // otherwise compute per face visit: 1 - w, and S/V of each cell's faces
+        // FP64 face, face-entry and cell constants, each the value the kernels
+        // would otherwise compute per face visit: 1 - w per face; for the
+        // Gauss gradients, with the face value v_f = w v_P + (1 - w) v_N and
+        // so_e = S/V of entry e's face seen from its cell c,
+        //   sum_e v_f so_e = v_c sum_e w_own so_e + sum_e v_across w_across so_e,
+        // the first sum a cell constant, w_across so_e an entry constant
+        // (w_own = w where c is P, 1 - w where c is N)
         std::vector<double> wN(nf);
         for (size_t f = 0; f < nf; ++f) wN[f] = 1.0 - d->w[f];
         if ((rc = uploadAs<T>(s, &p, wN.data(), nf))) return rc;
         a.wN = p;
-        const size_t ne = (size_t)d->cell_face_offsets[s->nc];
-        std::vector<double> so(D * ne);
-        for (int64_t c = 0; c < s->nc; ++c)
+        const size_t ne = (size_t)d->cell_face_offsets[s->nc], nc = (size_t)s->nc;
+        std::vector<double> soN(D * ne), soW(D * nc, 0.0);
+        for (size_t c = 0; c < nc; ++c)
             for (int64_t e = d->cell_face_offsets[c]; e < d->cell_face_offsets[c + 1]; ++e) {
                 const int64_t f = d->cell_faces[e];
+                const bool isP = d->cell_face_sign[e] > 0;
+                const double wOwn = isP ? d->w[f] : wN[(size_t)f], wAcross = isP ? wN[(size_t)f] : d->w[f];
                 for (size_t k = 0; k < D; ++k) {
                     const double Sk = d->S[k * nf + (size_t)f];
-                    so[k * ne + (size_t)e] = d->cell_face_sign[e] > 0 ? Sk * d->vol_inv[c] : -Sk * d->vol_inv[c];
+                    const double so = isP ? Sk * d->vol_inv[c] : -Sk * d->vol_inv[c];
+                    soN[k * ne + (size_t)e] = wAcross * so;
+                    soW[k * nc + c] += wOwn * so;
                 }
             }
-        if ((rc = uploadAs<T>(s, &p, so.data(), so.size()))) return rc;
-        a.cfSo = p;
+        if ((rc = uploadAs<T>(s, &p, soN.data(), soN.size()))) return rc;
+        a.cfSoN = p;
+        if ((rc = uploadAs<T>(s, &p, soW.data(), soW.size()))) return rc;
+        a.cellSoW = p;
     }
     a.volInv32 = nullptr;
     if (sizeof(T) == sizeof(float)) {

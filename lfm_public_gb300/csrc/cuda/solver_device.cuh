@@ -39,6 +39,16 @@ __device__ __forceinline__ double rcp64(double x) {
     return fma(y, e, y);
 }
 
+// -x and isfinite(x) of an FP64 value on the integer pipe (a sign-bit flip;
+// an exponent test), leaving GB300's FP64 pipe to the arithmetic.
+__device__ __forceinline__ double neg_bits(double x) {
+    return __hiloint2double(__double2hiint(x) ^ (int)0x80000000u, __double2loint(x));
+}
+__device__ __forceinline__ float neg_bits(float x) { return __uint_as_float(__float_as_uint(x) ^ 0x80000000u); }
+__device__ __forceinline__ bool finite_bits(double x) {
+    return ((unsigned)__double2hiint(x) & 0x7ff00000u) != 0x7ff00000u;
+}
+
 // interp with the weight of N given (1 - w, precomputed per face).
 template <typename T>
 __device__ __forceinline__ T interp2(T w, T wN, T a, T b) {
@@ -271,18 +281,24 @@ __device__ __forceinline__ void update_cell(const Args<T>& a, int c, double Ak, 
         int code[W];
 #pragma unroll
         for (int k = 0; k < W; ++k) code[k] = e0 + k < e1 ? a.cfList[e0 + k] : kEllPad;
+        // The face's sign (+ where c is P, - where N) goes on the value as a
+        // sign-bit flip on the integer pipe, so each entry costs one FP64 add
+        // (a - b is a + (-b) in IEEE arithmetic: the same bits)
         T fl[W][NQ];
 #pragma unroll
         for (int k = 0; k < W; ++k) {
             const int f = code[k] >= 0 ? code[k] : ~code[k];
 #pragma unroll
-            for (int v = 0; v < NQ; ++v) fl[k][v] = code[k] != kEllPad ? a.flux[v * nf + f] : T(0);
+            for (int v = 0; v < NQ; ++v) {
+                const T x = code[k] != kEllPad ? a.flux[v * nf + f] : T(0);
+                fl[k][v] = code[k] >= 0 ? x : neg_bits(x);
+            }
         }
 #pragma unroll
         for (int k = 0; k < W; ++k) {
             if (code[k] == kEllPad) continue;
 #pragma unroll
-            for (int v = 0; v < NQ; ++v) sum[v] = code[k] >= 0 ? sum[v] + fl[k][v] : sum[v] - fl[k][v];
+            for (int v = 0; v < NQ; ++v) sum[v] += fl[k][v];
         }
     } else {
         for (int e = e0; e < e1; ++e) {
@@ -314,7 +330,7 @@ __device__ __forceinline__ void update_cell(const Args<T>& a, int c, double Ak, 
     for (int v = 0; v < NQ; ++v) {
         a.dq[v * nc + c] = acc[v];
         qn[v] = qv[v] + Bk * acc[v];
-        finite = finite && isfinite(qn[v]);
+        finite = finite && finite_bits(qn[v]);
         a.q[v * nt + c] = qn[v];
         if (RES) a.res[v * nc + c] = (double)sum[v];
     }

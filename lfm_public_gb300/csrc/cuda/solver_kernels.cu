@@ -34,29 +34,40 @@ __global__ void __launch_bounds__(256) k_grad(Args<T> a) {
 #pragma unroll
         for (int l = 0; l < D; ++l) gu[k][l] = T(0);
     }
-    const size_t ne = (size_t)a.cfOff[a.nc];
-    for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
-        const int code = a.cfList[e];
-        const int f = code >= 0 ? code : ~code;
-        const int i = a.fP[f], j = a.fN[f];
-        const T w = a.w[f], wN = a.wN[f];
-        T so[D], UU[D];
+    // Gauss gradients of rho, p and u: the cell's own share through its
+    // constant cellSoW, each neighbour's through the entry constant cfSoN
+    // (the face values w v_P + (1 - w) v_N expanded)
+    const size_t ne = (size_t)a.cfOff[a.nc], nt = (size_t)a.nt, nc = (size_t)a.nc;
+    {
+        T sw[D], Uc[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) {
-            so[k] = a.cfSo[(size_t)k * ne + e];   // S / V seen from c
-            UU[k] = interp2(w, wN, a.prim[(size_t)(1 + k) * a.nt + i], a.prim[(size_t)(1 + k) * a.nt + j]);
+            sw[k] = a.cellSoW[(size_t)k * nc + c];
+            Uc[k] = a.prim[(size_t)(1 + k) * nt + c];
         }
-        const T rhoi = (T)a.q[i], rhoj = (T)a.q[j];
-        const T pi = rhoi * a.prim[(size_t)(D + 1) * a.nt + i];
-        const T pj = rhoj * a.prim[(size_t)(D + 1) * a.nt + j];
-        const T rho = interp2(w, wN, rhoi, rhoj);
-        const T p = interp2(w, wN, pi, pj);
+        const T rhoc = a.q[c];
+        const T pc = rhoc * a.prim[(size_t)(D + 1) * nt + c];
 #pragma unroll
         for (int x = 0; x < D; ++x) {
-            gp[x] += p * so[x];
-            gr[x] += rho * so[x];
+            gp[x] = pc * sw[x];
+            gr[x] = rhoc * sw[x];
 #pragma unroll
-            for (int b = 0; b < D; ++b) gu[b][x] += UU[b] * so[x];
+            for (int b = 0; b < D; ++b) gu[b][x] = Uc[b] * sw[x];
+        }
+    }
+    for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
+        const int j = a.cfNbr[e];
+        T so[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) so[k] = a.cfSoN[(size_t)k * ne + e];
+        const T rhoj = a.q[j];
+        const T pj = rhoj * a.prim[(size_t)(D + 1) * nt + j];
+#pragma unroll
+        for (int x = 0; x < D; ++x) {
+            gp[x] += pj * so[x];
+            gr[x] += rhoj * so[x];
+#pragma unroll
+            for (int b = 0; b < D; ++b) gu[b][x] += a.prim[(size_t)(1 + b) * nt + j] * so[x];
         }
     }
 #pragma unroll
@@ -84,21 +95,33 @@ __global__ void __launch_bounds__(256) k_vis(Args<T> a) {
         for (int l = 0; l < D; ++l) g[k][l] = T(0);
     }
     // Gauss gradients of u and of R psi (T = R psi / R: the 1/R factor is
-    // applied once to the sum); S / V of each face seen from c is a
-    // precomputed entry constant, 1 - w a face constant
-    const size_t ne = (size_t)a.cfOff[a.nc];
+    // applied once to the sum). With the face value v_f = w v_P + (1 - w) v_N
+    // and so = S/V seen from c, sum_f v_f so = v_c cellSoW_c + sum_e v_j
+    // cfSoN_e: the cell's own share through one cell constant, each
+    // neighbour's through an entry constant (the other cell j = cfNbr[e]).
+    const size_t ne = (size_t)a.cfOff[a.nc], nc = (size_t)a.nc;
+    {
+        T sw[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) sw[k] = a.cellSoW[(size_t)k * nc + c];
+        const T Rc = a.prim[(size_t)(D + 1) * a.nt + c];
+#pragma unroll
+        for (int x = 0; x < D; ++x) {
+            const T Ux = a.prim[(size_t)(1 + x) * a.nt + c];
+#pragma unroll
+            for (int y = 0; y < D; ++y) g[x][y] = Ux * sw[y];
+            gT[x] = Rc * sw[x];
+        }
+    }
     for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
-        const int code = a.cfList[e];
-        const int f = code >= 0 ? code : ~code;
-        const int i = a.fP[f], j = a.fN[f];
-        const T w = a.w[f], wN = a.wN[f];
+        const int j = a.cfNbr[e];
         T so[D], fU[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) {
-            so[k] = a.cfSo[(size_t)k * ne + e];
-            fU[k] = interp2(w, wN, a.prim[(size_t)(1 + k) * a.nt + i], a.prim[(size_t)(1 + k) * a.nt + j]);
+            so[k] = a.cfSoN[(size_t)k * ne + e];
+            fU[k] = a.prim[(size_t)(1 + k) * a.nt + j];
         }
-        const T fR = interp2(w, wN, a.prim[(size_t)(D + 1) * a.nt + i], a.prim[(size_t)(D + 1) * a.nt + j]);
+        const T fR = a.prim[(size_t)(D + 1) * a.nt + j];
 #pragma unroll
         for (int x = 0; x < D; ++x) {
 #pragma unroll

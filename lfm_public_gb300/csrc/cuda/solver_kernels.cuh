@@ -95,8 +95,11 @@ struct Args {
     const int* cfOff;         // nc + 1
     const int* cfList;        // face index, negative (~f) when the cell is N
     const int* cfNbr;         // per cfList entry: the cell (or ghost, halo) across the face
-    const T* cfSo;            // FP64 path: D x (cfList entries), S / V of the entry's face seen
-                              // from its cell (the Gauss-gradient weight)
+    const T* cfSoN;           // FP64 path: D x (cfList entries), the linear weight of the cell
+                              // across the entry's face times S / V seen from the entry's cell
+    const T* cellSoW;         // FP64 path: D x nc, the sum over the cell's faces of its own
+                              // linear weight times S / V (Gauss gradient of cell c:
+                              // v_c cellSoW_c + sum over entries of v_across cfSoN)
     const T* smagC;           // Smagorinsky LES: the constant each cell's tauMC is built with
                               // (V then holds D x D more rows: its SGS stress), or null
     const uint8_t* cellGhosts;  // FP32-bulk single case: boundary faces of each cell

@@ -212,7 +212,10 @@ __device__ __forceinline__ void gather32_ell(const Args<float>& a, int c, float*
     for (int k = 0; k < W; ++k) {
         const int f = code[k] >= 0 ? code[k] : ~code[k];
 #pragma unroll
-        for (int v = 0; v < NQ; ++v) fl[k][v] = code[k] != kEllPad ? a.flux[v * nf + f] : 0.0f;
+        for (int v = 0; v < NQ; ++v) {   // the face's sign as a sign-bit flip: one add per entry
+            const float x = code[k] != kEllPad ? a.flux[v * nf + f] : 0.0f;
+            fl[k][v] = code[k] >= 0 ? x : neg_bits(x);
+        }
     }
 #pragma unroll
     for (int v = 0; v < NQ; ++v) sum[v] = 0.0f;
@@ -220,7 +223,7 @@ __device__ __forceinline__ void gather32_ell(const Args<float>& a, int c, float*
     for (int k = 0; k < W; ++k) {
         if (code[k] == kEllPad) continue;
 #pragma unroll
-        for (int v = 0; v < NQ; ++v) sum[v] = code[k] >= 0 ? sum[v] + fl[k][v] : sum[v] - fl[k][v];
+        for (int v = 0; v < NQ; ++v) sum[v] += fl[k][v];
     }
 }
 
@@ -790,7 +793,7 @@ __device__ __forceinline__ void fluxupdate32(const Args<float>& a, int c, double
         float r[NQ];
         face_rhs32<D, SCH, true, LES, false>(a, code >= 0 ? code : ~code, r);
 #pragma unroll
-        for (int v = 0; v < NQ; ++v) sum[v] = code >= 0 ? sum[v] + r[v] : sum[v] - r[v];
+        for (int v = 0; v < NQ; ++v) sum[v] += code >= 0 ? r[v] : neg_bits(r[v]);
     }
     apply32<D, RES, GH>(a, c, sum, in, Ak, Bk, dt, dt32, first);
 }

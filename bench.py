@@ -22,8 +22,10 @@ geometry) with its own value, e2e, roofline and speed-up over FP64;
 ``accuracy`` -- the acoustic-pressure error of the FP32-bulk state against the
 FP64 state after --accuracy-steps time steps (all cells and 72 probes at
 r = 50 D); ``wake3d`` -- the 3D cylinder wake (384x256x96, 9.4M hex cells)
-device-timed in both precisions, the HBM-bound case; ``fp64_pipe`` -- the
-FP64 instruction roofline that bounds the plain method on GB300.
+device-timed in both precisions, the HBM-bound case; ``batch64`` -- the
+64-case batched sweep (15.5M cells, one persistent kernel per RK stage) with
+its roofline, e2e and the plain FP64 path on the same cases; ``fp64_pipe`` --
+the FP64 instruction roofline that bounds the plain method on GB300.
 
 --impl reference times the reference's CPU implementation of the same
 workload on the host cores (the oracle port, set up by its own code: one
@@ -575,6 +577,19 @@ def run_gpu(args):
     if args.wake and args.workload.startswith("cylinder2d"):
         wake_thread = threading.Thread(target=build_wake, daemon=True)
         wake_thread.start()
+    # and so are the 64 cases of the batched sweep
+    sweep_built, sweep_err = [None], [None]
+
+    def build_sweep():
+        try:
+            sweep_built[0] = _build_sweep(64, 20261203)
+        except Exception as e:   # reported in the line
+            sweep_err[0] = repr(e)
+
+    sweep_thread = None
+    if args.batch and args.workload.startswith("cylinder2d"):
+        sweep_thread = threading.Thread(target=build_sweep, daemon=True)
+        sweep_thread.start()
     accuracy = None
     if args.accuracy_steps:
         accuracy = _accuracy(N, acoustics, case, ch, dt, args.accuracy_steps, local,
@@ -583,6 +598,16 @@ def run_gpu(args):
     if wake_thread is not None:
         wake_thread.join()
         wake = _wake_record(N, wake_built[0], args, local, hbm, peak_src) if wake_built[0] else {"error": wake_err[0]}
+        wake_built[0] = None
+    batch = None
+    if sweep_thread is not None:
+        sweep_thread.join()
+        if sweep_built[0]:
+            spec, built = sweep_built[0]
+            batch = _batch_record(N, built, spec, local, None, 1, args.batch_steps, 3)
+        else:
+            batch = {"error": sweep_err[0]}
+        sweep_built[0] = None
 
     if rank != 0:
         return 0
@@ -609,6 +634,7 @@ def run_gpu(args):
         "plain_fp64": dict(other, speedup=head["value"] / other["value"]) if fp32_head else None,
         "accuracy": accuracy,
         "wake3d": wake,
+        "batch64": batch,
         "cpu_baseline": base,
         "gpu_launches": head["launches_per_step"] * args.steps,
         "clocks": clk.summary(),
@@ -638,24 +664,22 @@ def _build_sweep(n_cases: int, seed: int):
     return spec, out
 
 
-def run_batch(args):
-    """The batched form: all sweep cases in one batch, autotuned launch shape."""
-    ws, rank, local, pg = _dist()
-    import numpy as np
-    from lfm_public_gb300 import _native as N, acoustics
-    n_cases = args.batch_cases
-    spec, built = _build_sweep(n_cases, 20261203)
+def _batch_record(N, built, spec, local, pg, ws, steps, warmup, tuning_arg=None, clk=None):
+    """The batched form on the sweep's cases: autotuned (or given) launch
+    shape, device-timed steps from the initial states, the HBM roofline of
+    the stage kernel, e2e through lfm_batch_advance, and the plain FP64 path
+    on the same cases one solver at a time."""
     cells = sum(ch.desc.n_cells for _, ch in built)
     need = sum(N.Batch.case_bytes(ch) for _, ch in built)
-    b = N.Batch(device=local, arena_bytes=need + (64 << 20), max_cases=n_cases)
+    b = N.Batch(device=local, arena_bytes=need + (64 << 20), max_cases=len(built))
     slots = [b.add(ch, c.delta_t) for c, ch in built]
-    if args.tuning:
-        v = [int(x) for x in args.tuning.split(",")]
+    if tuning_arg:
+        v = [int(x) for x in tuning_arg.split(",")]
         b.set_tuning(v[0], v[1], v[2], phased=v[3] if len(v) > 3 else 0)
         tuning = b.tuning()
     else:
         tuning = b.autotune(trial_steps=2)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         b.step(1)
     # timed steps start from the initial states (the reference's central
     # schemes diverge on some jittered triangulations after a few hundred steps)
@@ -663,17 +687,18 @@ def run_batch(args):
         b.set_state(s, ch.q0())
     if pg:
         pg.barrier()
-    with ClockSampler(local) as clk:
+    if clk is not None:
         time.sleep(0.3)
         clk.mark()
-        times = b.bench(args.steps, 512 << 20)
+    times = b.bench(steps, 512 << 20)
+    if clk is not None:
         clk.mark()
     nonfinite = [k for k, s in enumerate(slots) if b.case_status(s) != N.LFM_OK]
     if pg:
         pg.barrier()
     total_ms = _allmax(pg, float(times.sum()))
     stages = 5
-    value = ws * cells * stages * args.steps / (total_ms / 1000.0)
+    value = ws * cells * stages * steps / (total_ms / 1000.0)
 
     # end to end through the C ABI: every case's state in from pinned host
     # memory, one step of the batch, every state back out, each step
@@ -682,7 +707,7 @@ def run_batch(args):
              for _, ch in built]
     for (c, ch), h in zip(built, hosts):
         h[:] = ch.q0()
-    e2e_steps = max(1, min(args.steps, 20))
+    e2e_steps = max(1, min(steps, 20))
     t0 = time.perf_counter()
     for _ in range(e2e_steps):   # lfm_batch_advance: every state in, one step, every state out
         b.advance(slots, hosts, 1, hosts)
@@ -693,7 +718,7 @@ def run_batch(args):
     b.close()
 
     # the plain FP64 path on the same cases, one solver per case in turn
-    k64 = max(1, min(args.steps, 20))
+    k64 = max(1, min(steps, 20))
     ms64 = 0.0
     for c, ch in built:
         s = N.Solver(ch, precision=N.LFM_FP64, device=local)
@@ -701,6 +726,37 @@ def run_batch(args):
         ms64 += float(s.bench(k64, c.delta_t, 0).sum())
         s.close()
     v64 = cells * stages * k64 / (ms64 / 1000.0)
+
+    hbm, peak_src = _peaks()
+    step_bytes = 0.0
+    for sp, (c, ch) in zip(spec, built):
+        kb = kernel_bytes(2, 4 if sp["kind"] == "quad" else 3, True, "M1" if sp["solver"] == 0 else "M2", False)
+        step_bytes += sum(v for k, v in kb.items() if k not in ("k_tile_stage", "k_flux_update")) * ch.desc.n_cells
+    stage_ms = total_ms / ws / steps / stages
+    achieved = step_bytes / (stage_ms * 1e-3) / 1e9
+    return {
+        "workload": BATCH_DESC, "cases": len(built), "cells": cells, "value": value, "unit": UNIT,
+        "steps": steps, "ms_per_step": total_ms / steps, "tuning": tuning, "nonfinite_after_timed_steps": nonfinite,
+        "roofline": {"bound": "hbm", "kernel": "k_batch_stage", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "peak_source": peak_src, "traffic": None,
+                     "algorithmic_bytes_per_stage": step_bytes, "cells_per_launch": cells},
+        "plain_fp64": {"value": v64, "unit": UNIT, "steps_per_case": k64, "speedup": value / v64,
+                       "how": "one FP64 solver per case, cases in turn, CUDA-event time summed"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes},
+        "launches_per_step": launches,
+    }
+
+
+def run_batch(args):
+    """The batched form: all sweep cases in one batch, autotuned launch shape."""
+    ws, rank, local, pg = _dist()
+    import numpy as np
+    from lfm_public_gb300 import _native as N, acoustics
+    n_cases = args.batch_cases
+    spec, built = _build_sweep(n_cases, 20261203)
+    with ClockSampler(local) as clk:
+        rec = _batch_record(N, built, spec, local, pg, ws, args.steps, args.warmup, args.tuning, clk)
+    need = sum(N.Batch.case_bytes(ch) for _, ch in built)
 
     # each case against its own FP64 run
     accuracy = None
@@ -741,31 +797,20 @@ def run_batch(args):
 
     if rank != 0:
         return 0
-    peaks = json.load(open(PEAKS_FILE)) if os.path.exists(PEAKS_FILE) else {}
-    hbm = peaks.get("hbm_gbs", 6800.0)
-    step_bytes = 0.0
-    for sp, (c, ch) in zip(spec, built):
-        kb = kernel_bytes(2, 4 if sp["kind"] == "quad" else 3, True, "M1" if sp["solver"] == 0 else "M2", False)
-        step_bytes += sum(v for k, v in kb.items() if k not in ("k_tile_stage", "k_flux_update")) * ch.desc.n_cells
-    stage_ms = total_ms / ws / args.steps / stages
-    achieved = step_bytes / (stage_ms * 1e-3) / 1e9
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32-flux/f64-rk", "data": "synthetic (generated meshes and initial fields)",
-        "config": {"workload": BATCH_DESC, "cases": len(built), "cells": cells, "rk_stages": stages,
+        "metric": METRIC, "value": rec["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": rec["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32-flux/f64-rk", "data": "synthetic (generated meshes and initial fields)",
+        "config": {"workload": BATCH_DESC, "cases": rec["cases"], "cells": rec["cells"], "rk_stages": 5,
                    "precision": "fp32-bulk", "l2": "512 MB write between timed steps",
-                   "parallelism": f"replicas x{ws}", "tuning": tuning,
-                   "nonfinite_after_timed_steps": nonfinite},
-        "roofline": {"bound": "hbm", "kernel": "k_batch_stage", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
-                     "traffic": None, "algorithmic_bytes_per_stage": step_bytes, "cells_per_launch": cells},
-        "plain_fp64": {"value": v64, "unit": UNIT, "steps_per_case": k64, "speedup": value / v64,
-                       "how": "one FP64 solver per case, cases in turn, CUDA-event time summed"},
+                   "parallelism": f"replicas x{ws}", "tuning": rec["tuning"],
+                   "nonfinite_after_timed_steps": rec["nonfinite_after_timed_steps"]},
+        "roofline": rec["roofline"],
+        "plain_fp64": rec["plain_fp64"],
         "accuracy": accuracy,
         "cpu_baseline": None,
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes},
-        "gpu_launches": launches * args.steps,
+        "e2e": rec["e2e"],
+        "gpu_launches": rec["launches_per_step"] * args.steps,
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -974,6 +1019,9 @@ def main():
     ap.add_argument("--no-wake", dest="wake", action="store_false",
                     help="skip the 3D wake sub-record of the 2D cylinder workloads")
     ap.add_argument("--wake-steps", type=int, default=10)
+    ap.add_argument("--no-batch", dest="batch", action="store_false",
+                    help="leave the 64-case batched sweep out of the default line")
+    ap.add_argument("--batch-steps", type=int, default=20, help="timed steps of the batched sweep in the default line")
     ap.add_argument("--batch-cases", type=int, default=64)
     ap.add_argument("--tuning", default=None, help="batch launch shape block,items_per_thread,blocks_per_sm[,phased] "
                                                    "(default: autotuned)")

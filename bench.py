@@ -921,7 +921,9 @@ def run_serve(args):
     arena = int(args.serve_arena_gb * (1 << 30))
     for ri, rate in enumerate(float(x) for x in args.serve_rates.split(",")):
         stream = serve_stream(rate, window, len(lib), args.serve_step_scale, 77 + ri)
-        srv = N.Server(device=local, arena_bytes=arena, chunk_steps=args.serve_chunk, max_cases=args.serve_slots)
+        tuning = tuple(int(x) for x in args.serve_tuning.split(",")) if args.serve_tuning else None
+        srv = N.Server(device=local, arena_bytes=arena, chunk_steps=args.serve_chunk, max_cases=args.serve_slots,
+                       tuning=tuning, solo_cells=args.serve_solo_cells, max_solo=args.serve_max_solo)
         ids, shed, depth = {}, [], []
         t_start = time.perf_counter() + 0.2
         # times of the server clock (seconds since its creation) are read
@@ -942,10 +944,12 @@ def run_serve(args):
         parts = [list(range(i, len(stream), nthreads)) for i in range(nthreads)]
         with ThreadPoolExecutor(max_workers=nthreads) as ex:
             futs = [ex.submit(submitter, p) for p in parts]
+            st0 = srv.stats()
             while time.perf_counter() < t_start + window:
                 st = srv.stats()
                 depth.append(st["queued"] + st["running"])
                 time.sleep(0.05)
+            st_end = srv.stats()   # the device work of the window, finished requests or not
             for f in futs:
                 f.result()
         t_end_srv = t0_srv + window
@@ -978,6 +982,10 @@ def run_serve(args):
             "p99_s": float(np.percentile(lat, 99)) if lat else None,
             "queue_depth_max": int(max(depth) if depth else 0),
             "queue_depth_mean": float(np.mean(depth)) if depth else 0.0,
+            "device_busy_fraction": (st_end["busy_s"] - st0["busy_s"]) / window,
+            "cell_stage_rate_in_window": (st_end["cell_stages"] - st0["cell_stages"]) / window,
+            "cell_stage_rate_while_busy": ((st_end["cell_stages"] - st0["cell_stages"]) /
+                                           max(st_end["busy_s"] - st0["busy_s"], 1e-9)),
             "fp64_serial": {"completed": len(lat64), "shed": shed64, "throughput": work64 / window,
                             "p50_s": float(np.percentile(lat64, 50)) if lat64 else None,
                             "p99_s": float(np.percentile(lat64, 99)) if lat64 else None},
@@ -992,6 +1000,8 @@ def run_serve(args):
         "config": {"workload": SERVE_DESC, "library_cases": len(lib), "library_cells": int(sum(cells)),
                    "step_scale": args.serve_step_scale, "arena_gb": args.serve_arena_gb,
                    "chunk_steps": args.serve_chunk, "slots": args.serve_slots, "rates": args.serve_rates,
+                   "tuning": args.serve_tuning or "batch default",
+                   "solo_cells": args.serve_solo_cells, "max_solo": args.serve_max_solo,
                    "window_s": window,
                    "client_queue_bound": args.serve_queue},
         "serving": per_rate,
@@ -1034,6 +1044,11 @@ def main():
     ap.add_argument("--serve-chunk", type=int, default=50)
     ap.add_argument("--serve-slots", type=int, default=8,
                     help="requests on the GPU at once (the server admits by arena footprint up to this many)")
+    ap.add_argument("--serve-solo-cells", type=int, default=0,
+                    help="requests of at least this many cells run on their own single-case solver (0: none)")
+    ap.add_argument("--serve-max-solo", type=int, default=2, help="solo requests on the GPU at once")
+    ap.add_argument("--serve-tuning", default=None,
+                    help="batch launch shape of the server block,items_per_thread,blocks_per_sm[,cooperative]")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--renumber", default="none", choices=["none", "rcm", "hilbert", "hpath"],
                     help="solver order of the cells (single-case workloads)")

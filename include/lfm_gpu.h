@@ -525,6 +525,13 @@ typedef struct lfm_server_opts {
     int chunk_steps;          /* most steps between admission passes; 0 = 50 */
     int max_bypass;           /* times the oldest waiting request may be passed over; 0 = 8, < 0 = never */
     lfm_batch_tuning tuning;  /* launch shape of the stage kernel; block 0 = default */
+    /* Requests of at least solo_cells cells (0: none) run on their own
+     * FP32-bulk single-case solver instead of in the batch, at most max_solo
+     * at once (0 = 2): the single-case kernels are faster than the batch's on
+     * large cases, and a case gives the same bits either way. Their device
+     * memory is allocated at admission, outside the arena. */
+    int64_t solo_cells;
+    int max_solo;
 } lfm_server_opts;
 
 typedef struct lfm_request_info {
@@ -535,6 +542,7 @@ typedef struct lfm_request_info {
     int steps;
     double t_submit, t_admit, t_done;   /* -1 when not reached */
     size_t footprint_bytes;
+    int steps_done;           /* time steps advanced so far */
 } lfm_request_info;
 
 typedef struct lfm_server_stats {
@@ -542,6 +550,8 @@ typedef struct lfm_server_stats {
     int64_t completed;
     int64_t chunks;           /* chunks of steps run so far */
     double t_now;
+    double busy_s;            /* seconds the worker spent advancing chunks (launch to synchronisation) */
+    double cell_stages;       /* cell-RK-stage updates advanced so far, finished requests or not */
 } lfm_server_stats;
 
 int lfm_server_create(const lfm_server_opts* opts, lfm_server** out);

@@ -106,13 +106,14 @@ class SolverTuning(C.Structure):
 
 class ServerOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("rk_order", C.c_int), ("arena_bytes", C.c_size_t), ("max_cases", C.c_int),
-                ("chunk_steps", C.c_int), ("max_bypass", C.c_int), ("tuning", BatchTuning)]
+                ("chunk_steps", C.c_int), ("max_bypass", C.c_int), ("tuning", BatchTuning), ("solo_cells", C.c_int64),
+                ("max_solo", C.c_int)]
 
 
 class RequestInfo(C.Structure):
     _fields_ = [("state", C.c_int), ("status", C.c_int), ("cells", C.c_int64), ("steps", C.c_int),
                 ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double),
-                ("footprint_bytes", C.c_size_t)]
+                ("footprint_bytes", C.c_size_t), ("steps_done", C.c_int)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -120,7 +121,7 @@ class RequestInfo(C.Structure):
 
 class ServerStats(C.Structure):
     _fields_ = [("queued", C.c_int), ("running", C.c_int), ("completed", C.c_int64), ("chunks", C.c_int64),
-                ("t_now", C.c_double)]
+                ("t_now", C.c_double), ("busy_s", C.c_double), ("cell_stages", C.c_double)]
 
 
 class LfmError(RuntimeError):
@@ -763,13 +764,15 @@ class Server:
     (thread-safe; the worker runs in the library)."""
 
     def __init__(self, device: int = 0, rk_order: int = 5, arena_bytes: int = 0, max_cases: int = 256,
-                 chunk_steps: int = 50, max_bypass: int = 0, tuning: Optional[tuple] = None):
+                 chunk_steps: int = 50, max_bypass: int = 0, tuning: Optional[tuple] = None, solo_cells: int = 0,
+                 max_solo: int = 0):
         t = BatchTuning()
         if tuning:
             t.block, t.items_per_thread, t.blocks_per_sm = tuning[:3]
             t.cooperative = tuning[3] if len(tuning) > 3 else 1
         opts = ServerOpts(device=device, rk_order=rk_order, arena_bytes=arena_bytes, max_cases=max_cases,
-                          chunk_steps=chunk_steps, max_bypass=max_bypass, tuning=t)
+                          chunk_steps=chunk_steps, max_bypass=max_bypass, tuning=t, solo_cells=solo_cells,
+                          max_solo=max_solo)
         h = C.c_void_p()
         check(load_library().lfm_server_create(C.byref(opts), C.byref(h)))
         self._h = h

@@ -12,7 +12,11 @@
 // requests that have finished (or whose state became non-finite), copying
 // their state out and freeing their slot and block. Requests arriving while
 // others run join at the next chunk boundary, so their work overlaps on the
-// device.
+// device. Large requests (solo_cells) run instead on their own single-case
+// FP32-bulk solver, created at admission from a host copy of their
+// description and stepped chunk by chunk on its own stream beside the batch
+// (the batch kernel is a generic one; the single-case kernels are faster on
+// large cases and give the same bits).
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -30,9 +34,66 @@
 
 namespace {
 
+// A host copy of a solver description (the caller's may be freed once
+// lfm_server_submit returns): every array it points to, owned.
+struct OwnedDesc {
+    lfm_solver_desc d{};
+    std::vector<int64_t> i64[8];
+    std::vector<double> f64[18];
+    std::vector<uint8_t> u8;
+    std::vector<int8_t> s8;
+    std::vector<int> ik;
+    std::vector<int32_t> i32;
+
+    template <typename T>
+    static const T* keep(std::vector<T>& v, const T* src, size_t n) {
+        if (!src) return nullptr;
+        v.assign(src, src + n);
+        return v.data();
+    }
+
+    explicit OwnedDesc(const lfm_solver_desc* s) : d(*s) {
+        const size_t nf = (size_t)s->n_faces, nc = (size_t)s->n_cells, ng = (size_t)s->n_ghosts;
+        const size_t D = (size_t)s->dim, nh = (size_t)s->n_halos;
+        const size_t ne = s->cell_face_offsets ? (size_t)s->cell_face_offsets[nc] : 0;
+        const size_t ns = s->cell_s_offsets ? (size_t)s->cell_s_offsets[nc] : 0;
+        d.face_p = keep(i64[0], s->face_p, nf);
+        d.face_n = keep(i64[1], s->face_n, nf);
+        d.face_ghost = keep(u8, s->face_ghost, nf);
+        d.S = keep(f64[0], s->S, D * nf);
+        d.d = keep(f64[1], s->d, D * nf);
+        d.w = keep(f64[2], s->w, nf);
+        d.smag = keep(f64[3], s->smag, nf);
+        d.dmag_inv = keep(f64[4], s->dmag_inv, nf);
+        d.dnorm = keep(f64[5], s->dnorm, D * nf);
+        d.delta_mag = keep(f64[6], s->delta_mag, nf);
+        d.K = keep(f64[7], s->K, D * nf);
+        d.vol_inv = keep(f64[8], s->vol_inv, nc);
+        d.sponge = keep(f64[9], s->sponge, nc);
+        d.ghost_cell = keep(i64[2], s->ghost_cell, ng);
+        d.ghost_kind = keep(ik, s->ghost_kind, ng);
+        d.cell_face_offsets = keep(i64[3], s->cell_face_offsets, nc + 1);
+        d.cell_faces = keep(i64[4], s->cell_faces, ne);
+        d.cell_face_sign = keep(s8, s->cell_face_sign, ne);
+        d.cell_s_offsets = keep(i64[5], s->cell_s_offsets, nc + 1);
+        d.cell_s = keep(f64[10], s->cell_s, D * ns);
+        d.q0 = keep(f64[11], s->q0, (size_t)s->nq * nc);
+        d.rkA = keep(f64[12], s->rkA, (size_t)std::max(s->rk_order, 0));
+        d.rkB = keep(f64[13], s->rkB, (size_t)std::max(s->rk_order, 0));
+        d.halo_src_part = keep(i64[6], s->halo_src_part, nh);
+        d.halo_src_cell = keep(i64[7], s->halo_src_cell, nh);
+        d.ghost_patch = keep(i32, s->ghost_patch, ng);
+        d.smag_c = keep(f64[14], s->smag_c, nc);
+    }
+};
+
 struct Request {
     int64_t id = 0;
     std::unique_ptr<lfm::batch::PreparedCase> pc;
+    // solo requests: their description until admission, then their solver
+    std::unique_ptr<OwnedDesc> desc;
+    lfm_solver* solver = nullptr;
+    double dt = 0;
     size_t bytes = 0;
     int nsteps = 0, remaining = 0;
     int slot = -1;
@@ -43,6 +104,10 @@ struct Request {
     double tSubmit = 0, tAdmit = -1, tDone = -1;
     int nq = 0, nc = 0;
     std::vector<double> result;
+
+    ~Request() {
+        if (solver) lfm_solver_destroy(solver);
+    }
 };
 
 double since(std::chrono::steady_clock::time_point t0) {
@@ -57,6 +122,9 @@ struct lfm_server {
     int rkOrder = 5;
     int chunkSteps = 50;
     int maxBypass = 8;
+    int64_t soloCells = 0;   // requests of at least this many cells run on their own solver (0: none)
+    int maxSolo = 2;
+    int soloActive = 0;
     std::chrono::steady_clock::time_point t0;
     std::mutex mu;
     std::condition_variable cvWork, cvDone;
@@ -66,6 +134,8 @@ struct lfm_server {
     int64_t nextId = 1;
     int64_t completed = 0;
     int64_t chunks = 0;
+    double busy = 0;          // seconds spent advancing chunks
+    double cellStages = 0;    // cell-RK-stage updates advanced
     bool stop = false;
     int workerError = LFM_OK;
     std::string workerMsg;
@@ -105,9 +175,30 @@ int admit(lfm_server* s) {
     std::vector<Request*> admitted, rejected;
     size_t largest = 0, total = 0, arena = 0;
     lfm_batch_memory(s->batch, &largest, &total, &arena);
+    int solo = s->soloActive;
     for (size_t k = 0; k < queue.size(); ++k) {
         Request* r = queue[k];
         r->tried = true;
+        if (r->desc) {   // its own solver, while fewer than maxSolo run
+            int rc = LFM_ERR_NOMEM;
+            if (solo < s->maxSolo) {
+                lfm_solver_opts o{LFM_FP32_BULK, s->device, 0};
+                rc = lfm_solver_create(&r->desc->d, &o, &r->solver);
+            }
+            if (rc == LFM_OK) {
+                ++solo;
+                admitted.push_back(r);
+                continue;
+            }
+            r->solver = nullptr;
+            if (rc != LFM_ERR_NOMEM) {   // a description the solver refuses
+                r->status = rc;
+                rejected.push_back(r);
+                continue;
+            }
+            if (++r->bypassed > s->maxBypass) break;
+            continue;
+        }
         if (r->bytes > arena) {   // can never fit
             rejected.push_back(r);
             continue;
@@ -127,14 +218,17 @@ int admit(lfm_server* s) {
     for (Request* r : admitted) {
         r->state = 1;
         r->tAdmit = now;
-        r->pc.reset();   // the image is on the device now
+        r->pc.reset();   // the image (or the solver's copy) is on the device now
+        r->desc.reset();
         s->active.push_back(r);
     }
+    s->soloActive = solo;
     for (Request* r : rejected) {
         r->state = 2;
-        r->status = LFM_ERR_NOMEM;
+        if (r->status == LFM_OK) r->status = LFM_ERR_NOMEM;
         r->tDone = now;
         r->pc.reset();
+        r->desc.reset();
     }
     if (!admitted.empty() || !rejected.empty()) {
         std::deque<Request*> rest;
@@ -180,29 +274,67 @@ void workerLoop(lfm_server* s) {
         }
         if (act.empty()) continue;
         int n = s->chunkSteps;
-        for (Request* r : act) n = std::min(n, r->remaining);
-        if ((rc = lfm_batch_step(s->batch, n)) != LFM_OK) {
+        bool batched = false;
+        for (Request* r : act) {
+            n = std::min(n, r->remaining);
+            batched = batched || !r->solver;
+        }
+        const double tChunk = since(s->t0);
+        // the solo requests' steps on their own streams, then the batch's;
+        // all run on the device together, one synchronisation each
+        for (Request* r : act)
+            if (r->solver && (rc = lfm_solver_step(r->solver, n, r->dt)) != LFM_OK) {
+                fail(s, rc);
+                return;
+            }
+        if (batched && (rc = lfm_batch_step(s->batch, n)) != LFM_OK) {
             fail(s, rc);
             return;
         }
-        rc = lfm_batch_sync(s->batch);
+        rc = batched ? lfm_batch_sync(s->batch) : LFM_OK;
         if (rc != LFM_OK && rc != LFM_ERR_NUMERIC) {
             fail(s, rc);
             return;
         }
-        ++s->chunks;
+        for (Request* r : act) {
+            if (!r->solver) continue;
+            const int st = lfm_solver_sync(r->solver);
+            if (st == LFM_ERR_NUMERIC) {
+                r->status = st;
+            } else if (st != LFM_OK) {
+                fail(s, st);
+                return;
+            }
+        }
+        {
+            double cells = 0;
+            for (Request* r : act) cells += (double)r->nc;
+            std::lock_guard<std::mutex> lk(s->mu);
+            ++s->chunks;
+            s->busy += since(s->t0) - tChunk;
+            s->cellStages += cells * (double)n * (double)s->rkOrder;
+            for (Request* r : act) r->remaining -= n;
+        }
         std::vector<Request*> done;
         for (Request* r : act) {
-            r->remaining -= n;
             int st = LFM_OK;
-            if (rc == LFM_ERR_NUMERIC && lfm_batch_case_status(s->batch, r->slot, &st) != LFM_OK) st = LFM_ERR_CUDA;
+            if (!r->solver && rc == LFM_ERR_NUMERIC && lfm_batch_case_status(s->batch, r->slot, &st) != LFM_OK)
+                st = LFM_ERR_CUDA;
             if (st != LFM_OK) r->status = st;
             if (r->remaining == 0 || r->status != LFM_OK) done.push_back(r);
         }
         for (Request* r : done) {
             r->result.resize((size_t)r->nq * r->nc);
-            int e1 = lfm_batch_get_state(s->batch, r->slot, r->result.data());
-            int e2 = lfm_batch_remove(s->batch, r->slot);
+            int e1, e2 = LFM_OK;
+            if (r->solver) {
+                e1 = lfm_solver_get_state(r->solver, r->result.data());
+                lfm_solver_destroy(r->solver);
+                r->solver = nullptr;
+                --s->soloActive;
+            } else {
+                e1 = lfm_batch_get_state(s->batch, r->slot, r->result.data());
+                e2 = lfm_batch_remove(s->batch, r->slot);
+            }
             if (e1 || e2) {
                 fail(s, e1 ? e1 : e2);
                 return;
@@ -235,6 +367,7 @@ void fillInfo(const lfm_server* s, const Request& r, lfm_request_info* info) {
     info->t_admit = r.tAdmit;
     info->t_done = r.tDone;
     info->footprint_bytes = r.bytes;
+    info->steps_done = r.nsteps - r.remaining;
 }
 
 }  // namespace
@@ -259,6 +392,8 @@ extern "C" int lfm_server_create(const lfm_server_opts* opts, lfm_server** out) 
     s->rkOrder = opts->rk_order;
     s->chunkSteps = opts->chunk_steps > 0 ? opts->chunk_steps : 50;
     s->maxBypass = opts->max_bypass == 0 ? 8 : std::max(0, opts->max_bypass);
+    s->soloCells = std::max<int64_t>(0, opts->solo_cells);
+    s->maxSolo = opts->max_solo > 0 ? opts->max_solo : 2;
     s->t0 = std::chrono::steady_clock::now();
     s->worker = std::thread(workerLoop, s);
     *out = s;
@@ -282,15 +417,30 @@ extern "C" int lfm_server_submit(lfm_server* s, const lfm_solver_desc* d, double
     *id = 0;
     if (nsteps <= 0) return lfm::setError(LFM_ERR_INVALID, "nsteps must be positive");
     const double tSubmit = since(s->t0);
-    lfm::batch::PreparedCase* pc = nullptr;
-    int rc = lfm::batch::prepareCase(d, dt, s->rkOrder, &pc);
-    if (rc) return rc;
     std::unique_ptr<Request> r(new Request);
-    r->pc.reset(pc);
-    r->bytes = pc->layout.total;
+    if (s->soloCells > 0 && d && d->n_cells >= s->soloCells && d->n_halos == 0) {
+        if (d->rk_order != s->rkOrder)
+            return lfm::setError(LFM_ERR_INVALID, "the request's rk_order differs from the server's");
+        if (!d->q0) return lfm::setError(LFM_ERR_INVALID, "the request has no initial state (desc->q0)");
+        if (!(dt > 0.0)) return lfm::setError(LFM_ERR_INVALID, "dt must be positive");
+        try {
+            r->desc.reset(new OwnedDesc(d));
+        } catch (const std::bad_alloc&) {
+            return lfm::setError(LFM_ERR_NOMEM, "host copy of the request");
+        }
+        r->nq = d->nq;
+        r->nc = (int)d->n_cells;
+        r->dt = dt;
+    } else {
+        lfm::batch::PreparedCase* pc = nullptr;
+        int rc = lfm::batch::prepareCase(d, dt, s->rkOrder, &pc);
+        if (rc) return rc;
+        r->pc.reset(pc);
+        r->bytes = pc->layout.total;
+        r->nq = pc->nq;
+        r->nc = pc->nc;
+    }
     r->nsteps = r->remaining = nsteps;
-    r->nq = pc->nq;
-    r->nc = pc->nc;
     r->tSubmit = tSubmit;
     {
         std::lock_guard<std::mutex> lk(s->mu);
@@ -352,6 +502,8 @@ extern "C" int lfm_server_get_stats(lfm_server* s, lfm_server_stats* st) {
     st->completed = s->completed;
     st->chunks = s->chunks;
     st->t_now = since(s->t0);
+    st->busy_s = s->busy;
+    st->cell_stages = s->cellStages;
     if (s->workerError) return lfm::setError(s->workerError, "server stopped: " + s->workerMsg);
     return LFM_OK;
 }

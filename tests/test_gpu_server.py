@@ -118,3 +118,47 @@ def test_nonfinite_request_is_retired_alone():
     assert ib["status"] == N.LFM_ERR_NUMERIC
     assert ig["status"] == N.LFM_OK
     assert np.array_equal(qg, _alone(chg, good.delta_t, 20))
+
+
+@pytest.mark.parametrize("max_solo", [1, 2])
+def test_solo_requests_give_the_batched_bits(max_solo):
+    """Requests of at least solo_cells cells run on their own single-case
+    FP32-bulk solver beside the batch; every result keeps the bits of the
+    same request run alone in the batch, and the server's counters add up
+    (cell-stage updates = cells x steps x stages of every request)."""
+    reqs = _requests()
+    sizes = [ch.desc.n_cells for _, ch, _ in reqs]
+    solo_cells = 2000
+    assert any(n >= solo_cells for n in sizes) and any(n < solo_cells for n in sizes)
+    srv = N.Server(arena_bytes=256 << 20, chunk_steps=7, solo_cells=solo_cells, max_solo=max_solo)
+    ids = [srv.submit(ch, c.delta_t, n) for c, ch, n in reqs]
+    for rid in ids:
+        assert srv.wait(rid, 60.0)
+    st = srv.stats()
+    results = [srv.result(rid) for rid in ids]
+    srv.close()
+    for (q, info), (c, ch, n) in zip(results, reqs):
+        assert info["status"] == N.LFM_OK and info["steps"] == n and info["steps_done"] == n
+        assert np.array_equal(q, _alone(ch, c.delta_t, n)), c.name
+    assert st["cell_stages"] == sum(ch.desc.n_cells * n * 5 for _, ch, n in reqs)
+    assert 0 < st["busy_s"] <= st["t_now"]
+
+
+def test_solo_request_runs_an_les_case():
+    """The batch refuses Smagorinsky LES cases; a solo request runs one on
+    its own solver, with the single-case FP32-bulk solver's bits."""
+    from tests.helpers import load_golden
+    case, _ = load_golden("les_cyl24x12_m2")
+    ch = N.CaseHandle.from_case(case)
+    n = 9
+    srv = N.Server(arena_bytes=64 << 20, solo_cells=1)
+    rid = srv.submit(ch, case.delta_t, n)
+    assert srv.wait(rid, 60.0)
+    q, info = srv.result(rid)
+    srv.close()
+    assert info["status"] == N.LFM_OK
+    s = N.Solver(ch, precision=N.LFM_FP32_BULK)
+    s.step(n, case.delta_t)
+    s.sync()
+    assert np.array_equal(q, s.get_state())
+    s.close()

@@ -1044,9 +1044,9 @@ def main():
     ap.add_argument("--serve-chunk", type=int, default=50)
     ap.add_argument("--serve-slots", type=int, default=8,
                     help="requests on the GPU at once (the server admits by arena footprint up to this many)")
-    ap.add_argument("--serve-solo-cells", type=int, default=0,
+    ap.add_argument("--serve-solo-cells", type=int, default=100000,
                     help="requests of at least this many cells run on their own single-case solver (0: none)")
-    ap.add_argument("--serve-max-solo", type=int, default=2, help="solo requests on the GPU at once")
+    ap.add_argument("--serve-max-solo", type=int, default=4, help="solo requests on the GPU at once")
     ap.add_argument("--serve-tuning", default=None,
                     help="batch launch shape of the server block,items_per_thread,blocks_per_sm[,cooperative]")
     ap.add_argument("--no-cpu-baseline", action="store_true")

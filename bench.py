@@ -24,7 +24,10 @@ FP64 state after --accuracy-steps time steps (all cells and 72 probes at
 r = 50 D); ``wake3d`` -- the 3D cylinder wake (384x256x96, 9.4M hex cells)
 device-timed in both precisions, the HBM-bound case; ``batch64`` -- the
 64-case batched sweep (15.5M cells, one persistent kernel per RK stage) with
-its roofline, e2e and the plain FP64 path on the same cases; ``fp64_pipe`` --
+its roofline, e2e and the plain FP64 path on the same cases; ``serve`` -- a
+30-second Poisson stream of solve requests into the request server (p50 /
+p99, throughput, against the same stream served one request at a time on the
+FP64 path); ``fp64_pipe`` --
 the FP64 instruction roofline that bounds the plain method on GB300.
 
 --impl reference times the reference's CPU implementation of the same
@@ -590,6 +593,19 @@ def run_gpu(args):
     if args.batch and args.workload.startswith("cylinder2d"):
         sweep_thread = threading.Thread(target=build_sweep, daemon=True)
         sweep_thread.start()
+    # and so is the serving library
+    lib_built, lib_err = [None], [None]
+
+    def build_lib():
+        try:
+            lib_built[0] = _serve_library(args.serve_library, local)
+        except Exception as e:   # reported in the line
+            lib_err[0] = repr(e)
+
+    lib_thread = None
+    if args.serve and args.workload.startswith("cylinder2d"):
+        lib_thread = threading.Thread(target=build_lib, daemon=True)
+        lib_thread.start()
     accuracy = None
     if args.accuracy_steps:
         accuracy = _accuracy(N, acoustics, case, ch, dt, args.accuracy_steps, local,
@@ -608,6 +624,18 @@ def run_gpu(args):
         else:
             batch = {"error": sweep_err[0]}
         sweep_built[0] = None
+    serve = None
+    if lib_thread is not None:
+        lib_thread.join()
+        if lib_built[0]:
+            lib = lib_built[0]
+            fp64 = _fp64_times(lib, local)
+            rate = float(args.serve_default_rate)
+            serve = dict(_serve_config(args, lib, args.serve_default_window, str(rate)),
+                         **_serve_rate(N, args, lib, fp64, rate, args.serve_default_window, 77, local))
+        else:
+            serve = {"error": lib_err[0]}
+        lib_built[0] = None
 
     if rank != 0:
         return 0
@@ -635,6 +663,7 @@ def run_gpu(args):
         "accuracy": accuracy,
         "wake3d": wake,
         "batch64": batch,
+        "serve": serve,
         "cpu_baseline": base,
         "gpu_launches": head["launches_per_step"] * args.steps,
         "clocks": clk.summary(),
@@ -870,24 +899,12 @@ def serve_stream(rate: float, window: float, n_lib: int, step_scale: float, seed
         out.append((t, int(rng.integers(0, n_lib)), max(1, int(round(rng.uniform(200, 5000) * step_scale)))))
 
 
-def run_serve(args):
-    """Continuous batching of a Poisson request stream at several rates, each
-    for a fixed window of wall time, against the same streams served one
-    request at a time on the plain FP64 path.
-
-    Every listed rate asks for more work than a GPU does (a request averages
-    about 9e9 cell-stage updates), so both servers are saturated: the client
-    sheds an arrival while --serve-queue requests already wait (both servers
-    the same bound), and a request counts when it completes inside the window.
-    Reported per rate: arrivals, shed, completed, throughput (cell-stage
-    updates of the completed requests per second of window), p50 / p99 time
-    to completion, queue depth. The FP64 server's timeline is replayed from
-    each library case's measured FP64 set-up, step and read-back times."""
-    ws, rank, local, pg = _dist()
-    import numpy as np
+def _serve_library(n: int, local: int):
+    """The request library (cases and handles, set up in parallel threads) and
+    each case's plain FP64 set-up, step and read-back times."""
     from concurrent.futures import ThreadPoolExecutor
     from lfm_public_gb300 import _native as N
-    spec = serve_spec(args.serve_library, 5150, 1.0)
+    spec = serve_spec(n, 5150, 1.0)
 
     def one(sp):
         c = serve_case(sp)
@@ -895,9 +912,11 @@ def run_serve(args):
 
     with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
         lib = list(ex.map(one, spec))
-    cells = [ch.desc.n_cells for _, ch in lib]
+    return lib
 
-    # the FP64 path per library case: set-up, ms per step, read-back
+
+def _fp64_times(lib, local):
+    from lfm_public_gb300 import _native as N
     fp64 = []
     for c, ch in lib:
         t0 = time.perf_counter()
@@ -915,81 +934,117 @@ def run_serve(args):
         t4 = time.perf_counter()
         s.close()
         fp64.append((t1 - t0, (t3 - t2) / k, t4 - t3))
+    return fp64
 
-    window = args.serve_window
-    per_rate = []
+
+def _serve_rate(N, args, lib, fp64, rate, window, seed, local):
+    """One Poisson stream of `rate` requests per second over `window` seconds
+    into a server, and the same stream replayed on the FP64 server."""
+    import numpy as np
+    from concurrent.futures import ThreadPoolExecutor
+    cells = [ch.desc.n_cells for _, ch in lib]
     arena = int(args.serve_arena_gb * (1 << 30))
-    for ri, rate in enumerate(float(x) for x in args.serve_rates.split(",")):
-        stream = serve_stream(rate, window, len(lib), args.serve_step_scale, 77 + ri)
-        tuning = tuple(int(x) for x in args.serve_tuning.split(",")) if args.serve_tuning else None
-        srv = N.Server(device=local, arena_bytes=arena, chunk_steps=args.serve_chunk, max_cases=args.serve_slots,
-                       tuning=tuning, solo_cells=args.serve_solo_cells, max_solo=args.serve_max_solo)
-        ids, shed, depth = {}, [], []
-        t_start = time.perf_counter() + 0.2
-        # times of the server clock (seconds since its creation) are read
-        # from the request infos; the window ends `window` after the start
-        t0_srv = srv.stats()["t_now"] + 0.2
+    stream = serve_stream(rate, window, len(lib), args.serve_step_scale, seed)
+    tuning = tuple(int(x) for x in args.serve_tuning.split(",")) if args.serve_tuning else None
+    srv = N.Server(device=local, arena_bytes=arena, chunk_steps=args.serve_chunk, max_cases=args.serve_slots,
+                   tuning=tuning, solo_cells=args.serve_solo_cells, max_solo=args.serve_max_solo)
+    ids, shed, depth = {}, [], []
+    t_start = time.perf_counter() + 0.2
+    # times of the server clock (seconds since its creation) are read
+    # from the request infos; the window ends `window` after the start
+    t0_srv = srv.stats()["t_now"] + 0.2
 
-        def submitter(part):
-            for k in part:
-                t, li, steps = stream[k]
-                time.sleep(max(0.0, t_start + t - time.perf_counter()))
-                if srv.stats()["queued"] >= args.serve_queue:
-                    shed.append(k)
-                    continue
-                c, ch = lib[li]
-                ids[k] = srv.submit(ch, c.delta_t, steps)
-
-        nthreads = 8
-        parts = [list(range(i, len(stream), nthreads)) for i in range(nthreads)]
-        with ThreadPoolExecutor(max_workers=nthreads) as ex:
-            futs = [ex.submit(submitter, p) for p in parts]
-            st0 = srv.stats()
-            while time.perf_counter() < t_start + window:
-                st = srv.stats()
-                depth.append(st["queued"] + st["running"])
-                time.sleep(0.05)
-            st_end = srv.stats()   # the device work of the window, finished requests or not
-            for f in futs:
-                f.result()
-        t_end_srv = t0_srv + window
-        lat, work_done = [], 0
-        for k, rid in ids.items():
-            info = srv.info(rid)
-            if info["state"] == 2 and info["status"] == N.LFM_OK and info["t_done"] <= t_end_srv:
-                lat.append(info["t_done"] - info["t_submit"])
-                _, li, steps = stream[k]
-                work_done += cells[li] * 5 * steps
-        srv.close()
-        # the FP64 server: first come, first served, one request at a time,
-        # the same queue bound
-        fin, lat64, work64, shed64, waiting = 0.0, [], 0, 0, []
-        for t, li, steps in stream:
-            waiting = [w for w in waiting if w > t]          # start times still ahead
-            if len(waiting) >= args.serve_queue:
-                shed64 += 1
+    def submitter(part):
+        for k in part:
+            t, li, steps = stream[k]
+            time.sleep(max(0.0, t_start + t - time.perf_counter()))
+            if srv.stats()["queued"] >= args.serve_queue:
+                shed.append(k)
                 continue
-            start = max(t, fin)
-            fin = start + fp64[li][0] + steps * fp64[li][1] + fp64[li][2]
-            waiting.append(start)
-            if fin <= window:
-                lat64.append(fin - t)
-                work64 += cells[li] * 5 * steps
-        per_rate.append({
-            "rate_per_s": rate, "window_s": window, "arrivals": len(stream), "shed": len(shed),
-            "completed": len(lat), "throughput": work_done / window,
-            "p50_s": float(np.percentile(lat, 50)) if lat else None,
-            "p99_s": float(np.percentile(lat, 99)) if lat else None,
-            "queue_depth_max": int(max(depth) if depth else 0),
-            "queue_depth_mean": float(np.mean(depth)) if depth else 0.0,
-            "device_busy_fraction": (st_end["busy_s"] - st0["busy_s"]) / window,
-            "cell_stage_rate_in_window": (st_end["cell_stages"] - st0["cell_stages"]) / window,
-            "cell_stage_rate_while_busy": ((st_end["cell_stages"] - st0["cell_stages"]) /
-                                           max(st_end["busy_s"] - st0["busy_s"], 1e-9)),
-            "fp64_serial": {"completed": len(lat64), "shed": shed64, "throughput": work64 / window,
-                            "p50_s": float(np.percentile(lat64, 50)) if lat64 else None,
-                            "p99_s": float(np.percentile(lat64, 99)) if lat64 else None},
-        })
+            c, ch = lib[li]
+            ids[k] = srv.submit(ch, c.delta_t, steps)
+
+    nthreads = 8
+    parts = [list(range(i, len(stream), nthreads)) for i in range(nthreads)]
+    with ThreadPoolExecutor(max_workers=nthreads) as ex:
+        futs = [ex.submit(submitter, p) for p in parts]
+        st0 = srv.stats()
+        while time.perf_counter() < t_start + window:
+            st = srv.stats()
+            depth.append(st["queued"] + st["running"])
+            time.sleep(0.05)
+        st_end = srv.stats()   # the device work of the window, finished requests or not
+        for f in futs:
+            f.result()
+    t_end_srv = t0_srv + window
+    lat, work_done = [], 0
+    for k, rid in ids.items():
+        info = srv.info(rid)
+        if info["state"] == 2 and info["status"] == N.LFM_OK and info["t_done"] <= t_end_srv:
+            lat.append(info["t_done"] - info["t_submit"])
+            _, li, steps = stream[k]
+            work_done += cells[li] * 5 * steps
+    srv.close()
+    # the FP64 server: first come, first served, one request at a time,
+    # the same queue bound
+    fin, lat64, work64, shed64, waiting = 0.0, [], 0, 0, []
+    for t, li, steps in stream:
+        waiting = [w for w in waiting if w > t]          # start times still ahead
+        if len(waiting) >= args.serve_queue:
+            shed64 += 1
+            continue
+        start = max(t, fin)
+        fin = start + fp64[li][0] + steps * fp64[li][1] + fp64[li][2]
+        waiting.append(start)
+        if fin <= window:
+            lat64.append(fin - t)
+            work64 += cells[li] * 5 * steps
+    return {
+        "rate_per_s": rate, "window_s": window, "arrivals": len(stream), "shed": len(shed),
+        "completed": len(lat), "throughput": work_done / window,
+        "p50_s": float(np.percentile(lat, 50)) if lat else None,
+        "p99_s": float(np.percentile(lat, 99)) if lat else None,
+        "queue_depth_max": int(max(depth) if depth else 0),
+        "queue_depth_mean": float(np.mean(depth)) if depth else 0.0,
+        "device_busy_fraction": (st_end["busy_s"] - st0["busy_s"]) / window,
+        "cell_stage_rate_in_window": (st_end["cell_stages"] - st0["cell_stages"]) / window,
+        "cell_stage_rate_while_busy": ((st_end["cell_stages"] - st0["cell_stages"]) /
+                                       max(st_end["busy_s"] - st0["busy_s"], 1e-9)),
+        "fp64_serial": {"completed": len(lat64), "shed": shed64, "throughput": work64 / window,
+                        "p50_s": float(np.percentile(lat64, 50)) if lat64 else None,
+                        "p99_s": float(np.percentile(lat64, 99)) if lat64 else None},
+    }
+
+
+def _serve_config(args, lib, window, rates):
+    return {"workload": SERVE_DESC, "library_cases": len(lib),
+            "library_cells": int(sum(ch.desc.n_cells for _, ch in lib)), "step_scale": args.serve_step_scale,
+            "arena_gb": args.serve_arena_gb, "chunk_steps": args.serve_chunk, "slots": args.serve_slots,
+            "rates": rates, "tuning": args.serve_tuning or "batch default", "solo_cells": args.serve_solo_cells,
+            "max_solo": args.serve_max_solo, "window_s": window, "client_queue_bound": args.serve_queue}
+
+
+def run_serve(args):
+    """Continuous batching of a Poisson request stream at several rates, each
+    for a fixed window of wall time, against the same streams served one
+    request at a time on the plain FP64 path.
+
+    Every listed rate asks for more work than a GPU does (a request averages
+    about 9e9 cell-stage updates), so both servers are saturated: the client
+    sheds an arrival while --serve-queue requests already wait (both servers
+    the same bound), and a request counts when it completes inside the window.
+    Reported per rate: arrivals, shed, completed, throughput (cell-stage
+    updates of the completed requests per second of window), p50 / p99 time
+    to completion, queue depth, the server's busy fraction and the work it
+    advanced in the window. The FP64 server's timeline is replayed from each
+    library case's measured FP64 set-up, step and read-back times."""
+    ws, rank, local, pg = _dist()
+    from lfm_public_gb300 import _native as N
+    lib = _serve_library(args.serve_library, local)
+    fp64 = _fp64_times(lib, local)
+    window = args.serve_window
+    per_rate = [_serve_rate(N, args, lib, fp64, rate, window, 77 + ri, local)
+                for ri, rate in enumerate(float(x) for x in args.serve_rates.split(","))]
     if rank != 0:
         return 0
     best = max(per_rate, key=lambda r: r["throughput"])
@@ -997,13 +1052,7 @@ def run_serve(args):
         "metric": METRIC, "value": best["throughput"], "unit": UNIT, "n_gpus": ws, "steps": None,
         "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32-flux/f64-rk", "data": "synthetic (generated meshes and initial fields)",
-        "config": {"workload": SERVE_DESC, "library_cases": len(lib), "library_cells": int(sum(cells)),
-                   "step_scale": args.serve_step_scale, "arena_gb": args.serve_arena_gb,
-                   "chunk_steps": args.serve_chunk, "slots": args.serve_slots, "rates": args.serve_rates,
-                   "tuning": args.serve_tuning or "batch default",
-                   "solo_cells": args.serve_solo_cells, "max_solo": args.serve_max_solo,
-                   "window_s": window,
-                   "client_queue_bound": args.serve_queue},
+        "config": _serve_config(args, lib, window, args.serve_rates),
         "serving": per_rate,
         "fp64_serial_note": "FP64 server: the same streams first come first served, one request at a time, the "
                             "same queue bound, timeline replayed from each library case's measured FP64 set-up, "
@@ -1044,6 +1093,12 @@ def main():
     ap.add_argument("--serve-chunk", type=int, default=50)
     ap.add_argument("--serve-slots", type=int, default=8,
                     help="requests on the GPU at once (the server admits by arena footprint up to this many)")
+    ap.add_argument("--no-serve", dest="serve", action="store_false",
+                    help="leave the serving stream out of the default line")
+    ap.add_argument("--serve-default-rate", type=float, default=20.0,
+                    help="arrival rate (1/s) of the default line's serving stream")
+    ap.add_argument("--serve-default-window", type=float, default=30.0,
+                    help="seconds of the default line's serving stream")
     ap.add_argument("--serve-solo-cells", type=int, default=100000,
                     help="requests of at least this many cells run on their own single-case solver (0: none)")
     ap.add_argument("--serve-max-solo", type=int, default=4, help="solo requests on the GPU at once")

@@ -528,8 +528,10 @@ typedef struct lfm_server_opts {
     /* Requests of at least solo_cells cells (0: none) run on their own
      * FP32-bulk single-case solver instead of in the batch, at most max_solo
      * at once (0 = 2): the single-case kernels are faster than the batch's on
-     * large cases, and a case gives the same bits either way. Their device
-     * memory is allocated at admission, outside the arena. */
+     * large cases, and a case gives the same bits either way. A second server
+     * thread builds their solvers ahead of admission while the batch runs;
+     * their device memory, outside the arena, is held from that build until
+     * the request retires (at most max_solo built or running at once). */
     int64_t solo_cells;
     int max_solo;
 } lfm_server_opts;

@@ -13,10 +13,11 @@
 // their state out and freeing their slot and block. Requests arriving while
 // others run join at the next chunk boundary, so their work overlaps on the
 // device. Large requests (solo_cells) run instead on their own single-case
-// FP32-bulk solver, created at admission from a host copy of their
-// description and stepped chunk by chunk on its own stream beside the batch
-// (the batch kernel is a generic one; the single-case kernels are faster on
-// large cases and give the same bits).
+// FP32-bulk solver, built from a host copy of their description by a second
+// thread (the preparer) while the worker's chunks run, admitted once built,
+// and stepped chunk by chunk on its own stream beside the batch (the batch
+// kernel is a generic one; the single-case kernels are faster on large cases
+// and give the same bits).
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -90,10 +91,16 @@ struct OwnedDesc {
 struct Request {
     int64_t id = 0;
     std::unique_ptr<lfm::batch::PreparedCase> pc;
-    // solo requests: their description until admission, then their solver
+    // solo requests: their description until admission, then their solver;
+    // prep (guarded by the server's mutex): 0 waiting for the preparer, 1
+    // being built, 2 built, 3 refused (status says why); nomemAt: the
+    // server's solo retirement count when a build ran out of memory (retried
+    // once another solo request has retired)
     std::unique_ptr<OwnedDesc> desc;
     lfm_solver* solver = nullptr;
     double dt = 0;
+    int prep = 0;
+    int64_t nomemAt = -1;
     size_t bytes = 0;
     int nsteps = 0, remaining = 0;
     int slot = -1;
@@ -124,7 +131,12 @@ struct lfm_server {
     int maxBypass = 8;
     int64_t soloCells = 0;   // requests of at least this many cells run on their own solver (0: none)
     int maxSolo = 2;
-    int soloActive = 0;
+    // guarded by mu: solo requests running, built or being built but not yet
+    // admitted, and retired so far
+    int soloActive = 0, soloPrepared = 0;
+    int64_t soloRetired = 0;
+    std::condition_variable cvPrep;
+    std::thread preparer;
     std::chrono::steady_clock::time_point t0;
     std::mutex mu;
     std::condition_variable cvWork, cvDone;
@@ -168,37 +180,28 @@ void fail(lfm_server* s, int code) {
 // maxBypass times nothing behind it is admitted until it fits.
 int admit(lfm_server* s) {
     std::vector<Request*> queue;
+    std::vector<int> prep;
     {
         std::lock_guard<std::mutex> lk(s->mu);
         queue.assign(s->pending.begin(), s->pending.end());
+        for (Request* r : queue) prep.push_back(r->prep);
     }
     std::vector<Request*> admitted, rejected;
     size_t largest = 0, total = 0, arena = 0;
     lfm_batch_memory(s->batch, &largest, &total, &arena);
-    int solo = s->soloActive;
+    int soloAdmitted = 0;
     for (size_t k = 0; k < queue.size(); ++k) {
         Request* r = queue[k];
-        r->tried = true;
-        if (r->desc) {   // its own solver, while fewer than maxSolo run
-            int rc = LFM_ERR_NOMEM;
-            if (solo < s->maxSolo) {
-                lfm_solver_opts o{LFM_FP32_BULK, s->device, 0};
-                rc = lfm_solver_create(&r->desc->d, &o, &r->solver);
-            }
-            if (rc == LFM_OK) {
-                ++solo;
+        if (r->desc) {   // its own solver, built by the preparer thread
+            if (prep[k] == 2) {
+                ++soloAdmitted;
                 admitted.push_back(r);
-                continue;
-            }
-            r->solver = nullptr;
-            if (rc != LFM_ERR_NOMEM) {   // a description the solver refuses
-                r->status = rc;
+            } else if (prep[k] == 3) {   // a description the solver refuses
                 rejected.push_back(r);
-                continue;
             }
-            if (++r->bypassed > s->maxBypass) break;
             continue;
         }
+        r->tried = true;
         if (r->bytes > arena) {   // can never fit
             rejected.push_back(r);
             continue;
@@ -222,7 +225,8 @@ int admit(lfm_server* s) {
         r->desc.reset();
         s->active.push_back(r);
     }
-    s->soloActive = solo;
+    s->soloActive += soloAdmitted;
+    s->soloPrepared -= soloAdmitted;
     for (Request* r : rejected) {
         r->state = 2;
         if (r->status == LFM_OK) r->status = LFM_ERR_NOMEM;
@@ -249,7 +253,14 @@ void workerLoop(lfm_server* s) {
     for (;;) {
         {
             std::unique_lock<std::mutex> lk(s->mu);
-            s->cvWork.wait(lk, [&] { return s->stop || !s->pending.empty() || !s->active.empty(); });
+            // something to run or to admit: a batched request, or a solo
+            // request whose solver the preparer has built (or refused)
+            s->cvWork.wait(lk, [&] {
+                if (s->stop || !s->active.empty()) return true;
+                for (const Request* r : s->pending)
+                    if (!r->desc || r->prep >= 2) return true;
+                return false;
+            });
             if (s->stop) return;
         }
         int rc = admit(s);
@@ -261,14 +272,19 @@ void workerLoop(lfm_server* s) {
         {
             std::lock_guard<std::mutex> lk(s->mu);
             act = s->active;
-            if (act.empty() && !s->pending.empty() && s->pending.front()->tried) {
-                // nothing runs and the oldest request still cannot be placed
-                Request* r = s->pending.front();
-                s->pending.pop_front();
-                r->state = 2;
-                r->status = LFM_ERR_NOMEM;
-                r->tDone = since(s->t0);
-                r->pc.reset();
+            Request* oldest = nullptr;   // the oldest batched request
+            for (Request* r : s->pending)
+                if (!r->desc) {
+                    oldest = r;
+                    break;
+                }
+            if (act.empty() && oldest && oldest->tried) {
+                // nothing runs and the oldest batched request still cannot be placed
+                s->pending.erase(std::find(s->pending.begin(), s->pending.end(), oldest));
+                oldest->state = 2;
+                oldest->status = LFM_ERR_NOMEM;
+                oldest->tDone = since(s->t0);
+                oldest->pc.reset();
                 s->cvDone.notify_all();
             }
         }
@@ -330,7 +346,12 @@ void workerLoop(lfm_server* s) {
                 e1 = lfm_solver_get_state(r->solver, r->result.data());
                 lfm_solver_destroy(r->solver);
                 r->solver = nullptr;
-                --s->soloActive;
+                {
+                    std::lock_guard<std::mutex> lk(s->mu);
+                    --s->soloActive;
+                    ++s->soloRetired;
+                }
+                s->cvPrep.notify_all();
             } else {
                 e1 = lfm_batch_get_state(s->batch, r->slot, r->result.data());
                 e2 = lfm_batch_remove(s->batch, r->slot);
@@ -354,6 +375,59 @@ void workerLoop(lfm_server* s) {
                             s->active.end());
             s->cvDone.notify_all();
         }
+    }
+}
+
+// The preparer thread builds the solvers of solo requests ahead of their
+// admission (host set-up and uploads, overlapping the chunks the worker runs),
+// in arrival order, while fewer than maxSolo are running or built. A build
+// that runs out of device memory is retried once another solo request has
+// retired; one the solver refuses marks the request for rejection.
+Request* nextToPrepare(lfm_server* s) {
+    if (s->soloActive + s->soloPrepared >= s->maxSolo) return nullptr;
+    for (Request* r : s->pending)
+        if (r->desc && r->prep == 0 && r->nomemAt < s->soloRetired) return r;
+    return nullptr;
+}
+
+void preparerLoop(lfm_server* s) {
+    if (cudaSetDevice(s->device) != cudaSuccess) {
+        lfm::setError(LFM_ERR_CUDA, "server preparer: cudaSetDevice failed");
+        fail(s, LFM_ERR_CUDA);
+        return;
+    }
+    for (;;) {
+        Request* r = nullptr;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            s->cvPrep.wait(lk, [&] { return s->stop || (r = nextToPrepare(s)) != nullptr; });
+            if (s->stop) return;
+            r->prep = 1;
+            ++s->soloPrepared;
+        }
+        // r stays in the pending queue and owned by the server while its
+        // prep is 1: nothing else touches its description
+        lfm_solver_opts o{LFM_FP32_BULK, s->device, 0};
+        lfm_solver* sv = nullptr;
+        const int rc = lfm_solver_create(&r->desc->d, &o, &sv);
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            if (rc == LFM_OK) {
+                r->solver = sv;
+                r->prep = 2;
+            } else {
+                --s->soloPrepared;
+                if (rc == LFM_ERR_NOMEM && s->soloActive + s->soloPrepared > 0) {
+                    // other solvers hold memory that their retirement frees
+                    r->prep = 0;
+                    r->nomemAt = s->soloRetired;
+                } else {   // refused, or out of memory with no other solver to wait for
+                    r->prep = 3;
+                    r->status = rc;
+                }
+            }
+        }
+        s->cvWork.notify_all();
     }
 }
 
@@ -396,6 +470,7 @@ extern "C" int lfm_server_create(const lfm_server_opts* opts, lfm_server** out) 
     s->maxSolo = opts->max_solo > 0 ? opts->max_solo : 2;
     s->t0 = std::chrono::steady_clock::now();
     s->worker = std::thread(workerLoop, s);
+    if (s->soloCells > 0) s->preparer = std::thread(preparerLoop, s);
     *out = s;
     return LFM_OK;
 }
@@ -407,7 +482,9 @@ extern "C" void lfm_server_destroy(lfm_server* s) {
         s->stop = true;
     }
     s->cvWork.notify_all();
+    s->cvPrep.notify_all();
     if (s->worker.joinable()) s->worker.join();
+    if (s->preparer.joinable()) s->preparer.join();
     lfm_batch_destroy(s->batch);
     delete s;
 }
@@ -451,6 +528,7 @@ extern "C" int lfm_server_submit(lfm_server* s, const lfm_solver_desc* d, double
         s->all[r->id] = std::move(r);
     }
     s->cvWork.notify_all();
+    s->cvPrep.notify_all();
     return LFM_OK;
 }
 

@@ -523,6 +523,15 @@ def _accuracy(N, acoustics, case, ch, dt, checkpoints, local, rings):
     return acc
 
 
+def _guarded(fn, *a):
+    """A sub-record of the default line; a failure there is reported in the
+    line (the headline stands) instead of ending the run."""
+    try:
+        return fn(*a)
+    except Exception as e:
+        return {"error": repr(e)}
+
+
 def _wake_record(N, built, args, local, hbm, peak_src):
     """Device-timed sub-record of the 3D cylinder wake (384x256x96, 9.4M hex
     cells, working set far beyond L2): FP32-bulk and FP64, no CPU leg."""
@@ -620,14 +629,15 @@ def run_gpu(args):
     wake = None
     if wake_thread is not None:
         wake_thread.join()
-        wake = _wake_record(N, wake_built[0], args, local, hbm, peak_src) if wake_built[0] else {"error": wake_err[0]}
+        wake = (_guarded(_wake_record, N, wake_built[0], args, local, hbm, peak_src) if wake_built[0]
+                else {"error": wake_err[0]})
         wake_built[0] = None
     batch = None
     if sweep_thread is not None:
         sweep_thread.join()
         if sweep_built[0]:
             spec, built = sweep_built[0]
-            batch = _batch_record(N, built, spec, local, None, 1, args.batch_steps, 3)
+            batch = _guarded(_batch_record, N, built, spec, local, None, 1, args.batch_steps, 3)
         else:
             batch = {"error": sweep_err[0]}
         sweep_built[0] = None
@@ -636,10 +646,13 @@ def run_gpu(args):
         lib_thread.join()
         if lib_built[0]:
             lib = lib_built[0]
-            fp64 = _fp64_times(lib, local)
-            rate = float(args.serve_default_rate)
-            serve = dict(_serve_config(args, lib, args.serve_default_window, str(rate)),
-                         **_serve_rate(N, args, lib, fp64, rate, args.serve_default_window, 77, local))
+            def serve_record():
+                fp64 = _fp64_times(lib, local)
+                rate = float(args.serve_default_rate)
+                return dict(_serve_config(args, lib, args.serve_default_window, str(rate)),
+                            **_serve_rate(N, args, lib, fp64, rate, args.serve_default_window, 77, local))
+
+            serve = _guarded(serve_record)
         else:
             serve = {"error": lib_err[0]}
         lib_built[0] = None

@@ -1063,8 +1063,12 @@ def run_serve(args):
     lib = _serve_library(args.serve_library, local)
     fp64 = _fp64_times(lib, local)
     window = args.serve_window
-    per_rate = [_serve_rate(N, args, lib, fp64, rate, window, 77 + ri, local)
-                for ri, rate in enumerate(float(x) for x in args.serve_rates.split(","))]
+    with ClockSampler(local) as clk:
+        per_rate = []
+        for ri, rate in enumerate(float(x) for x in args.serve_rates.split(",")):
+            clk.mark()
+            per_rate.append(_serve_rate(N, args, lib, fp64, rate, window, 77 + ri, local))
+            clk.mark()
     if rank != 0:
         return 0
     best = max(per_rate, key=lambda r: r["throughput"])
@@ -1074,6 +1078,7 @@ def run_serve(args):
         "dtype": "f32-flux/f64-rk", "data": "synthetic (generated meshes and initial fields)",
         "config": _serve_config(args, lib, window, args.serve_rates),
         "serving": per_rate,
+        "clocks": clk.summary(),
         "fp64_serial_note": "FP64 server: the same streams first come first served, one request at a time, the "
                             "same queue bound, timeline replayed from each library case's measured FP64 set-up, "
                             "step and read-back times",

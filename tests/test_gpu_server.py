@@ -101,14 +101,16 @@ def test_oversized_request_is_refused_and_others_run():
     assert np.array_equal(qs, _alone(chs, small.delta_t, 5))
 
 
-def test_nonfinite_request_is_retired_alone():
+@pytest.mark.parametrize("solo_cells", [0, 1])
+def test_nonfinite_request_is_retired_alone(solo_cells):
+    """Batched (solo_cells 0) or each on its own solver (solo_cells 1)."""
     # A patch without a boundary condition keeps a zero ghost state (as in the
     # reference): the first flux through it is non-finite.
     bad = cases.vortex_case(n=32)
     bad.patches = [dataclasses.replace(p, name="side") if p.name == "outlet" else p for p in bad.patches]
     good = cases.vortex_case(n=40)
     chb, chg = N.CaseHandle.from_case(bad), N.CaseHandle.from_case(good)
-    srv = N.Server(arena_bytes=64 << 20, chunk_steps=4)
+    srv = N.Server(arena_bytes=64 << 20, chunk_steps=4, solo_cells=solo_cells)
     rb = srv.submit(chb, bad.delta_t, 20)
     rg = srv.submit(chg, good.delta_t, 20)
     assert srv.wait(rb, 30.0) and srv.wait(rg, 30.0)
@@ -162,3 +164,22 @@ def test_solo_request_runs_an_les_case():
     s.sync()
     assert np.array_equal(q, s.get_state())
     s.close()
+
+
+def test_server_closes_while_solo_solvers_are_built():
+    """Closing a server with solo requests queued, being built and running
+    returns (the worker and the solver-building thread stop; their solvers
+    are freed), and a new server on the same device serves normally."""
+    c = cases.vortex_case(n=160, solver=0)
+    ch = N.CaseHandle.from_case(c)
+    srv = N.Server(arena_bytes=64 << 20, solo_cells=1, max_solo=2, chunk_steps=5)
+    for _ in range(6):
+        srv.submit(ch, c.delta_t, 200)
+    time.sleep(0.05)
+    t0 = time.time()
+    srv.close()
+    assert time.time() - t0 < 30.0
+    small = cases.vortex_case(n=24)
+    chs = N.CaseHandle.from_case(small)
+    q = _alone(chs, small.delta_t, 7)
+    assert np.isfinite(q).all()

@@ -593,7 +593,11 @@ def run_gpu(args):
             wake_err[0] = repr(e)
 
     wake_thread = None
-    if args.wake and args.workload.startswith("cylinder2d"):
+    # the accuracy runs and the sub-records are reported by rank 0 alone, and
+    # only rank 0 runs them (under torchrun the other ranks would only repeat
+    # them, each holding the large cases in host memory)
+    extras = rank == 0
+    if extras and args.wake and args.workload.startswith("cylinder2d"):
         wake_thread = threading.Thread(target=build_wake, daemon=True)
         wake_thread.start()
     # and so are the 64 cases of the batched sweep
@@ -606,7 +610,7 @@ def run_gpu(args):
             sweep_err[0] = repr(e)
 
     sweep_thread = None
-    if args.batch and args.workload.startswith("cylinder2d"):
+    if extras and args.batch and args.workload.startswith("cylinder2d"):
         sweep_thread = threading.Thread(target=build_sweep, daemon=True)
         sweep_thread.start()
     # and so is the serving library
@@ -619,11 +623,11 @@ def run_gpu(args):
             lib_err[0] = repr(e)
 
     lib_thread = None
-    if args.serve and args.workload.startswith("cylinder2d"):
+    if extras and args.serve and args.workload.startswith("cylinder2d"):
         lib_thread = threading.Thread(target=build_lib, daemon=True)
         lib_thread.start()
     accuracy = None
-    if args.accuracy_steps:
+    if extras and args.accuracy_steps:
         accuracy = _accuracy(N, acoustics, case, ch, dt, args.accuracy_steps, local,
                              RING_RADII if args.workload.startswith("cylinder") else ())
     wake = None

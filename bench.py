@@ -513,14 +513,21 @@ def _accuracy(N, acoustics, case, ch, dt, checkpoints, local, rings):
     acc["against"] = "FP64 device path (itself within 1e-12 of the oracle), same case and steps"
     if len(out) > 1:
         acc["longer"] = out[1:]
-    # the r = 50 D ring at the longest checkpoint its FP64 p' has reached (a
-    # ring the start-up pulse has not reached yet has p' = 0 and no error)
-    acc["probe_ring"] = None
-    for rec in out:
-        ring = next((x for x in rec["probe_rings"] if x["radius"] == 50.0), None)
-        if ring is not None and (acc["probe_ring"] is None or ring["rel_l2"] is not None):
-            acc["probe_ring"] = dict(ring, steps=rec["steps"])
+    acc["probe_ring"] = ring_at_longest(out, 50.0)
     return acc
+
+
+def ring_at_longest(checkpoints, radius):
+    """The probe ring of `radius` at the longest checkpoint its FP64 p' has
+    reached (a ring the start-up pulse has not reached yet has p' = 0 and no
+    error), with that checkpoint's step count; the first checkpoint's ring
+    when none has been reached."""
+    best = None
+    for rec in checkpoints:
+        ring = next((x for x in rec["probe_rings"] if x["radius"] == radius), None)
+        if ring is not None and (best is None or ring["rel_l2"] is not None):
+            best = dict(ring, steps=rec["steps"])
+    return best
 
 
 def _guarded(fn, *a):

@@ -175,9 +175,10 @@ void fail(lfm_server* s, int code) {
     s->cvDone.notify_all();
 }
 
-// Admission pass: arrival order; a request that does not fit is passed over,
-// except that once the oldest waiting request has been passed over
-// maxBypass times nothing behind it is admitted until it fits.
+// Admission pass: arrival order; a batched request that does not fit is
+// passed over, except that once the oldest waiting one has been passed over
+// maxBypass times no batched request behind it is admitted until it fits.
+// Solo requests take no arena: each is admitted once its solver is built.
 int admit(lfm_server* s) {
     std::vector<Request*> queue;
     std::vector<int> prep;
@@ -190,9 +191,10 @@ int admit(lfm_server* s) {
     size_t largest = 0, total = 0, arena = 0;
     lfm_batch_memory(s->batch, &largest, &total, &arena);
     int soloAdmitted = 0;
+    bool arenaClosed = false;   // a batched request waits: no batched request behind it goes first
     for (size_t k = 0; k < queue.size(); ++k) {
         Request* r = queue[k];
-        if (r->desc) {   // its own solver, built by the preparer thread
+        if (r->desc) {   // its own solver, built by the preparer thread (no arena)
             if (prep[k] == 2) {
                 ++soloAdmitted;
                 admitted.push_back(r);
@@ -201,6 +203,7 @@ int admit(lfm_server* s) {
             }
             continue;
         }
+        if (arenaClosed) continue;
         r->tried = true;
         if (r->bytes > arena) {   // can never fit
             rejected.push_back(r);
@@ -214,7 +217,7 @@ int admit(lfm_server* s) {
             continue;
         }
         if (rc != LFM_ERR_NOMEM) return rc;
-        if (++r->bypassed > s->maxBypass) break;
+        if (++r->bypassed > s->maxBypass) arenaClosed = true;
     }
     std::lock_guard<std::mutex> lk(s->mu);
     const double now = since(s->t0);

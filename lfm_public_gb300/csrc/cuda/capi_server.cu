@@ -315,16 +315,26 @@ void workerLoop(lfm_server* s) {
             fail(s, rc);
             return;
         }
-        for (Request* r : act) {
-            if (!r->solver) continue;
-            const int st = lfm_solver_sync(r->solver);
-            if (st == LFM_ERR_NUMERIC) {
-                r->status = st;
-            } else if (st != LFM_OK) {
-                fail(s, st);
-                return;
+        // each request's status after the chunk (applied under the lock
+        // below: lfm_server_info reads it from other threads)
+        std::vector<int> stat(act.size(), LFM_OK);
+        for (size_t k = 0; k < act.size(); ++k) {
+            Request* r = act[k];
+            if (r->solver) {
+                const int st = lfm_solver_sync(r->solver);
+                if (st == LFM_ERR_NUMERIC) {
+                    stat[k] = st;
+                } else if (st != LFM_OK) {
+                    fail(s, st);
+                    return;
+                }
+            } else if (rc == LFM_ERR_NUMERIC) {
+                int st = LFM_OK;
+                if (lfm_batch_case_status(s->batch, r->slot, &st) != LFM_OK) st = LFM_ERR_CUDA;
+                stat[k] = st;
             }
         }
+        std::vector<Request*> done;
         {
             double cells = 0;
             for (Request* r : act) cells += (double)r->nc;
@@ -332,15 +342,12 @@ void workerLoop(lfm_server* s) {
             ++s->chunks;
             s->busy += since(s->t0) - tChunk;
             s->cellStages += cells * (double)n * (double)s->rkOrder;
-            for (Request* r : act) r->remaining -= n;
-        }
-        std::vector<Request*> done;
-        for (Request* r : act) {
-            int st = LFM_OK;
-            if (!r->solver && rc == LFM_ERR_NUMERIC && lfm_batch_case_status(s->batch, r->slot, &st) != LFM_OK)
-                st = LFM_ERR_CUDA;
-            if (st != LFM_OK) r->status = st;
-            if (r->remaining == 0 || r->status != LFM_OK) done.push_back(r);
+            for (size_t k = 0; k < act.size(); ++k) {
+                Request* r = act[k];
+                r->remaining -= n;
+                if (stat[k] != LFM_OK) r->status = stat[k];
+                if (r->remaining == 0 || r->status != LFM_OK) done.push_back(r);
+            }
         }
         for (Request* r : done) {
             r->result.resize((size_t)r->nq * r->nc);

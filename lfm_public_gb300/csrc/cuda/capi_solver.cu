@@ -254,8 +254,8 @@ int buildArgs(lfm_solver* s, const lfm_solver_desc* d, Args<T>& a, const int* fP
                 for (size_t k = 0; k < D; ++k) {
                     const double Sk = d->S[k * nf + (size_t)f];
                     const double so = isP ? Sk * d->vol_inv[c] : -Sk * d->vol_inv[c];
-                    soN[k * ne + (size_t)e] = wAcross * so;
-                    soW[k * nc + c] += wOwn * so;
+                    soN[(size_t)e * D + k] = wAcross * so;   // entry-major: one entry's D values together
+                    soW[c * D + k] += wOwn * so;
                 }
             }
         if ((rc = uploadAs<T>(s, &p, soN.data(), soN.size()))) return rc;

@@ -20,6 +20,20 @@ __global__ void __launch_bounds__(256) k_prep(Args<T> a, int first) {
     prims64<D>(a, t, qv);
 }
 
+// D consecutive FP64 values starting at an index that is a multiple of D:
+// one 16-byte load in 2D (the constants of an incidence entry or a cell).
+template <int D>
+__device__ __forceinline__ void load_vec(const double* p, size_t i, double* out) {
+    if constexpr (D == 2) {
+        const double2 v = reinterpret_cast<const double2*>(p)[i];
+        out[0] = v.x;
+        out[1] = v.y;
+    } else {
+#pragma unroll
+        for (int k = 0; k < D; ++k) out[k] = p[i * D + k];
+    }
+}
+
 // ---------------------------------------------------------------------------
 // k_grad: gradients read by M2AUSM's minmod reconstruction.
 // ---------------------------------------------------------------------------
@@ -37,14 +51,12 @@ __global__ void __launch_bounds__(256) k_grad(Args<T> a) {
     // Gauss gradients of rho, p and u: the cell's own share through its
     // constant cellSoW, each neighbour's through the entry constant cfSoN
     // (the face values w v_P + (1 - w) v_N expanded)
-    const size_t ne = (size_t)a.cfOff[a.nc], nt = (size_t)a.nt, nc = (size_t)a.nc;
+    const size_t nt = (size_t)a.nt;
     {
         T sw[D], Uc[D];
+        load_vec<D>(a.cellSoW, (size_t)c, sw);
 #pragma unroll
-        for (int k = 0; k < D; ++k) {
-            sw[k] = a.cellSoW[(size_t)k * nc + c];
-            Uc[k] = a.prim[(size_t)(1 + k) * nt + c];
-        }
+        for (int k = 0; k < D; ++k) Uc[k] = a.prim[(size_t)(1 + k) * nt + c];
         const T rhoc = a.q[c];
         const T pc = rhoc * a.prim[(size_t)(D + 1) * nt + c];
 #pragma unroll
@@ -58,8 +70,7 @@ __global__ void __launch_bounds__(256) k_grad(Args<T> a) {
     for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
         const int j = a.cfNbr[e];
         T so[D];
-#pragma unroll
-        for (int k = 0; k < D; ++k) so[k] = a.cfSoN[(size_t)k * ne + e];
+        load_vec<D>(a.cfSoN, (size_t)e, so);
         const T rhoj = a.q[j];
         const T pj = rhoj * a.prim[(size_t)(D + 1) * nt + j];
 #pragma unroll
@@ -99,11 +110,9 @@ __global__ void __launch_bounds__(256) k_vis(Args<T> a) {
     // and so = S/V seen from c, sum_f v_f so = v_c cellSoW_c + sum_e v_j
     // cfSoN_e: the cell's own share through one cell constant, each
     // neighbour's through an entry constant (the other cell j = cfNbr[e]).
-    const size_t ne = (size_t)a.cfOff[a.nc], nc = (size_t)a.nc;
     {
         T sw[D];
-#pragma unroll
-        for (int k = 0; k < D; ++k) sw[k] = a.cellSoW[(size_t)k * nc + c];
+        load_vec<D>(a.cellSoW, (size_t)c, sw);
         const T Rc = a.prim[(size_t)(D + 1) * a.nt + c];
 #pragma unroll
         for (int x = 0; x < D; ++x) {
@@ -116,11 +125,9 @@ __global__ void __launch_bounds__(256) k_vis(Args<T> a) {
     for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
         const int j = a.cfNbr[e];
         T so[D], fU[D];
+        load_vec<D>(a.cfSoN, (size_t)e, so);
 #pragma unroll
-        for (int k = 0; k < D; ++k) {
-            so[k] = a.cfSoN[(size_t)k * ne + e];
-            fU[k] = a.prim[(size_t)(1 + k) * a.nt + j];
-        }
+        for (int k = 0; k < D; ++k) fU[k] = a.prim[(size_t)(1 + k) * a.nt + j];
         const T fR = a.prim[(size_t)(D + 1) * a.nt + j];
 #pragma unroll
         for (int x = 0; x < D; ++x) {

@@ -95,9 +95,9 @@ struct Args {
     const int* cfOff;         // nc + 1
     const int* cfList;        // face index, negative (~f) when the cell is N
     const int* cfNbr;         // per cfList entry: the cell (or ghost, halo) across the face
-    const T* cfSoN;           // FP64 path: D x (cfList entries), the linear weight of the cell
+    const T* cfSoN;           // FP64 path: (cfList entries) x D, the linear weight of the cell
                               // across the entry's face times S / V seen from the entry's cell
-    const T* cellSoW;         // FP64 path: D x nc, the sum over the cell's faces of its own
+    const T* cellSoW;         // FP64 path: nc x D, the sum over the cell's faces of its own
                               // linear weight times S / V (Gauss gradient of cell c:
                               // v_c cellSoW_c + sum over entries of v_across cfSoN)
     const T* smagC;           // Smagorinsky LES: the constant each cell's tauMC is built with
